@@ -1,0 +1,653 @@
+// C ABI of the GB300 SPH step: handle management, the per-step stage
+// sequence, read-back and boundary-map set-up.  See include/sph.h.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "sph_internal.h"
+
+using namespace sph;
+
+namespace {
+
+thread_local std::string g_lastError;
+
+// The reference's error message shape (util.h:24-39).
+sph_status fail(sph_status st, const char* file, int line, const std::string& msg) {
+    std::ostringstream s;
+    s << "Exception thrown in FILE: " << file << " LINE: " << line << "\n"
+      << "Error Message: " << msg << "\n";
+    g_lastError = s.str();
+    return st;
+}
+
+#define SPH_FAIL(st, msg) return fail((st), __FILE__, __LINE__, (msg))
+#define SPH_CUDA(call)                                                                   \
+    do {                                                                                 \
+        cudaError_t e_ = (call);                                                         \
+        if (e_ != cudaSuccess) {                                                         \
+            sph_status st_ = e_ == cudaErrorMemoryAllocation ? SPH_ERR_OUT_OF_MEMORY      \
+                                                             : SPH_ERR_CUDA;              \
+            return fail(st_, __FILE__, __LINE__, cudaGetErrorString(e_));                 \
+        }                                                                                \
+    } while (0)
+
+enum Stage { ST_HASH, ST_SCAN, ST_SCATTER, ST_RANK, ST_DENSITY, ST_FORCE, ST_COUNT };
+const char* kStageNames[ST_COUNT] = {"hash_count", "cell_scan", "scatter", "rank_gather",
+                                     "density", "force_integrate"};
+
+template <class T>
+cudaError_t dalloc(T** p, size_t count) {
+    return cudaMalloc((void**)p, sizeof(T) * (count > 0 ? count : 1));
+}
+
+}  // namespace
+
+struct sph_sim {
+    SimulationParameters P;
+    sph_options O;
+    int n = 0;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaStream_t ownStream = nullptr;
+
+    // state (particle order) and per-step sorted copies
+    float4 *pos = nullptr, *vel = nullptr;
+    float4 *posS = nullptr, *velS = nullptr, *rho4S = nullptr, *accS = nullptr;
+    SortBuffers sb{};
+    unsigned long long* scanBlock = nullptr;
+    unsigned int* status = nullptr;     // device status word
+    unsigned int* statusHost = nullptr; // pinned copy
+    float* staging = nullptr;           // device AoS staging, n*10 floats
+    std::vector<float> sdMass, sdEnergy;  // SD_MASS / SD_ENERGY columns (never touched by the step)
+
+    // boundary maps
+    float4* map4 = nullptr;
+    float* mapDist = nullptr;
+    MapDev map{};
+
+    unsigned int numTimeSteps = 0;
+    bool stepped = false;
+
+    // launch configuration (autotuned later)
+    int densityBlock = 128, forceBlock = 128, kahan = 1;
+
+    // CUDA graph of one plain step
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graphExec = nullptr;
+    bool graphValid = false;
+
+    // stage timing ring
+    int timingCap = 0, timingNext = 0, timingFilled = 0;
+    std::vector<cudaEvent_t> events;  // timingCap * (ST_COUNT + 1)
+};
+
+namespace {
+
+GridDev make_grid(const SimulationParameters& P, bool sub) {
+    GridDev g;
+    for (int a = 0; a < 3; a++) {
+        g.origin[a] = P.gridOrigin[a];
+        g.dim[a] = sub ? P.gridDimSubParticles[a] : P.gridDim[a];
+    }
+    g.spacing = sub ? P.gridSpacingSubParticles : P.gridSpacing;
+    g.numCells = g.dim[0] * g.dim[1] * g.dim[2];
+    return g;
+}
+
+PhysDev make_phys(const SimulationParameters& P, const sph_options& O) {
+    PhysDev ph;
+    ph.h = P.compactSupport;
+    ph.h2 = P.compactSupport * P.compactSupport;
+    ph.poly6m = P.poly6 * P.particleMass;
+    ph.mass = P.particleMass;
+    ph.stiffness = P.gasStiffness;
+    ph.restDensity = P.restDensity;
+    ph.pressCoef = -P.particleMass * P.gradSpiky;
+    ph.viscCoef = P.dynamicViscosity * P.particleMass * P.laplVisc;
+    ph.cgCoef = P.particleMass * P.gradPoly6;
+    ph.clCoef = P.particleMass * P.laplPoly6;
+    ph.tension = P.tensionCoefficient;
+    ph.normThresh = P.normThresh;
+    ph.dt = P.timeStep;
+    ph.dtCollide = P.timeStep;
+    ph.gravity = P.gravity;
+    ph.gravityAxis = O.gravityAxis;
+    for (int a = 0; a < 3; a++) {
+        ph.boxCen[a] = P.boxCen[a];
+        ph.boxDim[a] = P.boxDim[a];
+    }
+    ph.restitution = P.restitution;
+    return ph;
+}
+
+sph_status validate_params(const SimulationParameters* P, const sph_options* O) {
+    if (!P) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "params is NULL");
+    if (P->numParticles == 0 || P->numParticles > (1u << 30))
+        SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "numParticles must be in [1, 2^30]");
+    double cells = 1.0;
+    for (int a = 0; a < 3; a++) {
+        if (P->gridDim[a] <= 0) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "gridDim must be positive");
+        cells *= P->gridDim[a];
+    }
+    if (cells > 2147483000.0) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "too many grid cells");
+    if (!(P->gridSpacing > 0.0f) || !(P->compactSupport > 0.0f))
+        SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "gridSpacing and compactSupport must be positive");
+    if (P->compactSupport > P->gridSpacing)
+        SPH_FAIL(SPH_ERR_INVALID_ARGUMENT,
+                 "compactSupport exceeds gridSpacing: the 27-cell stencil would miss neighbours");
+    if (O && (O->gravityAxis < 0 || O->gravityAxis > 2))
+        SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "gravityAxis must be 0, 1 or 2");
+    return SPH_OK;
+}
+
+sph_status check_desc(const sph_boundary_desc* d, unsigned int dims[3]) {
+    if (!d) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "boundary desc is NULL");
+    if (d->numShapes < 1 || d->numShapes > 8)
+        SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "numShapes must be in [1, 8]");
+    for (int i = 0; i < d->numShapes; i++) {
+        int k = d->shapes[i].kind;
+        if (k != SPH_SHAPE_SPHERE && k != SPH_SHAPE_CONE && k != SPH_SHAPE_BOX)
+            SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "unknown shape kind");
+    }
+    if (!(d->gridSpacing > 0.0f) || !(d->particleSpacing > 0.0f) || !(d->compactSupport > 0.0f))
+        SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "boundary spacings must be positive");
+    double total = 1.0;
+    for (int a = 0; a < 3; a++) {
+        if (!(d->gridEnd[a] > d->gridStart[a]))
+            SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "invalid domain definition");  // SphInComplexShapes.cpp:43-47
+        // SphInComplexShapes.cpp:49-54
+        dims[a] = (unsigned int)((d->gridEnd[a] - d->gridStart[a]) / d->gridSpacing) + 1;
+        total *= dims[a];
+    }
+    if (total > 512.0 * 1024 * 1024) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "boundary grid too large");
+    return SPH_OK;
+}
+
+void free_all(sph_sim* s) {
+    if (s->graphExec) cudaGraphExecDestroy(s->graphExec);
+    if (s->graph) cudaGraphDestroy(s->graph);
+    for (cudaEvent_t e : s->events) cudaEventDestroy(e);
+    void* ptrs[] = {s->pos, s->vel, s->posS, s->velS, s->rho4S, s->accS, s->sb.cnt, s->sb.cellOffset,
+                    s->sb.keySlot, s->sb.tmpIds, s->sb.sortedHash, s->sb.sortedIds, s->scanBlock,
+                    s->status, s->staging, s->map4, s->mapDist};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    if (s->statusHost) cudaFreeHost(s->statusHost);
+    if (s->ownStream) cudaStreamDestroy(s->ownStream);
+}
+
+// Enqueues the plain step's stages (no host synchronisation).
+void enqueue_plain(sph_sim* s, bool timing) {
+    cudaStream_t st = s->stream;
+    const int n = s->n;
+    GridDev g = make_grid(s->P, false);
+    PhysDev ph = make_phys(s->P, s->O);
+    cudaEvent_t* ev = nullptr;
+    if (timing) {
+        ev = &s->events[(size_t)s->timingNext * (ST_COUNT + 1)];
+        s->timingNext = (s->timingNext + 1) % s->timingCap;
+        s->timingFilled = std::min(s->timingFilled + 1, s->timingCap);
+    }
+    auto mark = [&](int k) {
+        if (ev) cudaEventRecord(ev[k], st);
+    };
+    mark(ST_HASH);
+    launch_hash_count(n, s->pos, g, s->sb, s->status, st);
+    mark(ST_SCAN);
+    launch_cell_scan(g.numCells, s->sb, s->status, st);
+    mark(ST_SCATTER);
+    launch_scatter(n, s->sb, st);
+    mark(ST_RANK);
+    launch_rank_gather(n, s->sb, s->pos, s->vel, s->posS, s->velS, st);
+    mark(ST_DENSITY);
+    launch_density(n, s->posS, s->sb.cellOffset, g, ph, s->map, s->rho4S, s->kahan, s->densityBlock, st);
+    mark(ST_FORCE);
+    launch_force(n, s->posS, s->velS, s->rho4S, s->sb.sortedIds, s->sb.cellOffset, g, ph, s->map,
+                 s->O.boxCollision, s->pos, s->vel, s->accS, s->kahan, s->forceBlock, st);
+    mark(ST_COUNT);
+}
+
+sph_status latched_status(sph_sim* s) {
+    SPH_CUDA(cudaMemcpyAsync(s->statusHost, s->status, sizeof(unsigned int), cudaMemcpyDeviceToHost,
+                             s->stream));
+    SPH_CUDA(cudaStreamSynchronize(s->stream));
+    unsigned int v = *s->statusHost;
+    if (v & STATUS_NON_FINITE) SPH_FAIL(SPH_ERR_NON_FINITE, "a non-finite particle position entered the step");
+    if (v & STATUS_OUT_OF_DOMAIN)
+        SPH_FAIL(SPH_ERR_OUT_OF_DOMAIN, "a particle was hashed outside the cell grid");
+    if (v & STATUS_DEVICE_WAIT) SPH_FAIL(SPH_ERR_DEVICE_WAIT, "a bounded device-side wait gave up");
+    return SPH_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void sph_default_options(sph_options* o) {
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->gravityAxis = 1;
+    o->boxCollision = 0;
+    o->splitMin[0] = 0.2f;
+    o->splitMax[0] = 0.5f;
+    for (int a = 1; a < 3; a++) {
+        o->splitMin[a] = -3.0e38f;
+        o->splitMax[a] = 3.0e38f;
+    }
+}
+
+const char* sph_last_error(void) { return g_lastError.c_str(); }
+
+const char* sph_status_string(sph_status s) {
+    switch (s) {
+        case SPH_OK: return "ok";
+        case SPH_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case SPH_ERR_CUDA: return "CUDA error";
+        case SPH_ERR_OUT_OF_MEMORY: return "out of device memory";
+        case SPH_ERR_OUT_OF_DOMAIN: return "particle outside the cell grid";
+        case SPH_ERR_DEVICE_WAIT: return "device-side wait gave up";
+        case SPH_ERR_NOT_SUPPORTED: return "not supported";
+        case SPH_ERR_NON_FINITE: return "non-finite particle position";
+    }
+    return "unknown status";
+}
+
+const char* sph_stage_name(int stage) {
+    return stage >= 0 && stage < ST_COUNT ? kStageNames[stage] : "";
+}
+
+sph_status sph_boundary_dims(const sph_boundary_desc* desc, unsigned int dims[3]) {
+    if (!dims) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "dims is NULL");
+    return check_desc(desc, dims);
+}
+
+sph_status sph_boundary_maps(const sph_boundary_desc* desc, float* distance, float* density,
+                             float* viscosity) {
+    unsigned int dims[3];
+    sph_status st = check_desc(desc, dims);
+    if (st) return st;
+    size_t total = (size_t)dims[0] * dims[1] * dims[2];
+    float *d = nullptr, *r = nullptr, *v = nullptr;
+    SPH_CUDA(dalloc(&d, total));
+    cudaError_t e1 = dalloc(&r, total), e2 = dalloc(&v, total);
+    if (e1 != cudaSuccess || e2 != cudaSuccess) {
+        cudaFree(d);
+        if (r) cudaFree(r);
+        if (v) cudaFree(v);
+        SPH_FAIL(SPH_ERR_OUT_OF_MEMORY, "boundary map allocation failed");
+    }
+    launch_build_maps(*desc, dims, d, r, v, nullptr, 0);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess && distance) e = cudaMemcpy(distance, d, total * 4, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && density) e = cudaMemcpy(density, r, total * 4, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && viscosity) e = cudaMemcpy(viscosity, v, total * 4, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    cudaFree(d);
+    cudaFree(r);
+    cudaFree(v);
+    SPH_CUDA(e);
+    return SPH_OK;
+}
+
+sph_status sph_create(const SimulationParameters* params, const sph_options* opts, const float* vertexData,
+                      const float* simulationData, const sph_boundary_desc* boundary, sph_handle* out) {
+    if (!out) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "out is NULL");
+    *out = nullptr;
+    sph_status st = validate_params(params, opts);
+    if (st) return st;
+    if (!vertexData) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "vertexData is NULL");
+    unsigned int mdims[3] = {0, 0, 0};
+    if (boundary) {
+        st = check_desc(boundary, mdims);
+        if (st) return st;
+    }
+    sph_sim* s = new (std::nothrow) sph_sim();
+    if (!s) SPH_FAIL(SPH_ERR_OUT_OF_MEMORY, "host allocation failed");
+    s->P = *params;
+    if (opts) s->O = *opts;
+    else sph_default_options(&s->O);
+    s->n = (int)params->numParticles;
+    const int n = s->n;
+    const int C = params->gridDim[0] * params->gridDim[1] * params->gridDim[2];
+    const int tiles = (C + 1 + SCAN_TILE - 1) / SCAN_TILE;
+
+#define CREATE_CUDA(call)                                                  \
+    do {                                                                   \
+        cudaError_t e_ = (call);                                           \
+        if (e_ != cudaSuccess) {                                           \
+            free_all(s);                                                   \
+            delete s;                                                      \
+            return fail(e_ == cudaErrorMemoryAllocation ? SPH_ERR_OUT_OF_MEMORY : SPH_ERR_CUDA, \
+                        __FILE__, __LINE__, cudaGetErrorString(e_));       \
+        }                                                                  \
+    } while (0)
+
+    CREATE_CUDA(cudaGetDevice(&s->device));
+    CREATE_CUDA(cudaStreamCreateWithFlags(&s->ownStream, cudaStreamNonBlocking));
+    s->stream = s->ownStream;
+    CREATE_CUDA(dalloc(&s->pos, n));
+    CREATE_CUDA(dalloc(&s->vel, n));
+    CREATE_CUDA(dalloc(&s->posS, n));
+    CREATE_CUDA(dalloc(&s->velS, n));
+    CREATE_CUDA(dalloc(&s->rho4S, n));
+    CREATE_CUDA(dalloc(&s->accS, n));
+    CREATE_CUDA(dalloc(&s->sb.cnt, (size_t)C + 1 + SCAN_TILE));
+    CREATE_CUDA(dalloc(&s->sb.cellOffset, (size_t)C + 1 + SCAN_TILE));
+    CREATE_CUDA(dalloc(&s->sb.keySlot, n));
+    CREATE_CUDA(dalloc(&s->sb.tmpIds, n));
+    CREATE_CUDA(dalloc(&s->sb.sortedHash, n));
+    CREATE_CUDA(dalloc(&s->sb.sortedIds, n));
+    CREATE_CUDA(dalloc(&s->scanBlock, (size_t)tiles + 2));
+    s->sb.tileCounter = reinterpret_cast<unsigned int*>(s->scanBlock);
+    s->sb.scanFlags = s->scanBlock + 2;
+    s->sb.maxTiles = tiles;
+    CREATE_CUDA(dalloc(&s->status, 1));
+    CREATE_CUDA(cudaMallocHost((void**)&s->statusHost, sizeof(unsigned int)));
+    CREATE_CUDA(dalloc(&s->staging, (size_t)n * 10));
+    CREATE_CUDA(cudaMemsetAsync(s->sb.cnt, 0, sizeof(int) * ((size_t)C + 1 + SCAN_TILE), s->stream));
+    CREATE_CUDA(cudaMemsetAsync(s->status, 0, sizeof(unsigned int), s->stream));
+    CREATE_CUDA(cudaMemsetAsync(s->vel, 0, sizeof(float4) * n, s->stream));
+    CREATE_CUDA(cudaMemsetAsync(s->rho4S, 0, sizeof(float4) * n, s->stream));
+    CREATE_CUDA(cudaMemsetAsync(s->accS, 0, sizeof(float4) * n, s->stream));
+
+    // initial state: VD positions, SD velocities
+    CREATE_CUDA(cudaMemcpyAsync(s->staging, vertexData, sizeof(float) * 3 * (size_t)n,
+                                cudaMemcpyHostToDevice, s->stream));
+    launch_unpack_aos(s->staging, 3, 0, n, s->pos, s->stream);
+    s->sdMass.assign(n, 0.0f);
+    s->sdEnergy.assign(n, 0.0f);
+    if (simulationData) {
+        CREATE_CUDA(cudaStreamSynchronize(s->stream));
+        CREATE_CUDA(cudaMemcpyAsync(s->staging, simulationData, sizeof(float) * 10 * (size_t)n,
+                                    cudaMemcpyHostToDevice, s->stream));
+        launch_unpack_aos(s->staging, 10, 6, n, s->vel, s->stream);
+        for (int i = 0; i < n; i++) {
+            s->sdMass[i] = simulationData[(size_t)i * 10 + 0];
+            s->sdEnergy[i] = simulationData[(size_t)i * 10 + 9];
+        }
+    }
+    if (boundary) {
+        size_t total = (size_t)mdims[0] * mdims[1] * mdims[2];
+        CREATE_CUDA(dalloc(&s->map4, total));
+        CREATE_CUDA(dalloc(&s->mapDist, total));
+        launch_build_maps(*boundary, mdims, s->mapDist, nullptr, nullptr, s->map4, s->stream);
+        MapDev& m = s->map;
+        m.map4 = s->map4;
+        m.dist = s->mapDist;
+        for (int a = 0; a < 3; a++) {
+            m.origin[a] = boundary->gridStart[a];
+            m.dims[a] = (int)mdims[a];
+            m.dimsf[a] = (float)mdims[a];
+            m.length[a] = (float)(mdims[a] - 1) * boundary->gridSpacing;
+            m.du[a] = boundary->gridSpacing / m.length[a];
+        }
+        m.restDistance = boundary->restDistance;
+        m.present = 1;
+    }
+    CREATE_CUDA(cudaGetLastError());
+    CREATE_CUDA(cudaStreamSynchronize(s->stream));
+#undef CREATE_CUDA
+    *out = s;
+    return SPH_OK;
+}
+
+sph_status sph_destroy(sph_handle s) {
+    if (!s) return SPH_OK;
+    cudaStreamSynchronize(s->stream);
+    free_all(s);
+    delete s;
+    return SPH_OK;
+}
+
+sph_status sph_bind(sph_handle s, const SimulationParameters* params) {
+    if (!s) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "handle is NULL");
+    sph_status st = validate_params(params, &s->O);
+    if (st) return st;
+    if (params->numParticles != s->P.numParticles)
+        SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "numParticles cannot change after Init");
+    for (int a = 0; a < 3; a++)
+        if (params->gridDim[a] != s->P.gridDim[a] ||
+            params->gridDimSubParticles[a] != s->P.gridDimSubParticles[a])
+            SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "grid dimensions cannot change after Init");
+    s->P = *params;
+    s->graphValid = false;
+    return SPH_OK;
+}
+
+sph_status sph_set_stream(sph_handle s, void* stream) {
+    if (!s) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "handle is NULL");
+    SPH_CUDA(cudaStreamSynchronize(s->stream));
+    s->stream = stream ? (cudaStream_t)stream : s->ownStream;
+    s->graphValid = false;
+    return SPH_OK;
+}
+
+sph_status sph_step(sph_handle s, int mode) {
+    if (!s) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "handle is NULL");
+    if (mode != SPH_STEP_PLAIN)
+        SPH_FAIL(SPH_ERR_NOT_SUPPORTED, "step mode not available in this build");
+    enqueue_plain(s, s->timingCap > 0);
+    SPH_CUDA(cudaGetLastError());
+    s->numTimeSteps++;
+    s->stepped = true;
+    return SPH_OK;
+}
+
+sph_status sph_step_many(sph_handle s, int mode, int count) {
+    if (!s) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "handle is NULL");
+    if (mode != SPH_STEP_PLAIN)
+        SPH_FAIL(SPH_ERR_NOT_SUPPORTED, "step mode not available in this build");
+    if (count <= 0) return SPH_OK;
+    if (s->timingCap > 0) {
+        for (int i = 0; i < count; i++) {
+            sph_status st = sph_step(s, mode);
+            if (st) return st;
+        }
+        return SPH_OK;
+    }
+    if (!s->graphValid) {
+        if (s->graphExec) cudaGraphExecDestroy(s->graphExec);
+        if (s->graph) cudaGraphDestroy(s->graph);
+        s->graphExec = nullptr;
+        s->graph = nullptr;
+        SPH_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+        enqueue_plain(s, false);
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamEndCapture(s->stream, &g);
+        SPH_CUDA(e);
+        s->graph = g;
+        SPH_CUDA(cudaGraphInstantiate(&s->graphExec, s->graph, 0));
+        s->graphValid = true;
+    }
+    for (int i = 0; i < count; i++) SPH_CUDA(cudaGraphLaunch(s->graphExec, s->stream));
+    s->numTimeSteps += (unsigned int)count;
+    s->stepped = true;
+    return SPH_OK;
+}
+
+sph_status sph_synchronize(sph_handle s) {
+    if (!s) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "handle is NULL");
+    return latched_status(s);
+}
+
+sph_status sph_read(sph_handle s, int field, void* dst, size_t bytes) {
+    if (!s || !dst) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "NULL argument");
+    const int n = s->n;
+    size_t need = 0;
+    switch (field) {
+        case SPH_FIELD_VERTEX_DATA:
+        case SPH_FIELD_VELOCITY:
+        case SPH_FIELD_ACCELERATION: need = sizeof(float) * 3 * (size_t)n; break;
+        case SPH_FIELD_SIMULATION_DATA: need = sizeof(float) * 10 * (size_t)n; break;
+        case SPH_FIELD_DENSITY:
+        case SPH_FIELD_PRESSURE: need = sizeof(float) * (size_t)n; break;
+        case SPH_FIELD_STATE: need = (size_t)n; break;
+        default: SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "unknown field");
+    }
+    if (bytes < need) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "destination too small");
+    sph_status st = latched_status(s);
+    if (st) return st;
+    cudaStream_t q = s->stream;
+    switch (field) {
+        case SPH_FIELD_VERTEX_DATA: launch_pack_aos(s->pos, n, s->staging, 3, 0, q); break;
+        case SPH_FIELD_VELOCITY: launch_pack_aos(s->vel, n, s->staging, 3, 0, q); break;
+        case SPH_FIELD_ACCELERATION:
+            if (s->stepped) launch_unpermute(n, s->sb.sortedIds, s->accS, -1, s->staging, 3, 0, q);
+            else SPH_CUDA(cudaMemsetAsync(s->staging, 0, need, q));
+            break;
+        case SPH_FIELD_DENSITY:
+        case SPH_FIELD_PRESSURE:
+            if (s->stepped)
+                launch_unpermute(n, s->sb.sortedIds, s->rho4S, field == SPH_FIELD_DENSITY ? 0 : 1, s->staging,
+                                 1, 0, q);
+            else SPH_CUDA(cudaMemsetAsync(s->staging, 0, need, q));
+            break;
+        case SPH_FIELD_SIMULATION_DATA:
+            SPH_CUDA(cudaMemsetAsync(s->staging, 0, need, q));
+            if (s->stepped) {
+                launch_unpermute(n, s->sb.sortedIds, s->rho4S, 0, s->staging, 10, 1, q);
+                launch_unpermute(n, s->sb.sortedIds, s->rho4S, 1, s->staging, 10, 2, q);
+                launch_unpermute(n, s->sb.sortedIds, s->accS, -1, s->staging, 10, 3, q);
+            }
+            launch_pack_aos(s->vel, n, s->staging, 10, 6, q);
+            break;
+        case SPH_FIELD_STATE: SPH_CUDA(cudaMemsetAsync(s->staging, 0, need, q)); break;
+    }
+    SPH_CUDA(cudaGetLastError());
+    SPH_CUDA(cudaMemcpyAsync(dst, s->staging, need, cudaMemcpyDeviceToHost, q));
+    SPH_CUDA(cudaStreamSynchronize(q));
+    if (field == SPH_FIELD_SIMULATION_DATA) {
+        float* f = static_cast<float*>(dst);
+        for (int i = 0; i < n; i++) {
+            f[(size_t)i * 10 + 0] = s->sdMass[i];
+            f[(size_t)i * 10 + 9] = s->sdEnergy[i];
+        }
+    }
+    return SPH_OK;
+}
+
+sph_status sph_write(sph_handle s, int field, const void* src, size_t bytes) {
+    if (!s || !src) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "NULL argument");
+    const int n = s->n;
+    cudaStream_t q = s->stream;
+    switch (field) {
+        case SPH_FIELD_VERTEX_DATA:
+        case SPH_FIELD_VELOCITY:
+            if (bytes < sizeof(float) * 3 * (size_t)n) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "source too small");
+            SPH_CUDA(cudaMemcpyAsync(s->staging, src, sizeof(float) * 3 * (size_t)n, cudaMemcpyHostToDevice, q));
+            launch_unpack_aos(s->staging, 3, 0, n, field == SPH_FIELD_VERTEX_DATA ? s->pos : s->vel, q);
+            break;
+        case SPH_FIELD_SIMULATION_DATA:
+            if (bytes < sizeof(float) * 10 * (size_t)n) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "source too small");
+            SPH_CUDA(cudaMemcpyAsync(s->staging, src, sizeof(float) * 10 * (size_t)n, cudaMemcpyHostToDevice, q));
+            launch_unpack_aos(s->staging, 10, 6, n, s->vel, q);
+            for (int i = 0; i < n; i++) {
+                s->sdMass[i] = static_cast<const float*>(src)[(size_t)i * 10 + 0];
+                s->sdEnergy[i] = static_cast<const float*>(src)[(size_t)i * 10 + 9];
+            }
+            break;
+        default: SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "field is not writable");
+    }
+    SPH_CUDA(cudaGetLastError());
+    return SPH_OK;
+}
+
+sph_status sph_read_cells(sph_handle s, int level, int* sortedHash, int* sortedIds, int* cellStart,
+                          int* cellEnd) {
+    if (!s) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "handle is NULL");
+    if (level != 0) SPH_FAIL(SPH_ERR_NOT_SUPPORTED, "sub-particle level not available in this build");
+    if (!s->stepped) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "no step has run yet");
+    sph_status st = latched_status(s);
+    if (st) return st;
+    const int n = s->n;
+    const int C = s->P.gridDim[0] * s->P.gridDim[1] * s->P.gridDim[2];
+    cudaStream_t q = s->stream;
+    if (sortedHash)
+        SPH_CUDA(cudaMemcpyAsync(sortedHash, s->sb.sortedHash, sizeof(int) * n, cudaMemcpyDeviceToHost, q));
+    if (sortedIds)
+        SPH_CUDA(cudaMemcpyAsync(sortedIds, s->sb.sortedIds, sizeof(int) * n, cudaMemcpyDeviceToHost, q));
+    if (cellStart || cellEnd) {
+        // the per-cell counters are zero between steps: borrow them as the
+        // start/end staging area (2*C ints needed, C+1+tile available) in two rounds
+        int* tmp = s->sb.cnt;
+        if (cellStart) {
+            launch_cell_tables(C, s->sb.cellOffset, tmp, nullptr, q);
+            SPH_CUDA(cudaMemcpyAsync(cellStart, tmp, sizeof(int) * (size_t)C, cudaMemcpyDeviceToHost, q));
+        }
+        if (cellEnd) {
+            launch_cell_tables(C, s->sb.cellOffset, nullptr, tmp, q);
+            SPH_CUDA(cudaMemcpyAsync(cellEnd, tmp, sizeof(int) * (size_t)C, cudaMemcpyDeviceToHost, q));
+        }
+        SPH_CUDA(cudaMemsetAsync(tmp, 0, sizeof(int) * ((size_t)C + 1), q));
+    }
+    SPH_CUDA(cudaGetLastError());
+    SPH_CUDA(cudaStreamSynchronize(q));
+    return SPH_OK;
+}
+
+sph_status sph_get_counts(sph_handle s, sph_counts* out) {
+    if (!s || !out) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "NULL argument");
+    std::memset(out, 0, sizeof(*out));
+    out->numParticles = (unsigned int)s->n;
+    out->numParticlesDefault = (unsigned int)s->n;
+    out->numTimeSteps = s->numTimeSteps;
+    out->numCells = (unsigned int)(s->P.gridDim[0] * s->P.gridDim[1] * s->P.gridDim[2]);
+    out->numSubCells = (unsigned int)(s->P.gridDimSubParticles[0] * s->P.gridDimSubParticles[1] *
+                                      s->P.gridDimSubParticles[2]);
+    return SPH_OK;
+}
+
+sph_status sph_device_pointer(sph_handle s, int which, void** devicePtr) {
+    if (!s || !devicePtr) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (which == 0) *devicePtr = s->pos;
+    else if (which == 1) *devicePtr = s->vel;
+    else SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "unknown device field");
+    return SPH_OK;
+}
+
+sph_status sph_set_stage_timing(sph_handle s, int enable) {
+    if (!s) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "handle is NULL");
+    SPH_CUDA(cudaStreamSynchronize(s->stream));
+    for (cudaEvent_t e : s->events) cudaEventDestroy(e);
+    s->events.clear();
+    s->timingCap = s->timingNext = s->timingFilled = 0;
+    if (enable > 0) {
+        int cap = enable;
+        s->events.resize((size_t)cap * (ST_COUNT + 1));
+        for (auto& e : s->events) SPH_CUDA(cudaEventCreate(&e));
+        s->timingCap = cap;
+    }
+    return SPH_OK;
+}
+
+sph_status sph_stage_times(sph_handle s, float* ms, int* counts, int capacity, int* numStages) {
+    if (!s) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "handle is NULL");
+    if (numStages) *numStages = ST_COUNT;
+    if (!ms || capacity < ST_COUNT) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "capacity too small");
+    SPH_CUDA(cudaStreamSynchronize(s->stream));
+    for (int k = 0; k < ST_COUNT; k++) {
+        ms[k] = 0.0f;
+        if (counts) counts[k] = 0;
+    }
+    for (int slot = 0; slot < s->timingFilled; slot++) {
+        cudaEvent_t* ev = &s->events[(size_t)slot * (ST_COUNT + 1)];
+        for (int k = 0; k < ST_COUNT; k++) {
+            float t = 0.0f;
+            SPH_CUDA(cudaEventElapsedTime(&t, ev[k], ev[k + 1]));
+            ms[k] += t;
+            if (counts) counts[k]++;
+        }
+    }
+    s->timingNext = s->timingFilled = 0;
+    return SPH_OK;
+}
+
+}  // extern "C"

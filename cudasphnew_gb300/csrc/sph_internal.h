@@ -1,0 +1,101 @@
+// Internal declarations shared by the kernels (sph_kernels.cu) and the host
+// orchestration (sph_api.cu).  Not part of the public ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/sph.h"
+
+namespace sph {
+
+// Device-side status bits, latched per handle and mapped to sph_status.
+enum : unsigned int {
+    STATUS_OUT_OF_DOMAIN = 1u,
+    STATUS_DEVICE_WAIT = 2u,
+    STATUS_NON_FINITE = 4u,
+};
+
+// Uniform cell grid (gridOrigin/gridSpacing/gridDim of SimulationParameters).
+struct GridDev {
+    float origin[3];
+    float spacing;
+    int dim[3];
+    int numCells;
+};
+
+// Trilinear boundary maps: map4 = (signed distance, wall density, wall
+// viscosity, 0) per node, dist = signed distance alone (gradient samples).
+struct MapDev {
+    const float4* map4;
+    const float* dist;
+    float origin[3];
+    float length[3];   // (dims-1)*spacing, particle_simulation.cu:2628-2631
+    float dimsf[3];
+    int dims[3];
+    float du[3];       // spacing/length: the gradient step, :429-431
+    float restDistance;
+    int present;
+};
+
+// Per-level physical constants, pre-combined.
+struct PhysDev {
+    float h, h2;
+    float poly6m;      // poly6 * mass
+    float mass;
+    float stiffness, restDensity;
+    float pressCoef;   // -mass * gradSpiky (times rho_i per particle)
+    float viscCoef;    // mu * mass * laplVisc
+    float cgCoef;      // mass * gradPoly6
+    float clCoef;      // mass * laplPoly6
+    float tension, normThresh;
+    float dt;          // integration step of this level
+    float dtCollide;   // gSimParamsDev.timeStep (collision restitution term)
+    float gravity;
+    int gravityAxis;
+    float boxCen[3], boxDim[3], restitution;
+};
+
+// Scratch of the counting sort + cell scan.
+struct SortBuffers {
+    int* cnt;                 // [C+1] per-cell counters (kept zero between steps)
+    int* cellOffset;          // [C+1] exclusive scan of cnt: first sorted index of each cell
+    int2* keySlot;            // [n]   (hash, arrival slot in its cell)
+    int* tmpIds;              // [n]   ids scattered to their cell segment, unordered
+    int* sortedHash;          // [n]
+    int* sortedIds;           // [n]   the permutation
+    unsigned long long* scanFlags;  // decoupled look-back tile states
+    unsigned int* tileCounter;
+    int maxTiles;
+};
+
+constexpr int SCAN_THREADS = 256;
+constexpr int SCAN_ITEMS = 8;
+constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+
+// ---------------------------------------------------------------------------
+// Launch wrappers (sph_kernels.cu)
+// ---------------------------------------------------------------------------
+void launch_unpack_aos(const float* aos, int stride, int offset, int n, float4* out, cudaStream_t s);
+void launch_pack_aos(const float4* in, int n, float* aos, int stride, int offset, cudaStream_t s);
+void launch_hash_count(int n, const float4* pos, GridDev g, SortBuffers sb, unsigned int* status,
+                       cudaStream_t s);
+void launch_cell_scan(int numCells, SortBuffers sb, unsigned int* status, cudaStream_t s);
+void launch_scatter(int n, SortBuffers sb, cudaStream_t s);
+void launch_rank_gather(int n, SortBuffers sb, const float4* pos, const float4* vel, float4* posS,
+                        float4* velS, cudaStream_t s);
+void launch_density(int n, const float4* posS, const int* cellOffset, GridDev g, PhysDev ph,
+                    MapDev map, float4* rho4S, int kahan, int blockSize, cudaStream_t s);
+void launch_force(int n, const float4* posS, const float4* velS, const float4* rho4S,
+                  const int* sortedIds, const int* cellOffset, GridDev g, PhysDev ph, MapDev map,
+                  int collide, float4* pos, float4* vel, float4* accS, int kahan, int blockSize,
+                  cudaStream_t s);
+void launch_unpermute(int n, const int* sortedIds, const float4* srcS, int comp, float* dst,
+                      int stride, int offset, cudaStream_t s);
+void launch_cell_tables(int numCells, const int* cellOffset, int* start, int* end, cudaStream_t s);
+
+// Boundary maps.
+void launch_build_maps(const sph_boundary_desc& d, const unsigned int dims[3], float* dist,
+                       float* dens, float* visc, float4* map4, cudaStream_t s);
+
+}  // namespace sph

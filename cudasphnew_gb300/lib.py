@@ -1,0 +1,247 @@
+"""ctypes binding of libsph_gb300.so (include/sph.h) and a Python mirror of the
+reference's ``ParticleSimulation`` class (CUDASPHNEW/particle_simulation.h:113-324).
+
+There is no CPU fallback: if the shared library has not been built this module
+raises on first use.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from .params import BoundaryDesc, Options, SimulationParameters
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "_build", "libsph_gb300.so")
+
+SPH_STEP_PLAIN, SPH_STEP_TWO_SCALE, SPH_STEP_SUB_ONLY = 0, 1, 2
+(FIELD_VERTEX_DATA, FIELD_SIMULATION_DATA, FIELD_VELOCITY, FIELD_ACCELERATION,
+ FIELD_DENSITY, FIELD_PRESSURE, FIELD_STATE) = range(7)
+
+STATUS = {0: "SPH_OK", 1: "SPH_ERR_INVALID_ARGUMENT", 2: "SPH_ERR_CUDA",
+          3: "SPH_ERR_OUT_OF_MEMORY", 4: "SPH_ERR_OUT_OF_DOMAIN", 5: "SPH_ERR_DEVICE_WAIT",
+          6: "SPH_ERR_NOT_SUPPORTED", 7: "SPH_ERR_NON_FINITE"}
+
+# Every function include/sph.h declares, with its ctypes signature.
+_vp = ctypes.c_void_p
+_u = ctypes.c_uint
+_i = ctypes.c_int
+SIGNATURES = {
+    "sph_default_options": (None, [_vp]),
+    "sph_create": (_i, [_vp, _vp, _vp, _vp, _vp, _vp]),
+    "sph_destroy": (_i, [_vp]),
+    "sph_bind": (_i, [_vp, _vp]),
+    "sph_set_stream": (_i, [_vp, _vp]),
+    "sph_step": (_i, [_vp, _i]),
+    "sph_step_many": (_i, [_vp, _i, _i]),
+    "sph_synchronize": (_i, [_vp]),
+    "sph_read": (_i, [_vp, _i, _vp, ctypes.c_size_t]),
+    "sph_write": (_i, [_vp, _i, _vp, ctypes.c_size_t]),
+    "sph_read_cells": (_i, [_vp, _i, _vp, _vp, _vp, _vp]),
+    "sph_get_counts": (_i, [_vp, _vp]),
+    "sph_device_pointer": (_i, [_vp, _i, _vp]),
+    "sph_boundary_dims": (_i, [_vp, _vp]),
+    "sph_boundary_maps": (_i, [_vp, _vp, _vp, _vp]),
+    "sph_set_stage_timing": (_i, [_vp, _i]),
+    "sph_stage_times": (_i, [_vp, _vp, _vp, _i, _vp]),
+    "sph_stage_name": (ctypes.c_char_p, [_i]),
+    "sph_last_error": (ctypes.c_char_p, []),
+    "sph_status_string": (ctypes.c_char_p, [_i]),
+}
+
+
+class Counts(ctypes.Structure):
+    _fields_ = [(name, ctypes.c_uint) for name in (
+        "numParticles", "numParticlesDefault", "numParticlesSplit", "numParticlesBoundary",
+        "numSubParticles", "numTimeSteps", "numCells", "numSubCells")]
+
+
+class SphError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS.get(status, status)}: {message}")
+        self.status = status
+
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Loads the shared library; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(path):
+            raise RuntimeError(
+                f"{path} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+        L = ctypes.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(status: int) -> None:
+    if status != 0:
+        raise SphError(status, load().sph_last_error().decode(errors="replace"))
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def boundary_maps(desc: BoundaryDesc):
+    """Boundary maps built on the GPU: (distance, density, viscosity) as
+    (nz, ny, nx) float32 arrays."""
+    L = load()
+    dims = np.zeros(3, np.uint32)
+    check(L.sph_boundary_dims(ctypes.byref(desc), _p(dims)))
+    shape = (int(dims[2]), int(dims[1]), int(dims[0]))
+    out = [np.zeros(shape, np.float32) for _ in range(3)]
+    check(L.sph_boundary_maps(ctypes.byref(desc), *[_p(a) for a in out]))
+    return tuple(out)
+
+
+class ParticleSimulation:
+    """Headless ``ParticleSimulation``: Init + Bind happen in the constructor
+    (sph_create); the OpenGL buffer getters are replaced by device pointers
+    and host reads."""
+
+    def __init__(self, params: SimulationParameters, positions: np.ndarray,
+                 velocities: np.ndarray | None = None, options: Options | None = None,
+                 boundary: BoundaryDesc | None = None, simulation_data: np.ndarray | None = None):
+        L = load()
+        n = int(params.numParticles)
+        vd = np.ascontiguousarray(positions, np.float32).reshape(n, 3)
+        if simulation_data is None and velocities is not None:
+            simulation_data = np.zeros((n, 10), np.float32)
+            simulation_data[:, 6:9] = np.asarray(velocities, np.float32).reshape(n, 3)
+        sd = None if simulation_data is None else np.ascontiguousarray(simulation_data, np.float32)
+        self._params = params
+        self.options = options if options is not None else Options()
+        if options is None:
+            L.sph_default_options(ctypes.byref(self.options))
+        self.n = n
+        h = ctypes.c_void_p()
+        check(L.sph_create(ctypes.byref(params), ctypes.byref(self.options), _p(vd),
+                           None if sd is None else _p(sd),
+                           None if boundary is None else ctypes.byref(boundary), ctypes.byref(h)))
+        self._h = h
+
+    # -- lifetime ----------------------------------------------------------
+    def close(self) -> None:
+        if getattr(self, "_h", None) and self._h.value:
+            load().sph_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- reference API -------------------------------------------------------
+    def Bind(self, params: SimulationParameters | None = None) -> None:
+        if params is not None:
+            self._params = params
+        check(load().sph_bind(self._h, ctypes.byref(self._params)))
+
+    def Advance(self) -> None:
+        check(load().sph_step(self._h, SPH_STEP_PLAIN))
+
+    def AdvanceTwoScale(self) -> None:
+        check(load().sph_step(self._h, SPH_STEP_TWO_SCALE))
+
+    def AdvanceSubParticles(self) -> None:
+        check(load().sph_step(self._h, SPH_STEP_SUB_ONLY))
+
+    def GetNumParticles(self) -> int:
+        return self.counts().numParticles
+
+    def GetNumTimesSteps(self) -> int:
+        return self.counts().numTimeSteps
+
+    def GetParticleRadius(self) -> float:
+        """(3V/(4 pi N))^(1/3) (particle_simulation.cu:2227-2231)."""
+        p = self._params
+        return float(np.float32((3.0 * p.fluidVolume) / (4.0 * np.pi * p.numParticles)) ** np.float32(1.0 / 3.0))
+
+    def GetSubParticleRadius(self) -> float:
+        return 0.5 * self.GetParticleRadius()
+
+    # -- extended API --------------------------------------------------------
+    def step(self, mode: int = SPH_STEP_PLAIN, count: int = 1) -> None:
+        L = load()
+        if count == 1:
+            check(L.sph_step(self._h, mode))
+        else:
+            check(L.sph_step_many(self._h, mode, count))
+
+    def synchronize(self) -> None:
+        check(load().sph_synchronize(self._h))
+
+    def counts(self) -> Counts:
+        c = Counts()
+        check(load().sph_get_counts(self._h, ctypes.byref(c)))
+        return c
+
+    def read(self, field: int) -> np.ndarray:
+        n = self.n
+        shapes = {FIELD_VERTEX_DATA: ((n, 3), np.float32), FIELD_VELOCITY: ((n, 3), np.float32),
+                  FIELD_ACCELERATION: ((n, 3), np.float32), FIELD_SIMULATION_DATA: ((n, 10), np.float32),
+                  FIELD_DENSITY: ((n,), np.float32), FIELD_PRESSURE: ((n,), np.float32),
+                  FIELD_STATE: ((n,), np.int8)}
+        shape, dt = shapes[field]
+        out = np.zeros(shape, dt)
+        check(load().sph_read(self._h, field, _p(out), out.nbytes))
+        return out
+
+    def write(self, field: int, data: np.ndarray) -> None:
+        a = np.ascontiguousarray(data, np.float32)
+        check(load().sph_write(self._h, field, _p(a), a.nbytes))
+
+    def positions(self) -> np.ndarray:
+        return self.read(FIELD_VERTEX_DATA)
+
+    def velocities(self) -> np.ndarray:
+        return self.read(FIELD_VELOCITY)
+
+    def cells(self, level: int = 0):
+        """(sorted hash, sorted ids, cell start, cell end) of the last step."""
+        n = self.n if level == 0 else None
+        c = self.counts()
+        C = c.numCells if level == 0 else c.numSubCells
+        h = np.zeros(n, np.int32)
+        ids = np.zeros(n, np.int32)
+        s = np.zeros(C, np.int32)
+        e = np.zeros(C, np.int32)
+        check(load().sph_read_cells(self._h, level, _p(h), _p(ids), _p(s), _p(e)))
+        return h, ids, s, e
+
+    def device_pointer(self, which: int) -> int:
+        p = ctypes.c_void_p()
+        check(load().sph_device_pointer(self._h, which, ctypes.byref(p)))
+        return int(p.value or 0)
+
+    def set_stream(self, stream_handle: int | None) -> None:
+        check(load().sph_set_stream(self._h, ctypes.c_void_p(stream_handle or 0)))
+
+    def set_stage_timing(self, capacity_steps: int) -> None:
+        check(load().sph_set_stage_timing(self._h, int(capacity_steps)))
+
+    def stage_times(self):
+        """{stage name: (total ms, launches)} since the last call."""
+        L = load()
+        ms = np.zeros(32, np.float32)
+        cnt = np.zeros(32, np.int32)
+        k = ctypes.c_int()
+        check(L.sph_stage_times(self._h, _p(ms), _p(cnt), 32, ctypes.byref(k)))
+        return {L.sph_stage_name(i).decode(): (float(ms[i]), int(cnt[i])) for i in range(k.value)}

@@ -1,0 +1,238 @@
+/*
+ * sph.h -- C ABI of the GB300 SPH step (libsph_gb300.so).
+ *
+ * This is the thin C layer under the drop-in C++ class `ParticleSimulation`
+ * (include/particle_simulation.h), which keeps the public interface of
+ * CUDASPHNEW/particle_simulation.h.  Each entry point names the reference
+ * interface it replaces.  All pointers are plain host pointers unless a name
+ * says "device"; sizes are element counts unless a name says "bytes".
+ *
+ * Threading: one handle is not thread-safe (as the reference's object is not);
+ * distinct handles are independent (parameters live per handle, not in one
+ * global __constant__ symbol as at particle_simulation.cu:26).
+ *
+ * Asynchrony: sph_step() only enqueues work on the handle's stream.  Device-side
+ * errors (a particle hashed outside the cell grid, a bounded device wait that
+ * gave up) are latched in a device status word and reported by the next
+ * sph_synchronize() or sph_read*() call on that handle.
+ */
+#ifndef SPH_GB300_H
+#define SPH_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPH_ABI_VERSION 1
+
+/* Byte-identical to the reference's struct (particle_simulation.h:54-111). */
+#ifndef SPH_SIMULATION_PARAMETERS_DEFINED
+#define SPH_SIMULATION_PARAMETERS_DEFINED
+struct SimulationParameters {
+    float gridOrigin[3];
+    float gridSpacing;
+    int gridDim[3];
+    float gridSpacingSubParticles;
+    int gridDimSubParticles[3];
+    unsigned int numParticles;
+    float compactSupport;
+    float compactSupportSub;
+    int kernelParticles;
+    float timeStep;
+    float timeStepSubParticles;
+    float particleMass;
+    float subParticleMass;
+    float gasStiffness;
+    float restDensity;
+    float dynamicViscosity;
+    float gravity;
+    float tensionCoefficient;
+    float normThresh;
+    float fluidVolume;
+    float poly6;
+    float gradPoly6;
+    float laplPoly6;
+    float gradSpiky;
+    float laplVisc;
+    float poly6Sub;
+    float gradPoly6Sub;
+    float laplPoly6Sub;
+    float gradSpikySub;
+    float laplViscSub;
+    float cmDistanceThresh;
+    float nPartTresh;
+    float boxDim[3];
+    float boxCen[3];
+    float restitution;
+};
+#endif
+typedef struct SimulationParameters SimulationParameters;
+
+/* Behaviour the reference hard-codes.  sph_default_options() gives the
+ * reference's values. */
+typedef struct sph_options {
+    int gravityAxis;    /* axis the gravity acts along (negative direction);
+                           reference: 1, particle_simulation.cu:471 */
+    int boxCollision;   /* 1: collision_handling after integrate in every
+                           step (AdvanceTwoScale, :2170); 0: Advance (:2106) */
+    int reserved0;
+    int reserved1;
+    float splitMin[3];  /* two-scale split region; reference: 0.2 <= x <= 0.5 */
+    float splitMax[3];  /* (find_split_particles, :948) */
+} sph_options;
+
+/* Boundary solids ("SPH in complex shapes", SphInComplexShapes.h:18-93). */
+enum {
+    SPH_SHAPE_SPHERE = 1, /* p = (cx, cy, cz, r): solid sphere */
+    SPH_SHAPE_CONE = 2,   /* p = (bx, by, bz, R, H): solid cone on its base, axis +z */
+    SPH_SHAPE_BOX = 3     /* p = (cx, cy, cz, ex, ey, ez): container, fluid inside
+                             (SetBox, SphInComplexShapes.cpp:203-313) */
+};
+
+typedef struct sph_shape {
+    int kind;
+    float p[7];
+} sph_shape;
+
+/* The arguments of SphInComplexShapes' constructor (SphInComplexShapes.h:21-23)
+ * plus the solids.  The maps (signed distance, wall density, wall viscosity)
+ * are built on the GPU at sph_create and read trilinearly during the step. */
+typedef struct sph_boundary_desc {
+    float gridStart[3];
+    float gridEnd[3];
+    float gridSpacing;
+    float restDistance;
+    float compactSupport;
+    float particleMass;
+    float restDensity;
+    float viscosity;
+    float particleSpacing;
+    int numShapes;
+    sph_shape shapes[8];
+} sph_boundary_desc;
+
+typedef enum sph_status {
+    SPH_OK = 0,
+    SPH_ERR_INVALID_ARGUMENT = 1,
+    SPH_ERR_CUDA = 2,
+    SPH_ERR_OUT_OF_MEMORY = 3,
+    SPH_ERR_OUT_OF_DOMAIN = 4, /* a particle hashed outside the cell grid */
+    SPH_ERR_DEVICE_WAIT = 5,   /* a bounded device-side wait gave up */
+    SPH_ERR_NOT_SUPPORTED = 6,
+    SPH_ERR_NON_FINITE = 7     /* a NaN/inf position entered the step */
+} sph_status;
+
+typedef enum sph_step_mode {
+    SPH_STEP_PLAIN = 0,     /* Advance (particle_simulation.cu:2085-2117) */
+    SPH_STEP_TWO_SCALE = 1, /* AdvanceTwoScale (:2145-2182) */
+    SPH_STEP_SUB_ONLY = 2   /* AdvanceSubParticles (:2119-2143) */
+} sph_step_mode;
+
+/* Per-particle fields, returned in particle-index order. */
+typedef enum sph_field {
+    SPH_FIELD_VERTEX_DATA = 0,     /* float[n*3]  VD layout (particle_simulation.h:17-23) */
+    SPH_FIELD_SIMULATION_DATA = 1, /* float[n*10] SD layout (particle_simulation.h:28-41) */
+    SPH_FIELD_VELOCITY = 2,        /* float[n*3] */
+    SPH_FIELD_ACCELERATION = 3,    /* float[n*3] */
+    SPH_FIELD_DENSITY = 4,         /* float[n] */
+    SPH_FIELD_PRESSURE = 5,        /* float[n] */
+    SPH_FIELD_STATE = 6            /* char[n] (GetParticleState) */
+} sph_field;
+
+typedef struct sph_counts {
+    unsigned int numParticles;
+    unsigned int numParticlesDefault;  /* GetNumParticlesDefault */
+    unsigned int numParticlesSplit;
+    unsigned int numParticlesBoundary;
+    unsigned int numSubParticles;      /* GetNumSubParticles */
+    unsigned int numTimeSteps;         /* GetNumTimesSteps */
+    unsigned int numCells;
+    unsigned int numSubCells;
+} sph_counts;
+
+typedef struct sph_sim* sph_handle;
+
+/* Reference defaults for sph_options. */
+void sph_default_options(sph_options* opts);
+
+/* Init (particle_simulation.cu:1882-2005) + Bind (:2078-2083): allocates all
+ * device memory, uploads the initial vertex data (float[n*3]) and optionally
+ * the simulation data (float[n*10], velocities taken from SD_VEL0_*; NULL means
+ * zero), and builds the boundary maps when `boundary` is not NULL
+ * (setUpSphInComplexShapes, :2592-2683).  n = params->numParticles.
+ * `opts` NULL means sph_default_options(). */
+sph_status sph_create(const SimulationParameters* params, const sph_options* opts,
+                      const float* vertexData, const float* simulationData,
+                      const sph_boundary_desc* boundary, sph_handle* out);
+
+/* ~ParticleSimulation (:1691-1743). */
+sph_status sph_destroy(sph_handle h);
+
+/* Bind (:2078-2083) with new parameters (SetNPartThresh etc. re-Bind,
+ * :2255-2276).  numParticles and the grid dimensions must not change. */
+sph_status sph_bind(sph_handle h, const SimulationParameters* params);
+
+/* Runs later work of this handle on `stream` (a cudaStream_t; NULL restores
+ * the handle's own stream). */
+sph_status sph_set_stream(sph_handle h, void* stream);
+
+/* Advance / AdvanceTwoScale / AdvanceSubParticles: enqueues one step. */
+sph_status sph_step(sph_handle h, int mode);
+
+/* Enqueues `count` plain steps (one CUDA-graph launch each once captured). */
+sph_status sph_step_many(sph_handle h, int mode, int count);
+
+/* Waits for the handle's stream; returns the latched device status. */
+sph_status sph_synchronize(sph_handle h);
+
+/* Copies a field to host memory (GetParticleState, SaveParticleInfo,
+ * :2238-2243, :2785-2852).  `bytes` must be at least the field's size. */
+sph_status sph_read(sph_handle h, int field, void* dst, size_t bytes);
+
+/* Overwrites a field from host memory (SPH_FIELD_VERTEX_DATA,
+ * SPH_FIELD_VELOCITY or SPH_FIELD_SIMULATION_DATA). */
+sph_status sph_write(sph_handle h, int field, const void* src, size_t bytes);
+
+/* The neighbour-search tables of the last step (SaveInfoTable, :2709-2783):
+ * sorted hashes, sorted particle ids (the sort permutation), and the
+ * cell start/end lists with 0xFFFFFFFF for empty cells.  level 0 is the
+ * particle grid, level 1 the sub-particle grid.  Any pointer may be NULL. */
+sph_status sph_read_cells(sph_handle h, int level, int* sortedHash, int* sortedIds,
+                          int* cellStart, int* cellEnd);
+
+/* Particle counts (GetNumParticles*, GetNumSubParticles*, GetNumTimesSteps). */
+sph_status sph_get_counts(sph_handle h, sph_counts* out);
+
+/* Device pointer of a field in the handle's layout, for zero-copy consumers
+ * (replaces the OpenGL VBO getters, :2278-2301): 0 = positions (float4[n],
+ * particle order), 1 = velocities (float4[n]). */
+sph_status sph_device_pointer(sph_handle h, int which, void** devicePtr);
+
+/* The boundary maps of `desc`, built on the GPU, copied to host grids of
+ * dims[0]*dims[1]*dims[2] floats each, x fastest (CreateDistanceTextureData
+ * etc., SphInComplexShapes.cpp:366-427).  Any output may be NULL. */
+sph_status sph_boundary_dims(const sph_boundary_desc* desc, unsigned int dims[3]);
+sph_status sph_boundary_maps(const sph_boundary_desc* desc, float* distance,
+                             float* density, float* viscosity);
+
+/* Stage timing with CUDA events on the handle's stream (CudaTimer,
+ * util.cpp:6-41, generalised to every stage).  After enabling, each step
+ * records events between its stages; sph_stage_times() returns the summed
+ * milliseconds per stage since the last call and resets them. */
+sph_status sph_set_stage_timing(sph_handle h, int enable);
+sph_status sph_stage_times(sph_handle h, float* ms, int* counts, int capacity, int* numStages);
+const char* sph_stage_name(int stage);
+
+/* Human-readable message of the last failing call on this thread, in the
+ * reference's "Exception thrown in FILE: ... LINE: ..." shape (util.h:24-39). */
+const char* sph_last_error(void);
+const char* sph_status_string(sph_status s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPH_GB300_H */

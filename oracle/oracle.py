@@ -1,0 +1,183 @@
+"""ctypes binding of the CPU oracle (oracle/sph_oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+CPU legs of bench.py, never by the cudasphnew_gb300 package.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+from cudasphnew_gb300.params import BoundaryDesc, Options, SimulationParameters
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libsph_oracle.so")
+
+
+def build() -> str:
+    subprocess.run(["sh", os.path.join(HERE, "build_oracle.sh")], check=True)
+    return LIB_PATH
+
+
+class Maps(ctypes.Structure):
+    _fields_ = [
+        ("origin", ctypes.c_float * 3),
+        ("spacing", ctypes.c_float),
+        ("dims", ctypes.c_uint * 3),
+        ("restDistance", ctypes.c_float),
+        ("dist", ctypes.c_void_p),
+        ("dens", ctypes.c_void_p),
+        ("visc", ctypes.c_void_p),
+    ]
+
+
+_P = ctypes.POINTER
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = ctypes.CDLL(LIB_PATH)
+        vp = ctypes.c_void_p
+        L.orc_set_threads.argtypes = [ctypes.c_int]
+        L.orc_max_threads.restype = ctypes.c_int
+        L.orc_hash.argtypes = [_P(SimulationParameters), vp, ctypes.c_int, vp, vp]
+        L.orc_hash.restype = ctypes.c_int
+        L.orc_sort.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int]
+        L.orc_sort.restype = ctypes.c_int
+        L.orc_cells.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp, vp]
+        L.orc_step_plain_f32.argtypes = [_P(SimulationParameters), _P(Options), _P(Maps),
+                                         ctypes.c_int] + [vp] * 9
+        L.orc_step_plain_f32.restype = ctypes.c_int
+        L.orc_step_plain_f64.argtypes = [_P(SimulationParameters), _P(Options), _P(Maps),
+                                         ctypes.c_int] + [vp] * 11
+        L.orc_step_plain_f64.restype = ctypes.c_int
+        L.orc_tex3d.argtypes = [_P(Maps), ctypes.c_int, vp, ctypes.c_int, vp]
+        L.orc_boundary_dims.argtypes = [_P(BoundaryDesc), vp]
+        L.orc_boundary_maps.argtypes = [_P(BoundaryDesc), vp, vp, vp]
+        L.orc_boundary_maps.restype = ctypes.c_int
+        _lib = L
+    return _lib
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def set_threads(n: int) -> None:
+    lib().orc_set_threads(int(n))
+
+
+def max_threads() -> int:
+    return int(lib().orc_max_threads())
+
+
+class BoundaryMaps:
+    """Dense x-fastest grids (distance, density, viscosity) + texture metadata."""
+
+    def __init__(self, desc: BoundaryDesc, dist, dens, visc):
+        self.desc = desc
+        self.dims = tuple(int(d) for d in dist.shape[::-1])
+        self.dist, self.dens, self.visc = dist, dens, visc
+        m = Maps()
+        for a in range(3):
+            m.origin[a] = desc.gridStart[a]
+            m.dims[a] = self.dims[a]
+        m.spacing = desc.gridSpacing
+        m.restDistance = desc.restDistance
+        m.dist = self.dist.ctypes.data
+        m.dens = self.dens.ctypes.data
+        m.visc = self.visc.ctypes.data
+        self.maps = m
+
+
+def boundary_maps(desc: BoundaryDesc) -> BoundaryMaps:
+    dims = np.zeros(3, np.uint32)
+    lib().orc_boundary_dims(ctypes.byref(desc), _ptr(dims))
+    shape = (int(dims[2]), int(dims[1]), int(dims[0]))
+    dist = np.zeros(shape, np.float32)
+    dens = np.zeros(shape, np.float32)
+    visc = np.zeros(shape, np.float32)
+    rc = lib().orc_boundary_maps(ctypes.byref(desc), _ptr(dist), _ptr(dens), _ptr(visc))
+    assert rc == 0
+    return BoundaryMaps(desc, dist, dens, visc)
+
+
+def tex3d(bm: BoundaryMaps, which: int, xyz: np.ndarray) -> np.ndarray:
+    xyz = np.ascontiguousarray(xyz, np.float64)
+    out = np.zeros(len(xyz), np.float64)
+    lib().orc_tex3d(ctypes.byref(bm.maps), which, _ptr(xyz), len(xyz), _ptr(out))
+    return out
+
+
+def hash_sort_cells(p: SimulationParameters, pos: np.ndarray):
+    """compute_particle_hash + sort_by_key + compute_cell_start_end (FP32)."""
+    n = len(pos)
+    pos = np.ascontiguousarray(pos, np.float32)
+    h = np.zeros(n, np.int32)
+    ids = np.zeros(n, np.int32)
+    bad = lib().orc_hash(ctypes.byref(p), _ptr(pos), n, _ptr(h), _ptr(ids))
+    if bad:
+        raise ValueError(f"{bad} particles outside the hash range")
+    C = p.num_cells
+    if lib().orc_sort(_ptr(h), _ptr(ids), n, C):
+        raise ValueError("hash outside [0, numCells)")
+    start = np.zeros(C, np.int32)
+    end = np.zeros(C, np.int32)
+    lib().orc_cells(_ptr(h), n, C, _ptr(start), _ptr(end))
+    return h, ids, start, end
+
+
+def step_plain(p: SimulationParameters, o: Options, bm: BoundaryMaps | None,
+               pos: np.ndarray, vel: np.ndarray, fp64: bool = False):
+    """One plain step.  Returns a dict with the step's outputs; ``pos``/``vel``
+    in the dict are the updated state (inputs are not modified)."""
+    n = len(pos)
+    dt = np.float64 if fp64 else np.float32
+    pos = np.array(pos, dt, order="C", copy=True)
+    vel = np.array(vel, dt, order="C", copy=True)
+    rho = np.zeros(n, dt)
+    prs = np.zeros(n, dt)
+    acc = np.zeros((n, 3), dt)
+    C = p.num_cells
+    h = np.zeros(n, np.int32)
+    ids = np.zeros(n, np.int32)
+    start = np.zeros(C, np.int32)
+    end = np.zeros(C, np.int32)
+    mp = ctypes.byref(bm.maps) if bm is not None else None
+    out = dict(pos=pos, vel=vel, rho=rho, p=prs, acc=acc, hash=h, ids=ids, start=start, end=end)
+    if fp64:
+        srho = np.zeros(n, np.float64)
+        sacc = np.zeros(n, np.float64)
+        rc = lib().orc_step_plain_f64(ctypes.byref(p), ctypes.byref(o), mp, n, _ptr(pos), _ptr(vel),
+                                      _ptr(rho), _ptr(prs), _ptr(acc), _ptr(srho), _ptr(sacc),
+                                      _ptr(h), _ptr(ids), _ptr(start), _ptr(end))
+        out.update(scale_rho=srho, scale_acc=sacc)
+    else:
+        rc = lib().orc_step_plain_f32(ctypes.byref(p), ctypes.byref(o), mp, n, _ptr(pos), _ptr(vel),
+                                      _ptr(rho), _ptr(prs), _ptr(acc), _ptr(h), _ptr(ids),
+                                      _ptr(start), _ptr(end))
+    if rc:
+        raise ValueError(f"oracle step failed ({rc})")
+    return out
+
+
+def jet_slice(values: np.ndarray, scale: float) -> np.ndarray:
+    """PortablePixmap::setJET over a (W, H) slice (portable_pixmap.cpp:49-62),
+    returned as the P3 file's value order (rows top to bottom, RGB)."""
+    s = (values.astype(np.float32) / np.float32(scale)).astype(np.float32)
+    t = (s * np.float32(4.0)).astype(np.float32)
+    r = np.minimum(t - np.float32(1.5), -t + np.float32(4.5))
+    g = np.minimum(t - np.float32(0.5), -t + np.float32(3.5))
+    b = np.minimum(t + np.float32(0.5), -t + np.float32(2.5))
+    rgb = [np.clip(c, 0.0, 1.0).astype(np.float32) for c in (r, g, b)]
+    px = [np.floor(np.float32(255.0) * c).astype(np.int64) for c in rgb]
+    img = np.stack(px, axis=-1)          # (W, H, 3) indexed [i, j]
+    img = img[:, ::-1, :]                # set() stores row H-j-1
+    return np.transpose(img, (1, 0, 2))  # (H, W, 3) row-major like the file
