@@ -1,0 +1,338 @@
+"""Benchmark of the GB300 SPH step (one JSON line on rank 0).
+
+Workload: the SDF-obstacle dam break, 1,048,576 particles (128x128x64 block),
+h = 0.025, in a [0,4]x[0,4]x[0,1] tank with a sphere + cone obstacle on a 128^3
+boundary map.  A "step" is one plain SPH step of that scene (hash, sort, cell
+table, density, forces + wall terms + integration + box collision).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference algorithm on the host cores (the oracle's
+FP32 restatement: the reference itself does not build here) on the same scene.
+Multi-GPU runs are independent replicas (one scene per GPU, no exchange).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s @1M: plain vs learned-4×dt at ≤1% density err; HBM GB/s"
+UNIT = "particle-steps/s"
+L2_BYTES = 129 * 1024 * 1024
+
+# Algorithmic bytes per particle of the force kernel (k_force): reads sorted
+# position, velocity, (rho, p, p/rho^2, 1/rho) float4s and the sorted id
+# (16+16+16+4), writes position, velocity and acceleration float4s (3*16).
+FORCE_BYTES_PER_PARTICLE = 100
+# Per launch it also reads the (C+1)-entry cell-offset table once (4 B/cell).
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=500)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="config2")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_setup(n_gpus):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist  # noqa: F811
+        dist.init_process_group("gloo")
+    return rank, world, local, dist
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            pk = json.load(f)
+        return float(pk["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.samples = []
+        self.proc = None
+        self.gpu = gpu_index
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.samples.append((time.time(), parts))
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self, t0, t1):
+        inside = [s for t, s in self.samples if t0 <= t <= t1]
+        window = "timed_region"
+        if len(inside) < 2:
+            inside = [s for _, s in self.samples]
+            window = "warmup_and_timed_region"
+        if not inside:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"],
+                    "samples": 0}
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [num(s[1]) for s in inside if num(s[1]) is not None]
+        mx = [num(s[2]) for s in inside if num(s[2]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in inside for k in range(4) if s[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(inside), "window": window}
+
+
+def make_scene(name):
+    from cudasphnew_gb300 import scenes
+    return getattr(scenes, name)()
+
+
+def working_set_bytes(sc):
+    n = sc.n
+    C = sc.params.num_cells
+    maps = 0
+    if sc.boundary is not None:
+        d = sc.boundary.dims()
+        maps = d[0] * d[1] * d[2] * 20
+    return n * (16 * 6 + 8 + 4 * 3) + 8 * (C + 1) + maps
+
+
+def cpu_baseline(sc, max_seconds=20.0):
+    """The oracle's FP32 restatement of the reference step on all host cores,
+    on a bounded number of full steps of the same scene."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle  # the reference algorithm restated for the CPU
+    if not os.path.exists(oracle.LIB_PATH):
+        oracle.build()
+    cores = os.cpu_count() or 1
+    oracle.set_threads(cores)
+    bm = oracle.boundary_maps(sc.boundary) if sc.boundary is not None else None
+    x, v = sc.positions, sc.velocities
+    r = oracle.step_plain(sc.params, sc.options, bm, x, v)  # warm-up step
+    x, v = r["pos"], r["vel"]
+    steps, t0 = 0, time.perf_counter()
+    while True:
+        r = oracle.step_plain(sc.params, sc.options, bm, x, v)
+        x, v = r["pos"], r["vel"]
+        steps += 1
+        el = time.perf_counter() - t0
+        if el > max_seconds or steps >= 50:
+            break
+    return {"value": sc.n * steps / el, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{steps} full steps of the {sc.n}-particle scene after 1 warm-up step "
+                      f"({el:.1f} s, FP32 restatement of the reference, OpenMP over particles)"}
+
+
+def run_reference(args):
+    rank, world, local, dist = dist_setup(args.gpus)
+    if rank != 0:
+        return
+    sc = make_scene(args.config)
+    # each step is one full CPU step of the workload; the run is kept to a few
+    # minutes by bounding the number of steps actually timed
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    if not os.path.exists(oracle.LIB_PATH):
+        oracle.build()
+    cores = os.cpu_count() or 1
+    oracle.set_threads(cores)
+    bm = oracle.boundary_maps(sc.boundary) if sc.boundary is not None else None
+    x, v = sc.positions, sc.velocities
+    for _ in range(min(args.warmup, 2)):
+        r = oracle.step_plain(sc.params, sc.options, bm, x, v)
+        x, v = r["pos"], r["vel"]
+    steps, t0 = 0, time.perf_counter()
+    while steps < args.steps:
+        r = oracle.step_plain(sc.params, sc.options, bm, x, v)
+        x, v = r["pos"], r["vel"]
+        steps += 1
+        if time.perf_counter() - t0 > 120.0:
+            break
+    el = time.perf_counter() - t0
+    val = sc.n * steps / el
+    out = {"metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus, "steps": steps,
+           "warmup": min(args.warmup, 2), "ms_per_step": el / steps * 1e3, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "impl": "reference",
+           "config": {"workload": sc.name, "particles": sc.n, "cells": sc.params.num_cells,
+                      "parallelism": "replicas"},
+           "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores, "kind": "port",
+                            "sample": f"{steps} of {args.steps} requested full steps "
+                                      f"(bounded to ~2 min), FP32 restatement of the reference "
+                                      f"(the reference itself does not build: Windows/GL headers, "
+                                      f"removed CUDA texture references)"},
+           "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    rank, world, local, dist = dist_setup(args.gpus)
+    torch.cuda.set_device(local)
+    from cudasphnew_gb300 import _build, lib
+    _build.build()
+    lib.load()
+    sc = make_scene(args.config)
+    n = sc.n
+    stream = torch.cuda.Stream()
+    sim = lib.ParticleSimulation(sc.params, sc.positions, sc.velocities, sc.options, sc.boundary)
+    sim.set_stream(stream.cuda_stream)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    def max_over_ranks(x):
+        if dist is None:
+            return x
+        t = torch.tensor([x], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    # ---- warm-up (also captures the step graph) ---------------------------
+    clocks = ClockSampler(local)
+    clocks.start()
+    sim.step(count=max(args.warmup, 3))
+    sim.synchronize()
+
+    # ---- timed region: K graph-launched steps, device-resident ----------
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    barrier()
+    torch.cuda.synchronize()
+    t_wall0 = time.time()
+    with torch.cuda.stream(stream):
+        e0.record()
+        sim.step(count=args.steps)
+        e1.record()
+    torch.cuda.synchronize()
+    t_wall1 = time.time()
+    barrier()
+    sim.synchronize()  # raises on a latched device error
+    ms = max_over_ranks(e0.elapsed_time(e1))
+    clocks.stop()
+    clk = clocks.summary(t_wall0, t_wall1)
+    value = world * n * args.steps / (ms / 1e3)
+
+    # ---- per-kernel times (stage events on the same stream) ---------------
+    kt = min(args.steps, 200)
+    sim.set_stage_timing(kt)
+    for _ in range(kt):
+        sim.Advance()
+    stages = sim.stage_times()
+    sim.set_stage_timing(0)
+    force_ms, force_cnt = stages["force_integrate"]
+    force_avg_s = force_ms / force_cnt / 1e3
+    peak, peak_kind = load_peaks()
+    C = sc.params.num_cells
+    alg = n * FORCE_BYTES_PER_PARTICLE + 4 * (C + 1)
+    achieved = alg / force_avg_s / 1e9
+
+    # ---- e2e: host buffers through the C ABI, copies inside the region ----
+    pin_pos = torch.empty((n, 3), dtype=torch.float32, pin_memory=True)
+    pin_vel = torch.empty((n, 3), dtype=torch.float32, pin_memory=True)
+    pin_out = torch.empty((n, 3), dtype=torch.float32, pin_memory=True)
+    pin_pos.numpy()[:] = sim.positions()
+    pin_vel.numpy()[:] = sim.velocities()
+    L = lib.load()
+    import ctypes
+    e2e_steps = max(1, min(args.steps, 100))
+    torch.cuda.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        lib.check(L.sph_write(sim._h, lib.FIELD_VERTEX_DATA, ctypes.c_void_p(pin_pos.data_ptr()), n * 12))
+        lib.check(L.sph_write(sim._h, lib.FIELD_VELOCITY, ctypes.c_void_p(pin_vel.data_ptr()), n * 12))
+        lib.check(L.sph_step(sim._h, lib.SPH_STEP_PLAIN))
+        lib.check(L.sph_read(sim._h, lib.FIELD_VERTEX_DATA, ctypes.c_void_p(pin_out.data_ptr()), n * 12))
+    el = max_over_ranks(time.perf_counter() - t0)
+    barrier()
+    e2e_value = world * n * e2e_steps / el
+    sim.close()
+
+    if rank != 0:
+        return
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": sc.name, "particles": n, "cells": C,
+                      "boundary_map": list(sc.boundary.dims()) if sc.boundary is not None else None,
+                      "parallelism": "replicas" if world > 1 else "single",
+                      "l2": f"no flush: per-step working set {working_set_bytes(sc) / 2**20:.0f} MiB "
+                            f"> {L2_BYTES / 2**20:.0f} MiB L2",
+                      "graph": "one CUDA graph launch per step"},
+           "clocks": clk,
+           "gpu_launches": 6 * args.steps,
+           "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * n * 12,
+                   "d2h_bytes_per_step": n * 12, "steps": e2e_steps,
+                   "path": "sph_write(VD, VEL) + sph_step + sph_read(VD), pinned host buffers"},
+           "roofline": {"bound": "hbm", "kernel": "k_force", "achieved": achieved, "peak": peak,
+                        "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                        "peak_source": peak_kind,
+                        "algorithmic_bytes_per_launch": alg,
+                        "avg_launch_us": force_avg_s * 1e6},
+           "stages_us": {k: round(v[0] / v[1] * 1e3, 2) for k, v in stages.items()}}
+    if not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(sc)
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -75,8 +75,10 @@ __device__ __forceinline__ Tri tri_setup(const MapDev& m, float u, float v, floa
     return t;
 }
 
+// v0 + a*(v1 - v0): exact for a constant field, so the clamped region of the
+// distance map (-restDistance everywhere) never trips the wall test.
 __device__ __forceinline__ float lerp_ref(float v0, float v1, float a) {
-    return __fadd_rn(__fmul_rn(v0, __fsub_rn(1.0f, a)), __fmul_rn(v1, a));
+    return __fadd_rn(v0, __fmul_rn(a, __fsub_rn(v1, v0)));
 }
 
 __device__ __forceinline__ size_t node(const MapDev& m, int x, int y, int z) {

@@ -215,7 +215,10 @@ def dam_break_params(box_lo, box_hi, num_particles: int, dt: float = 1e-4,
                      restitution: float = 0.0) -> SimulationParameters:
     """WCSPH dam break: h = 0.025, lattice pitch h/2, m = rho0*(h/2)^3,
     p = k(rho - rho0), gravity 9.81, tension off.  The cell grid has cell size
-    h and is padded by one cell on every side of the container box."""
+    h and is padded by two cells on every side of the container box: with one
+    cell, a particle resting on an upper wall has (x + h - origin)/h == dim and
+    compute_grid_coordinate's `% dim` (particle_simulation.cu:1249) wraps its
+    neighbour range to nothing."""
     p = SimulationParameters()
     p.numParticles = num_particles
     p.kernelParticles = 34
@@ -230,8 +233,8 @@ def dam_break_params(box_lo, box_hi, num_particles: int, dt: float = 1e-4,
     kernel_constants(p, H)
     p.timeStep = _f32(dt)
     p.timeStepSubParticles = _f32(dt)
-    lo = [float(np.float32(b) - np.float32(H)) for b in box_lo]
-    hi = [float(np.float32(b) + np.float32(H)) for b in box_hi]
+    lo = [float(np.float32(b) - np.float32(2 * H)) for b in box_lo]
+    hi = [float(np.float32(b) + np.float32(2 * H)) for b in box_hi]
     set_simulation_domain(p, lo, hi, H, H / 2)
     p.fluidVolume = _f32(num_particles * SPACING ** 3)
     p.restitution = restitution

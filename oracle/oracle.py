@@ -56,7 +56,7 @@ def lib():
                                          ctypes.c_int] + [vp] * 9
         L.orc_step_plain_f32.restype = ctypes.c_int
         L.orc_step_plain_f64.argtypes = [_P(SimulationParameters), _P(Options), _P(Maps),
-                                         ctypes.c_int] + [vp] * 11
+                                         ctypes.c_int] + [vp] * 12
         L.orc_step_plain_f64.restype = ctypes.c_int
         L.orc_tex3d.argtypes = [_P(Maps), ctypes.c_int, vp, ctypes.c_int, vp]
         L.orc_boundary_dims.argtypes = [_P(BoundaryDesc), vp]
@@ -155,10 +155,11 @@ def step_plain(p: SimulationParameters, o: Options, bm: BoundaryMaps | None,
     if fp64:
         srho = np.zeros(n, np.float64)
         sacc = np.zeros(n, np.float64)
+        sdir = np.zeros(n, np.float64)
         rc = lib().orc_step_plain_f64(ctypes.byref(p), ctypes.byref(o), mp, n, _ptr(pos), _ptr(vel),
                                       _ptr(rho), _ptr(prs), _ptr(acc), _ptr(srho), _ptr(sacc),
-                                      _ptr(h), _ptr(ids), _ptr(start), _ptr(end))
-        out.update(scale_rho=srho, scale_acc=sacc)
+                                      _ptr(sdir), _ptr(h), _ptr(ids), _ptr(start), _ptr(end))
+        out.update(scale_rho=srho, scale_acc=sacc, scale_acc_direct=sdir)
     else:
         rc = lib().orc_step_plain_f32(ctypes.byref(p), ctypes.byref(o), mp, n, _ptr(pos), _ptr(vel),
                                       _ptr(rho), _ptr(prs), _ptr(acc), _ptr(h), _ptr(ids),

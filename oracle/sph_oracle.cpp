@@ -144,7 +144,10 @@ bool particle_hash(const R* x, const float* origin, R spacing, const int* dim,
 // (set_up_3d_float_texture, particle_simulation.cu:3003-3007).  Texel-space
 // coordinate is u*N - 0.5 as for any CUDA normalised-coordinate fetch; the
 // interpolation weights are exact (not the 9-bit fixed-point weights of the
-// texture unit), matching the GPU library's software trilinear path.
+// texture unit), matching the GPU library's software trilinear path.  Each
+// linear blend is evaluated as v0 + a*(v1 - v0), which reproduces a constant
+// field exactly: in the maps' clamped region (distance == -restDistance) the
+// wall test distWall < restDistance must not fire on a rounding error.
 // --------------------------------------------------------------------------
 template <class R>
 R tex3d(const float* g, const unsigned int* dims, R u, R v, R w) {
@@ -164,13 +167,12 @@ R tex3d(const float* g, const unsigned int* dims, R u, R v, R w) {
     auto at = [&](int x, int y, int z) -> R {
         return R(g[(size_t)x + (size_t)dims[0] * ((size_t)y + (size_t)dims[1] * (size_t)z)]);
     };
-    R c00 = at(i0[0], i0[1], i0[2]) * (R(1) - a[0]) + at(i1[0], i0[1], i0[2]) * a[0];
-    R c10 = at(i0[0], i1[1], i0[2]) * (R(1) - a[0]) + at(i1[0], i1[1], i0[2]) * a[0];
-    R c01 = at(i0[0], i0[1], i1[2]) * (R(1) - a[0]) + at(i1[0], i0[1], i1[2]) * a[0];
-    R c11 = at(i0[0], i1[1], i1[2]) * (R(1) - a[0]) + at(i1[0], i1[1], i1[2]) * a[0];
-    R c0 = c00 * (R(1) - a[1]) + c10 * a[1];
-    R c1 = c01 * (R(1) - a[1]) + c11 * a[1];
-    return c0 * (R(1) - a[2]) + c1 * a[2];
+    auto lerp = [](R v0, R v1, R t) -> R { return v0 + t * (v1 - v0); };
+    R c00 = lerp(at(i0[0], i0[1], i0[2]), at(i1[0], i0[1], i0[2]), a[0]);
+    R c10 = lerp(at(i0[0], i1[1], i0[2]), at(i1[0], i1[1], i0[2]), a[0]);
+    R c01 = lerp(at(i0[0], i0[1], i1[2]), at(i1[0], i0[1], i1[2]), a[0]);
+    R c11 = lerp(at(i0[0], i1[1], i1[2]), at(i1[0], i1[1], i1[2]), a[0]);
+    return lerp(lerp(c00, c10, a[1]), lerp(c01, c11, a[1]), a[2]);
 }
 
 template <class R>
@@ -266,14 +268,21 @@ void density_one(const OrcParams& P, const Level<R>& L, const OrcMaps* M, bool w
 // compute_sub_particle_viscosity_pressure_forces_cell (:1558-1643) when
 // `sub` is set (single force accumulator, no wall terms, tension always).
 // colLapl starts at 0 (uninitialised in the reference, :381).
-// `scale` receives sum |terms| / rho + |g|, with every pressure p entering as
-// k*(rho + rho0) (the magnitude that FP32 rounding of rho perturbs).
+// `scale` receives the rounding-error scale of the FP32 evaluation: the sum of
+// the magnitudes of every quantity that enters a sum or a difference, divided
+// by rho, plus |g|.  A pressure p enters as k*(rho + rho0) (the magnitude that
+// rounding of rho perturbs); the wall penalty coefficient
+// rho/dt^2*(restDist - distWall) enters as rho/dt^2*(restDist + |distWall|) and
+// each gradient component (t+ - t-)/(2 dX) as (|t+| + |t-|)/(2 dX).
+// `scaleDirect` (optional) is the same sum with the wall terms taken at their
+// own magnitude; it bounds differences between two evaluations that share the
+// reference's operation order for the wall terms.
 // --------------------------------------------------------------------------
 template <class R>
 void force_one(const OrcParams& P, const OrcOptions& O, const Level<R>& L,
                const OrcMaps* M, bool sub, const R* pos, const R* vel, const R* rhoA,
                const R* prsA, const int* ids, const int* start, const int* end,
-               size_t i, R* acc, R* scale) {
+               size_t i, R* acc, R* scale, R* scaleDirect = nullptr) {
     const R* xi = pos + 3 * i;
     const R* vi = vel + 3 * i;
     R rhoi = rhoA[i], pi = prsA[i];
@@ -321,7 +330,7 @@ void force_one(const OrcParams& P, const OrcOptions& O, const Level<R>& L,
     });
 
     R force[3];
-    double wallScale = 0.0, tensScale = 0.0;
+    double wallScale = 0.0, wallDirect = 0.0, tensScale = 0.0;
     bool tension = true;
     if (!sub) {
         for (int a = 0; a < 3; a++) force[a] = R(0) + vF[a];
@@ -333,9 +342,14 @@ void force_one(const OrcParams& P, const OrcOptions& O, const Level<R>& L,
             R rest = R(M->restDistance);
             R dt = R(P.timeStep);
             R coeff = rhoi / (dt * dt) * (rest - distWall);
-            if (distWall < rest) {
-                tension = false;
+            // within rounding of the band edge either branch is a correct
+            // FP32 outcome: the scale then covers the wall term as well
+            bool nearEdge = (double)distWall < (double)rest * (1.0 + 1e-5);
+            if (distWall < rest || (scale && nearEdge)) {
+                bool taken = distWall < rest;
+                if (taken) tension = false;
                 R dX[3], gN[3];
+                double gAbs2 = 0.0;
                 for (int a = 0; a < 3; a++)
                     dX[a] = R(M->spacing) / R((float)(M->dims[a] - 1) * M->spacing);
                 R up[3], dn[3];
@@ -346,19 +360,26 @@ void force_one(const OrcParams& P, const OrcOptions& O, const Level<R>& L,
                     }
                     up[a] = uvw[a] + dX[a];
                     dn[a] = uvw[a] - dX[a];
-                    gN[a] = (tex3d<R>(M->dist, M->dims, up[0], up[1], up[2]) -
-                             tex3d<R>(M->dist, M->dims, dn[0], dn[1], dn[2])) /
-                            (R(2) * dX[a]);
+                    R tp = tex3d<R>(M->dist, M->dims, up[0], up[1], up[2]);
+                    R tm = tex3d<R>(M->dist, M->dims, dn[0], dn[1], dn[2]);
+                    gN[a] = (tp - tm) / (R(2) * dX[a]);
+                    double ga = (std::fabs((double)tp) + std::fabs((double)tm)) / (2.0 * (double)dX[a]);
+                    gAbs2 += ga * ga;
                 }
-                for (int a = 0; a < 3; a++) force[a] -= coeff * gN[a];
                 R vw = tex3d<R>(M->visc, M->dims, uvw[0], uvw[1], uvw[2]);
-                for (int a = 0; a < 3; a++) force[a] -= vi[a] * vw;
+                if (taken) {
+                    for (int a = 0; a < 3; a++) force[a] -= coeff * gN[a];
+                    for (int a = 0; a < 3; a++) force[a] -= vi[a] * vw;
+                }
                 if (scale) {
                     double gn = std::sqrt((double)gN[0] * gN[0] + (double)gN[1] * gN[1] +
                                           (double)gN[2] * gN[2]);
                     double vn = std::sqrt((double)vi[0] * vi[0] + (double)vi[1] * vi[1] +
                                           (double)vi[2] * vi[2]);
-                    wallScale = std::fabs((double)coeff) * gn + vn * std::fabs((double)vw);
+                    double cAbs = (double)rhoi / ((double)dt * (double)dt) *
+                                  ((double)rest + std::fabs((double)distWall));
+                    wallScale = cAbs * std::sqrt(gAbs2) + vn * std::fabs((double)vw);
+                    wallDirect = std::fabs((double)coeff) * gn + vn * std::fabs((double)vw);
                 }
             }
         }
@@ -378,6 +399,10 @@ void force_one(const OrcParams& P, const OrcOptions& O, const Level<R>& L,
     if (scale) {
         *scale = R((sc + wallScale + tensScale) / std::fabs((double)rhoi) +
                    std::fabs((double)P.gravity));
+    }
+    if (scaleDirect) {
+        *scaleDirect = R((sc + wallDirect + tensScale) / std::fabs((double)rhoi) +
+                         std::fabs((double)P.gravity));
     }
 }
 
@@ -478,8 +503,8 @@ int num_cells(const int* dim) { return dim[0] * dim[1] * dim[2]; }
 // plus handleCollisions when O.boxCollision (AdvanceTwoScale, :2170).
 template <class R>
 int step_plain(const OrcParams& P, const OrcOptions& O, const OrcMaps* M, int n, R* pos,
-               R* vel, R* rho, R* prs, R* acc, R* scaleRho, R* scaleAcc, int* hash, int* ids,
-               int* start, int* end) {
+               R* vel, R* rho, R* prs, R* acc, R* scaleRho, R* scaleAcc, R* scaleAccDirect,
+               int* hash, int* ids, int* start, int* end) {
     Level<R> L = coarse_level<R>(P);
     int C = num_cells(P.gridDim);
     if (hash_all<R>(P, L, pos, n, hash, ids)) return 1;
@@ -494,7 +519,8 @@ int step_plain(const OrcParams& P, const OrcOptions& O, const OrcMaps* M, int n,
 #pragma omp parallel for schedule(dynamic, 256) num_threads(g_threads)
     for (int i = 0; i < n; i++)
         force_one<R>(P, O, L, M, false, pos, vel, rho, prs, ids, start, end, (size_t)i,
-                     acc + 3 * (size_t)i, scaleAcc ? &scaleAcc[i] : nullptr);
+                     acc + 3 * (size_t)i, scaleAcc ? &scaleAcc[i] : nullptr,
+                     scaleAccDirect ? &scaleAccDirect[i] : nullptr);
 #pragma omp parallel for schedule(static) num_threads(g_threads)
     for (int i = 0; i < n; i++) {
         integrate_one<R>(R(P.timeStep), acc + 3 * (size_t)i, pos + 3 * (size_t)i,
@@ -539,17 +565,17 @@ void orc_cells(const int* sortedHash, int n, int numCells, int* start, int* end)
 int orc_step_plain_f32(const OrcParams* P, const OrcOptions* O, const OrcMaps* M, int n,
                        float* pos, float* vel, float* rho, float* prs, float* acc, int* hash,
                        int* ids, int* start, int* end) {
-    return step_plain<float>(*P, *O, M, n, pos, vel, rho, prs, acc, nullptr, nullptr, hash,
-                             ids, start, end);
+    return step_plain<float>(*P, *O, M, n, pos, vel, rho, prs, acc, nullptr, nullptr, nullptr,
+                             hash, ids, start, end);
 }
 
 // The same step in FP64, with the tolerance scales.
 int orc_step_plain_f64(const OrcParams* P, const OrcOptions* O, const OrcMaps* M, int n,
                        double* pos, double* vel, double* rho, double* prs, double* acc,
-                       double* scaleRho, double* scaleAcc, int* hash, int* ids, int* start,
-                       int* end) {
-    return step_plain<double>(*P, *O, M, n, pos, vel, rho, prs, acc, scaleRho, scaleAcc, hash,
-                              ids, start, end);
+                       double* scaleRho, double* scaleAcc, double* scaleAccDirect, int* hash,
+                       int* ids, int* start, int* end) {
+    return step_plain<double>(*P, *O, M, n, pos, vel, rho, prs, acc, scaleRho, scaleAcc,
+                              scaleAccDirect, hash, ids, start, end);
 }
 
 // Trilinear sample of one map at world positions (checks the emulated tex3D).
