@@ -61,6 +61,8 @@ struct sph_sim {
     // state (particle order) and per-step sorted copies
     float4 *pos = nullptr, *vel = nullptr;
     float4 *posS = nullptr, *velS = nullptr, *rho4S = nullptr, *accS = nullptr;
+    int* rowStart = nullptr;          // [9][n] neighbour-row windows recorded by the density stage
+    unsigned int* rowMask = nullptr;  // [9][n] their neighbour masks
     SortBuffers sb{};
     unsigned long long* scanBlock = nullptr;
     unsigned int* status = nullptr;     // device status word
@@ -76,8 +78,8 @@ struct sph_sim {
     unsigned int numTimeSteps = 0;
     bool stepped = false;
 
-    // launch configuration (autotuned later)
-    int densityBlock = 128, forceBlock = 128, kahan = 1;
+    // launch configuration
+    StepConfig cfg;
 
     // CUDA graph of one plain step
     cudaGraph_t graph = nullptr;
@@ -90,6 +92,8 @@ struct sph_sim {
 };
 
 namespace {
+
+RowTables rows_of(const sph_sim* s) { return RowTables{s->sb.cellOffset, s->sb.halfOffset}; }
 
 GridDev make_grid(const SimulationParameters& P, bool sub) {
     GridDev g;
@@ -176,8 +180,9 @@ void free_all(sph_sim* s) {
     if (s->graph) cudaGraphDestroy(s->graph);
     for (cudaEvent_t e : s->events) cudaEventDestroy(e);
     void* ptrs[] = {s->pos, s->vel, s->posS, s->velS, s->rho4S, s->accS, s->sb.cnt, s->sb.cellOffset,
-                    s->sb.keySlot, s->sb.tmpIds, s->sb.sortedHash, s->sb.sortedIds, s->scanBlock,
-                    s->status, s->staging, s->map4, s->mapDist};
+                    s->sb.keySlot, s->sb.tmpIds, s->sb.sortedHash, s->sb.sortedIds, s->sb.workIds,
+                    s->sb.xS, s->sb.halfOffset, s->scanBlock,
+                    s->status, s->staging, s->map4, s->mapDist, s->rowStart, s->rowMask};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (s->statusHost) cudaFreeHost(s->statusHost);
@@ -206,12 +211,13 @@ void enqueue_plain(sph_sim* s, bool timing) {
     mark(ST_SCATTER);
     launch_scatter(n, s->sb, st);
     mark(ST_RANK);
-    launch_rank_gather(n, s->sb, s->pos, s->vel, s->posS, s->velS, st);
+    launch_rank_gather(n, s->sb, s->pos, s->vel, g, s->posS, s->velS, st);
     mark(ST_DENSITY);
-    launch_density(n, s->posS, s->sb.cellOffset, g, ph, s->map, s->rho4S, s->kahan, s->densityBlock, st);
+    // density and forces read the sorted copies only
+    launch_density(n, s->posS, rows_of(s), g, ph, s->map, s->rho4S, s->rowStart, s->rowMask, s->cfg, st);
     mark(ST_FORCE);
-    launch_force(n, s->posS, s->velS, s->rho4S, s->sb.sortedIds, s->sb.cellOffset, g, ph, s->map,
-                 s->O.boxCollision, s->pos, s->vel, s->accS, s->kahan, s->forceBlock, st);
+    launch_force(n, s->posS, s->velS, s->rho4S, s->sb.workIds, rows_of(s), g, ph, s->map,
+                 s->O.boxCollision, s->rowStart, s->rowMask, s->pos, s->vel, s->accS, s->cfg, st);
     mark(ST_COUNT);
 }
 
@@ -339,12 +345,18 @@ sph_status sph_create(const SimulationParameters* params, const sph_options* opt
     CREATE_CUDA(dalloc(&s->velS, n));
     CREATE_CUDA(dalloc(&s->rho4S, n));
     CREATE_CUDA(dalloc(&s->accS, n));
+    CREATE_CUDA(dalloc(&s->rowStart, (size_t)9 * n));
+    CREATE_CUDA(dalloc(&s->rowMask, (size_t)9 * n));
     CREATE_CUDA(dalloc(&s->sb.cnt, (size_t)C + 1 + SCAN_TILE));
     CREATE_CUDA(dalloc(&s->sb.cellOffset, (size_t)C + 1 + SCAN_TILE));
     CREATE_CUDA(dalloc(&s->sb.keySlot, n));
     CREATE_CUDA(dalloc(&s->sb.tmpIds, n));
     CREATE_CUDA(dalloc(&s->sb.sortedHash, n));
     CREATE_CUDA(dalloc(&s->sb.sortedIds, n));
+    CREATE_CUDA(dalloc(&s->sb.workIds, n));
+    CREATE_CUDA(dalloc(&s->sb.xS, n));
+    CREATE_CUDA(dalloc(&s->sb.halfOffset, (size_t)C + 1));
+    CREATE_CUDA(cudaMemsetAsync(s->sb.halfOffset, 0, sizeof(int) * ((size_t)C + 1), s->stream));
     CREATE_CUDA(dalloc(&s->scanBlock, (size_t)tiles + 2));
     s->sb.tileCounter = reinterpret_cast<unsigned int*>(s->scanBlock);
     s->sb.scanFlags = s->scanBlock + 2;
@@ -500,22 +512,22 @@ sph_status sph_read(sph_handle s, int field, void* dst, size_t bytes) {
         case SPH_FIELD_VERTEX_DATA: launch_pack_aos(s->pos, n, s->staging, 3, 0, q); break;
         case SPH_FIELD_VELOCITY: launch_pack_aos(s->vel, n, s->staging, 3, 0, q); break;
         case SPH_FIELD_ACCELERATION:
-            if (s->stepped) launch_unpermute(n, s->sb.sortedIds, s->accS, -1, s->staging, 3, 0, q);
+            if (s->stepped) launch_unpermute(n, s->sb.workIds, s->accS, -1, s->staging, 3, 0, q);
             else SPH_CUDA(cudaMemsetAsync(s->staging, 0, need, q));
             break;
         case SPH_FIELD_DENSITY:
         case SPH_FIELD_PRESSURE:
             if (s->stepped)
-                launch_unpermute(n, s->sb.sortedIds, s->rho4S, field == SPH_FIELD_DENSITY ? 0 : 1, s->staging,
+                launch_unpermute(n, s->sb.workIds, s->rho4S, field == SPH_FIELD_DENSITY ? 0 : 1, s->staging,
                                  1, 0, q);
             else SPH_CUDA(cudaMemsetAsync(s->staging, 0, need, q));
             break;
         case SPH_FIELD_SIMULATION_DATA:
             SPH_CUDA(cudaMemsetAsync(s->staging, 0, need, q));
             if (s->stepped) {
-                launch_unpermute(n, s->sb.sortedIds, s->rho4S, 0, s->staging, 10, 1, q);
-                launch_unpermute(n, s->sb.sortedIds, s->rho4S, 1, s->staging, 10, 2, q);
-                launch_unpermute(n, s->sb.sortedIds, s->accS, -1, s->staging, 10, 3, q);
+                launch_unpermute(n, s->sb.workIds, s->rho4S, 0, s->staging, 10, 1, q);
+                launch_unpermute(n, s->sb.workIds, s->rho4S, 1, s->staging, 10, 2, q);
+                launch_unpermute(n, s->sb.workIds, s->accS, -1, s->staging, 10, 3, q);
             }
             launch_pack_aos(s->vel, n, s->staging, 10, 6, q);
             break;
@@ -625,6 +637,146 @@ sph_status sph_set_stage_timing(sph_handle s, int enable) {
         for (auto& e : s->events) SPH_CUDA(cudaEventCreate(&e));
         s->timingCap = cap;
     }
+    return SPH_OK;
+}
+
+sph_status sph_get_tuning(sph_handle s, sph_tuning* out) {
+    if (!s || !out) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "NULL argument");
+    out->densityBlock = s->cfg.densityBlock;
+    out->forceBlock = s->cfg.forceBlock;
+    out->forceVariant = s->cfg.forceVariant;
+    out->prune = s->cfg.prune;
+    out->kahan = s->cfg.kahan;
+    return SPH_OK;
+}
+
+sph_status sph_set_tuning(sph_handle s, const sph_tuning* t) {
+    if (!s || !t) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "NULL argument");
+    auto okBlock = [](int b) { return b == 64 || b == 128 || b == 256; };
+    if (!okBlock(t->densityBlock) || !okBlock(t->forceBlock))
+        SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "block sizes must be 64, 128 or 256");
+    if (t->forceVariant < FORCE_DIRECT || t->forceVariant > FORCE_PRETESTED)
+        SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "unknown force variant");
+    s->cfg.densityBlock = t->densityBlock;
+    s->cfg.forceBlock = t->forceBlock;
+    s->cfg.forceVariant = t->forceVariant;
+    s->cfg.prune = t->prune ? 1 : 0;
+    s->cfg.kahan = t->kahan ? 1 : 0;
+    s->graphValid = false;
+    return SPH_OK;
+}
+
+sph_status sph_autotune(sph_handle s, int reps, sph_tuning* chosen) {
+    if (!s) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "handle is NULL");
+    reps = std::max(reps, 1);
+    const int n = s->n;
+    const int C = s->P.gridDim[0] * s->P.gridDim[1] * s->P.gridDim[2];
+    cudaStream_t st = s->stream;
+    SPH_CUDA(cudaStreamSynchronize(st));
+    // keep the last step's sorted data (read-back) and write forces to scratch
+    struct Buf {
+        void* dst;
+        void* save;
+        size_t bytes;
+    } bufs[] = {{s->posS, nullptr, sizeof(float4) * n},       {s->velS, nullptr, sizeof(float4) * n},
+                {s->rho4S, nullptr, sizeof(float4) * n},      {s->sb.sortedHash, nullptr, sizeof(int) * n},
+                {s->sb.sortedIds, nullptr, sizeof(int) * n},  {s->sb.cellOffset, nullptr, sizeof(int) * ((size_t)C + 1)},
+                {s->sb.workIds, nullptr, sizeof(int) * n},    {s->sb.xS, nullptr, sizeof(float) * n},
+                {s->sb.halfOffset, nullptr, sizeof(int) * ((size_t)C + 1)}};
+    float4* scratch = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    auto cleanup = [&]() {
+        for (auto& b : bufs)
+            if (b.save) cudaFree(b.save);
+        if (scratch) cudaFree(scratch);
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+    };
+#define TUNE_CUDA(call)                                                                  \
+    do {                                                                                 \
+        cudaError_t e_ = (call);                                                         \
+        if (e_ != cudaSuccess) {                                                         \
+            cleanup();                                                                   \
+            return fail(SPH_ERR_CUDA, __FILE__, __LINE__, cudaGetErrorString(e_));       \
+        }                                                                                \
+    } while (0)
+    for (auto& b : bufs) {
+        TUNE_CUDA(cudaMalloc(&b.save, b.bytes));
+        TUNE_CUDA(cudaMemcpyAsync(b.save, b.dst, b.bytes, cudaMemcpyDeviceToDevice, st));
+    }
+    TUNE_CUDA(cudaMalloc((void**)&scratch, sizeof(float4) * 3 * (size_t)n));
+    TUNE_CUDA(cudaEventCreate(&e0));
+    TUNE_CUDA(cudaEventCreate(&e1));
+    GridDev g = make_grid(s->P, false);
+    PhysDev ph = make_phys(s->P, s->O);
+    auto sortStages = [&]() {
+        launch_hash_count(n, s->pos, g, s->sb, s->status, st);
+        launch_cell_scan(g.numCells, s->sb, s->status, st);
+        launch_scatter(n, s->sb, st);
+        launch_rank_gather(n, s->sb, s->pos, s->vel, g, s->posS, s->velS, st);
+    };
+    // each candidate is timed in step context: the sort stages run before
+    // every timed launch, so caches hold what they hold in a real step
+    auto timeit = [&](auto&& before, auto&& launch) -> float {
+        float total = 0.f;
+        for (int r = 0; r < reps + 1; r++) {
+            before();
+            cudaEventRecord(e0, st);
+            launch();
+            cudaEventRecord(e1, st);
+            cudaEventSynchronize(e1);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (r > 0) total += ms;  // the first launch warms up
+        }
+        return total / reps;
+    };
+    const int blocks[3] = {64, 128, 256};
+    StepConfig best = s->cfg;
+    float bestTotal = 3.0e38f;
+    for (int prune = 0; prune <= 1; prune++)
+        for (int v = FORCE_DIRECT; v <= FORCE_PRETESTED; v++) {
+            StepConfig c = s->cfg;
+            c.prune = prune;
+            c.forceVariant = v;  // the density stage records masks for the pretested form
+            float bestD = 3.0e38f;
+            int bestDB = c.densityBlock;
+            for (int b : blocks) {
+                c.densityBlock = b;
+                float t = timeit(sortStages, [&] {
+                    launch_density(n, s->posS, rows_of(s), g, ph, s->map, s->rho4S, s->rowStart, s->rowMask, c, st);
+                });
+                if (t < bestD) {
+                    bestD = t;
+                    bestDB = b;
+                }
+            }
+            c.densityBlock = bestDB;
+            auto beforeForce = [&]() {
+                sortStages();
+                launch_density(n, s->posS, rows_of(s), g, ph, s->map, s->rho4S, s->rowStart, s->rowMask, c, st);
+            };
+            for (int b : blocks) {
+                c.forceBlock = b;
+                float t = timeit(beforeForce, [&] {
+                    launch_force(n, s->posS, s->velS, s->rho4S, s->sb.workIds, rows_of(s), g, ph, s->map,
+                                 s->O.boxCollision, s->rowStart, s->rowMask, scratch, scratch + n,
+                                 scratch + 2 * (size_t)n, c, st);
+                });
+                if (bestD + t < bestTotal) {
+                    bestTotal = bestD + t;
+                    best = c;
+                }
+            }
+        }
+    TUNE_CUDA(cudaGetLastError());
+    for (auto& b : bufs) TUNE_CUDA(cudaMemcpyAsync(b.dst, b.save, b.bytes, cudaMemcpyDeviceToDevice, st));
+    TUNE_CUDA(cudaStreamSynchronize(st));
+#undef TUNE_CUDA
+    cleanup();
+    s->cfg = best;
+    s->graphValid = false;
+    if (chosen) return sph_get_tuning(s, chosen);
     return SPH_OK;
 }
 

@@ -1,0 +1,230 @@
+// Device helpers shared by the step kernels: the reference's grid arithmetic
+// (bit-exact), the software trilinear boundary-map fetch, neighbour-row
+// iteration over the 27-cell stencil, compensated summation and the box
+// collision response.
+#pragma once
+
+#include "sph_internal.h"
+
+namespace sph {
+
+// compute_particle_hash (particle_simulation.cu:100-115): (int) truncation,
+// C remainder, x-fastest hash.  Rounded operations are spelled out so no FMA
+// contraction can change the cell a particle falls in.
+__device__ __forceinline__ int particle_hash(float4 p, const GridDev& g, bool* outside) {
+    int c[3];
+    float v[3] = {p.x, p.y, p.z};
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        float f = __fdiv_rn(__fsub_rn(v[a], g.origin[a]), g.spacing);
+        c[a] = (int)f;
+        c[a] = c[a] % g.dim[a];
+    }
+    int h = g.dim[0] * (g.dim[1] * c[2] + c[1]) + c[0];
+    if (h < 0 || h >= g.numCells) {
+        *outside = true;
+        h = min(max(h, 0), g.numCells - 1);
+    }
+    return h;
+}
+
+// compute_grid_coordinate (particle_simulation.cu:1238-1258): the (unsigned)
+// conversion saturates negative values to 0, then remainder and clamp.
+__device__ __forceinline__ int grid_coord(float p, float d, float origin, float spacing, int dim) {
+    float f = __fdiv_rn(__fsub_rn(__fadd_rn(p, d), origin), spacing);
+    unsigned int u = (unsigned int)f;
+    int c = (int)u;
+    c = c % dim;
+    return min(max(c, 0), dim - 1);
+}
+
+// ---------------------------------------------------------------------------
+// Software trilinear fetch with CUDA's normalised-coordinate addressing
+// (texel coordinate u*N - 0.5, clamp), exact FP32 weights.
+// ---------------------------------------------------------------------------
+struct Tri {
+    int i0[3], i1[3];
+    float a[3];
+};
+
+__device__ __forceinline__ Tri tri_setup(const MapDev& m, float u, float v, float w) {
+    Tri t;
+    float c[3] = {u, v, w};
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        float x = __fsub_rn(__fmul_rn(c[k], m.dimsf[k]), 0.5f);
+        float f = floorf(x);
+        t.a[k] = __fsub_rn(x, f);
+        int lo = (int)f;  // saturating conversion; clamped below
+        t.i0[k] = min(max(lo, 0), m.dims[k] - 1);
+        t.i1[k] = min(max(lo + 1, 0), m.dims[k] - 1);
+    }
+    return t;
+}
+
+// v0 + a*(v1 - v0): exact for a constant field, so the clamped region of the
+// distance map (-restDistance everywhere) never trips the wall test.
+__device__ __forceinline__ float lerp_ref(float v0, float v1, float a) {
+    return __fadd_rn(v0, __fmul_rn(a, __fsub_rn(v1, v0)));
+}
+
+__device__ __forceinline__ size_t map_node(const MapDev& m, int x, int y, int z) {
+    return (size_t)x + (size_t)m.dims[0] * ((size_t)y + (size_t)m.dims[1] * (size_t)z);
+}
+
+__device__ __forceinline__ float tri_scalar(const MapDev& m, const float* __restrict__ g, float u,
+                                            float v, float w) {
+    Tri t = tri_setup(m, u, v, w);
+    float c00 = lerp_ref(__ldg(g + map_node(m, t.i0[0], t.i0[1], t.i0[2])),
+                         __ldg(g + map_node(m, t.i1[0], t.i0[1], t.i0[2])), t.a[0]);
+    float c10 = lerp_ref(__ldg(g + map_node(m, t.i0[0], t.i1[1], t.i0[2])),
+                         __ldg(g + map_node(m, t.i1[0], t.i1[1], t.i0[2])), t.a[0]);
+    float c01 = lerp_ref(__ldg(g + map_node(m, t.i0[0], t.i0[1], t.i1[2])),
+                         __ldg(g + map_node(m, t.i1[0], t.i0[1], t.i1[2])), t.a[0]);
+    float c11 = lerp_ref(__ldg(g + map_node(m, t.i0[0], t.i1[1], t.i1[2])),
+                         __ldg(g + map_node(m, t.i1[0], t.i1[1], t.i1[2])), t.a[0]);
+    return lerp_ref(lerp_ref(c00, c10, t.a[1]), lerp_ref(c01, c11, t.a[1]), t.a[2]);
+}
+
+__device__ __forceinline__ float4 lerp4(float4 p, float4 q, float a) {
+    return make_float4(lerp_ref(p.x, q.x, a), lerp_ref(p.y, q.y, a), lerp_ref(p.z, q.z, a), 0.f);
+}
+
+// (distance, wall density, wall viscosity) at one point, from the
+// interleaved float4 map: one pass over the 8 corner nodes.
+__device__ __forceinline__ float4 tri_vec(const MapDev& m, float u, float v, float w) {
+    Tri t = tri_setup(m, u, v, w);
+    const float4* g = m.map4;
+    float4 c00 = lerp4(__ldg(g + map_node(m, t.i0[0], t.i0[1], t.i0[2])),
+                       __ldg(g + map_node(m, t.i1[0], t.i0[1], t.i0[2])), t.a[0]);
+    float4 c10 = lerp4(__ldg(g + map_node(m, t.i0[0], t.i1[1], t.i0[2])),
+                       __ldg(g + map_node(m, t.i1[0], t.i1[1], t.i0[2])), t.a[0]);
+    float4 c01 = lerp4(__ldg(g + map_node(m, t.i0[0], t.i0[1], t.i1[2])),
+                       __ldg(g + map_node(m, t.i1[0], t.i0[1], t.i1[2])), t.a[0]);
+    float4 c11 = lerp4(__ldg(g + map_node(m, t.i0[0], t.i1[1], t.i1[2])),
+                       __ldg(g + map_node(m, t.i1[0], t.i1[1], t.i1[2])), t.a[0]);
+    return lerp4(lerp4(c00, c10, t.a[1]), lerp4(c01, c11, t.a[1]), t.a[2]);
+}
+
+// u = (pos - origin)/gridLength (particle_simulation.cu:243-245).
+__device__ __forceinline__ void map_uvw(const MapDev& m, float4 x, float* uvw) {
+    uvw[0] = __fdiv_rn(__fsub_rn(x.x, m.origin[0]), m.length[0]);
+    uvw[1] = __fdiv_rn(__fsub_rn(x.y, m.origin[1]), m.length[1]);
+    uvw[2] = __fdiv_rn(__fsub_rn(x.z, m.origin[2]), m.length[2]);
+}
+
+// ---------------------------------------------------------------------------
+// Neighbour rows: the 3x3 (z, y) rows of the 27-cell stencil
+// (particle_simulation.cu:225-238).  Cells of one row are consecutive hashes,
+// so the candidates of a row are one contiguous range [s, e) of the sorted
+// arrays, visited in the reference's k, j, i order.
+//
+// With `window`, a row whose (y, z) cell rectangle lies farther than h from
+// the particle is skipped, and the others are cut to the half-cells (in x)
+// that the sphere of radius h reaches at that (y, z) gap: the working order
+// sorts each cell by x and records where its upper half starts, so the cut
+// is a table lookup.  The gap is shrunk and the reach grown by 1e-3 h -- far
+// more than the rounding of any cell boundary or distance -- so every particle
+// within h stays a candidate; the candidates dropped all lie beyond h and
+// contribute exactly nothing in the reference either.
+// ---------------------------------------------------------------------------
+struct Stencil {
+    int x0, x1, y0, y1, z0, z1;
+};
+
+__device__ __forceinline__ Stencil stencil(float4 x, float h, const GridDev& g) {
+    Stencil s;
+    s.x0 = grid_coord(x.x, -h, g.origin[0], g.spacing, g.dim[0]);
+    s.x1 = grid_coord(x.x, h, g.origin[0], g.spacing, g.dim[0]);
+    s.y0 = grid_coord(x.y, -h, g.origin[1], g.spacing, g.dim[1]);
+    s.y1 = grid_coord(x.y, h, g.origin[1], g.spacing, g.dim[1]);
+    s.z0 = grid_coord(x.z, -h, g.origin[2], g.spacing, g.dim[2]);
+    s.z1 = grid_coord(x.z, h, g.origin[2], g.spacing, g.dim[2]);
+    return s;
+}
+
+__device__ __forceinline__ float cell_gap(float p, int c, float origin, float spacing, float eps) {
+    float lo = origin + (float)c * spacing;
+    float hi = lo + spacing;
+    return fmaxf(fmaxf(lo - p, p - hi) - eps, 0.0f);
+}
+
+// Squared distance with every rounding spelled out, so the density stage
+// (which records neighbour masks) and the force stage (which uses them or
+// tests again) decide each pair identically.
+__device__ __forceinline__ float dist2(float4 a, float4 b) {
+    const float dx = __fsub_rn(a.x, b.x), dy = __fsub_rn(a.y, b.y), dz = __fsub_rn(a.z, b.z);
+    return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+}
+
+// Candidate range [s, e) of stencil row r (0..8: k outer, j inner).  Rows
+// outside the stencil and rows the window cut removes are empty (s == e).
+__device__ __forceinline__ void row_range(float4 xi, const Stencil& st, float h, const GridDev& g, RowTables T,
+                                          bool window, int r, int& s, int& e) {
+    s = e = 0;
+    const int z = st.z0 + r / 3, y = st.y0 + r % 3;
+    if (z > st.z1 || y > st.y1) return;
+    const int row = g.dim[0] * (g.dim[1] * z + y);
+    if (!window) {
+        s = __ldg(T.cellOffset + row + st.x0);
+        e = __ldg(T.cellOffset + row + st.x1 + 1);
+        return;
+    }
+    const float eps = 1e-3f * h;
+    const float h2 = h * h;
+    const float gz = cell_gap(xi.z, z, g.origin[2], g.spacing, eps);
+    const float gy = cell_gap(xi.y, y, g.origin[1], g.spacing, eps);
+    const float g2 = gy * gy + gz * gz;
+    if (g2 > h2) return;
+    const float inv = 1.0f / g.spacing;
+    const float rx = sqrtf(h2 - g2) + eps;
+    const float xl = xi.x - rx, xr = xi.x + rx;
+    const int cl = max(st.x0, (int)floorf((xl - g.origin[0]) * inv));
+    const int cr = min(st.x1, (int)floorf((xr - g.origin[0]) * inv));
+    if (cl > cr) return;
+    const int a0 = __ldg(T.cellOffset + row + cl), a1 = __ldg(T.cellOffset + row + cl + 1);
+    const int b0 = __ldg(T.cellOffset + row + cr), b1 = __ldg(T.cellOffset + row + cr + 1);
+    const float midL = g.origin[0] + ((float)cl + 0.5f) * g.spacing;
+    const float midR = g.origin[0] + ((float)cr + 0.5f) * g.spacing;
+    s = a0;
+    e = b1;
+    if (xl >= midL) s = min(max(__ldg(T.halfOffset + row + cl), a0), a1);
+    if (xr < midR) e = min(max(__ldg(T.halfOffset + row + cr), b0), b1);
+    if (e < s) e = s;
+}
+
+__device__ __forceinline__ void kahan_add(float& sum, float& comp, float term) {
+    float y = __fsub_rn(term, comp);
+    float t = __fadd_rn(sum, y);
+    comp = __fsub_rn(__fsub_rn(t, sum), y);
+    sum = t;
+}
+
+// collision_handling (particle_simulation.cu:742-834) for one particle, with
+// two guards the reference lacks (it yields NaN there): |v| == 0 drops the
+// restitution term, and a contact point that rounds onto the particle leaves
+// it untouched.
+__device__ __forceinline__ void collide(const PhysDev& ph, float3& x, float3& v) {
+    float lx = x.x - ph.boxCen[0], ly = x.y - ph.boxCen[1], lz = x.z - ph.boxCen[2];
+    float dist = fmaxf(fmaxf(fabsf(lx) - ph.boxDim[0], fabsf(ly) - ph.boxDim[1]),
+                       fabsf(lz) - ph.boxDim[2]);
+    if (!(dist > 0.f)) return;
+    float cx = fminf(ph.boxDim[0], fmaxf(-ph.boxDim[0], lx)) + ph.boxCen[0];
+    float cy = fminf(ph.boxDim[1], fmaxf(-ph.boxDim[1], ly)) + ph.boxCen[1];
+    float cz = fminf(ph.boxDim[2], fmaxf(-ph.boxDim[2], lz)) + ph.boxCen[2];
+    float nx = x.x - cx, ny = x.y - cy, nz = x.z - cz;
+    float depth = sqrtf(nx * nx + ny * ny + nz * nz);
+    if (!(depth > 0.f)) return;
+    nx /= depth;
+    ny /= depth;
+    nz /= depth;
+    float velNorm = sqrtf(v.x * v.x + v.y * v.y + v.z * v.z);
+    float dp = nx * v.x + ny * v.y + nz * v.z;
+    float coeff = velNorm > 0.f ? (1.f + ph.restitution * depth / (ph.dtCollide * velNorm)) * dp : dp;
+    v.x -= coeff * nx;
+    v.y -= coeff * ny;
+    v.z -= coeff * nz;
+    x = make_float3(cx, cy, cz);
+}
+
+}  // namespace sph

@@ -63,10 +63,31 @@ struct SortBuffers {
     int2* keySlot;            // [n]   (hash, arrival slot in its cell)
     int* tmpIds;              // [n]   ids scattered to their cell segment, unordered
     int* sortedHash;          // [n]
-    int* sortedIds;           // [n]   the permutation
+    int* sortedIds;           // [n]   the reference's permutation (cell, id)
+    int* workIds;             // [n]   the working order (cell, x, id) of the sorted arrays
+    float* xS;                // [n]   x coordinate in the working order
+    int* halfOffset;          // [C+1] first working index of each cell's upper x-half
+                              //       (meaningful for occupied cells only)
     unsigned long long* scanFlags;  // decoupled look-back tile states
     unsigned int* tileCounter;
     int maxTiles;
+};
+
+// Per-row lookup tables of the neighbour search.
+struct RowTables {
+    const int* cellOffset;  // [C+1]
+    const int* halfOffset;  // [C+1], valid for occupied cells
+};
+
+// Launch configuration of the step (chosen per handle; see the autotuner).
+enum ForceVariant { FORCE_DIRECT = 0, FORCE_MASK = 1, FORCE_PRETESTED = 2 };
+
+struct StepConfig {
+    int densityBlock = 128;
+    int forceBlock = 128;
+    int forceVariant = FORCE_PRETESTED;
+    int prune = 1;   // row / half-cell window cut (sph_device.cuh)
+    int kahan = 1;
 };
 
 constexpr int SCAN_THREADS = 256;
@@ -82,14 +103,15 @@ void launch_hash_count(int n, const float4* pos, GridDev g, SortBuffers sb, unsi
                        cudaStream_t s);
 void launch_cell_scan(int numCells, SortBuffers sb, unsigned int* status, cudaStream_t s);
 void launch_scatter(int n, SortBuffers sb, cudaStream_t s);
-void launch_rank_gather(int n, SortBuffers sb, const float4* pos, const float4* vel, float4* posS,
-                        float4* velS, cudaStream_t s);
-void launch_density(int n, const float4* posS, const int* cellOffset, GridDev g, PhysDev ph,
-                    MapDev map, float4* rho4S, int kahan, int blockSize, cudaStream_t s);
+void launch_rank_gather(int n, SortBuffers sb, const float4* pos, const float4* vel, GridDev g,
+                        float4* posS, float4* velS, cudaStream_t s);
+void launch_density(int n, const float4* posS, RowTables T, GridDev g, PhysDev ph, MapDev map,
+                    float4* rho4S, int* rowStart, unsigned int* rowMask, const StepConfig& cfg,
+                    cudaStream_t s);
 void launch_force(int n, const float4* posS, const float4* velS, const float4* rho4S,
-                  const int* sortedIds, const int* cellOffset, GridDev g, PhysDev ph, MapDev map,
-                  int collide, float4* pos, float4* vel, float4* accS, int kahan, int blockSize,
-                  cudaStream_t s);
+                  const int* workIds, RowTables T, GridDev g, PhysDev ph, MapDev map, int collide,
+                  const int* rowStart, const unsigned int* rowMask, float4* pos, float4* vel,
+                  float4* accS, const StepConfig& cfg, cudaStream_t s);
 void launch_unpermute(int n, const int* sortedIds, const float4* srcS, int comp, float* dst,
                       int stride, int offset, cudaStream_t s);
 void launch_cell_tables(int numCells, const int* cellOffset, int* start, int* end, cudaStream_t s);

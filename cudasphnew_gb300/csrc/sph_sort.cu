@@ -1,0 +1,328 @@
+// Sorting stages of the GB300 SPH step and read-back helpers.
+//
+// Data layout in HBM (one handle, n particles, C cells):
+//   pos, vel           float4[n]  particle-index order (the state; .w unused)
+//   posS, velS         float4[n]  copies in sorted (cell, id) order, per step
+//   rho4S              float4[n]  (rho, p, p/rho^2, 1/rho) in sorted order
+//   accS               float4[n]  acceleration in sorted order
+//   cnt, cellOffset    int[C+1]   per-cell counts / their exclusive scan
+// The sort is a counting sort: every particle takes an arrival slot in its
+// cell with one atomic, a single-pass decoupled look-back scan turns counts
+// into cell offsets, and a rank pass orders each cell's members by particle
+// id.  The result is the permutation of a stable sort by hash -- the order
+// thrust::sort_by_key produces in the reference (particle_simulation.cu:2340).
+#include <cuda/atomic>
+
+#include "sph_device.cuh"
+
+namespace sph {
+
+// ---------------------------------------------------------------------------
+// AoS <-> float4 conversion (VD/SD layouts of particle_simulation.h:17-41)
+// ---------------------------------------------------------------------------
+__global__ void k_unpack_aos(const float* __restrict__ aos, int stride, int offset, int n,
+                             float4* __restrict__ out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float* p = aos + (size_t)i * stride + offset;
+    out[i] = make_float4(p[0], p[1], p[2], 0.0f);
+}
+
+__global__ void k_pack_aos(const float4* __restrict__ in, int n, float* __restrict__ aos, int stride,
+                           int offset) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 v = in[i];
+    float* p = aos + (size_t)i * stride + offset;
+    p[0] = v.x;
+    p[1] = v.y;
+    p[2] = v.z;
+}
+
+void launch_unpack_aos(const float* aos, int stride, int offset, int n, float4* out, cudaStream_t s) {
+    if (n <= 0) return;
+    k_unpack_aos<<<(n + 255) / 256, 256, 0, s>>>(aos, stride, offset, n, out);
+}
+
+void launch_pack_aos(const float4* in, int n, float* aos, int stride, int offset, cudaStream_t s) {
+    if (n <= 0) return;
+    k_pack_aos<<<(n + 255) / 256, 256, 0, s>>>(in, n, aos, stride, offset);
+}
+
+// ---------------------------------------------------------------------------
+// Stage 1: hash + per-cell arrival slot
+// ---------------------------------------------------------------------------
+__global__ void k_hash_count(int n, const float4* __restrict__ pos, GridDev g, int* __restrict__ cnt,
+                             int2* __restrict__ keySlot, unsigned int* status) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 p = pos[i];
+    bool outside = false;
+    if (!(isfinite(p.x) && isfinite(p.y) && isfinite(p.z))) {
+        atomicOr(status, STATUS_NON_FINITE);
+        p = make_float4(g.origin[0], g.origin[1], g.origin[2], 0.f);
+    }
+    int h = particle_hash(p, g, &outside);
+    if (outside) atomicOr(status, STATUS_OUT_OF_DOMAIN);
+    int slot = atomicAdd(cnt + h, 1);
+    keySlot[i] = make_int2(h, slot);
+}
+
+void launch_hash_count(int n, const float4* pos, GridDev g, SortBuffers sb, unsigned int* status,
+                       cudaStream_t s) {
+    if (n <= 0) return;
+    k_hash_count<<<(n + 255) / 256, 256, 0, s>>>(n, pos, g, sb.cnt, sb.keySlot, status);
+}
+
+// ---------------------------------------------------------------------------
+// Stage 2: exclusive scan of the C+1 cell counts into cell offsets, one pass
+// with decoupled look-back (Merrill & Garland).  Counts are cleared as they
+// are read, ready for the next step.  Tiles take their index from an atomic
+// counter, so every tile a block waits on has already started; each wait is
+// bounded and latches STATUS_DEVICE_WAIT if it ever gives up.
+// ---------------------------------------------------------------------------
+constexpr unsigned long long FLAG_AGG = 1ull << 32;
+constexpr unsigned long long FLAG_INC = 2ull << 32;
+constexpr int SPIN_LIMIT = 1 << 22;
+
+__global__ void __launch_bounds__(SCAN_THREADS)
+k_cell_scan(int total, int* __restrict__ cnt, int* __restrict__ out, unsigned long long* flags,
+            unsigned int* tileCounter, unsigned int* status) {
+    __shared__ int s_tile;
+    __shared__ int s_warp[SCAN_THREADS / 32];
+    __shared__ int s_prefix;
+    if (threadIdx.x == 0) s_tile = (int)atomicAdd(tileCounter, 1u);
+    __syncthreads();
+    const int tile = s_tile;
+    const int base = tile * SCAN_TILE + threadIdx.x * SCAN_ITEMS;
+    int v[SCAN_ITEMS];
+    if (base + SCAN_ITEMS <= total) {
+        int4 a = *reinterpret_cast<const int4*>(cnt + base);
+        int4 b = *reinterpret_cast<const int4*>(cnt + base + 4);
+        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+        v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+        *reinterpret_cast<int4*>(cnt + base) = make_int4(0, 0, 0, 0);
+        *reinterpret_cast<int4*>(cnt + base + 4) = make_int4(0, 0, 0, 0);
+    } else {
+#pragma unroll
+        for (int k = 0; k < SCAN_ITEMS; k++) {
+            int idx = base + k;
+            v[k] = idx < total ? cnt[idx] : 0;
+            if (idx < total) cnt[idx] = 0;
+        }
+    }
+    int local = 0;
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; k++) local += v[k];
+    // block-wide exclusive scan of `local`
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int incl = local;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+    }
+    if (lane == 31) s_warp[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        int w = lane < SCAN_THREADS / 32 ? s_warp[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int t = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += t;
+        }
+        if (lane < SCAN_THREADS / 32) s_warp[lane] = w;  // inclusive warp totals
+    }
+    __syncthreads();
+    const int warpExcl = warp > 0 ? s_warp[warp - 1] : 0;
+    const int aggregate = s_warp[SCAN_THREADS / 32 - 1];
+    int excl = warpExcl + incl - local;
+
+    // publish + look back (warp 0)
+    if (warp == 0) {
+        cuda::atomic_ref<unsigned long long, cuda::thread_scope_device> mine(flags[tile]);
+        if (lane == 0) {
+            mine.store((tile == 0 ? FLAG_INC : FLAG_AGG) | (unsigned int)aggregate,
+                       cuda::memory_order_release);
+        }
+        int prefix = 0;
+        if (tile > 0) {
+            int look = tile - 1;
+            bool done = false;
+            while (!done) {
+                int t = look - lane;
+                unsigned long long f = FLAG_INC;  // below tile 0: neutral, inclusive
+                if (t >= 0) {
+                    cuda::atomic_ref<unsigned long long, cuda::thread_scope_device> other(flags[t]);
+                    int spins = 0;
+                    f = other.load(cuda::memory_order_acquire);
+                    while ((f >> 32) == 0ull) {
+                        if (++spins > SPIN_LIMIT) {
+                            atomicOr(status, STATUS_DEVICE_WAIT);
+                            f = FLAG_INC;  // give up: treat as zero, result flagged
+                            break;
+                        }
+                        __nanosleep(32);
+                        f = other.load(cuda::memory_order_acquire);
+                    }
+                    if (t < 0) f = FLAG_INC;
+                }
+                unsigned int incMask = __ballot_sync(0xffffffffu, (f >> 32) == 2ull);
+                int val = (int)(unsigned int)(f & 0xffffffffull);
+                int first = incMask ? __ffs(incMask) - 1 : 32;  // nearest inclusive
+                int contrib = lane <= first ? val : 0;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) contrib += __shfl_xor_sync(0xffffffffu, contrib, o);
+                prefix += contrib;
+                if (incMask) done = true;
+                look -= 32;
+            }
+            if (lane == 0)
+                mine.store(FLAG_INC | (unsigned int)(prefix + aggregate), cuda::memory_order_release);
+        }
+        if (lane == 0) s_prefix = prefix;
+    }
+    __syncthreads();
+    int run = s_prefix + excl;
+    if (base + SCAN_ITEMS <= total) {
+        int o[SCAN_ITEMS];
+#pragma unroll
+        for (int k = 0; k < SCAN_ITEMS; k++) {
+            o[k] = run;
+            run += v[k];
+        }
+        *reinterpret_cast<int4*>(out + base) = make_int4(o[0], o[1], o[2], o[3]);
+        *reinterpret_cast<int4*>(out + base + 4) = make_int4(o[4], o[5], o[6], o[7]);
+    } else {
+#pragma unroll
+        for (int k = 0; k < SCAN_ITEMS; k++) {
+            if (base + k < total) out[base + k] = run;
+            run += v[k];
+        }
+    }
+}
+
+void launch_cell_scan(int numCells, SortBuffers sb, unsigned int* status, cudaStream_t s) {
+    int total = numCells + 1;
+    int tiles = (total + SCAN_TILE - 1) / SCAN_TILE;
+    // tile counter (first 16 bytes) and the tile states that follow it
+    cudaMemsetAsync(sb.tileCounter, 0, 16 + sizeof(unsigned long long) * (size_t)tiles, s);
+    k_cell_scan<<<tiles, SCAN_THREADS, 0, s>>>(total, sb.cnt, sb.cellOffset, sb.scanFlags,
+                                               sb.tileCounter, status);
+}
+
+// ---------------------------------------------------------------------------
+// Stage 3: scatter ids into their cell segments (arrival order)
+// ---------------------------------------------------------------------------
+__global__ void k_scatter(int n, const int2* __restrict__ keySlot, const int* __restrict__ cellOffset,
+                          int* __restrict__ tmpIds, int* __restrict__ sortedHash) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int2 ks = keySlot[i];
+    int dst = __ldg(cellOffset + ks.x) + ks.y;
+    tmpIds[dst] = i;
+    sortedHash[dst] = ks.x;
+}
+
+void launch_scatter(int n, SortBuffers sb, cudaStream_t s) {
+    if (n <= 0) return;
+    k_scatter<<<(n + 255) / 256, 256, 0, s>>>(n, sb.keySlot, sb.cellOffset, sb.tmpIds, sb.sortedHash);
+}
+
+// ---------------------------------------------------------------------------
+// Stage 4: order each cell's members and gather the state into sorted order.
+// Two orders come out of one pass over the cell segment:
+//   by particle id   -> sortedIds, the reference's permutation (stable sort
+//                       by hash, particle_simulation.cu:2340), kept for the API;
+//   by (x, id)       -> workIds, the order the neighbour kernels use.  A row of
+//                       three x-adjacent cells is then sorted by x as a whole,
+//                       so a binary search narrows it to the particles within
+//                       reach of a given x.
+// Ranks count the smaller keys in the segment; x is compared through its
+// order-preserving integer image so the order is total (NaN included).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned int ordered_bits(float x) {
+    unsigned int u = __float_as_uint(x);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+// The same pass records, per cell, where its upper x-half starts in the
+// working order (halfOffset[c] = first index with x >= the cell's mid-plane),
+// so a neighbour search can cut a row at half-cell granularity from a table.
+__global__ void k_rank_gather(int n, const int* __restrict__ sortedHash, const int* __restrict__ cellOffset,
+                              const int* __restrict__ tmpIds, const float4* __restrict__ pos,
+                              const float4* __restrict__ vel, GridDev g, int* __restrict__ sortedIds,
+                              int* __restrict__ workIds, int* __restrict__ halfOffset,
+                              float4* __restrict__ posS, float4* __restrict__ velS, float* __restrict__ xS) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    int c = sortedHash[k];
+    int s = __ldg(cellOffset + c), e = __ldg(cellOffset + c + 1);
+    int my = tmpIds[k];
+    float4 p = __ldg(pos + my);
+    unsigned int key = ordered_bits(p.x);
+    const float mid = g.origin[0] + ((float)(c % g.dim[0]) + 0.5f) * g.spacing;
+    int rId = 0, rX = 0, below = 0;
+    for (int t = s; t < e; t++) {
+        int o = __ldg(tmpIds + t);
+        float xo = __ldg(&pos[o].x);
+        unsigned int ko = ordered_bits(xo);
+        rId += o < my;
+        rX += (ko < key) || (ko == key && o < my);
+        below += xo < mid;
+    }
+    sortedIds[s + rId] = my;
+    workIds[s + rX] = my;
+    posS[s + rX] = p;
+    velS[s + rX] = __ldg(vel + my);
+    xS[s + rX] = p.x;
+    if (rX == 0) halfOffset[c] = s + below;
+}
+
+void launch_rank_gather(int n, SortBuffers sb, const float4* pos, const float4* vel, GridDev g, float4* posS,
+                        float4* velS, cudaStream_t s) {
+    if (n <= 0) return;
+    k_rank_gather<<<(n + 255) / 256, 256, 0, s>>>(n, sb.sortedHash, sb.cellOffset, sb.tmpIds, pos, vel, g,
+                                                  sb.sortedIds, sb.workIds, sb.halfOffset, posS, velS, sb.xS);
+}
+
+// ---------------------------------------------------------------------------
+// Read-back helpers
+// ---------------------------------------------------------------------------
+__global__ void k_unpermute(int n, const int* __restrict__ ids, const float4* __restrict__ src, int comp,
+                            float* __restrict__ dst, int stride, int offset) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    float4 v = src[k];
+    float* o = dst + (size_t)ids[k] * stride + offset;
+    if (comp < 0) {
+        o[0] = v.x;
+        o[1] = v.y;
+        o[2] = v.z;
+    } else {
+        o[0] = comp == 0 ? v.x : comp == 1 ? v.y : comp == 2 ? v.z : v.w;
+    }
+}
+
+void launch_unpermute(int n, const int* sortedIds, const float4* srcS, int comp, float* dst, int stride,
+                      int offset, cudaStream_t s) {
+    if (n <= 0) return;
+    k_unpermute<<<(n + 255) / 256, 256, 0, s>>>(n, sortedIds, srcS, comp, dst, stride, offset);
+}
+
+// Reference cell tables from the offsets: EMPTY (0xFFFFFFFF) for empty cells.
+__global__ void k_cell_tables(int numCells, const int* __restrict__ off, int* start, int* end) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= numCells) return;
+    int s = off[c], e = off[c + 1];
+    bool occ = e > s;
+    if (start) start[c] = occ ? s : -1;
+    if (end) end[c] = occ ? e : -1;
+}
+
+void launch_cell_tables(int numCells, const int* cellOffset, int* start, int* end, cudaStream_t s) {
+    if (numCells <= 0) return;
+    k_cell_tables<<<(numCells + 255) / 256, 256, 0, s>>>(numCells, cellOffset, start, end);
+}
+
+}  // namespace sph

@@ -1,0 +1,333 @@
+// Density and force stages of the GB300 SPH step.
+//
+// Both run one thread per particle in the working order (cell, x, id) and
+// walk the nine rows of the 27-cell stencil (sph_device.cuh), each cut to its
+// candidate window.  Each row's terms are summed in plain FP32 (a row holds a
+// handful of neighbours) and the row sums are added with Kahan compensation;
+// a row that contributes exactly nothing is not added, so the window cut
+// (which drops only zero terms) changes no result bit.
+//
+// The force stage comes in three forms that sum the same terms in the same
+// order:
+//   direct    -- distance test and pair interaction in one loop (the
+//                reference's structure); a warp runs the interaction whenever
+//                any lane's candidate is a neighbour;
+//   mask      -- a row is tested in chunks of up to 32 candidates into a
+//                register bit mask first, then only the set bits interact;
+//   pretested -- the density stage, which tests every candidate anyway,
+//                records each row's window start and a 32-bit neighbour mask;
+//                the force stage runs the interactions of the set bits only
+//                (rows longer than 32 candidates fall back to testing).
+#include "sph_device.cuh"
+
+namespace sph {
+
+// ---------------------------------------------------------------------------
+// Density + pressure (compute_particle_density_pressure,
+// particle_simulation.cu:196-256; compute_particle_density_cell :1385-1419).
+// Branch-free poly6 accumulation: max(h^2 - r^2, 0)^3.  Writes
+// (rho, p, p/rho^2, 1/rho) for the force stage.
+// ---------------------------------------------------------------------------
+struct RowMasks {
+    int* start;          // [9][n] window start, bit 31 set when the row was not masked
+    unsigned int* mask;  // [9][n] neighbour bits relative to start, or the window end
+};
+
+template <bool KAHAN, bool EMIT>
+__global__ void __launch_bounds__(256)
+k_density(int n, const float4* __restrict__ posS, RowTables T, GridDev g, PhysDev ph, MapDev map, int window,
+          float4* __restrict__ rho4S, RowMasks M) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 xi = posS[i];
+    const Stencil st = stencil(xi, ph.h, g);
+    const float h2 = ph.h2;
+    float sum = 0.f, comp = 0.f;
+#pragma unroll
+    for (int r = 0; r < 9; r++) {
+        int s, e;
+        row_range(xi, st, ph.h, g, T, window != 0, r, s, e);
+        float rs = 0.f;
+        unsigned int m = 0u, bit = 1u;
+        for (int t = s; t < e; t++) {
+            const float r2 = dist2(xi, __ldg(posS + t));
+            const float w = fmaxf(h2 - r2, 0.f);
+            rs = fmaf(w * w, w, rs);
+            if (EMIT) {
+                m |= (r2 <= h2 && r2 > 0.f) ? bit : 0u;
+                bit <<= 1;
+            }
+        }
+        if (KAHAN) {
+            if (rs > 0.f) kahan_add(sum, comp, rs);
+        } else {
+            sum += rs;
+        }
+        if (EMIT) {
+            const bool fits = e - s <= 32;
+            M.start[(size_t)r * n + i] = fits ? s : (s | (int)0x80000000);
+            M.mask[(size_t)r * n + i] = fits ? m : (unsigned int)e;
+        }
+    }
+    float rho = (KAHAN ? __fsub_rn(sum, comp) : sum) * ph.poly6m;
+    if (map.present) {
+        float uvw[3];
+        map_uvw(map, xi, uvw);
+        rho += tri_vec(map, uvw[0], uvw[1], uvw[2]).y;  // wall density, :242-248
+    }
+    const float p = ph.stiffness * (rho - ph.restDensity);
+    const float inv = 1.0f / rho;
+    rho4S[i] = make_float4(rho, p, p * inv * inv, inv);
+}
+
+// ---------------------------------------------------------------------------
+// Pair interaction (compute_viscosity_pressure_forces_and_ifsurf_cell,
+// :1459-1556), per-row partial sums, compensated totals.
+// ---------------------------------------------------------------------------
+template <bool TENSION>
+struct RowSums {
+    float fp[3], fv[3], cg[3], cl;
+    int hits;
+    __device__ __forceinline__ void clear() {
+#pragma unroll
+        for (int a = 0; a < 3; a++) fp[a] = fv[a] = cg[a] = 0.f;
+        cl = 0.f;
+        hits = 0;
+    }
+    __device__ __forceinline__ void add(const PhysDev& ph, float4 xi, float4 vi, float qi, float4 xj, float4 vj,
+                                        float4 rj) {
+        const float dx = __fsub_rn(xi.x, xj.x), dy = __fsub_rn(xi.y, xj.y), dz = __fsub_rn(xi.z, xj.z);
+        const float r2 = dist2(xi, xj);
+        const float rinv = rsqrtf(r2);
+        const float hr = ph.h - r2 * rinv;
+        const float sp = (qi + rj.z) * hr * hr * rinv;  // (p_i/rho_i^2 + p_j/rho_j^2)(h-r)^2/r
+        const float sv = rj.w * hr;                     // (h-r)/rho_j
+        fp[0] = fmaf(sp, dx, fp[0]);
+        fp[1] = fmaf(sp, dy, fp[1]);
+        fp[2] = fmaf(sp, dz, fp[2]);
+        fv[0] = fmaf(sv, vj.x - vi.x, fv[0]);
+        fv[1] = fmaf(sv, vj.y - vi.y, fv[1]);
+        fv[2] = fmaf(sv, vj.z - vi.z, fv[2]);
+        if (TENSION) {
+            const float d2 = ph.h2 - r2;
+            const float sc = rj.w * d2 * d2;
+            cg[0] = fmaf(sc, dx, cg[0]);
+            cg[1] = fmaf(sc, dy, cg[1]);
+            cg[2] = fmaf(sc, dz, cg[2]);
+            cl = fmaf(rj.w * d2, 3.f * ph.h2 - 7.f * r2, cl);
+        }
+        hits++;
+    }
+};
+
+template <bool KAHAN, bool TENSION>
+struct ForceTotals {
+    float fp[3] = {0.f, 0.f, 0.f}, cp[3] = {0.f, 0.f, 0.f};
+    float fv[3] = {0.f, 0.f, 0.f}, cv[3] = {0.f, 0.f, 0.f};
+    float cg[3] = {0.f, 0.f, 0.f}, cl = 0.f;
+    __device__ __forceinline__ void add(const RowSums<TENSION>& r) {
+        if (r.hits == 0) return;
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            if (KAHAN) {
+                kahan_add(fp[a], cp[a], r.fp[a]);
+                kahan_add(fv[a], cv[a], r.fv[a]);
+            } else {
+                fp[a] += r.fp[a];
+                fv[a] += r.fv[a];
+            }
+            if (TENSION) cg[a] += r.cg[a];
+        }
+        if (TENSION) cl += r.cl;
+    }
+};
+
+// Wall terms, surface tension, a = F/rho - g, symplectic Euler, box
+// collision, and the write-back (compute_particle_acceleration_ifsurf
+// :407-473, integrate_euler :632-665, collision_handling :742-834).  The wall
+// terms follow the reference's operation order exactly.
+template <bool KAHAN, bool TENSION>
+__device__ __forceinline__ void force_epilogue(const ForceTotals<KAHAN, TENSION>& A, int i, float4 xi,
+                                               float4 vi, float4 ri, const PhysDev& ph, const MapDev& map,
+                                               int collideFlag, const int* __restrict__ workIds,
+                                               float4* __restrict__ pos, float4* __restrict__ vel,
+                                               float4* __restrict__ accS) {
+    const float rho = ri.x;
+    const float pc = ph.pressCoef * rho;
+    float force[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const float P = KAHAN ? __fsub_rn(A.fp[a], A.cp[a]) : A.fp[a];
+        const float V = KAHAN ? __fsub_rn(A.fv[a], A.cv[a]) : A.fv[a];
+        force[a] = ph.viscCoef * V + pc * P;
+    }
+    bool tension = TENSION;
+    if (map.present) {
+        float uvw[3];
+        map_uvw(map, xi, uvw);
+        const float4 s = tri_vec(map, uvw[0], uvw[1], uvw[2]);
+        const float distWall = -s.x;
+        if (distWall < map.restDistance) {
+            tension = false;
+            const float coeff = rho / (ph.dtCollide * ph.dtCollide) * (map.restDistance - distWall);
+            float gN[3];
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                float up[3] = {uvw[0], uvw[1], uvw[2]}, dn[3] = {uvw[0], uvw[1], uvw[2]};
+                up[a] = __fadd_rn(uvw[a], map.du[a]);
+                dn[a] = __fsub_rn(uvw[a], map.du[a]);
+                gN[a] = __fdiv_rn(__fsub_rn(tri_scalar(map, map.dist, up[0], up[1], up[2]),
+                                            tri_scalar(map, map.dist, dn[0], dn[1], dn[2])),
+                                  __fmul_rn(2.f, map.du[a]));
+            }
+            force[0] -= coeff * gN[0];
+            force[1] -= coeff * gN[1];
+            force[2] -= coeff * gN[2];
+            force[0] -= vi.x * s.z;
+            force[1] -= vi.y * s.z;
+            force[2] -= vi.z * s.z;
+        }
+    }
+    if (TENSION && tension) {
+        const float cgx = ph.cgCoef * A.cg[0], cgy = ph.cgCoef * A.cg[1], cgz = ph.cgCoef * A.cg[2];
+        const float norm = sqrtf(cgx * cgx + cgy * cgy + cgz * cgz);
+        if (norm > ph.normThresh) {
+            const float fc = ph.tension * (ph.clCoef * A.cl) / norm;
+            force[0] -= fc * cgx;
+            force[1] -= fc * cgy;
+            force[2] -= fc * cgz;
+        }
+    }
+    float acc[3] = {force[0] / rho, force[1] / rho, force[2] / rho};
+    acc[0] -= ph.gravityAxis == 0 ? ph.gravity : 0.f;
+    acc[1] -= ph.gravityAxis == 1 ? ph.gravity : 0.f;
+    acc[2] -= ph.gravityAxis == 2 ? ph.gravity : 0.f;
+    float3 v = make_float3(vi.x + ph.dt * acc[0], vi.y + ph.dt * acc[1], vi.z + ph.dt * acc[2]);
+    float3 x = make_float3(xi.x + ph.dt * v.x, xi.y + ph.dt * v.y, xi.z + ph.dt * v.z);
+    if (collideFlag) collide(ph, x, v);
+    const int id = workIds[i];
+    pos[id] = make_float4(x.x, x.y, x.z, 0.f);
+    vel[id] = make_float4(v.x, v.y, v.z, 0.f);
+    accS[i] = make_float4(acc[0], acc[1], acc[2], 0.f);
+}
+
+struct ForceArgs {
+    int n;
+    const float4* posS;
+    const float4* velS;
+    const float4* rho4S;
+    const int* workIds;
+    RowTables T;
+    GridDev g;
+    PhysDev ph;
+    MapDev map;
+    int collide;
+    int window;
+    RowMasks M;
+    float4* pos;
+    float4* vel;
+    float4* accS;
+};
+
+template <bool KAHAN, bool TENSION, int FORM>
+__global__ void __launch_bounds__(256, 2) k_force(ForceArgs F) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= F.n) return;
+    const float4 xi = F.posS[i];
+    const float4 vi = F.velS[i];
+    const float4 ri = F.rho4S[i];
+    const float h2 = F.ph.h2;
+    Stencil st;
+    if (FORM != FORCE_PRETESTED) st = stencil(xi, F.ph.h, F.g);
+    ForceTotals<KAHAN, TENSION> A;
+    auto direct = [&](RowSums<TENSION>& R, int s, int e) {
+        for (int t = s; t < e; t++) {
+            const float4 xj = __ldg(F.posS + t);
+            const float r2 = dist2(xi, xj);
+            if (r2 <= h2 && r2 > 0.f) R.add(F.ph, xi, vi, ri.z, xj, __ldg(F.velS + t), __ldg(F.rho4S + t));
+        }
+    };
+    auto bits = [&](RowSums<TENSION>& R, int base, unsigned int m) {
+        while (m) {
+            const int t = base + __ffs(m) - 1;
+            m &= m - 1u;
+            R.add(F.ph, xi, vi, ri.z, __ldg(F.posS + t), __ldg(F.velS + t), __ldg(F.rho4S + t));
+        }
+    };
+#pragma unroll
+    for (int r = 0; r < 9; r++) {
+        RowSums<TENSION> R;
+        R.clear();
+        if (FORM == FORCE_PRETESTED) {
+            const int sv = __ldg(F.M.start + (size_t)r * F.n + i);
+            const unsigned int m = __ldg(F.M.mask + (size_t)r * F.n + i);
+            if (sv < 0) direct(R, sv & 0x7fffffff, (int)m);
+            else bits(R, sv, m);
+        } else {
+            int s, e;
+            row_range(xi, st, F.ph.h, F.g, F.T, F.window != 0, r, s, e);
+            if (FORM == FORCE_DIRECT) {
+                direct(R, s, e);
+            } else {
+                for (int base = s; base < e; base += 32) {
+                    const int cnt = min(32, e - base);
+                    unsigned int m = 0u;
+                    for (int k = 0; k < cnt; k++) {
+                        const float r2 = dist2(xi, __ldg(F.posS + base + k));
+                        m |= (r2 <= h2 && r2 > 0.f) ? (1u << k) : 0u;
+                    }
+                    bits(R, base, m);
+                }
+            }
+        }
+        A.add(R);
+    }
+    force_epilogue(A, i, xi, vi, ri, F.ph, F.map, F.collide, F.workIds, F.pos, F.vel, F.accS);
+}
+
+// ---------------------------------------------------------------------------
+// Launchers
+// ---------------------------------------------------------------------------
+void launch_density(int n, const float4* posS, RowTables T, GridDev g, PhysDev ph, MapDev map, float4* rho4S,
+                    int* rowStart, unsigned int* rowMask, const StepConfig& cfg, cudaStream_t s) {
+    if (n <= 0) return;
+    const int bs = cfg.densityBlock > 0 ? cfg.densityBlock : 128;
+    const int grid = (n + bs - 1) / bs;
+    const RowMasks M{rowStart, rowMask};
+    const bool emit = cfg.forceVariant == FORCE_PRETESTED;
+    if (cfg.kahan) {
+        if (emit) k_density<true, true><<<grid, bs, 0, s>>>(n, posS, T, g, ph, map, cfg.prune, rho4S, M);
+        else k_density<true, false><<<grid, bs, 0, s>>>(n, posS, T, g, ph, map, cfg.prune, rho4S, M);
+    } else {
+        if (emit) k_density<false, true><<<grid, bs, 0, s>>>(n, posS, T, g, ph, map, cfg.prune, rho4S, M);
+        else k_density<false, false><<<grid, bs, 0, s>>>(n, posS, T, g, ph, map, cfg.prune, rho4S, M);
+    }
+}
+
+template <bool KAHAN, bool TENSION>
+static void force_dispatch(const ForceArgs& F, const StepConfig& cfg, cudaStream_t s) {
+    const int bs = cfg.forceBlock > 0 ? cfg.forceBlock : 128;
+    const int grid = (F.n + bs - 1) / bs;
+    if (cfg.forceVariant == FORCE_PRETESTED) k_force<KAHAN, TENSION, FORCE_PRETESTED><<<grid, bs, 0, s>>>(F);
+    else if (cfg.forceVariant == FORCE_MASK) k_force<KAHAN, TENSION, FORCE_MASK><<<grid, bs, 0, s>>>(F);
+    else k_force<KAHAN, TENSION, FORCE_DIRECT><<<grid, bs, 0, s>>>(F);
+}
+
+void launch_force(int n, const float4* posS, const float4* velS, const float4* rho4S, const int* workIds,
+                  RowTables T, GridDev g, PhysDev ph, MapDev map, int collide, const int* rowStart,
+                  const unsigned int* rowMask, float4* pos, float4* vel, float4* accS, const StepConfig& cfg,
+                  cudaStream_t s) {
+    if (n <= 0) return;
+    ForceArgs F{n,  posS, velS, rho4S, workIds, T, g, ph, map, collide, cfg.prune,
+                RowMasks{const_cast<int*>(rowStart), const_cast<unsigned int*>(rowMask)}, pos, vel, accS};
+    const bool tension = ph.tension != 0.0f;
+    if (cfg.kahan) {
+        if (tension) force_dispatch<true, true>(F, cfg, s);
+        else force_dispatch<true, false>(F, cfg, s);
+    } else {
+        if (tension) force_dispatch<false, true>(F, cfg, s);
+        else force_dispatch<false, false>(F, cfg, s);
+    }
+}
+
+}  // namespace sph

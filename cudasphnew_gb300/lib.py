@@ -44,6 +44,9 @@ SIGNATURES = {
     "sph_device_pointer": (_i, [_vp, _i, _vp]),
     "sph_boundary_dims": (_i, [_vp, _vp]),
     "sph_boundary_maps": (_i, [_vp, _vp, _vp, _vp]),
+    "sph_get_tuning": (_i, [_vp, _vp]),
+    "sph_set_tuning": (_i, [_vp, _vp]),
+    "sph_autotune": (_i, [_vp, _i, _vp]),
     "sph_set_stage_timing": (_i, [_vp, _i]),
     "sph_stage_times": (_i, [_vp, _vp, _vp, _i, _vp]),
     "sph_stage_name": (ctypes.c_char_p, [_i]),
@@ -56,6 +59,14 @@ class Counts(ctypes.Structure):
     _fields_ = [(name, ctypes.c_uint) for name in (
         "numParticles", "numParticlesDefault", "numParticlesSplit", "numParticlesBoundary",
         "numSubParticles", "numTimeSteps", "numCells", "numSubCells")]
+
+
+class Tuning(ctypes.Structure):
+    _fields_ = [(name, ctypes.c_int) for name in (
+        "densityBlock", "forceBlock", "forceVariant", "prune", "kahan")]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
 
 
 class SphError(RuntimeError):
@@ -233,6 +244,22 @@ class ParticleSimulation:
 
     def set_stream(self, stream_handle: int | None) -> None:
         check(load().sph_set_stream(self._h, ctypes.c_void_p(stream_handle or 0)))
+
+    def tuning(self) -> Tuning:
+        t = Tuning()
+        check(load().sph_get_tuning(self._h, ctypes.byref(t)))
+        return t
+
+    def set_tuning(self, **kw) -> None:
+        t = self.tuning()
+        for k, v in kw.items():
+            setattr(t, k, int(v))
+        check(load().sph_set_tuning(self._h, ctypes.byref(t)))
+
+    def autotune(self, reps: int = 5) -> Tuning:
+        t = Tuning()
+        check(load().sph_autotune(self._h, int(reps), ctypes.byref(t)))
+        return t
 
     def set_stage_timing(self, capacity_steps: int) -> None:
         check(load().sph_set_stage_timing(self._h, int(capacity_steps)))

@@ -218,6 +218,30 @@ sph_status sph_boundary_dims(const sph_boundary_desc* desc, unsigned int dims[3]
 sph_status sph_boundary_maps(const sph_boundary_desc* desc, float* distance,
                              float* density, float* viscosity);
 
+/* Launch configuration of the step's neighbour kernels.  None of these
+ * fields changes a result bit: pruned stencil cells hold no particle within
+ * the support radius, and both force forms sum the same terms in the same
+ * order.  (kahan selects compensated summation, which does change rounding,
+ * and is never altered by the autotuner.)  No reference counterpart: the
+ * reference hard-codes 256 threads per block (particle_simulation.cu:2943-2957). */
+typedef struct sph_tuning {
+    int densityBlock;  /* 64, 128 or 256 */
+    int forceBlock;    /* 64, 128 or 256 */
+    int forceVariant;  /* 0: direct loop, 1: per-chunk hit mask, then interactions,
+                          2: neighbour masks recorded by the density stage */
+    int prune;         /* 1: cut stencil rows to the half-cells within reach of h */
+    int kahan;         /* 1: compensated density and force sums */
+} sph_tuning;
+
+sph_status sph_get_tuning(sph_handle h, sph_tuning* out);
+sph_status sph_set_tuning(sph_handle h, const sph_tuning* t);
+
+/* Times every candidate launch configuration of the density and force
+ * kernels on the handle's current particle state (`reps` launches each, CUDA
+ * events on the handle's stream), keeps the fastest and returns it.  The
+ * simulation state is left untouched.  No reference counterpart. */
+sph_status sph_autotune(sph_handle h, int reps, sph_tuning* chosen);
+
 /* Stage timing with CUDA events on the handle's stream (CudaTimer,
  * util.cpp:6-41, generalised to every stage).  After enabling, each step
  * records events between its stages; sph_stage_times() returns the summed

@@ -180,10 +180,28 @@ def test_boundary_maps_match_oracle(sphlib, orc, name):
     np.testing.assert_allclose(visc, bm.visc, rtol=1e-6, atol=1e-6 * float(bm.visc.max()))
 
 
-def test_out_of_domain_is_reported(sphlib):
+def test_far_particle_wraps_like_the_reference(sphlib, orc):
+    """compute_particle_hash wraps coordinates beyond the grid with `% dim`
+    (particle_simulation.cu:108-112): no error, same cell as the reference."""
     sc = SCENES["tiny"]()
     pos = sc.positions.copy()
-    pos[3] = (5.0, 5.0, 5.0)  # beyond the padded grid
+    pos[3] = (5.0, 5.0, 5.0)
+    with sphlib.ParticleSimulation(sc.params, pos, options=sc.options) as sim:
+        sim.Advance()
+        sim.synchronize()
+        h, ids, start, end = sim.cells()
+    r = orc.hash_sort_cells(sc.params, pos)
+    np.testing.assert_array_equal(h, r[0])
+    np.testing.assert_array_equal(ids, r[1])
+
+
+def test_out_of_domain_is_reported(sphlib):
+    """Far below the origin the truncated coordinate is negative and so is the
+    hash: the reference would write outside its cell table; here the step
+    clamps the write and reports SPH_ERR_OUT_OF_DOMAIN."""
+    sc = SCENES["tiny"]()
+    pos = sc.positions.copy()
+    pos[3] = (-5.0, -5.0, -5.0)
     with sphlib.ParticleSimulation(sc.params, pos, options=sc.options) as sim:
         sim.Advance()
         with pytest.raises(sphlib.SphError) as e:
@@ -235,3 +253,50 @@ def test_full_size_one_step(sphlib, orc):
     # size-independent properties
     assert np.array_equal(np.sort(g["ids"]), np.arange(sc.n))
     assert (np.diff(g["hash"]) >= 0).all()
+
+
+@pytest.mark.parametrize("kahan", [0, 1])
+def test_tunings_are_bit_identical(sphlib, kahan):
+    """Block sizes, the force form and stencil pruning change no result bit."""
+    sc = obstacle_block()
+    configs = [dict(forceVariant=0, prune=0, forceBlock=128, densityBlock=128),
+               dict(forceVariant=1, prune=1, forceBlock=64, densityBlock=256),
+               dict(forceVariant=1, prune=0, forceBlock=256, densityBlock=64),
+               dict(forceVariant=0, prune=1, forceBlock=256, densityBlock=128),
+               dict(forceVariant=2, prune=1, forceBlock=128, densityBlock=128),
+               dict(forceVariant=2, prune=0, forceBlock=64, densityBlock=64)]
+    outs = []
+    for cfg in configs:
+        with sphlib.ParticleSimulation(sc.params, sc.positions, sc.velocities, sc.options,
+                                       sc.boundary) as sim:
+            sim.set_tuning(kahan=kahan, **cfg)
+            for _ in range(3):
+                sim.Advance()
+            outs.append([sim.read(sphlib.FIELD_DENSITY), sim.read(sphlib.FIELD_ACCELERATION),
+                         sim.positions(), sim.velocities()])
+    for o in outs[1:]:
+        for a, b in zip(outs[0], o):
+            np.testing.assert_array_equal(a, b)
+
+
+def test_autotune_leaves_state_untouched(sphlib):
+    sc = scenes.config1()
+    with sphlib.ParticleSimulation(sc.params, sc.positions, sc.velocities, sc.options) as sim, \
+            sphlib.ParticleSimulation(sc.params, sc.positions, sc.velocities, sc.options) as ref:
+        for _ in range(3):
+            sim.Advance()
+            ref.Advance()
+        before = [sim.read(f) for f in (sphlib.FIELD_DENSITY, sphlib.FIELD_ACCELERATION,
+                                        sphlib.FIELD_VERTEX_DATA, sphlib.FIELD_VELOCITY)]
+        cells_before = sim.cells()
+        t = sim.autotune(reps=2)
+        assert t.densityBlock in (64, 128, 256) and t.forceVariant in (0, 1, 2)
+        after = [sim.read(f) for f in (sphlib.FIELD_DENSITY, sphlib.FIELD_ACCELERATION,
+                                       sphlib.FIELD_VERTEX_DATA, sphlib.FIELD_VELOCITY)]
+        for a, b in zip(before, after):
+            np.testing.assert_array_equal(a, b)
+        for a, b in zip(cells_before, sim.cells()):
+            np.testing.assert_array_equal(a, b)
+        sim.Advance()
+        ref.Advance()
+        np.testing.assert_array_equal(sim.positions(), ref.positions())
