@@ -119,3 +119,13 @@ def test_missing_library_fails_loudly(tmp_path):
             sphmod.load(str(tmp_path / "nope.so"))
         finally:
             sphmod._lib = sphmod._lib_backup
+
+
+def test_cpp_header_compiles_and_links(sphlib, tmp_path):
+    """include/particle_simulation.h builds a program that links the library."""
+    src = os.path.join(ROOT, "tests", "cpp", "example01_driver.cpp")
+    exe = tmp_path / "example01_driver"
+    libdir = os.path.dirname(sphlib.LIB_PATH)
+    subprocess.run(["g++", "-std=c++17", "-O1", "-I", os.path.join(ROOT, "include"), src, "-o", str(exe),
+                    "-L", libdir, "-lsph_gb300", f"-Wl,-rpath,{libdir}"], check=True)
+    assert exe.exists()
