@@ -50,6 +50,14 @@ cudaError_t dalloc(T** p, size_t count) {
 
 }  // namespace
 
+namespace sph {
+// Records a failure in the per-thread message sph_last_error() returns, for
+// entry points defined in other translation units.
+sph_status record_error(sph_status st, const char* file, int line, const std::string& msg) {
+    return fail(st, file, line, msg);
+}
+}  // namespace sph
+
 struct sph_sim {
     SimulationParameters P;
     sph_options O;

@@ -50,6 +50,7 @@ SIGNATURES = {
     "sph_set_stage_timing": (_i, [_vp, _i]),
     "sph_stage_times": (_i, [_vp, _vp, _vp, _i, _vp]),
     "sph_stage_name": (ctypes.c_char_p, [_i]),
+    "sph_cell_tables_noalloc": (_i, [_vp, _vp, _u, _vp, _vp, _vp, _vp, _vp]),
     "sph_last_error": (ctypes.c_char_p, []),
     "sph_status_string": (ctypes.c_char_p, [_i]),
 }

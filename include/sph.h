@@ -250,6 +250,35 @@ sph_status sph_set_stage_timing(sph_handle h, int enable);
 sph_status sph_stage_times(sph_handle h, float* ms, int* counts, int capacity, int* numStages);
 const char* sph_stage_name(int stage);
 
+/* Largest inputs sph_cell_tables_noalloc() accepts. */
+#define SPH_NOALLOC_MAX_PARTICLES 65536
+#define SPH_NOALLOC_MAX_CELLS 262144
+
+/* The neighbour-search tables of one set of positions -- sorted hashes, the
+ * sort permutation, and cell start/end with 0xFFFFFFFF for empty cells, as
+ * sph_step() + sph_read_cells() give them -- built without allocating any
+ * memory, for callers that cannot call cudaMalloc where they need the tables
+ * (a frame loop an allocation would stall, or an application whose device
+ * memory is all handed to its own allocator).  No counterpart in the
+ * reference; it follows computeParticleHash, sortParticleIdsByHash and
+ * computeCellStartEndList (particle_simulation.cu:2320-2369).
+ *
+ * Inputs and outputs are device pointers the caller owns: devVertexData
+ * float[n*3] (the VD layout), devSortedHash and devSortedIds int[n],
+ * devCellStart and devCellEnd int[gridDim[0]*gridDim[1]*gridDim[2]].  All
+ * intermediate data lives in one fixed device array of about 2.9 MB that the
+ * library holds on every GPU it runs on until the process exits; n above
+ * SPH_NOALLOC_MAX_PARTICLES or more cells than SPH_NOALLOC_MAX_CELLS are
+ * rejected with SPH_ERR_INVALID_ARGUMENT.  Calls share that array: calls whose
+ * work overlaps on the GPU race and must be serialised by the caller.  The
+ * first call on a device looks the array up for that device; make it before
+ * capturing work on that device into a CUDA graph.  The call enqueues its
+ * work on `stream` (a cudaStream_t, NULL for the default stream) and returns
+ * once that work is done. */
+sph_status sph_cell_tables_noalloc(const SimulationParameters* params, const float* devVertexData,
+                                   unsigned int n, int* devSortedHash, int* devSortedIds,
+                                   int* devCellStart, int* devCellEnd, void* stream);
+
 /* Human-readable message of the last failing call on this thread, in the
  * reference's "Exception thrown in FILE: ... LINE: ..." shape (util.h:24-39). */
 const char* sph_last_error(void);
