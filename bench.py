@@ -34,6 +34,10 @@ L2_BYTES = 129 * 1024 * 1024
 # (16+16+16+4), writes position, velocity and acceleration float4s (3*16).
 FORCE_BYTES_PER_PARTICLE = 100
 # Per launch it also reads the (C+1)-entry cell-offset table once (4 B/cell).
+# DRAM bytes (read + write) of one k_force launch of the 1,048,576-particle
+# obstacle scene, pretested form, measured with ncu (dram__bytes_read.sum +
+# dram__bytes_write.sum).  Other scenes report no traffic figure.
+FORCE_DRAM_BYTES_1M = 130.137088e6 + 29.085440e6
 
 
 def parse():
@@ -44,6 +48,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="config2")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the library's default launch shapes (for profiling runs)")
     return ap.parse_args()
 
 
@@ -243,7 +249,10 @@ def run_ours(args):
     clocks.start()
     sim.step(count=max(args.warmup, 3))
     sim.synchronize()
-    tuning = sim.autotune(reps=5).as_dict()  # launch shapes; state untouched
+    if args.no_autotune:
+        tuning = sim.tuning().as_dict()
+    else:
+        tuning = sim.autotune(reps=5).as_dict()  # launch shapes; state untouched
     sim.step(count=3)  # re-capture the step graph with the chosen shapes
     sim.synchronize()
 
@@ -319,7 +328,8 @@ def run_ours(args):
                    "d2h_bytes_per_step": n * 12, "steps": e2e_steps,
                    "path": "sph_write(VD, VEL) + sph_step + sph_read(VD), pinned host buffers"},
            "roofline": {"bound": "hbm", "kernel": "k_force", "achieved": achieved, "peak": peak,
-                        "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                        "unit": "GB/s", "frac": achieved / peak,
+                        "traffic": FORCE_DRAM_BYTES_1M if (n == 1048576 and tuning["forceVariant"] == 2) else None,
                         "peak_source": peak_kind,
                         "algorithmic_bytes_per_launch": alg,
                         "avg_launch_us": force_avg_s * 1e6},
