@@ -89,10 +89,17 @@ struct sph_sim {
     // launch configuration
     StepConfig cfg;
 
-    // CUDA graph of one plain step
+    // two-scale pass (allocated on first use)
+    TwoScaleDev ts{};
+    SortBuffers subSb{};
+    unsigned long long* subScanBlock = nullptr;
+    bool tsReady = false;
+
+    // CUDA graph of one step of graphMode
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graphExec = nullptr;
     bool graphValid = false;
+    int graphMode = -1;
 
     // stage timing ring
     int timingCap = 0, timingNext = 0, timingFilled = 0;
@@ -193,12 +200,103 @@ void free_all(sph_sim* s) {
                     s->status, s->staging, s->map4, s->mapDist, s->rowStart, s->rowMask};
     for (void* p : ptrs)
         if (p) cudaFree(p);
+    void* tsPtrs[] = {s->ts.state,     s->ts.blockCounts, s->ts.blockOffsets, s->ts.counts,
+                      s->ts.splitIds,  s->ts.boundaryIds, s->ts.defaultIds,  s->ts.subIds,
+                      s->ts.subPos,    s->ts.subVel,      s->ts.subAcc,      s->ts.subRho,
+                      s->ts.subCnt,    s->ts.subOffset,   s->ts.subKeySlot,  s->ts.subTmp,
+                      s->ts.subSortedHash, s->ts.subSortedIds, s->subScanBlock};
+    for (void* p : tsPtrs)
+        if (p) cudaFree(p);
     if (s->statusHost) cudaFreeHost(s->statusHost);
     if (s->ownStream) cudaStreamDestroy(s->ownStream);
 }
 
-// Enqueues the plain step's stages (no host synchronisation).
-void enqueue_plain(sph_sim* s, bool timing) {
+PhysDev make_sub_phys(const SimulationParameters& P, const sph_options& O) {
+    PhysDev ph = make_phys(P, O);
+    ph.h = P.compactSupportSub;
+    ph.h2 = P.compactSupportSub * P.compactSupportSub;
+    ph.poly6m = P.poly6Sub * P.subParticleMass;
+    ph.mass = P.subParticleMass;
+    ph.pressCoef = -P.subParticleMass * P.gradSpikySub;
+    ph.viscCoef = P.dynamicViscosity * P.subParticleMass * P.laplViscSub;
+    ph.cgCoef = P.subParticleMass * P.gradPoly6Sub;
+    ph.clCoef = P.subParticleMass * P.laplPoly6Sub;
+    ph.dt = P.timeStepSubParticles;
+    ph.dtCollide = P.timeStep;  // collision_handling_sub_particles uses the coarse step (:916)
+    return ph;
+}
+
+// Allocates the two-scale state on first use: 8n child slots and the fine
+// level's counting-sort buffers.
+sph_status ensure_two_scale(sph_sim* s) {
+    if (s->tsReady) return SPH_OK;
+    const size_t n = (size_t)s->n;
+    const size_t n4 = (n + 3) & ~(size_t)3;
+    const size_t nb = (n + 1023) / 1024;
+    const size_t Cs = (size_t)s->P.gridDimSubParticles[0] * s->P.gridDimSubParticles[1] * s->P.gridDimSubParticles[2];
+    const size_t tiles = (Cs + 1 + SCAN_TILE - 1) / SCAN_TILE;
+    TwoScaleDev& T = s->ts;
+    SPH_CUDA(dalloc(&T.state, n4));
+    SPH_CUDA(dalloc(&T.blockCounts, 3 * nb));
+    SPH_CUDA(dalloc(&T.blockOffsets, 3 * nb));
+    SPH_CUDA(dalloc(&T.counts, 4));
+    SPH_CUDA(dalloc(&T.splitIds, n));
+    SPH_CUDA(dalloc(&T.boundaryIds, n));
+    SPH_CUDA(dalloc(&T.defaultIds, n));
+    SPH_CUDA(dalloc(&T.subIds, 8 * n));
+    SPH_CUDA(dalloc(&T.subPos, 8 * n));
+    SPH_CUDA(dalloc(&T.subVel, 8 * n));
+    SPH_CUDA(dalloc(&T.subAcc, 8 * n));
+    SPH_CUDA(dalloc(&T.subRho, 8 * n));
+    SPH_CUDA(dalloc(&T.subCnt, Cs + 1 + SCAN_TILE));
+    SPH_CUDA(dalloc(&T.subOffset, Cs + 1 + SCAN_TILE));
+    SPH_CUDA(dalloc(&T.subKeySlot, 8 * n));
+    SPH_CUDA(dalloc(&T.subTmp, 8 * n));
+    SPH_CUDA(dalloc(&T.subSortedHash, 8 * n));
+    SPH_CUDA(dalloc(&T.subSortedIds, 8 * n));
+    SPH_CUDA(dalloc(&s->subScanBlock, tiles + 2));
+    cudaStream_t q = s->stream;
+    SPH_CUDA(cudaMemsetAsync(T.state, 0, n4, q));
+    SPH_CUDA(cudaMemsetAsync(T.counts, 0, sizeof(int) * 4, q));
+    SPH_CUDA(cudaMemsetAsync(T.subPos, 0, sizeof(float4) * 8 * n, q));
+    SPH_CUDA(cudaMemsetAsync(T.subVel, 0, sizeof(float4) * 8 * n, q));
+    SPH_CUDA(cudaMemsetAsync(T.subAcc, 0, sizeof(float4) * 8 * n, q));
+    SPH_CUDA(cudaMemsetAsync(T.subRho, 0, sizeof(float2) * 8 * n, q));
+    SPH_CUDA(cudaMemsetAsync(T.subCnt, 0, sizeof(int) * (Cs + 1 + SCAN_TILE), q));
+    SPH_CUDA(cudaMemsetAsync(T.subOffset, 0, sizeof(int) * (Cs + 1 + SCAN_TILE), q));
+    for (int a = 0; a < 3; a++) {
+        T.splitMin[a] = s->O.splitMin[a];
+        T.splitMax[a] = s->O.splitMax[a];
+    }
+    s->subSb.cnt = T.subCnt;
+    s->subSb.cellOffset = T.subOffset;
+    s->subSb.tileCounter = reinterpret_cast<unsigned int*>(s->subScanBlock);
+    s->subSb.scanFlags = s->subScanBlock + 2;
+    s->subSb.maxTiles = (int)tiles;
+    SPH_CUDA(cudaStreamSynchronize(q));
+    s->tsReady = true;
+    return SPH_OK;
+}
+
+// Enqueues one step of `mode` (no host synchronisation).
+void enqueue_step(sph_sim* s, int mode, bool timing) {
+    if (mode == SPH_STEP_SUB_ONLY) {
+        if (!s->tsReady) return;
+        // AdvanceSubParticles (:2119-2143) on the current lists
+        cudaStream_t st = s->stream;
+        const int cap = 8 * s->n;
+        GridDev sg = make_grid(s->P, true);
+        PhysDev sph = make_sub_phys(s->P, s->O);
+        launch_ts_sub_sort(sg, s->ts, s->subSb, cap, s->status, st);
+        launch_ts_sub_density(sg, sph, s->ts, cap, st);
+        if (s->stepped)
+            launch_ts_project(s->pos, s->sb.workIds, 1, s->rho4S, s->sb.cellOffset, make_grid(s->P, false),
+                              s->P.compactSupportSub, s->ts, cap, st);
+        launch_ts_sub_force(sg, sph, s->ts, cap, st);
+        launch_ts_sub_integrate(sph, s->ts, cap, st);
+        return;
+    }
+    const bool twoScale = mode == SPH_STEP_TWO_SCALE;
     cudaStream_t st = s->stream;
     const int n = s->n;
     GridDev g = make_grid(s->P, false);
@@ -223,10 +321,29 @@ void enqueue_plain(sph_sim* s, bool timing) {
     mark(ST_DENSITY);
     // density and forces read the sorted copies only
     launch_density(n, s->posS, rows_of(s), g, ph, s->map, s->rho4S, s->rowStart, s->rowMask, s->cfg, st);
+    if (twoScale) {
+        // computeParticleState, collect, initializeSubParticles, projectQuantities
+        // (:2157-2160) from the pre-integration sorted state
+        launch_ts_states(n, s->posS, s->sb.workIds, s->sb.cellOffset, g, s->P.compactSupport, s->ts, st);
+        launch_ts_children(n, s->posS, s->velS, s->rho4S, s->sb.workIds, s->P.particleMass, s->ts, st);
+        launch_ts_project(s->posS, s->sb.workIds, 0, s->rho4S, s->sb.cellOffset, g, s->P.compactSupportSub,
+                          s->ts, 8 * n, st);
+    }
     mark(ST_FORCE);
+    // AdvanceTwoScale always runs handleCollisions (:2170)
     launch_force(n, s->posS, s->velS, s->rho4S, s->sb.workIds, rows_of(s), g, ph, s->map,
-                 s->O.boxCollision, s->rowStart, s->rowMask, s->pos, s->vel, s->accS, s->cfg, st);
+                 twoScale ? 1 : s->O.boxCollision, s->rowStart, s->rowMask, s->pos, s->vel, s->accS, s->cfg, st);
     mark(ST_COUNT);
+    if (twoScale) {
+        // the fine level (:2162-2171)
+        const int cap = 8 * n;
+        GridDev sg = make_grid(s->P, true);
+        PhysDev sph = make_sub_phys(s->P, s->O);
+        launch_ts_sub_sort(sg, s->ts, s->subSb, cap, s->status, st);
+        launch_ts_sub_density(sg, sph, s->ts, cap, st);
+        launch_ts_sub_force(sg, sph, s->ts, cap, st);
+        launch_ts_sub_integrate(sph, s->ts, cap, st);
+    }
 }
 
 sph_status latched_status(sph_sim* s) {
@@ -452,20 +569,34 @@ sph_status sph_set_stream(sph_handle s, void* stream) {
 
 sph_status sph_step(sph_handle s, int mode) {
     if (!s) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "handle is NULL");
-    if (mode != SPH_STEP_PLAIN)
-        SPH_FAIL(SPH_ERR_NOT_SUPPORTED, "step mode not available in this build");
-    enqueue_plain(s, s->timingCap > 0);
+    if (mode < SPH_STEP_PLAIN || mode > SPH_STEP_SUB_ONLY) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "unknown step mode");
+    if (mode != SPH_STEP_PLAIN) {
+        sph_status st = ensure_two_scale(s);
+        if (st) return st;
+    }
+    enqueue_step(s, mode, mode != SPH_STEP_SUB_ONLY && s->timingCap > 0);
     SPH_CUDA(cudaGetLastError());
-    s->numTimeSteps++;
-    s->stepped = true;
+    if (mode != SPH_STEP_SUB_ONLY) {
+        s->numTimeSteps++;
+        s->stepped = true;
+    }
     return SPH_OK;
 }
 
 sph_status sph_step_many(sph_handle s, int mode, int count) {
     if (!s) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "handle is NULL");
-    if (mode != SPH_STEP_PLAIN)
-        SPH_FAIL(SPH_ERR_NOT_SUPPORTED, "step mode not available in this build");
+    if (mode < SPH_STEP_PLAIN || mode > SPH_STEP_SUB_ONLY) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "unknown step mode");
     if (count <= 0) return SPH_OK;
+    if (mode != SPH_STEP_PLAIN) {
+        sph_status st = ensure_two_scale(s);
+        if (st) return st;
+    }
+    if (mode == SPH_STEP_SUB_ONLY && !s->stepped) {
+        for (int i = 0; i < count; i++) enqueue_step(s, mode, false);
+        SPH_CUDA(cudaGetLastError());
+        return SPH_OK;
+    }
+    if (s->graphMode != mode) s->graphValid = false;
     if (s->timingCap > 0) {
         for (int i = 0; i < count; i++) {
             sph_status st = sph_step(s, mode);
@@ -479,17 +610,20 @@ sph_status sph_step_many(sph_handle s, int mode, int count) {
         s->graphExec = nullptr;
         s->graph = nullptr;
         SPH_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
-        enqueue_plain(s, false);
+        enqueue_step(s, mode, false);
         cudaGraph_t g = nullptr;
         cudaError_t e = cudaStreamEndCapture(s->stream, &g);
         SPH_CUDA(e);
         s->graph = g;
         SPH_CUDA(cudaGraphInstantiate(&s->graphExec, s->graph, 0));
         s->graphValid = true;
+        s->graphMode = mode;
     }
     for (int i = 0; i < count; i++) SPH_CUDA(cudaGraphLaunch(s->graphExec, s->stream));
-    s->numTimeSteps += (unsigned int)count;
-    s->stepped = true;
+    if (mode != SPH_STEP_SUB_ONLY) {
+        s->numTimeSteps += (unsigned int)count;
+        s->stepped = true;
+    }
     return SPH_OK;
 }
 
@@ -498,8 +632,70 @@ sph_status sph_synchronize(sph_handle s) {
     return latched_status(s);
 }
 
+namespace {
+
+// Device-side two-scale counts: split, boundary, default, children.
+sph_status two_scale_counts(sph_sim* s, int out[4]) {
+    out[0] = out[1] = out[3] = 0;
+    out[2] = s->n;
+    if (!s->tsReady) return SPH_OK;
+    SPH_CUDA(cudaMemcpyAsync(out, s->ts.counts, sizeof(int) * 4, cudaMemcpyDeviceToHost, s->stream));
+    SPH_CUDA(cudaStreamSynchronize(s->stream));
+    return SPH_OK;
+}
+
+// Fields of the two-scale pass (states, lists, child slots).
+sph_status read_two_scale(sph_sim* s, int field, void* dst, size_t bytes) {
+    const size_t n = (size_t)s->n;
+    int c[4];
+    sph_status st = two_scale_counts(s, c);
+    if (st) return st;
+    cudaStream_t q = s->stream;
+    size_t need = 0;
+    const void* src = nullptr;
+    switch (field) {
+        case SPH_FIELD_STATE: need = n; src = s->ts.state; break;
+        case SPH_FIELD_SUB_IDS: need = sizeof(int) * (size_t)c[3]; src = s->ts.subIds; break;
+        case SPH_FIELD_SPLIT_IDS: need = sizeof(int) * (size_t)c[0]; src = s->ts.splitIds; break;
+        case SPH_FIELD_BOUNDARY_IDS: need = sizeof(int) * (size_t)c[1]; src = s->ts.boundaryIds; break;
+        case SPH_FIELD_DEFAULT_IDS: need = sizeof(int) * (size_t)c[2]; src = s->ts.defaultIds; break;
+        case SPH_FIELD_SUB_VERTEX_DATA: need = sizeof(float) * 3 * 8 * n; break;
+        case SPH_FIELD_SUB_SIMULATION_DATA: need = sizeof(float) * 10 * 8 * n; break;
+    }
+    if (bytes < need) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "destination too small");
+    if (!s->tsReady) {
+        // before any two-scale step: every particle is in the default state
+        if (field == SPH_FIELD_DEFAULT_IDS)
+            for (size_t i = 0; i < n; i++) static_cast<int*>(dst)[i] = (int)i;
+        else std::memset(dst, 0, need);
+        return SPH_OK;
+    }
+    if (src) {
+        if (need) SPH_CUDA(cudaMemcpyAsync(dst, src, need, cudaMemcpyDeviceToHost, q));
+        SPH_CUDA(cudaStreamSynchronize(q));
+        return SPH_OK;
+    }
+    float* tmp = nullptr;
+    SPH_CUDA(cudaMalloc((void**)&tmp, need));
+    if (field == SPH_FIELD_SUB_VERTEX_DATA) launch_pack_aos(s->ts.subPos, (int)(8 * n), tmp, 3, 0, q);
+    else launch_ts_pack_sd(s->ts, (int)(8 * n), tmp, q);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dst, tmp, need, cudaMemcpyDeviceToHost, q);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(q);
+    cudaFree(tmp);
+    SPH_CUDA(e);
+    return SPH_OK;
+}
+
+}  // namespace
+
 sph_status sph_read(sph_handle s, int field, void* dst, size_t bytes) {
     if (!s || !dst) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (field == SPH_FIELD_STATE || (field >= SPH_FIELD_SUB_VERTEX_DATA && field <= SPH_FIELD_DEFAULT_IDS)) {
+        sph_status st = latched_status(s);
+        if (st) return st;
+        return read_two_scale(s, field, dst, bytes);
+    }
     const int n = s->n;
     size_t need = 0;
     switch (field) {
@@ -509,7 +705,6 @@ sph_status sph_read(sph_handle s, int field, void* dst, size_t bytes) {
         case SPH_FIELD_SIMULATION_DATA: need = sizeof(float) * 10 * (size_t)n; break;
         case SPH_FIELD_DENSITY:
         case SPH_FIELD_PRESSURE: need = sizeof(float) * (size_t)n; break;
-        case SPH_FIELD_STATE: need = (size_t)n; break;
         default: SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "unknown field");
     }
     if (bytes < need) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "destination too small");
@@ -539,7 +734,6 @@ sph_status sph_read(sph_handle s, int field, void* dst, size_t bytes) {
             }
             launch_pack_aos(s->vel, n, s->staging, 10, 6, q);
             break;
-        case SPH_FIELD_STATE: SPH_CUDA(cudaMemsetAsync(s->staging, 0, need, q)); break;
     }
     SPH_CUDA(cudaGetLastError());
     SPH_CUDA(cudaMemcpyAsync(dst, s->staging, need, cudaMemcpyDeviceToHost, q));
@@ -583,10 +777,40 @@ sph_status sph_write(sph_handle s, int field, const void* src, size_t bytes) {
 sph_status sph_read_cells(sph_handle s, int level, int* sortedHash, int* sortedIds, int* cellStart,
                           int* cellEnd) {
     if (!s) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "handle is NULL");
-    if (level != 0) SPH_FAIL(SPH_ERR_NOT_SUPPORTED, "sub-particle level not available in this build");
+    if (level != 0 && level != 1) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "level must be 0 or 1");
     if (!s->stepped) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "no step has run yet");
     sph_status st = latched_status(s);
     if (st) return st;
+    if (level == 1) {
+        // the fine level of the last two-scale step: arrays of numSubParticles
+        if (!s->tsReady) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "no two-scale step has run yet");
+        int c[4];
+        st = two_scale_counts(s, c);
+        if (st) return st;
+        const int Cs = s->P.gridDimSubParticles[0] * s->P.gridDimSubParticles[1] * s->P.gridDimSubParticles[2];
+        cudaStream_t q = s->stream;
+        if (sortedHash && c[3])
+            SPH_CUDA(cudaMemcpyAsync(sortedHash, s->ts.subSortedHash, sizeof(int) * c[3], cudaMemcpyDeviceToHost, q));
+        if (sortedIds && c[3])
+            SPH_CUDA(cudaMemcpyAsync(sortedIds, s->ts.subSortedIds, sizeof(int) * c[3], cudaMemcpyDeviceToHost, q));
+        if (cellStart || cellEnd) {
+            int* tmp = nullptr;
+            SPH_CUDA(cudaMalloc((void**)&tmp, sizeof(int) * 2 * (size_t)Cs));
+            if (c[3]) {
+                launch_cell_tables(Cs, s->ts.subOffset, tmp, tmp + Cs, q);
+            } else {
+                cudaMemsetAsync(tmp, 0xFF, sizeof(int) * 2 * (size_t)Cs, q);
+            }
+            cudaError_t e = cudaGetLastError();
+            if (e == cudaSuccess && cellStart) e = cudaMemcpyAsync(cellStart, tmp, sizeof(int) * Cs, cudaMemcpyDeviceToHost, q);
+            if (e == cudaSuccess && cellEnd) e = cudaMemcpyAsync(cellEnd, tmp + Cs, sizeof(int) * Cs, cudaMemcpyDeviceToHost, q);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(q);
+            cudaFree(tmp);
+            SPH_CUDA(e);
+        }
+        SPH_CUDA(cudaStreamSynchronize(q));
+        return SPH_OK;
+    }
     const int n = s->n;
     const int C = s->P.gridDim[0] * s->P.gridDim[1] * s->P.gridDim[2];
     cudaStream_t q = s->stream;
@@ -616,8 +840,14 @@ sph_status sph_read_cells(sph_handle s, int level, int* sortedHash, int* sortedI
 sph_status sph_get_counts(sph_handle s, sph_counts* out) {
     if (!s || !out) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "NULL argument");
     std::memset(out, 0, sizeof(*out));
+    int c[4];
+    sph_status st = two_scale_counts(s, c);
+    if (st) return st;
     out->numParticles = (unsigned int)s->n;
-    out->numParticlesDefault = (unsigned int)s->n;
+    out->numParticlesSplit = (unsigned int)c[0];
+    out->numParticlesBoundary = (unsigned int)c[1];
+    out->numParticlesDefault = (unsigned int)c[2];
+    out->numSubParticles = (unsigned int)c[3];
     out->numTimeSteps = s->numTimeSteps;
     out->numCells = (unsigned int)(s->P.gridDim[0] * s->P.gridDim[1] * s->P.gridDim[2]);
     out->numSubCells = (unsigned int)(s->P.gridDimSubParticles[0] * s->P.gridDimSubParticles[1] *

@@ -73,6 +73,30 @@ struct SortBuffers {
     int maxTiles;
 };
 
+// Two-scale state (AdvanceTwoScale): particle states, the three-way lists,
+// persistent child slots 8*parent + k, and the fine level's sort.
+struct TwoScaleDev {
+    unsigned char* state;       // [n rounded up to 4] 2-bit history per particle
+    int* blockCounts;           // [3 * blocks] per-block class counts
+    int* blockOffsets;          // [3 * blocks]
+    int* counts;                // [4] split, boundary, default, children (device side)
+    int* splitIds;              // [n]
+    int* boundaryIds;           // [n]
+    int* defaultIds;            // [n]
+    int* subIds;                // [8n] child list: split children, then boundary children
+    float4* subPos;             // [8n] slots
+    float4* subVel;
+    float4* subAcc;
+    float2* subRho;             // (density, pressure)
+    int* subCnt;                // [Cs+1] fine-level counters (kept zero between steps)
+    int* subOffset;             // [Cs+1] fine-level cell offsets
+    int2* subKeySlot;           // [8n]
+    int* subTmp;                // [8n]
+    int* subSortedHash;         // [8n]
+    int* subSortedIds;          // [8n] slots in (fine cell, list position) order
+    float splitMin[3], splitMax[3];
+};
+
 // Per-row lookup tables of the neighbour search.
 struct RowTables {
     const int* cellOffset;  // [C+1]
@@ -115,6 +139,21 @@ void launch_force(int n, const float4* posS, const float4* velS, const float4* r
 void launch_unpermute(int n, const int* sortedIds, const float4* srcS, int comp, float* dst,
                       int stride, int offset, cudaStream_t s);
 void launch_cell_tables(int numCells, const int* cellOffset, int* start, int* end, cudaStream_t s);
+
+// Two-scale pass (sph_twoscale.cu).
+void launch_ts_states(int n, const float4* posS, const int* workIds, const int* cellOffset, GridDev g, float h,
+                      const TwoScaleDev& T, cudaStream_t s);
+void launch_ts_children(int n, const float4* posS, const float4* velS, const float4* rho4S, const int* workIds,
+                        float mass, const TwoScaleDev& T, cudaStream_t s);
+void launch_ts_project(const float4* coarsePos, const int* workIds, int byId, const float4* rho4S,
+                       const int* cellOffset, GridDev g, float hs, const TwoScaleDev& T, int capacity,
+                       cudaStream_t s);
+void launch_ts_sub_sort(GridDev sg, const TwoScaleDev& T, SortBuffers subSb, int capacity, unsigned int* status,
+                        cudaStream_t s);
+void launch_ts_sub_density(GridDev sg, PhysDev sph, const TwoScaleDev& T, int capacity, cudaStream_t s);
+void launch_ts_sub_force(GridDev sg, PhysDev sph, const TwoScaleDev& T, int capacity, cudaStream_t s);
+void launch_ts_sub_integrate(PhysDev sph, const TwoScaleDev& T, int capacity, cudaStream_t s);
+void launch_ts_pack_sd(const TwoScaleDev& T, int slots, float* dst, cudaStream_t s);
 
 // Boundary maps.
 void launch_build_maps(const sph_boundary_desc& d, const unsigned int dims[3], float* dist,

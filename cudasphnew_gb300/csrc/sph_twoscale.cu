@@ -1,0 +1,474 @@
+// The two-scale pass (AdvanceTwoScale, particle_simulation.cu:2145-2182, and
+// AdvanceSubParticles, :2119-2143) on the GPU.
+//
+// Every coarse particle keeps a 2-bit state history (split / boundary /
+// default); split and boundary particles get 8 children each, in persistent
+// slots 8*parent + k of the child arrays.  Children of split particles
+// ("regular") get densities and forces at h/2 on the fine grid; children of
+// boundary particles get the mean coarse density and pressure around them.
+// All children are integrated and collided; nothing feeds back into the
+// coarse particles, as in the reference.
+//
+// Counts stay on the device: the kernels of the fine level loop over the
+// device-side counts (grid-stride), so a two-scale step needs no host
+// synchronisation.
+#include <cuda/atomic>
+
+#include "sph_device.cuh"
+
+namespace sph {
+
+namespace {
+
+__device__ __forceinline__ bool in_region(const TwoScaleDev& T, float4 x) {
+    return x.x >= T.splitMin[0] && x.x <= T.splitMax[0] && x.y >= T.splitMin[1] && x.y <= T.splitMax[1] &&
+           x.z >= T.splitMin[2] && x.z <= T.splitMax[2];
+}
+
+// r^2 as find_boundary_particles and project_quantities_cell form it
+// (:1002-1005, 1317-1321): three products summed left to right, each rounded.
+__device__ __forceinline__ float ref_r2(float4 a, float4 b) {
+    const float rx = __fsub_rn(a.x, b.x), ry = __fsub_rn(a.y, b.y), rz = __fsub_rn(a.z, b.z);
+    return __fadd_rn(__fadd_rn(__fmul_rn(rx, rx), __fmul_rn(ry, ry)), __fmul_rn(rz, rz));
+}
+
+inline int stride_grid(long long work, int bs) {
+    long long g = (work + bs - 1) / bs;
+    return (int)(g < 1 ? 1 : (g > 4096 ? 4096 : g));
+}
+
+// ---------------------------------------------------------------------------
+// shift_state + find_split_particles (:730-740, 932-952)
+// ---------------------------------------------------------------------------
+__global__ void k_ts_state(int n, const float4* __restrict__ posS, const int* __restrict__ workIds, TwoScaleDev T) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int id = workIds[k];
+    unsigned int s = ((unsigned int)T.state[id] << 2) & 0xFFu;
+    if (in_region(T, posS[k])) s |= 1u;
+    T.state[id] = (unsigned char)s;
+}
+
+// find_boundary_particles (:954-1017) as a race-free scatter: every split
+// particle (decided from its position, not from a state other threads are
+// changing) marks all particles of its 27-cell stencil within compactSupport,
+// itself included, with a word-wide atomic OR.
+__global__ void k_ts_mark(int n, const float4* __restrict__ posS, const int* __restrict__ workIds,
+                          const int* __restrict__ cellOffset, GridDev g, float h, TwoScaleDev T) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const float4 xs = posS[k];
+    if (!in_region(T, xs)) return;
+    const Stencil st = stencil(xs, h, g);
+    const float h2 = __fmul_rn(h, h);
+    unsigned int* words = reinterpret_cast<unsigned int*>(T.state);
+    for (int z = st.z0; z <= st.z1; z++)
+        for (int y = st.y0; y <= st.y1; y++) {
+            const int row = g.dim[0] * (g.dim[1] * z + y);
+            const int s = __ldg(cellOffset + row + st.x0), e = __ldg(cellOffset + row + st.x1 + 1);
+            for (int t = s; t < e; t++) {
+                if (ref_r2(xs, __ldg(posS + t)) <= h2) {
+                    const int v = workIds[t];
+                    atomicOr(words + (v >> 2), 2u << (8 * (v & 3)));
+                }
+            }
+        }
+}
+
+// ---------------------------------------------------------------------------
+// collect (:2509-2567): stable three-way compaction in particle order.
+// ---------------------------------------------------------------------------
+constexpr int TS_BLOCK = 1024;
+
+__device__ __forceinline__ int ts_class(unsigned char s) {
+    const int c = s & 3;
+    return c == 0 ? 2 : (c == 2 ? 1 : 0);  // 0 split, 1 boundary, 2 default
+}
+
+__global__ void __launch_bounds__(TS_BLOCK) k_ts_count(int n, TwoScaleDev T) {
+    __shared__ int s_cnt[3];
+    if (threadIdx.x < 3) s_cnt[threadIdx.x] = 0;
+    __syncthreads();
+    const int i = blockIdx.x * TS_BLOCK + threadIdx.x;
+    if (i < n) atomicAdd(&s_cnt[ts_class(T.state[i])], 1);
+    __syncthreads();
+    if (threadIdx.x < 3) T.blockCounts[3 * blockIdx.x + threadIdx.x] = s_cnt[threadIdx.x];
+}
+
+// Exclusive scan of the per-block counts (one block, looping), totals into
+// the device counters.
+__global__ void __launch_bounds__(TS_BLOCK) k_ts_scan_blocks(int nb, TwoScaleDev T) {
+    __shared__ int s_warp[3][TS_BLOCK / 32];
+    __shared__ int s_carry[3];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x < 3) s_carry[threadIdx.x] = 0;
+    __syncthreads();
+    for (int base = 0; base < nb; base += TS_BLOCK) {
+        const int b = base + threadIdx.x;
+        int x[3], incl[3];
+        for (int c = 0; c < 3; c++) {
+            x[c] = b < nb ? T.blockCounts[3 * b + c] : 0;
+            incl[c] = x[c];
+            for (int o = 1; o < 32; o <<= 1) {
+                int t = __shfl_up_sync(0xffffffffu, incl[c], o);
+                if (lane >= o) incl[c] += t;
+            }
+            if (lane == 31) s_warp[c][warp] = incl[c];
+        }
+        __syncthreads();
+        if (warp == 0) {
+            for (int c = 0; c < 3; c++) {
+                int w = s_warp[c][lane];
+                for (int o = 1; o < 32; o <<= 1) {
+                    int t = __shfl_up_sync(0xffffffffu, w, o);
+                    if (lane >= o) w += t;
+                }
+                s_warp[c][lane] = w;
+            }
+        }
+        __syncthreads();
+        int excl[3];
+        for (int c = 0; c < 3; c++) {
+            excl[c] = s_carry[c] + (warp > 0 ? s_warp[c][warp - 1] : 0) + incl[c] - x[c];
+            if (b < nb) T.blockOffsets[3 * b + c] = excl[c];
+        }
+        __syncthreads();
+        if (threadIdx.x == TS_BLOCK - 1)
+            for (int c = 0; c < 3; c++) s_carry[c] = excl[c] + x[c];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        T.counts[0] = s_carry[0];
+        T.counts[1] = s_carry[1];
+        T.counts[2] = s_carry[2];
+        T.counts[3] = 8 * (s_carry[0] + s_carry[1]);
+    }
+}
+
+// collect_ids (:1118-1162): id lists, and the child list -- split children
+// first, then boundary children, 8 consecutive slots per parent.
+__global__ void __launch_bounds__(TS_BLOCK) k_ts_lists(int n, TwoScaleDev T) {
+    __shared__ int s_warp[3][TS_BLOCK / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int i = blockIdx.x * TS_BLOCK + threadIdx.x;
+    const int cls = i < n ? ts_class(T.state[i]) : -1;
+    int rank[3];
+    for (int c = 0; c < 3; c++) {
+        const unsigned int m = __ballot_sync(0xffffffffu, cls == c);
+        rank[c] = __popc(m & ((1u << lane) - 1u));
+        if (lane == 0) s_warp[c][warp] = __popc(m);
+    }
+    __syncthreads();
+    if (warp == 0) {
+        for (int c = 0; c < 3; c++) {
+            int w = s_warp[c][lane];
+            int incl = w;
+            for (int o = 1; o < 32; o <<= 1) {
+                int t = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += t;
+            }
+            s_warp[c][lane] = incl - w;  // exclusive warp offsets
+        }
+    }
+    __syncthreads();
+    if (cls < 0) return;
+    const int r = T.blockOffsets[3 * blockIdx.x + cls] + s_warp[cls][warp] + rank[cls];
+    if (cls == 0) {
+        T.splitIds[r] = i;
+        for (int k = 0; k < 8; k++) T.subIds[8 * r + k] = 8 * i + k;
+    } else if (cls == 1) {
+        T.boundaryIds[r] = i;
+        const int base = 8 * (T.counts[0] + r);
+        for (int k = 0; k < 8; k++) T.subIds[base + k] = 8 * i + k;
+    } else {
+        T.defaultIds[r] = i;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// initialize_sub_particles (:1023-1090): 8 children on the cube diagonals at
+// the radius (3m/(4 pi rho))^(1/3), the parent's velocity.  The radicand is
+// formed in double and pow(r, 1.0f/3.0f) evaluated in double and rounded to
+// float once; pos + dir*radius is one fused multiply-add, as the reference's
+// kernel compiles it.
+// ---------------------------------------------------------------------------
+__global__ void k_ts_init(int n, const float4* __restrict__ posS, const float4* __restrict__ velS,
+                          const float4* __restrict__ rho4S, const int* __restrict__ workIds, float mass,
+                          TwoScaleDev T) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int id = workIds[k];
+    if ((T.state[id] & 3) == 0) return;
+    const double rad = (double)(3.0f * mass) / (4.0 * 3.14159265358979323846 * (double)rho4S[k].x);
+    const float radicand = (float)rad;
+    const float radius = (float)pow((double)radicand, (double)(1.0f / 3.0f));
+    const float4 x = posS[k], v = velS[k];
+    const float d = (float)0.577350269;
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+        const float sx = (c & 4) ? -d : d, sy = (c & 2) ? -d : d, sz = (c & 1) ? -d : d;
+        const size_t slot = 8 * (size_t)id + c;
+        T.subPos[slot] = make_float4(__fmaf_rn(sx, radius, x.x), __fmaf_rn(sy, radius, x.y),
+                                     __fmaf_rn(sz, radius, x.z), 0.f);
+        T.subVel[slot] = make_float4(v.x, v.y, v.z, 0.f);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// project_quantities (:570-622, 1328-1381): boundary children take the mean
+// coarse density and pressure within compactSupportSub, searched on the
+// coarse grid.  A child with nothing in reach gets 0 (the reference divides
+// 0 by 0).  Coarse positions come from `coarsePos` in the working order, or
+// through workIds from the particle-order state when `byId` is set.
+// ---------------------------------------------------------------------------
+__global__ void k_ts_project(const float4* __restrict__ coarsePos, const int* __restrict__ workIds, int byId,
+                             const float4* __restrict__ rho4S, const int* __restrict__ cellOffset, GridDev g,
+                             float hs, TwoScaleDev T) {
+    const int nSplit = T.counts[0];
+    const int nSub = T.counts[3];
+    const float hs2 = __fmul_rn(hs, hs);
+    for (int idx = 8 * nSplit + blockIdx.x * blockDim.x + threadIdx.x; idx < nSub; idx += gridDim.x * blockDim.x) {
+        const int slot = T.subIds[idx];
+        const float4 x = T.subPos[slot];
+        const Stencil st = stencil(x, hs, g);
+        float d = 0.f, p = 0.f, cnt = 0.f;
+        for (int z = st.z0; z <= st.z1; z++)
+            for (int y = st.y0; y <= st.y1; y++) {
+                const int row = g.dim[0] * (g.dim[1] * z + y);
+                const int s = __ldg(cellOffset + row + st.x0), e = __ldg(cellOffset + row + st.x1 + 1);
+                for (int t = s; t < e; t++) {
+                    const float4 xj = byId ? coarsePos[workIds[t]] : coarsePos[t];
+                    if (ref_r2(x, xj) <= hs2) {
+                        const float4 rj = rho4S[t];
+                        d += rj.x;
+                        p += rj.y;
+                        cnt += 1.f;
+                    }
+                }
+            }
+        T.subRho[slot] = cnt > 0.f ? make_float2(d / cnt, p / cnt) : make_float2(0.f, 0.f);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// The fine level's sort: compute_sub_particle_hash (:121-153) over the child
+// list, then the same counting sort as the coarse level, stable in list order.
+// ---------------------------------------------------------------------------
+__global__ void k_ts_subhash(GridDev g, TwoScaleDev T, unsigned int* status) {
+    const int nSub = T.counts[3];
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < nSub; idx += gridDim.x * blockDim.x) {
+        float4 x = T.subPos[T.subIds[idx]];
+        bool outside = false;
+        if (!(isfinite(x.x) && isfinite(x.y) && isfinite(x.z))) {
+            atomicOr(status, STATUS_NON_FINITE);
+            x = make_float4(g.origin[0], g.origin[1], g.origin[2], 0.f);
+        }
+        const int h = particle_hash(x, g, &outside);
+        if (outside) atomicOr(status, STATUS_OUT_OF_DOMAIN);
+        T.subKeySlot[idx] = make_int2(h, atomicAdd(T.subCnt + h, 1));
+    }
+}
+
+__global__ void k_ts_subscatter(TwoScaleDev T) {
+    const int nSub = T.counts[3];
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < nSub; idx += gridDim.x * blockDim.x) {
+        const int2 ks = T.subKeySlot[idx];
+        const int dst = T.subOffset[ks.x] + ks.y;
+        T.subTmp[dst] = idx;
+        T.subSortedHash[dst] = ks.x;
+    }
+}
+
+__global__ void k_ts_subrank(TwoScaleDev T) {
+    const int nSub = T.counts[3];
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nSub; k += gridDim.x * blockDim.x) {
+        const int c = T.subSortedHash[k];
+        const int s = T.subOffset[c], e = T.subOffset[c + 1];
+        const int my = T.subTmp[k];
+        int r = 0;
+        for (int t = s; t < e; t++) r += T.subTmp[t] < my;
+        T.subSortedIds[s + r] = T.subIds[my];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// compute_sub_particle_density_pressure (:259-313) for regular children.
+// ---------------------------------------------------------------------------
+__global__ void k_ts_subdensity(GridDev g, PhysDev ph, TwoScaleDev T) {
+    const int nReg = 8 * T.counts[0];
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < nReg; idx += gridDim.x * blockDim.x) {
+        const int slot = T.subIds[idx];
+        const float4 x = T.subPos[slot];
+        const Stencil st = stencil(x, ph.h, g);
+        float sum = 0.f, comp = 0.f;
+        for (int z = st.z0; z <= st.z1; z++)
+            for (int y = st.y0; y <= st.y1; y++) {
+                const int row = g.dim[0] * (g.dim[1] * z + y);
+                const int s = __ldg(T.subOffset + row + st.x0), e = __ldg(T.subOffset + row + st.x1 + 1);
+                float rs = 0.f;
+                for (int t = s; t < e; t++) {
+                    const float r2 = dist2(x, T.subPos[T.subSortedIds[t]]);
+                    const float w = fmaxf(ph.h2 - r2, 0.f);
+                    rs = fmaf(w * w, w, rs);
+                }
+                if (rs > 0.f) kahan_add(sum, comp, rs);
+            }
+        const float rho = __fsub_rn(sum, comp) * ph.poly6m;
+        T.subRho[slot] = make_float2(rho, ph.stiffness * (rho - ph.restDensity));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// compute_sub_particle_acceleration (:477-568): pressure, viscosity and the
+// colour field of the regular children; surface tension is always tested
+// (no wall terms at this level).
+// ---------------------------------------------------------------------------
+__global__ void k_ts_subforce(GridDev g, PhysDev ph, TwoScaleDev T) {
+    const int nReg = 8 * T.counts[0];
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < nReg; idx += gridDim.x * blockDim.x) {
+        const int slot = T.subIds[idx];
+        const float4 xi = T.subPos[slot], vi = T.subVel[slot];
+        const float2 ri = T.subRho[slot];
+        const float rhoi = ri.x;
+        const float qi = ri.y / (rhoi * rhoi);
+        const Stencil st = stencil(xi, ph.h, g);
+        float fp[3] = {0.f, 0.f, 0.f}, fv[3] = {0.f, 0.f, 0.f}, cg[3] = {0.f, 0.f, 0.f}, cl = 0.f;
+        for (int z = st.z0; z <= st.z1; z++)
+            for (int y = st.y0; y <= st.y1; y++) {
+                const int row = g.dim[0] * (g.dim[1] * z + y);
+                const int s = __ldg(T.subOffset + row + st.x0), e = __ldg(T.subOffset + row + st.x1 + 1);
+                for (int t = s; t < e; t++) {
+                    const int j = T.subSortedIds[t];
+                    const float4 xj = T.subPos[j];
+                    const float r2 = dist2(xi, xj);
+                    if (!(r2 <= ph.h2 && r2 > 0.f)) continue;
+                    const float4 vj = T.subVel[j];
+                    const float2 rj = T.subRho[j];
+                    const float invj = 1.0f / rj.x;
+                    const float dx = __fsub_rn(xi.x, xj.x), dy = __fsub_rn(xi.y, xj.y), dz = __fsub_rn(xi.z, xj.z);
+                    const float rinv = rsqrtf(r2);
+                    const float hr = ph.h - r2 * rinv;
+                    const float sp = (qi + rj.y * invj * invj) * hr * hr * rinv;
+                    const float sv = invj * hr;
+                    fp[0] = fmaf(sp, dx, fp[0]);
+                    fp[1] = fmaf(sp, dy, fp[1]);
+                    fp[2] = fmaf(sp, dz, fp[2]);
+                    fv[0] = fmaf(sv, vj.x - vi.x, fv[0]);
+                    fv[1] = fmaf(sv, vj.y - vi.y, fv[1]);
+                    fv[2] = fmaf(sv, vj.z - vi.z, fv[2]);
+                    const float d2 = ph.h2 - r2;
+                    const float sc = invj * d2 * d2;
+                    cg[0] = fmaf(sc, dx, cg[0]);
+                    cg[1] = fmaf(sc, dy, cg[1]);
+                    cg[2] = fmaf(sc, dz, cg[2]);
+                    cl = fmaf(invj * d2, 3.f * ph.h2 - 7.f * r2, cl);
+                }
+            }
+        const float pc = ph.pressCoef * rhoi;
+        float force[3];
+        for (int a = 0; a < 3; a++) force[a] = ph.viscCoef * fv[a] + pc * fp[a];
+        const float cgx = ph.cgCoef * cg[0], cgy = ph.cgCoef * cg[1], cgz = ph.cgCoef * cg[2];
+        const float norm = sqrtf(cgx * cgx + cgy * cgy + cgz * cgz);
+        if (norm > ph.normThresh) {
+            const float fc = ph.tension * (ph.clCoef * cl) / norm;
+            force[0] -= fc * cgx;
+            force[1] -= fc * cgy;
+            force[2] -= fc * cgz;
+        }
+        float acc[3] = {force[0] / rhoi, force[1] / rhoi, force[2] / rhoi};
+        acc[0] -= ph.gravityAxis == 0 ? ph.gravity : 0.f;
+        acc[1] -= ph.gravityAxis == 1 ? ph.gravity : 0.f;
+        acc[2] -= ph.gravityAxis == 2 ? ph.gravity : 0.f;
+        T.subAcc[slot] = make_float4(acc[0], acc[1], acc[2], 0.f);
+    }
+}
+
+// integrate_sub_particles_euler (:667-696) + collision_handling_sub_particles
+// (:836-930) for every child of the list.  Children of boundary particles use
+// whatever acceleration their slot holds (the reference computes none for
+// them).
+__global__ void k_ts_subintegrate(PhysDev ph, TwoScaleDev T) {
+    const int nSub = T.counts[3];
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < nSub; idx += gridDim.x * blockDim.x) {
+        const int slot = T.subIds[idx];
+        const float4 a = T.subAcc[slot];
+        const float4 v0 = T.subVel[slot], x0 = T.subPos[slot];
+        float3 v = make_float3(v0.x + ph.dt * a.x, v0.y + ph.dt * a.y, v0.z + ph.dt * a.z);
+        float3 x = make_float3(x0.x + ph.dt * v.x, x0.y + ph.dt * v.y, x0.z + ph.dt * v.z);
+        collide(ph, x, v);
+        T.subPos[slot] = make_float4(x.x, x.y, x.z, 0.f);
+        T.subVel[slot] = make_float4(v.x, v.y, v.z, 0.f);
+    }
+}
+
+// SD layout of the child slots (particle_simulation.h:28-41): mass and
+// energy columns are never written by the reference (0).
+__global__ void k_ts_pack_sd(TwoScaleDev T, int slots, float* __restrict__ dst) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= slots) return;
+    float* o = dst + 10 * (size_t)k;
+    const float2 r = T.subRho[k];
+    const float4 a = T.subAcc[k], v = T.subVel[k];
+    o[0] = 0.f;
+    o[1] = r.x;
+    o[2] = r.y;
+    o[3] = a.x;
+    o[4] = a.y;
+    o[5] = a.z;
+    o[6] = v.x;
+    o[7] = v.y;
+    o[8] = v.z;
+    o[9] = 0.f;
+}
+
+}  // namespace
+
+void launch_ts_pack_sd(const TwoScaleDev& T, int slots, float* dst, cudaStream_t s) {
+    if (slots <= 0) return;
+    k_ts_pack_sd<<<(slots + 255) / 256, 256, 0, s>>>(T, slots, dst);
+}
+
+void launch_ts_states(int n, const float4* posS, const int* workIds, const int* cellOffset, GridDev g, float h,
+                      const TwoScaleDev& T, cudaStream_t s) {
+    if (n <= 0) return;
+    k_ts_state<<<(n + 255) / 256, 256, 0, s>>>(n, posS, workIds, T);
+    k_ts_mark<<<(n + 127) / 128, 128, 0, s>>>(n, posS, workIds, cellOffset, g, h, T);
+    const int nb = (n + TS_BLOCK - 1) / TS_BLOCK;
+    k_ts_count<<<nb, TS_BLOCK, 0, s>>>(n, T);
+    k_ts_scan_blocks<<<1, TS_BLOCK, 0, s>>>(nb, T);
+    k_ts_lists<<<nb, TS_BLOCK, 0, s>>>(n, T);
+}
+
+void launch_ts_children(int n, const float4* posS, const float4* velS, const float4* rho4S, const int* workIds,
+                        float mass, const TwoScaleDev& T, cudaStream_t s) {
+    if (n <= 0) return;
+    k_ts_init<<<(n + 127) / 128, 128, 0, s>>>(n, posS, velS, rho4S, workIds, mass, T);
+}
+
+void launch_ts_project(const float4* coarsePos, const int* workIds, int byId, const float4* rho4S,
+                       const int* cellOffset, GridDev g, float hs, const TwoScaleDev& T, int capacity,
+                       cudaStream_t s) {
+    k_ts_project<<<stride_grid(capacity, 128), 128, 0, s>>>(coarsePos, workIds, byId, rho4S, cellOffset, g, hs, T);
+}
+
+void launch_ts_sub_sort(GridDev sg, const TwoScaleDev& T, SortBuffers subSb, int capacity, unsigned int* status,
+                        cudaStream_t s) {
+    k_ts_subhash<<<stride_grid(capacity, 256), 256, 0, s>>>(sg, T, status);
+    launch_cell_scan(sg.numCells, subSb, status, s);
+    k_ts_subscatter<<<stride_grid(capacity, 256), 256, 0, s>>>(T);
+    k_ts_subrank<<<stride_grid(capacity, 256), 256, 0, s>>>(T);
+}
+
+void launch_ts_sub_density(GridDev sg, PhysDev sph, const TwoScaleDev& T, int capacity, cudaStream_t s) {
+    k_ts_subdensity<<<stride_grid(capacity, 128), 128, 0, s>>>(sg, sph, T);
+}
+
+void launch_ts_sub_force(GridDev sg, PhysDev sph, const TwoScaleDev& T, int capacity, cudaStream_t s) {
+    k_ts_subforce<<<stride_grid(capacity, 128), 128, 0, s>>>(sg, sph, T);
+}
+
+void launch_ts_sub_integrate(PhysDev sph, const TwoScaleDev& T, int capacity, cudaStream_t s) {
+    k_ts_subintegrate<<<stride_grid(capacity, 256), 256, 0, s>>>(sph, T);
+}
+
+}  // namespace sph

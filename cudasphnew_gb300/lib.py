@@ -18,7 +18,8 @@ LIB_PATH = os.path.join(PKG, "_build", "libsph_gb300.so")
 
 SPH_STEP_PLAIN, SPH_STEP_TWO_SCALE, SPH_STEP_SUB_ONLY = 0, 1, 2
 (FIELD_VERTEX_DATA, FIELD_SIMULATION_DATA, FIELD_VELOCITY, FIELD_ACCELERATION,
- FIELD_DENSITY, FIELD_PRESSURE, FIELD_STATE) = range(7)
+ FIELD_DENSITY, FIELD_PRESSURE, FIELD_STATE, FIELD_SUB_VERTEX_DATA, FIELD_SUB_SIMULATION_DATA,
+ FIELD_SUB_IDS, FIELD_SPLIT_IDS, FIELD_BOUNDARY_IDS, FIELD_DEFAULT_IDS) = range(13)
 
 STATUS = {0: "SPH_OK", 1: "SPH_ERR_INVALID_ARGUMENT", 2: "SPH_ERR_CUDA",
           3: "SPH_ERR_OUT_OF_MEMORY", 4: "SPH_ERR_OUT_OF_DOMAIN", 5: "SPH_ERR_DEVICE_WAIT",
@@ -210,7 +211,13 @@ class ParticleSimulation:
         shapes = {FIELD_VERTEX_DATA: ((n, 3), np.float32), FIELD_VELOCITY: ((n, 3), np.float32),
                   FIELD_ACCELERATION: ((n, 3), np.float32), FIELD_SIMULATION_DATA: ((n, 10), np.float32),
                   FIELD_DENSITY: ((n,), np.float32), FIELD_PRESSURE: ((n,), np.float32),
-                  FIELD_STATE: ((n,), np.int8)}
+                  FIELD_STATE: ((n,), np.uint8), FIELD_SUB_VERTEX_DATA: ((8 * n, 3), np.float32),
+                  FIELD_SUB_SIMULATION_DATA: ((8 * n, 10), np.float32)}
+        if field in (FIELD_SUB_IDS, FIELD_SPLIT_IDS, FIELD_BOUNDARY_IDS, FIELD_DEFAULT_IDS):
+            c = self.counts()
+            count = {FIELD_SUB_IDS: c.numSubParticles, FIELD_SPLIT_IDS: c.numParticlesSplit,
+                     FIELD_BOUNDARY_IDS: c.numParticlesBoundary, FIELD_DEFAULT_IDS: c.numParticlesDefault}[field]
+            shapes[field] = ((count,), np.int32)
         shape, dt = shapes[field]
         out = np.zeros(shape, dt)
         check(load().sph_read(self._h, field, _p(out), out.nbytes))
@@ -228,8 +235,8 @@ class ParticleSimulation:
 
     def cells(self, level: int = 0):
         """(sorted hash, sorted ids, cell start, cell end) of the last step."""
-        n = self.n if level == 0 else None
         c = self.counts()
+        n = self.n if level == 0 else c.numSubParticles
         C = c.numCells if level == 0 else c.numSubCells
         h = np.zeros(n, np.int32)
         ids = np.zeros(n, np.int32)

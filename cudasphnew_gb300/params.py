@@ -126,13 +126,20 @@ def kernel_constants(p: SimulationParameters, h: float) -> None:
     the value is computed in double and rounded once to float.
     """
     hf = float(np.float32(h))
+
+    def prod(c, k):  # c * h * h * ... (k factors), left to right in double
+        v = c
+        for _ in range(k):
+            v = v * hf
+        return v
+
     p.compactSupport = hf
     p.compactSupportSub = _f32(np.float32(hf) / np.float32(2.0))
-    p.poly6 = _f32(315.0 / (64.0 * math.pi * hf ** 9))
-    p.gradPoly6 = _f32(-945.0 / (32.0 * math.pi * hf ** 9))
-    p.laplPoly6 = _f32(-945.0 / (32.0 * math.pi * hf ** 9))
-    p.gradSpiky = _f32(-45.0 / (math.pi * hf ** 6))
-    p.laplVisc = _f32(45.0 / (math.pi * hf ** 6))
+    p.poly6 = _f32(315.0 / prod(64.0 * math.pi, 9))
+    p.gradPoly6 = _f32(-945.0 / prod(32.0 * math.pi, 9))
+    p.laplPoly6 = _f32(-945.0 / prod(32.0 * math.pi, 9))
+    p.gradSpiky = _f32(-45.0 / prod(math.pi, 6))
+    p.laplVisc = _f32(45.0 / prod(math.pi, 6))
     p.poly6Sub = _f32(np.float32(p.poly6) * np.float32(512.0))
     p.gradPoly6Sub = _f32(np.float32(p.gradPoly6) * np.float32(512.0))
     p.laplPoly6Sub = _f32(np.float32(p.laplPoly6) * np.float32(512.0))
@@ -165,7 +172,9 @@ def example01_params(num_particles: int = 39304) -> SimulationParameters:
     p.gravity = _f32(9.81)
     p.tensionCoefficient = _f32(0.0728)
     p.normThresh = _f32(15.065)
-    h = _f32(math.pow((3.0 * 0.5 * 0.5 * 0.5 * 20) / (4.0 * math.pi * num_particles), 1.0 / 3.0))
+    # powf of the float argument, as particle_simulation.cu:1774-1775 evaluates it
+    h = float(np.power(np.float32((3.0 * 0.5 * 0.5 * 0.5 * 20) / (4.0 * math.pi * num_particles)),
+                       np.float32(1.0 / 3.0)))
     kernel_constants(p, h)
     p.timeStep = _f32(0.003)
     p.timeStepSubParticles = _f32(0.001)
@@ -194,7 +203,8 @@ def example01_boundary(p: SimulationParameters) -> BoundaryDesc:
     d.particleMass = p.particleMass
     d.restDensity = p.restDensity
     d.viscosity = p.dynamicViscosity
-    d.particleSpacing = _f32(math.pow(float(np.float32(p.particleMass) / np.float32(p.restDensity)), 1.0 / 3.0))
+    # std::powf(mass/restDensity, 1.0f/3.0f), particle_simulation.cu:2603
+    d.particleSpacing = float(np.power(np.float32(p.particleMass) / np.float32(p.restDensity), np.float32(1.0 / 3.0)))
     d.numShapes = 1
     d.shapes[0].kind = SHAPE_BOX
     for a, v in enumerate((0.0, 0.0, 0.0, 0.7, 0.5, 0.3)):
@@ -270,7 +280,7 @@ def obstacle_boundary(p: SimulationParameters, grid_start, n_nodes: int, shapes)
     d.particleMass = p.particleMass
     d.restDensity = p.restDensity
     d.viscosity = p.dynamicViscosity
-    d.particleSpacing = _f32(math.pow(float(np.float32(p.particleMass) / np.float32(p.restDensity)), 1.0 / 3.0))
+    d.particleSpacing = float(np.power(np.float32(p.particleMass) / np.float32(p.restDensity), np.float32(1.0 / 3.0)))
     d.numShapes = len(shapes)
     for i, (kind, vals) in enumerate(shapes):
         d.shapes[i].kind = kind

@@ -115,3 +115,21 @@ def small_obstacle(nx=24, ny=24, nz=12) -> Scene:
     s = dam_break(nx, ny, nz, (0.0, 0.0, 0.0), (1.0, 1.0, 0.5), 7, "sdf_obstacle_small", 10,
                   obstacle=True)
     return s
+
+
+def two_scale(nb=64, region=(0.4, 0.6), box=1.0, seed=3, name="two_scale_262k") -> Scene:
+    """Two-scale run: an nb^3 block in the corner of a box of side `box`;
+    particles inside the axis-aligned region [region[0], region[1]]^3 split
+    into 8 children of half the smoothing length.  nb = 64 is the
+    262,144-particle configuration."""
+    pos = lattice_block(nb, nb, nb, (0.0, 0.0, 0.0), P.SPACING, seed, 0.01 * P.H)
+    p = P.dam_break_params((0, 0, 0), (box, box, box), len(pos))
+    o = P.default_options(gravity_axis=2, box_collision=True)
+    for a in range(3):
+        o.splitMin[a] = region[0]
+        o.splitMax[a] = region[1]
+    return Scene(name, p, o, pos, np.zeros_like(pos), None, 500)
+
+
+def config3() -> Scene:
+    return two_scale()

@@ -139,7 +139,14 @@ typedef enum sph_field {
     SPH_FIELD_ACCELERATION = 3,    /* float[n*3] */
     SPH_FIELD_DENSITY = 4,         /* float[n] */
     SPH_FIELD_PRESSURE = 5,        /* float[n] */
-    SPH_FIELD_STATE = 6            /* char[n] (GetParticleState) */
+    SPH_FIELD_STATE = 6,           /* char[n] (GetParticleState) */
+    /* two-scale pass: child slots 8*parent + k (capacity 8n), lists */
+    SPH_FIELD_SUB_VERTEX_DATA = 7,     /* float[8n*3] child positions by slot */
+    SPH_FIELD_SUB_SIMULATION_DATA = 8, /* float[8n*10] child SD by slot */
+    SPH_FIELD_SUB_IDS = 9,             /* int[numSubParticles] active child slots */
+    SPH_FIELD_SPLIT_IDS = 10,          /* int[numParticlesSplit] */
+    SPH_FIELD_BOUNDARY_IDS = 11,       /* int[numParticlesBoundary] */
+    SPH_FIELD_DEFAULT_IDS = 12         /* int[numParticlesDefault] */
 } sph_field;
 
 typedef struct sph_counts {
@@ -179,10 +186,13 @@ sph_status sph_bind(sph_handle h, const SimulationParameters* params);
  * the handle's own stream). */
 sph_status sph_set_stream(sph_handle h, void* stream);
 
-/* Advance / AdvanceTwoScale / AdvanceSubParticles: enqueues one step. */
+/* Advance / AdvanceTwoScale / AdvanceSubParticles: enqueues one step.  The
+ * plain step does not run the two-scale bookkeeping (particle states, lists,
+ * children): it does not change the coarse particles; the two-scale step
+ * does, with its counts kept on the device. */
 sph_status sph_step(sph_handle h, int mode);
 
-/* Enqueues `count` plain steps (one CUDA-graph launch each once captured). */
+/* Enqueues `count` steps of `mode` (one CUDA-graph launch each once captured). */
 sph_status sph_step_many(sph_handle h, int mode, int count);
 
 /* Waits for the handle's stream; returns the latched device status. */

@@ -182,3 +182,91 @@ def jet_slice(values: np.ndarray, scale: float) -> np.ndarray:
     img = np.stack(px, axis=-1)          # (W, H, 3) indexed [i, j]
     img = img[:, ::-1, :]                # set() stores row H-j-1
     return np.transpose(img, (1, 0, 2))  # (H, W, 3) row-major like the file
+
+
+class TwoScale:
+    """Two-scale state of the oracle (particle states, lists and 8n child slots)."""
+
+    WHAT = {"state": 0, "split": 1, "boundary": 2, "default": 3, "sub_ids": 4, "sub_hash": 5,
+            "sorted_sub_ids": 6, "sub_start": 7, "sub_end": 8, "sub_pos": 10, "sub_vel": 11,
+            "sub_acc": 12, "sub_rho": 13, "sub_p": 14, "sub_scale_acc": 15}
+
+    def __init__(self, n: int, fp64: bool = False):
+        L = lib()
+        vp = ctypes.c_void_p
+        L.orc_ts_new.restype = vp
+        L.orc_ts_new.argtypes = [ctypes.c_int, ctypes.c_int]
+        L.orc_ts_free.argtypes = [vp, ctypes.c_int]
+        for name in ("orc_ts_step_f32", "orc_ts_step_f64"):
+            getattr(L, name).argtypes = [vp, _P(SimulationParameters), _P(Options), _P(Maps)] + [vp] * 9
+            getattr(L, name).restype = ctypes.c_int
+        for name in ("orc_ts_part_f32", "orc_ts_part_f64"):
+            getattr(L, name).argtypes = [vp, _P(SimulationParameters), _P(Options)] + [vp] * 7
+            getattr(L, name).restype = ctypes.c_int
+        for name in ("orc_ts_sub_only_f32", "orc_ts_sub_only_f64"):
+            getattr(L, name).argtypes = [vp, _P(SimulationParameters), _P(Options)] + [vp] * 6
+            getattr(L, name).restype = ctypes.c_int
+        L.orc_ts_counts.argtypes = [vp, ctypes.c_int, vp]
+        L.orc_ts_get.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp]
+        self.n, self.fp64 = n, fp64
+        self.dt = np.float64 if fp64 else np.float32
+        self._h = ctypes.c_void_p(L.orc_ts_new(n, 1 if fp64 else 0))
+
+    def __del__(self):
+        try:
+            lib().orc_ts_free(self._h, 1 if self.fp64 else 0)
+        except Exception:
+            pass
+
+    def counts(self):
+        c = np.zeros(5, np.int32)
+        lib().orc_ts_counts(self._h, 1 if self.fp64 else 0, _ptr(c))
+        return dict(split=int(c[0]), boundary=int(c[1]), default=int(c[2]), sub=int(c[3]), sub_cells=int(c[4]))
+
+    def get(self, what: str) -> np.ndarray:
+        c = self.counts()
+        n = self.n
+        sizes = {"state": (n, np.uint8), "split": (c["split"], np.int32), "boundary": (c["boundary"], np.int32),
+                 "default": (c["default"], np.int32), "sub_ids": (c["sub"], np.int32),
+                 "sub_hash": (c["sub"], np.int32), "sorted_sub_ids": (c["sub"], np.int32),
+                 "sub_start": (c["sub_cells"], np.int32), "sub_end": (c["sub_cells"], np.int32),
+                 "sub_pos": ((8 * n, 3), self.dt), "sub_vel": ((8 * n, 3), self.dt),
+                 "sub_acc": ((8 * n, 3), self.dt), "sub_rho": (8 * n, self.dt), "sub_p": (8 * n, self.dt),
+                 "sub_scale_acc": (8 * n, self.dt)}
+        shape, dt = sizes[what]
+        out = np.zeros(shape, dt)
+        if out.size:
+            lib().orc_ts_get(self._h, 1 if self.fp64 else 0, self.WHAT[what], _ptr(out))
+        return out
+
+    def set_state(self, state: np.ndarray) -> None:
+        a = np.ascontiguousarray(state, np.uint8)
+        lib().orc_ts_get(self._h, 1 if self.fp64 else 0, 20, _ptr(a))
+
+    def step(self, p, o, bm, pos, vel):
+        """AdvanceTwoScale; returns the coarse outputs like step_plain."""
+        n = self.n
+        dt = self.dt
+        pos = np.array(pos, dt, order="C", copy=True)
+        vel = np.array(vel, dt, order="C", copy=True)
+        rho, prs, acc = np.zeros(n, dt), np.zeros(n, dt), np.zeros((n, 3), dt)
+        C = p.num_cells
+        h, ids = np.zeros(n, np.int32), np.zeros(n, np.int32)
+        start, end = np.zeros(C, np.int32), np.zeros(C, np.int32)
+        fn = lib().orc_ts_step_f64 if self.fp64 else lib().orc_ts_step_f32
+        mp = ctypes.byref(bm.maps) if bm is not None else None
+        rc = fn(self._h, ctypes.byref(p), ctypes.byref(o), mp, _ptr(pos), _ptr(vel), _ptr(rho), _ptr(prs),
+                _ptr(acc), _ptr(h), _ptr(ids), _ptr(start), _ptr(end))
+        if rc:
+            raise ValueError(f"oracle two-scale step failed ({rc})")
+        return dict(pos=pos, vel=vel, rho=rho, p=prs, acc=acc, hash=h, ids=ids, start=start, end=end)
+
+    def part(self, p, o, pos, vel, rho, prs, ids, start, end):
+        """The two-scale part of AdvanceTwoScale from given coarse results."""
+        dt = self.dt
+        arrs = [np.ascontiguousarray(a, dt) for a in (pos, vel, rho, prs)]
+        ints = [np.ascontiguousarray(a, np.int32) for a in (ids, start, end)]
+        fn = lib().orc_ts_part_f64 if self.fp64 else lib().orc_ts_part_f32
+        rc = fn(self._h, ctypes.byref(p), ctypes.byref(o), *[_ptr(a) for a in arrs], *[_ptr(a) for a in ints])
+        if rc:
+            raise ValueError(f"oracle two-scale part failed ({rc})")

@@ -27,6 +27,7 @@
 // =============================================================================
 #include <algorithm>
 #include <cmath>
+#include <type_traits>
 #include <cstdint>
 #include <cstring>
 #include <vector>
@@ -307,7 +308,9 @@ void force_one(const OrcParams& P, const OrcOptions& O, const Level<R>& L,
                 R d = (h - rn) * (h - rn);
                 for (int a = 0; a < 3; a++) pF[a] -= pressure * grad * d / rn * r[a];
                 d = (h - rn);
-                for (int a = 0; a < 3; a++) vF[a] += mu * (vj[a] - vi[a]) * m / rhoj * lapl * d;
+                // the sub-particle kernel adds both into one force (:1619-1628)
+                R* vacc = sub ? pF : vF;
+                for (int a = 0; a < 3; a++) vacc[a] += mu * (vj[a] - vi[a]) * m / rhoj * lapl * d;
                 d = (h * h - rn * rn) * (h * h - rn * rn);
                 for (int a = 0; a < 3; a++) cg[a] += m / rhoj * grad2 * d * r[a];
                 d = (h * h - rn * rn) * (R(3) * h * h - R(7) * rn * rn);
@@ -384,7 +387,7 @@ void force_one(const OrcParams& P, const OrcOptions& O, const Level<R>& L,
             }
         }
     } else {
-        for (int a = 0; a < 3; a++) force[a] = pF[a] + vF[a];
+        for (int a = 0; a < 3; a++) force[a] = pF[a];
     }
     if (tension) {
         R colGraNorm = std::sqrt(cg[0] * cg[0] + cg[1] * cg[1] + cg[2] * cg[2]);
@@ -829,6 +832,357 @@ int orc_boundary_maps(const OrcBoundaryDesc* Dp, float* dist, float* dens, float
         if (visc) visc[n] = viscs[node];
     }
     return 0;
+}
+
+}  // extern "C"
+
+// =============================================================================
+//  Two-scale pass (AdvanceTwoScale, particle_simulation.cu:2145-2182, and
+//  AdvanceSubParticles, :2119-2143)
+// =============================================================================
+namespace {
+
+// split region test (find_split_particles, :932-952; reference region
+// 0.2 <= x <= 0.5 is the default AABB of the options)
+template <class R>
+bool in_split_region(const OrcOptions& O, const R* x) {
+    for (int a = 0; a < 3; a++)
+        if (!(x[a] >= R(O.splitMin[a]) && x[a] <= R(O.splitMax[a]))) return false;
+    return true;
+}
+
+// initialize_sub_particles radius (:1057-1059): the radicand is formed in
+// double (M_PI is a double) and stored as float; pow(r, 1.0f/3.0f) is
+// evaluated in double and rounded once to float, identically on every
+// platform.  Children are always placed in the reference's float arithmetic
+// (also by the FP64 restatement), so both restatements refine the same
+// children.
+inline float child_radius(float mass, float density) {
+    double rad = (double)(3.0f * mass) / (4.0 * 3.14159265358979323846 * (double)density);
+    float radicand = (float)rad;
+    return (float)std::pow((double)radicand, (double)(1.0f / 3.0f));
+}
+
+const float kDir[8][3] = {{1, 1, 1}, {1, 1, -1}, {1, -1, 1}, {1, -1, -1},
+                          {-1, 1, 1}, {-1, 1, -1}, {-1, -1, 1}, {-1, -1, -1}};
+const float kSqrt3Inv = (float)0.577350269;  // SQRT3INV, :1028
+
+template <class R>
+struct TwoScale {
+    int n = 0;
+    std::vector<unsigned char> state;
+    std::vector<R> subPos, subVel, subAcc, subRho, subPrs;  // 8n slots
+    std::vector<int> splitIds, boundaryIds, defaultIds, subIds;
+    std::vector<int> subHash, sortedSubIds, subStart, subEnd;
+    std::vector<R> subScaleAcc;  // rounding-error scale of the children's accelerations
+    int subCells = 0;
+    explicit TwoScale(int n_) : n(n_), state(n_, 0), subPos(24 * (size_t)n_, R(0)),
+        subVel(24 * (size_t)n_, R(0)), subAcc(24 * (size_t)n_, R(0)), subRho(8 * (size_t)n_, R(0)),
+        subPrs(8 * (size_t)n_, R(0)), subScaleAcc(8 * (size_t)n_, R(0)) {}
+};
+
+// computeParticleState (:2495-2504) with find_boundary_particles read as the
+// race-free scatter: every particle that is split after find_split_particles
+// marks all particles of its stencil within compactSupport (self included),
+// with r^2 = rx*rx + ry*ry + rz*rz as the reference forms it (:1002-1007).
+// (In the reference a split particle that a neighbour has already marked
+// reads state 3 and does not propagate -- an order-dependent outcome.)
+template <class R>
+void particle_state(const OrcParams& P, const OrcOptions& O, TwoScale<R>& T, const R* pos, const int* ids,
+                    const int* start, const int* end) {
+    const int n = T.n;
+    for (int i = 0; i < n; i++) T.state[i] = (unsigned char)(T.state[i] << 2);
+    for (int u = 0; u < n; u++) {
+        int id = ids[u];
+        if (in_split_region<R>(O, pos + 3 * (size_t)id)) T.state[id] |= 1;
+    }
+    std::vector<unsigned char> split(n);
+    for (int i = 0; i < n; i++) split[i] = (T.state[i] & 3) == 1;
+    Level<R> L = coarse_level<R>(P);
+    R h2 = L.h * L.h;
+    for (int u = 0; u < n; u++) {
+        int id = ids[u];
+        if (!split[id]) continue;
+        const R* xs = pos + 3 * (size_t)id;
+        for_each_cell<R>(P, xs, L.h, L.spacing, L.dim, start, end, [&](int s, int e) {
+            for (int t = s; t < e; t++) {
+                int v = ids[t];
+                const R* xv = pos + 3 * (size_t)v;
+                R rx = xs[0] - xv[0], ry = xs[1] - xv[1], rz = xs[2] - xv[2];
+                R rn = rx * rx + ry * ry + rz * rz;
+                if (rn <= h2) T.state[v] |= 2;
+            }
+        });
+    }
+}
+
+// collect (:2509-2567) + collect_ids (:1118-1162): stable three-way split.
+template <class R>
+void collect(TwoScale<R>& T) {
+    T.splitIds.clear();
+    T.boundaryIds.clear();
+    T.defaultIds.clear();
+    for (int i = 0; i < T.n; i++) {
+        int c = T.state[i] & 3;
+        if (c == 0) T.defaultIds.push_back(i);
+        else if (c == 2) T.boundaryIds.push_back(i);
+        else T.splitIds.push_back(i);
+    }
+    T.subIds.clear();
+    for (int p : T.splitIds)
+        for (int k = 0; k < 8; k++) T.subIds.push_back(8 * p + k);
+    for (int p : T.boundaryIds)
+        for (int k = 0; k < 8; k++) T.subIds.push_back(8 * p + k);
+}
+
+// initialize_sub_particles (:1023-1090) for split and boundary parents.
+template <class R>
+void init_children(const OrcParams& P, TwoScale<R>& T, const R* pos, const R* vel, const R* rho) {
+    auto seed = [&](int id) {
+        float radius = child_radius(P.particleMass, (float)rho[id]);
+        for (int k = 0; k < 8; k++) {
+            size_t slot = 8 * (size_t)id + k;
+            for (int a = 0; a < 3; a++) {
+                T.subVel[3 * slot + a] = vel[3 * (size_t)id + a];
+                // pos + dir*radius, contracted to one fused multiply-add as
+                // nvcc contracts it in the reference's kernel (:1080-1085)
+                float d = kDir[k][a] * kSqrt3Inv;
+                T.subPos[3 * slot + a] = R(std::fmaf(d, radius, (float)pos[3 * (size_t)id + a]));
+            }
+        }
+    };
+    for (int p : T.splitIds) seed(p);
+    for (int p : T.boundaryIds) seed(p);
+}
+
+// project_quantities (:570-622, 1328-1381): unweighted mean of the coarse
+// density and pressure within compactSupportSub, searched on the coarse grid.
+// A child with no coarse particle in reach gets 0 (the reference divides 0 by 0).
+template <class R>
+void project(const OrcParams& P, TwoScale<R>& T, const R* pos, const R* rho, const R* prs, const int* ids,
+             const int* start, const int* end) {
+    const int nSplit = (int)T.splitIds.size();
+    R hs = R(P.compactSupportSub);
+    R hs2 = hs * hs;
+    R spacing = R(P.gridSpacing);
+    for (size_t idx = 8 * (size_t)nSplit; idx < T.subIds.size(); idx++) {
+        size_t slot = (size_t)T.subIds[idx];
+        const R* x = &T.subPos[3 * slot];
+        R d = R(0), p = R(0), count = R(0);
+        for_each_cell<R>(P, x, hs, spacing, P.gridDim, start, end, [&](int s, int e) {
+            for (int t = s; t < e; t++) {
+                int j = ids[t];
+                const R* xj = pos + 3 * (size_t)j;
+                R dx = x[0] - xj[0], dy = x[1] - xj[1], dz = x[2] - xj[2];
+                R sq = dx * dx + dy * dy + dz * dz;
+                if (sq <= hs2) {
+                    d += rho[j];
+                    p += prs[j];
+                    count += R(1);
+                }
+            }
+        });
+        T.subRho[slot] = count > R(0) ? d / count : R(0);
+        T.subPrs[slot] = count > R(0) ? p / count : R(0);
+    }
+}
+
+// The fine level (:2327-2437, 2464-2493): hash, sort, cells, density and
+// forces of the regular children, integration and collision of all children.
+template <class R>
+void sub_level_step(const OrcParams& P, const OrcOptions& O, TwoScale<R>& T, bool density, bool forces) {
+    Level<R> L = sub_level<R>(P);
+    const int nSub = (int)T.subIds.size();
+    const int nReg = 8 * (int)T.splitIds.size();
+    T.subCells = num_cells(P.gridDimSubParticles);
+    T.subHash.assign(nSub, 0);
+    T.sortedSubIds = T.subIds;
+    for (int idx = 0; idx < nSub; idx++)
+        particle_hash<R>(&T.subPos[3 * (size_t)T.subIds[idx]], P.gridOrigin, L.spacing, L.dim, &T.subHash[idx]);
+    std::vector<int> sh = T.subHash;
+    stable_sort_by_hash(sh.data(), T.sortedSubIds.data(), nSub, T.subCells);
+    T.subStart.assign(T.subCells, EMPTY);
+    T.subEnd.assign(T.subCells, EMPTY);
+    if (nSub > 0) cell_start_end(sh.data(), nSub, T.subCells, T.subStart.data(), T.subEnd.data());
+    T.subHash = sh;
+    if (density) {
+        for (int idx = 0; idx < nReg; idx++) {
+            size_t slot = (size_t)T.subIds[idx];
+            density_one<R>(P, L, nullptr, false, T.subPos.data(), T.sortedSubIds.data(), T.subStart.data(),
+                           T.subEnd.data(), &T.subPos[3 * slot], &T.subRho[slot], &T.subPrs[slot]);
+        }
+    }
+    if (forces) {
+        for (int idx = 0; idx < nReg; idx++) {
+            size_t slot = (size_t)T.subIds[idx];
+            force_one<R>(P, O, L, nullptr, true, T.subPos.data(), T.subVel.data(), T.subRho.data(),
+                         T.subPrs.data(), T.sortedSubIds.data(), T.subStart.data(), T.subEnd.data(), slot,
+                         &T.subAcc[3 * slot], &T.subScaleAcc[slot]);
+        }
+    }
+}
+
+template <class R>
+void sub_integrate_collide(const OrcParams& P, TwoScale<R>& T) {
+    R dt = R(P.timeStepSubParticles);
+    for (int slot : T.subIds) {
+        integrate_one<R>(dt, &T.subAcc[3 * (size_t)slot], &T.subPos[3 * (size_t)slot], &T.subVel[3 * (size_t)slot]);
+        collide_one<R>(P, &T.subPos[3 * (size_t)slot], &T.subVel[3 * (size_t)slot]);
+    }
+}
+
+template <class R>
+int step_two_scale(const OrcParams& P, const OrcOptions& O, const OrcMaps* M, TwoScale<R>& T, R* pos, R* vel,
+                   R* rho, R* prs, R* acc, int* hash, int* ids, int* start, int* end) {
+    const int n = T.n;
+    Level<R> L = coarse_level<R>(P);
+    int C = num_cells(P.gridDim);
+    if (hash_all<R>(P, L, pos, n, hash, ids)) return 1;
+    if (!stable_sort_by_hash(hash, ids, n, C)) return 2;
+    cell_start_end(hash, n, C, start, end);
+    for (int i = 0; i < n; i++)
+        density_one<R>(P, L, M, true, pos, ids, start, end, pos + 3 * (size_t)i, &rho[i], &prs[i]);
+    for (int i = 0; i < n; i++)
+        force_one<R>(P, O, L, M, false, pos, vel, rho, prs, ids, start, end, (size_t)i, acc + 3 * (size_t)i,
+                     nullptr);
+    particle_state<R>(P, O, T, pos, ids, start, end);
+    collect<R>(T);
+    init_children<R>(P, T, pos, vel, rho);
+    project<R>(P, T, pos, rho, prs, ids, start, end);
+    sub_level_step<R>(P, O, T, true, true);
+    for (int i = 0; i < n; i++)
+        integrate_one<R>(R(P.timeStep), acc + 3 * (size_t)i, pos + 3 * (size_t)i, vel + 3 * (size_t)i);
+    // integrateSubParticles + handleSubParticleCollisions act on each child
+    // alone, so they are fused per child; the coarse collision likewise
+    sub_integrate_collide<R>(P, T);
+    for (int i = 0; i < n; i++) collide_one<R>(P, pos + 3 * (size_t)i, vel + 3 * (size_t)i);
+    return 0;
+}
+
+// The two-scale part of AdvanceTwoScale (:2157-2171) from given coarse
+// results: pre-integration positions and velocities, densities and
+// pressures, and the coarse sort and cell tables.
+template <class R>
+int two_scale_part(const OrcParams& P, const OrcOptions& O, TwoScale<R>& T, const R* pos, const R* vel,
+                   const R* rho, const R* prs, const int* ids, const int* start, const int* end) {
+    particle_state<R>(P, O, T, pos, ids, start, end);
+    collect<R>(T);
+    init_children<R>(P, T, pos, vel, rho);
+    project<R>(P, T, pos, rho, prs, ids, start, end);
+    sub_level_step<R>(P, O, T, true, true);
+    sub_integrate_collide<R>(P, T);
+    return 0;
+}
+
+// AdvanceSubParticles (:2119-2143) on the current lists: fine hash, sort,
+// cells, density, projection, forces, integration and collision.
+template <class R>
+int step_sub_only(const OrcParams& P, const OrcOptions& O, TwoScale<R>& T, const R* pos, const R* rho,
+                  const R* prs, const int* ids, const int* start, const int* end) {
+    sub_level_step<R>(P, O, T, true, false);
+    project<R>(P, T, pos, rho, prs, ids, start, end);
+    sub_level_step<R>(P, O, T, false, true);
+    sub_integrate_collide<R>(P, T);
+    return 0;
+}
+
+}  // namespace
+
+// =============================================================================
+//  C entry points of the two-scale pass
+// =============================================================================
+extern "C" {
+
+struct OrcTwoScale;  // opaque: TwoScale<float> or TwoScale<double>
+
+void* orc_ts_new(int n, int fp64) {
+    if (fp64) return new TwoScale<double>(n);
+    return new TwoScale<float>(n);
+}
+
+void orc_ts_free(void* h, int fp64) {
+    if (fp64) delete static_cast<TwoScale<double>*>(h);
+    else delete static_cast<TwoScale<float>*>(h);
+}
+
+// mode 1: AdvanceTwoScale; coarse state updated in place, coarse outputs filled.
+int orc_ts_step_f32(void* h, const OrcParams* P, const OrcOptions* O, const OrcMaps* M, float* pos, float* vel,
+                    float* rho, float* prs, float* acc, int* hash, int* ids, int* start, int* end) {
+    return step_two_scale<float>(*P, *O, M, *static_cast<TwoScale<float>*>(h), pos, vel, rho, prs, acc, hash, ids,
+                                 start, end);
+}
+
+int orc_ts_step_f64(void* h, const OrcParams* P, const OrcOptions* O, const OrcMaps* M, double* pos, double* vel,
+                    double* rho, double* prs, double* acc, int* hash, int* ids, int* start, int* end) {
+    return step_two_scale<double>(*P, *O, M, *static_cast<TwoScale<double>*>(h), pos, vel, rho, prs, acc, hash,
+                                  ids, start, end);
+}
+
+int orc_ts_sub_only_f32(void* h, const OrcParams* P, const OrcOptions* O, const float* pos, const float* rho,
+                        const float* prs, const int* ids, const int* start, const int* end) {
+    return step_sub_only<float>(*P, *O, *static_cast<TwoScale<float>*>(h), pos, rho, prs, ids, start, end);
+}
+
+int orc_ts_sub_only_f64(void* h, const OrcParams* P, const OrcOptions* O, const double* pos, const double* rho,
+                        const double* prs, const int* ids, const int* start, const int* end) {
+    return step_sub_only<double>(*P, *O, *static_cast<TwoScale<double>*>(h), pos, rho, prs, ids, start, end);
+}
+
+int orc_ts_part_f32(void* h, const OrcParams* P, const OrcOptions* O, const float* pos, const float* vel,
+                    const float* rho, const float* prs, const int* ids, const int* start, const int* end) {
+    return two_scale_part<float>(*P, *O, *static_cast<TwoScale<float>*>(h), pos, vel, rho, prs, ids, start, end);
+}
+
+int orc_ts_part_f64(void* h, const OrcParams* P, const OrcOptions* O, const double* pos, const double* vel,
+                    const double* rho, const double* prs, const int* ids, const int* start, const int* end) {
+    return two_scale_part<double>(*P, *O, *static_cast<TwoScale<double>*>(h), pos, vel, rho, prs, ids, start,
+                                  end);
+}
+
+// counts: split, boundary, default, sub-particles, sub cells
+void orc_ts_counts(void* h, int fp64, int* out) {
+    auto fill = [&](auto& T) {
+        out[0] = (int)T.splitIds.size();
+        out[1] = (int)T.boundaryIds.size();
+        out[2] = (int)T.defaultIds.size();
+        out[3] = (int)T.subIds.size();
+        out[4] = T.subCells;
+    };
+    if (fp64) fill(*static_cast<TwoScale<double>*>(h));
+    else fill(*static_cast<TwoScale<float>*>(h));
+}
+
+// what: 0 state (uint8[n]), 1 split ids, 2 boundary ids, 3 default ids,
+// 4 sub ids, 5 sub hash (sorted), 6 sorted sub ids, 7 sub cell start,
+// 8 sub cell end (int arrays); 10 sub positions, 11 sub velocities,
+// 12 sub accelerations (R[8n*3]), 13 sub density, 14 sub pressure (R[8n]);
+// 20 state (write, uint8[n]).
+void orc_ts_get(void* h, int fp64, int what, void* dst) {
+    auto get = [&](auto& T) {
+        using R = typename std::remove_reference<decltype(T.subPos[0])>::type;
+        auto ci = [&](const std::vector<int>& v) { std::memcpy(dst, v.data(), sizeof(int) * v.size()); };
+        auto cr = [&](const std::vector<R>& v) { std::memcpy(dst, v.data(), sizeof(R) * v.size()); };
+        switch (what) {
+            case 0: std::memcpy(dst, T.state.data(), T.state.size()); break;
+            case 1: ci(T.splitIds); break;
+            case 2: ci(T.boundaryIds); break;
+            case 3: ci(T.defaultIds); break;
+            case 4: ci(T.subIds); break;
+            case 5: ci(T.subHash); break;
+            case 6: ci(T.sortedSubIds); break;
+            case 7: ci(T.subStart); break;
+            case 8: ci(T.subEnd); break;
+            case 10: cr(T.subPos); break;
+            case 11: cr(T.subVel); break;
+            case 12: cr(T.subAcc); break;
+            case 13: cr(T.subRho); break;
+            case 14: cr(T.subPrs); break;
+            case 15: cr(T.subScaleAcc); break;
+            case 20: std::memcpy(T.state.data(), dst, T.state.size()); break;
+        }
+    };
+    if (fp64) get(*static_cast<TwoScale<double>*>(h));
+    else get(*static_cast<TwoScale<float>*>(h));
 }
 
 }  // extern "C"
