@@ -101,6 +101,9 @@ struct sph_sim {
     bool graphValid = false;
     int graphMode = -1;
 
+    // FP64 diagnostics scratch: partial rows then the DIAG_TERMS results
+    double* diagBuf = nullptr;
+
     // stage timing ring
     int timingCap = 0, timingNext = 0, timingFilled = 0;
     std::vector<cudaEvent_t> events;  // timingCap * (ST_COUNT + 1)
@@ -164,6 +167,7 @@ sph_status validate_params(const SimulationParameters* P, const sph_options* O) 
                  "compactSupport exceeds gridSpacing: the 27-cell stencil would miss neighbours");
     if (O && (O->gravityAxis < 0 || O->gravityAxis > 2))
         SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "gravityAxis must be 0, 1 or 2");
+    if (O && (O->childMode < 0 || O->childMode > 1)) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "childMode must be 0 or 1");
     return SPH_OK;
 }
 
@@ -197,7 +201,7 @@ void free_all(sph_sim* s) {
     void* ptrs[] = {s->pos, s->vel, s->posS, s->velS, s->rho4S, s->accS, s->sb.cnt, s->sb.cellOffset,
                     s->sb.keySlot, s->sb.tmpIds, s->sb.sortedHash, s->sb.sortedIds, s->sb.workIds,
                     s->sb.xS, s->sb.halfOffset, s->scanBlock,
-                    s->status, s->staging, s->map4, s->mapDist, s->rowStart, s->rowMask};
+                    s->status, s->staging, s->map4, s->mapDist, s->rowStart, s->rowMask, s->diagBuf};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     void* tsPtrs[] = {s->ts.state,     s->ts.blockCounts, s->ts.blockOffsets, s->ts.counts,
@@ -268,6 +272,7 @@ sph_status ensure_two_scale(sph_sim* s) {
         T.splitMin[a] = s->O.splitMin[a];
         T.splitMax[a] = s->O.splitMax[a];
     }
+    T.childMode = s->O.childMode;
     s->subSb.cnt = T.subCnt;
     s->subSb.cellOffset = T.subOffset;
     s->subSb.tileCounter = reinterpret_cast<unsigned int*>(s->subScanBlock);
@@ -321,20 +326,22 @@ void enqueue_step(sph_sim* s, int mode, bool timing) {
     mark(ST_DENSITY);
     // density and forces read the sorted copies only
     launch_density(n, s->posS, rows_of(s), g, ph, s->map, s->rho4S, s->rowStart, s->rowMask, s->cfg, st);
+    mark(ST_FORCE);
+    // AdvanceTwoScale always runs handleCollisions (:2170)
+    const int collide = twoScale ? 1 : s->O.boxCollision;
+    launch_force(n, s->posS, s->velS, s->rho4S, s->sb.workIds, rows_of(s), g, ph, s->map, collide, s->rowStart,
+                 s->rowMask, s->pos, s->vel, s->accS, s->cfg, st);
+    mark(ST_COUNT);
     if (twoScale) {
         // computeParticleState, collect, initializeSubParticles, projectQuantities
-        // (:2157-2160) from the pre-integration sorted state
+        // (:2157-2160) from the pre-integration sorted state, which the force
+        // stage leaves as it was (it writes the new state in particle order)
         launch_ts_states(n, s->posS, s->sb.workIds, s->sb.cellOffset, g, s->P.compactSupport, s->ts, st);
+        if (s->O.childMode == 1)
+            launch_ts_merge(n, s->posS, s->velS, s->accS, s->sb.workIds, ph, collide, s->pos, s->vel, s->ts, st);
         launch_ts_children(n, s->posS, s->velS, s->rho4S, s->sb.workIds, s->P.particleMass, s->ts, st);
         launch_ts_project(s->posS, s->sb.workIds, 0, s->rho4S, s->sb.cellOffset, g, s->P.compactSupportSub,
                           s->ts, 8 * n, st);
-    }
-    mark(ST_FORCE);
-    // AdvanceTwoScale always runs handleCollisions (:2170)
-    launch_force(n, s->posS, s->velS, s->rho4S, s->sb.workIds, rows_of(s), g, ph, s->map,
-                 twoScale ? 1 : s->O.boxCollision, s->rowStart, s->rowMask, s->pos, s->vel, s->accS, s->cfg, st);
-    mark(ST_COUNT);
-    if (twoScale) {
         // the fine level (:2162-2171)
         const int cap = 8 * n;
         GridDev sg = make_grid(s->P, true);
@@ -852,6 +859,30 @@ sph_status sph_get_counts(sph_handle s, sph_counts* out) {
     out->numCells = (unsigned int)(s->P.gridDim[0] * s->P.gridDim[1] * s->P.gridDim[2]);
     out->numSubCells = (unsigned int)(s->P.gridDimSubParticles[0] * s->P.gridDimSubParticles[1] *
                                       s->P.gridDimSubParticles[2]);
+    return SPH_OK;
+}
+
+sph_status sph_get_diagnostics(sph_handle s, sph_diagnostics* out) {
+    if (!s || !out) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "NULL argument");
+    const int rows = diag_partial_rows();
+    if (!s->diagBuf) SPH_CUDA(dalloc(&s->diagBuf, (size_t)(rows + 1) * DIAG_TERMS));
+    double* res = s->diagBuf + (size_t)rows * DIAG_TERMS;
+    launch_diagnostics(s->n, s->pos, s->vel, s->rho4S, s->stepped ? 1 : 0, (double)s->P.particleMass,
+                       (double)s->P.gravity, (double)s->P.restDensity, s->O.gravityAxis, s->diagBuf, res,
+                       s->stream);
+    SPH_CUDA(cudaGetLastError());
+    double h[DIAG_TERMS];
+    SPH_CUDA(cudaMemcpyAsync(h, res, sizeof(h), cudaMemcpyDeviceToHost, s->stream));
+    sph_status st = latched_status(s);
+    if (st) return st;
+    out->mass = h[DIAG_MASS];
+    out->momentum[0] = h[DIAG_MOM_X];
+    out->momentum[1] = h[DIAG_MOM_Y];
+    out->momentum[2] = h[DIAG_MOM_Z];
+    out->kineticEnergy = h[DIAG_KINETIC];
+    out->potentialEnergy = h[DIAG_POTENTIAL];
+    out->densityMean = h[DIAG_RHO_SUM] / (double)s->n;
+    out->densityMaxRelError = h[DIAG_RHO_MAXERR];
     return SPH_OK;
 }
 

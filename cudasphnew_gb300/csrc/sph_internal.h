@@ -95,6 +95,7 @@ struct TwoScaleDev {
     int* subSortedHash;         // [8n]
     int* subSortedIds;          // [8n] slots in (fine cell, list position) order
     float splitMin[3], splitMax[3];
+    int childMode;              // sph_options.childMode
 };
 
 // Per-row lookup tables of the neighbour search.
@@ -145,6 +146,8 @@ void launch_ts_states(int n, const float4* posS, const int* workIds, const int* 
                       const TwoScaleDev& T, cudaStream_t s);
 void launch_ts_children(int n, const float4* posS, const float4* velS, const float4* rho4S, const int* workIds,
                         float mass, const TwoScaleDev& T, cudaStream_t s);
+void launch_ts_merge(int n, float4* posS, float4* velS, const float4* accS, const int* workIds, PhysDev ph,
+                     int collide, float4* pos, float4* vel, const TwoScaleDev& T, cudaStream_t s);
 void launch_ts_project(const float4* coarsePos, const int* workIds, int byId, const float4* rho4S,
                        const int* cellOffset, GridDev g, float hs, const TwoScaleDev& T, int capacity,
                        cudaStream_t s);
@@ -154,6 +157,15 @@ void launch_ts_sub_density(GridDev sg, PhysDev sph, const TwoScaleDev& T, int ca
 void launch_ts_sub_force(GridDev sg, PhysDev sph, const TwoScaleDev& T, int capacity, cudaStream_t s);
 void launch_ts_sub_integrate(PhysDev sph, const TwoScaleDev& T, int capacity, cudaStream_t s);
 void launch_ts_pack_sd(const TwoScaleDev& T, int slots, float* dst, cudaStream_t s);
+
+// FP64 diagnostics (sph_diag.cu): out[DIAG_TERMS] in this order; the maximum
+// relative density error is the last term.
+enum { DIAG_MASS = 0, DIAG_MOM_X, DIAG_MOM_Y, DIAG_MOM_Z, DIAG_KINETIC, DIAG_POTENTIAL, DIAG_RHO_SUM,
+       DIAG_RHO_MAXERR, DIAG_TERMS };
+int diag_partial_rows();
+void launch_diagnostics(int n, const float4* pos, const float4* vel, const float4* rho4S, int haveRho,
+                        double mass, double gravity, double rest0, int axis, double* partial, double* out,
+                        cudaStream_t s);
 
 // Boundary maps.
 void launch_build_maps(const sph_boundary_desc& d, const unsigned int dims[3], float* dist,

@@ -6,8 +6,11 @@
 // slots 8*parent + k of the child arrays.  Children of split particles
 // ("regular") get densities and forces at h/2 on the fine grid; children of
 // boundary particles get the mean coarse density and pressure around them.
-// All children are integrated and collided; nothing feeds back into the
-// coarse particles, as in the reference.
+// All children are integrated and collided.  With childMode 0 children are
+// re-seeded in every step and nothing feeds back into the coarse particles,
+// as in the reference; with childMode 1 they persist while their parent keeps
+// its class, and a parent leaving the split class takes its children's mean
+// position and velocity (merge-back).
 //
 // Counts stay on the device: the kernels of the fine level loop over the
 // device-side counts (grid-stride), so a two-scale step needs no host
@@ -31,6 +34,9 @@ __device__ __forceinline__ float ref_r2(float4 a, float4 b) {
     const float rx = __fsub_rn(a.x, b.x), ry = __fsub_rn(a.y, b.y), rz = __fsub_rn(a.z, b.z);
     return __fadd_rn(__fadd_rn(__fmul_rn(rx, rx), __fmul_rn(ry, ry)), __fmul_rn(rz, rz));
 }
+
+// Class of a 2-bit state: 1 split (bit 0, as collect reads it), 2 boundary, 0 default.
+__device__ __forceinline__ int state_class(unsigned int c) { return (c & 1u) ? 1 : (c == 2u ? 2 : 0); }
 
 inline int stride_grid(long long work, int bs) {
     long long g = (work + bs - 1) / bs;
@@ -198,7 +204,10 @@ __global__ void k_ts_init(int n, const float4* __restrict__ posS, const float4* 
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const int id = workIds[k];
-    if ((T.state[id] & 3) == 0) return;
+    const unsigned int code = T.state[id] & 15u;
+    if ((code & 3u) == 0) return;
+    // childMode 1: seed only on a class change (:1052-1055)
+    if (T.childMode == 1 && state_class(code >> 2) == state_class(code & 3u)) return;
     const double rad = (double)(3.0f * mass) / (4.0 * 3.14159265358979323846 * (double)rho4S[k].x);
     const float radicand = (float)rad;
     const float radius = (float)pow((double)radicand, (double)(1.0f / 3.0f));
@@ -212,6 +221,46 @@ __global__ void k_ts_init(int n, const float4* __restrict__ posS, const float4* 
                                      __fmaf_rn(sz, radius, x.z), 0.f);
         T.subVel[slot] = make_float4(v.x, v.y, v.z, 0.f);
     }
+}
+
+// ---------------------------------------------------------------------------
+// Merge-back (childMode 1, no reference counterpart).  Runs after the coarse
+// force stage, before the children are re-seeded: a parent whose class went
+// from split to boundary or default takes the mean of its eight children
+// (summed in slot order, times 1/8) as its pre-integration position and
+// velocity -- written to the sorted copies, which seeding and projection read
+// next -- and is integrated and collided again from there with the
+// acceleration the force stage computed at its own position.
+// ---------------------------------------------------------------------------
+__global__ void k_ts_merge(int n, float4* __restrict__ posS, float4* __restrict__ velS,
+                           const float4* __restrict__ accS, const int* __restrict__ workIds, PhysDev ph,
+                           int collideFlag, float4* __restrict__ pos, float4* __restrict__ vel, TwoScaleDev T) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int id = workIds[k];
+    const unsigned int code = T.state[id] & 15u;
+    if (state_class(code >> 2) != 1 || state_class(code & 3u) == 1) return;
+    float sx = 0.f, sy = 0.f, sz = 0.f, ux = 0.f, uy = 0.f, uz = 0.f;
+    for (int c = 0; c < 8; c++) {
+        const float4 a = T.subPos[8 * (size_t)id + c], b = T.subVel[8 * (size_t)id + c];
+        sx = __fadd_rn(sx, a.x);
+        sy = __fadd_rn(sy, a.y);
+        sz = __fadd_rn(sz, a.z);
+        ux = __fadd_rn(ux, b.x);
+        uy = __fadd_rn(uy, b.y);
+        uz = __fadd_rn(uz, b.z);
+    }
+    const float4 x0 = posS[k], v0 = velS[k];
+    const float3 xm = make_float3(sx * 0.125f, sy * 0.125f, sz * 0.125f);
+    const float3 vm = make_float3(ux * 0.125f, uy * 0.125f, uz * 0.125f);
+    posS[k] = make_float4(xm.x, xm.y, xm.z, x0.w);
+    velS[k] = make_float4(vm.x, vm.y, vm.z, v0.w);
+    const float4 a = accS[k];
+    float3 v = make_float3(vm.x + ph.dt * a.x, vm.y + ph.dt * a.y, vm.z + ph.dt * a.z);
+    float3 x = make_float3(xm.x + ph.dt * v.x, xm.y + ph.dt * v.y, xm.z + ph.dt * v.z);
+    if (collideFlag) collide(ph, x, v);
+    pos[id] = make_float4(x.x, x.y, x.z, 0.f);
+    vel[id] = make_float4(v.x, v.y, v.z, 0.f);
 }
 
 // ---------------------------------------------------------------------------
@@ -443,6 +492,11 @@ void launch_ts_children(int n, const float4* posS, const float4* velS, const flo
                         float mass, const TwoScaleDev& T, cudaStream_t s) {
     if (n <= 0) return;
     k_ts_init<<<(n + 127) / 128, 128, 0, s>>>(n, posS, velS, rho4S, workIds, mass, T);
+}
+
+void launch_ts_merge(int n, float4* posS, float4* velS, const float4* accS, const int* workIds, PhysDev ph,
+                     int collide, float4* pos, float4* vel, const TwoScaleDev& T, cudaStream_t s) {
+    k_ts_merge<<<(n + 255) / 256, 256, 0, s>>>(n, posS, velS, accS, workIds, ph, collide, pos, vel, T);
 }
 
 void launch_ts_project(const float4* coarsePos, const int* workIds, int byId, const float4* rho4S,

@@ -42,6 +42,7 @@ SIGNATURES = {
     "sph_write": (_i, [_vp, _i, _vp, ctypes.c_size_t]),
     "sph_read_cells": (_i, [_vp, _i, _vp, _vp, _vp, _vp]),
     "sph_get_counts": (_i, [_vp, _vp]),
+    "sph_get_diagnostics": (_i, [_vp, _vp]),
     "sph_device_pointer": (_i, [_vp, _i, _vp]),
     "sph_boundary_dims": (_i, [_vp, _vp]),
     "sph_boundary_maps": (_i, [_vp, _vp, _vp, _vp]),
@@ -61,6 +62,14 @@ class Counts(ctypes.Structure):
     _fields_ = [(name, ctypes.c_uint) for name in (
         "numParticles", "numParticlesDefault", "numParticlesSplit", "numParticlesBoundary",
         "numSubParticles", "numTimeSteps", "numCells", "numSubCells")]
+
+
+class Diagnostics(ctypes.Structure):
+    """sph_diagnostics: FP64 conservation terms of the coarse particles."""
+
+    _fields_ = [("mass", ctypes.c_double), ("momentum", ctypes.c_double * 3),
+                ("kineticEnergy", ctypes.c_double), ("potentialEnergy", ctypes.c_double),
+                ("densityMean", ctypes.c_double), ("densityMaxRelError", ctypes.c_double)]
 
 
 class Tuning(ctypes.Structure):
@@ -205,6 +214,11 @@ class ParticleSimulation:
         c = Counts()
         check(load().sph_get_counts(self._h, ctypes.byref(c)))
         return c
+
+    def diagnostics(self) -> Diagnostics:
+        d = Diagnostics()
+        check(load().sph_get_diagnostics(self._h, ctypes.byref(d)))
+        return d
 
     def read(self, field: int) -> np.ndarray:
         n = self.n

@@ -73,7 +73,7 @@ class Options(ctypes.Structure):
     _fields_ = [
         ("gravityAxis", ctypes.c_int),
         ("boxCollision", ctypes.c_int),
-        ("reserved0", ctypes.c_int),
+        ("childMode", ctypes.c_int),
         ("reserved1", ctypes.c_int),
         ("splitMin", F3),
         ("splitMax", F3),

@@ -78,7 +78,15 @@ typedef struct sph_options {
                            reference: 1, particle_simulation.cu:471 */
     int boxCollision;   /* 1: collision_handling after integrate in every
                            step (AdvanceTwoScale, :2170); 0: Advance (:2106) */
-    int reserved0;
+    int childMode;      /* two-scale children.  0: re-seeded from their parent
+                           in every step, as the reference runs
+                           (initialize_sub_particles, :1023-1090).  1: kept
+                           while the parent stays in its class; seeded when
+                           the parent enters the split or boundary class or
+                           moves between them (the transitions listed at
+                           :1052-1055); a parent leaving the split class
+                           first takes its children's mean position and
+                           velocity (merge-back, no reference counterpart) */
     int reserved1;
     float splitMin[3];  /* two-scale split region; reference: 0.2 <= x <= 0.5 */
     float splitMax[3];  /* (find_split_particles, :948) */
@@ -215,6 +223,23 @@ sph_status sph_read_cells(sph_handle h, int level, int* sortedHash, int* sortedI
 
 /* Particle counts (GetNumParticles*, GetNumSubParticles*, GetNumTimesSteps). */
 sph_status sph_get_counts(sph_handle h, sph_counts* out);
+
+/* FP64 conservation diagnostics of the coarse particles (no reference
+ * counterpart; the reference's SD_ENERGY column, particle_simulation.h:40, is
+ * never filled).  mass, momentum and energies are of the current state,
+ * potential = sum m*g*x[gravityAxis]; the density terms are of the last
+ * density pass (zero before the first step).  Reduced on the GPU in double
+ * precision in a fixed order, so repeated calls on one state agree bit for
+ * bit.  Synchronises the handle's stream. */
+typedef struct sph_diagnostics {
+    double mass;
+    double momentum[3];
+    double kineticEnergy;
+    double potentialEnergy;
+    double densityMean;
+    double densityMaxRelError; /* max |rho - restDensity| / restDensity */
+} sph_diagnostics;
+sph_status sph_get_diagnostics(sph_handle h, sph_diagnostics* out);
 
 /* Device pointer of a field in the handle's layout, for zero-copy consumers
  * (replaces the OpenGL VBO getters, :2278-2301): 0 = positions (float4[n],

@@ -243,6 +243,12 @@ class TwoScale:
         a = np.ascontiguousarray(state, np.uint8)
         lib().orc_ts_get(self._h, 1 if self.fp64 else 0, 20, _ptr(a))
 
+    def set_children(self, pos: np.ndarray, vel: np.ndarray) -> None:
+        """Overwrites the 8n child positions and velocities (slot order)."""
+        for what, a in ((21, pos), (22, vel)):
+            a = np.ascontiguousarray(np.asarray(a).reshape(8 * self.n, 3), self.dt)
+            lib().orc_ts_get(self._h, 1 if self.fp64 else 0, what, _ptr(a))
+
     def step(self, p, o, bm, pos, vel):
         """AdvanceTwoScale; returns the coarse outputs like step_plain."""
         n = self.n

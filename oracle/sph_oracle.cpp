@@ -73,7 +73,7 @@ struct OrcParams {
 struct OrcOptions {
     int gravityAxis;      // reference: 1 (acc.y -= gravity, particle_simulation.cu:471)
     int boxCollision;     // run collision_handling after integrate (AdvanceTwoScale order)
-    int reserved0;
+    int childMode;        // 0: children re-seeded every step; 1: persistent + merge-back
     int reserved1;
     float splitMin[3];    // two-scale split region (reference: 0.2 <= x <= 0.5)
     float splitMax[3];
@@ -935,9 +935,38 @@ void collect(TwoScale<R>& T) {
         for (int k = 0; k < 8; k++) T.subIds.push_back(8 * p + k);
 }
 
-// initialize_sub_particles (:1023-1090) for split and boundary parents.
+// Class of a 2-bit state: 1 split (bit 0, collect's c == 1 || c == 3),
+// 2 boundary, 0 default.
+inline int state_class(int c) { return (c & 1) ? 1 : (c == 2 ? 2 : 0); }
+
+// Merge-back (childMode 1; no reference counterpart): a parent whose class
+// changes from split to boundary or default takes the mean position and
+// velocity of its eight children (summed in slot order, times 1/8) before its
+// coarse integration.  Its coarse acceleration stays the one computed at its
+// own position.
 template <class R>
-void init_children(const OrcParams& P, TwoScale<R>& T, const R* pos, const R* vel, const R* rho) {
+void merge_back(TwoScale<R>& T, R* pos, R* vel) {
+    for (int i = 0; i < T.n; i++) {
+        int code = T.state[i] & 15;
+        if (state_class(code >> 2) != 1 || state_class(code & 3) == 1) continue;
+        for (int a = 0; a < 3; a++) {
+            R sx = R(0), sv = R(0);
+            for (int k = 0; k < 8; k++) {
+                sx += T.subPos[3 * (8 * (size_t)i + k) + a];
+                sv += T.subVel[3 * (8 * (size_t)i + k) + a];
+            }
+            pos[3 * (size_t)i + a] = sx * R(0.125);
+            vel[3 * (size_t)i + a] = sv * R(0.125);
+        }
+    }
+}
+
+// initialize_sub_particles (:1023-1090) for split and boundary parents; with
+// childMode 1 only for parents whose class changed (the transitions that
+// the reference lists at :1052-1055 and leaves commented out).
+template <class R>
+void init_children(const OrcParams& P, const OrcOptions& O, TwoScale<R>& T, const R* pos, const R* vel,
+                   const R* rho) {
     auto seed = [&](int id) {
         float radius = child_radius(P.particleMass, (float)rho[id]);
         for (int k = 0; k < 8; k++) {
@@ -951,8 +980,14 @@ void init_children(const OrcParams& P, TwoScale<R>& T, const R* pos, const R* ve
             }
         }
     };
-    for (int p : T.splitIds) seed(p);
-    for (int p : T.boundaryIds) seed(p);
+    auto changed = [&](int id) {
+        int code = T.state[id] & 15;
+        return O.childMode == 0 || state_class(code >> 2) != state_class(code & 3);
+    };
+    for (int p : T.splitIds)
+        if (changed(p)) seed(p);
+    for (int p : T.boundaryIds)
+        if (changed(p)) seed(p);
 }
 
 // project_quantities (:570-622, 1328-1381): unweighted mean of the coarse
@@ -1046,8 +1081,9 @@ int step_two_scale(const OrcParams& P, const OrcOptions& O, const OrcMaps* M, Tw
         force_one<R>(P, O, L, M, false, pos, vel, rho, prs, ids, start, end, (size_t)i, acc + 3 * (size_t)i,
                      nullptr);
     particle_state<R>(P, O, T, pos, ids, start, end);
+    if (O.childMode == 1) merge_back<R>(T, pos, vel);
     collect<R>(T);
-    init_children<R>(P, T, pos, vel, rho);
+    init_children<R>(P, O, T, pos, vel, rho);
     project<R>(P, T, pos, rho, prs, ids, start, end);
     sub_level_step<R>(P, O, T, true, true);
     for (int i = 0; i < n; i++)
@@ -1066,9 +1102,11 @@ template <class R>
 int two_scale_part(const OrcParams& P, const OrcOptions& O, TwoScale<R>& T, const R* pos, const R* vel,
                    const R* rho, const R* prs, const int* ids, const int* start, const int* end) {
     particle_state<R>(P, O, T, pos, ids, start, end);
+    std::vector<R> mpos(pos, pos + 3 * (size_t)T.n), mvel(vel, vel + 3 * (size_t)T.n);
+    if (O.childMode == 1) merge_back<R>(T, mpos.data(), mvel.data());
     collect<R>(T);
-    init_children<R>(P, T, pos, vel, rho);
-    project<R>(P, T, pos, rho, prs, ids, start, end);
+    init_children<R>(P, O, T, mpos.data(), mvel.data(), rho);
+    project<R>(P, T, mpos.data(), rho, prs, ids, start, end);
     sub_level_step<R>(P, O, T, true, true);
     sub_integrate_collide<R>(P, T);
     return 0;
@@ -1179,6 +1217,8 @@ void orc_ts_get(void* h, int fp64, int what, void* dst) {
             case 14: cr(T.subPrs); break;
             case 15: cr(T.subScaleAcc); break;
             case 20: std::memcpy(T.state.data(), dst, T.state.size()); break;
+            case 21: std::memcpy(T.subPos.data(), dst, sizeof(R) * T.subPos.size()); break;
+            case 22: std::memcpy(T.subVel.data(), dst, sizeof(R) * T.subVel.size()); break;
         }
     };
     if (fp64) get(*static_cast<TwoScale<double>*>(h));

@@ -42,6 +42,8 @@ int main(void) {
     printf("sph_options %zu\n", sizeof(sph_options));
     printf("sph_boundary_desc %zu\n", sizeof(sph_boundary_desc));
     printf("sph_counts %zu\n", sizeof(sph_counts));
+    printf("sph_diagnostics %zu\n", sizeof(sph_diagnostics));
+    O(sph_diagnostics, kineticEnergy); O(sph_diagnostics, densityMaxRelError);
     O(SimulationParameters, numParticles); O(SimulationParameters, timeStep);
     O(SimulationParameters, poly6); O(SimulationParameters, laplViscSub);
     O(SimulationParameters, boxDim); O(SimulationParameters, restitution);
@@ -65,12 +67,13 @@ def test_struct_layouts_match_header():
     assert lay["sph_options"] == ctypes.sizeof(P.Options)
     assert lay["sph_boundary_desc"] == ctypes.sizeof(P.BoundaryDesc)
     assert lay["sph_counts"] == ctypes.sizeof(sphmod.Counts)
+    assert lay["sph_diagnostics"] == ctypes.sizeof(sphmod.Diagnostics)
     for key, v in lay.items():
         if "." not in key:
             continue
         t, f = key.split(".")
         cls = {"SimulationParameters": P.SimulationParameters, "sph_options": P.Options,
-               "sph_boundary_desc": P.BoundaryDesc}[t]
+               "sph_boundary_desc": P.BoundaryDesc, "sph_diagnostics": sphmod.Diagnostics}[t]
         assert getattr(cls, f).offset == v, key
 
 

@@ -300,3 +300,40 @@ def test_autotune_leaves_state_untouched(sphlib):
         sim.Advance()
         ref.Advance()
         np.testing.assert_array_equal(sim.positions(), ref.positions())
+
+
+def test_fp64_diagnostics(sphlib):
+    """sph_get_diagnostics against an FP64 numpy sum of the same state."""
+    sc = scenes.config1()
+    with sphlib.ParticleSimulation(sc.params, sc.positions, sc.velocities, sc.options, sc.boundary) as sim:
+        d0 = sim.diagnostics()
+        assert d0.densityMean == 0.0 and d0.densityMaxRelError == 0.0
+        sim.step(count=20)
+        d = sim.diagnostics()
+        d2 = sim.diagnostics()
+        x = sim.positions().astype(np.float64)
+        v = sim.velocities().astype(np.float64)
+        rho = sim.read(sphlib.FIELD_DENSITY).astype(np.float64)
+    assert bytes(d) == bytes(d2)  # fixed reduction order
+    m = float(np.float32(sc.params.particleMass))
+    g = float(np.float32(sc.params.gravity))
+    rest = float(np.float32(sc.params.restDensity))
+    n = len(x)
+    rel = 1e-12
+    assert abs(d.mass - n * m) <= rel * n * m
+    mom = m * v.sum(0)
+    scale = m * np.abs(v).sum(0)
+    for a in range(3):
+        assert abs(d.momentum[a] - mom[a]) <= rel * scale[a] + 1e-300
+    ke = 0.5 * m * (v * v).sum()
+    assert abs(d.kineticEnergy - ke) <= rel * ke
+    ax = sc.options.gravityAxis
+    pe = m * g * x[:, ax].sum()
+    assert abs(d.potentialEnergy - pe) <= rel * m * g * np.abs(x[:, ax]).sum()
+    # the density terms are of the last density pass, which saw the state
+    # before the last integration; FIELD_DENSITY reads that same pass
+    assert abs(d.densityMean - rho.mean()) <= rel * rho.mean()
+    assert d.densityMaxRelError == np.abs(rho - rest).max() / rest or \
+        abs(d.densityMaxRelError - np.abs(rho - rest).max() / rest) <= 1e-15
+    # the dam break falls: the potential energy drops and kinetic energy appears
+    assert d.kineticEnergy > 0.0

@@ -15,8 +15,20 @@ pytestmark = pytest.mark.gpu
 TOL = 1e-5
 
 
-def small_scene():
-    return scenes.two_scale(nb=24, region=(0.1, 0.2), box=0.5, name="two_scale_small")
+def small_scene(child_mode=0):
+    sc = scenes.two_scale(nb=24, region=(0.1, 0.2), box=0.5, name="two_scale_small")
+    sc.options.childMode = child_mode
+    return sc
+
+
+def merge_scene():
+    """Persistent children; the block moves down at 1 m/s with the split
+    region's lower faces just below a lattice plane, so split parents leave
+    the region within a few steps."""
+    sc = scenes.two_scale(nb=24, region=(0.106, 0.2), box=0.5, name="two_scale_merge")
+    sc.options.childMode = 1
+    sc.velocities[:, 2] = -1.0
+    return sc
 
 
 def coarse_inputs(sphlib, sim):
@@ -134,8 +146,59 @@ def test_sub_only_step(sphlib, orc):
     assert np.abs(after[ids] - pos64[ids]).max() < 1e-5
 
 
-def test_two_scale_graph_matches_eager_and_is_deterministic(sphlib):
-    sc = small_scene()
+def test_persistent_children_and_merge_back(sphlib, orc):
+    sc = merge_scene()
+    n = sc.n
+    o32 = orc.TwoScale(n)
+    o64 = orc.TwoScale(n, fp64=True)
+    dt = np.float32(sc.params.timeStep)
+    merged = kept = 0
+    with sphlib.ParticleSimulation(sc.params, sc.positions, sc.velocities, sc.options) as sim:
+        sp = sv = None
+        for step in range(6):
+            x0, v0 = sim.positions(), sim.velocities()
+            if step > 0:
+                sp = sim.read(sphlib.FIELD_SUB_VERTEX_DATA)
+                sv = sim.read(sphlib.FIELD_SUB_SIMULATION_DATA)[:, 6:9].copy()
+                for T in (o32, o64):
+                    T.set_children(sp, sv)
+            sim.AdvanceTwoScale()
+            g = gpu_two_scale(sphlib, sim)
+            check_against_oracle(orc, sc, g, o32, o64, x0, v0, coarse_inputs(sphlib, sim))
+            code = g["state"].astype(np.int32) & 15
+            if step == 0:
+                continue
+            # parents split in both steps keep their children: not re-seeded
+            stay = np.nonzero(code == 15)[0]
+            kept += len(stay)
+            # parents leaving the split class: mean of the children, then integrated
+            leave = np.nonzero((((code >> 2) & 1) == 1) & ((code & 1) == 0))[0]
+            if len(leave) == 0:
+                continue
+            merged += len(leave)
+            cx = sp.reshape(n, 8, 3)[leave]
+            cv = sv.reshape(n, 8, 3)[leave]
+            mx = np.zeros((len(leave), 3), np.float32)
+            mv = np.zeros((len(leave), 3), np.float32)
+            for k in range(8):
+                mx += cx[:, k]
+                mv += cv[:, k]
+            mx *= np.float32(0.125)
+            mv *= np.float32(0.125)
+            acc = sim.read(sphlib.FIELD_ACCELERATION)[leave]
+            v = mv + dt * acc
+            x = mx + dt * v
+            gx, gv = sim.positions()[leave], sim.velocities()[leave]
+            np.testing.assert_allclose(gv, v, rtol=0, atol=float(4 * np.spacing(np.abs(v).max())))
+            np.testing.assert_allclose(gx, x, rtol=0, atol=float(4 * np.spacing(np.abs(x).max())))
+            # the merged position is not where the coarse particle alone would be
+            assert np.abs(gx - (x0[leave] + dt * (v0[leave] + dt * acc))).max() > 0
+    assert merged > 0 and kept > 0
+
+
+@pytest.mark.parametrize("child_mode", [0, 1])
+def test_two_scale_graph_matches_eager_and_is_deterministic(sphlib, child_mode):
+    sc = small_scene(child_mode)
     outs = []
     for graph in (False, True, True):
         with sphlib.ParticleSimulation(sc.params, sc.positions, sc.velocities, sc.options) as sim:
