@@ -11,7 +11,7 @@
 #include <string>
 #include <vector>
 
-#include "sph_internal.h"
+#include "sph_sim.h"
 
 using namespace sph;
 
@@ -28,25 +28,8 @@ sph_status fail(sph_status st, const char* file, int line, const std::string& ms
     return st;
 }
 
-#define SPH_FAIL(st, msg) return fail((st), __FILE__, __LINE__, (msg))
-#define SPH_CUDA(call)                                                                   \
-    do {                                                                                 \
-        cudaError_t e_ = (call);                                                         \
-        if (e_ != cudaSuccess) {                                                         \
-            sph_status st_ = e_ == cudaErrorMemoryAllocation ? SPH_ERR_OUT_OF_MEMORY      \
-                                                             : SPH_ERR_CUDA;              \
-            return fail(st_, __FILE__, __LINE__, cudaGetErrorString(e_));                 \
-        }                                                                                \
-    } while (0)
-
-enum Stage { ST_HASH, ST_SCAN, ST_SCATTER, ST_RANK, ST_DENSITY, ST_FORCE, ST_COUNT };
 const char* kStageNames[ST_COUNT] = {"hash_count", "cell_scan", "scatter", "rank_gather",
                                      "density", "force_integrate"};
-
-template <class T>
-cudaError_t dalloc(T** p, size_t count) {
-    return cudaMalloc((void**)p, sizeof(T) * (count > 0 ? count : 1));
-}
 
 }  // namespace
 
@@ -58,58 +41,8 @@ sph_status record_error(sph_status st, const char* file, int line, const std::st
 }
 }  // namespace sph
 
-struct sph_sim {
-    SimulationParameters P;
-    sph_options O;
-    int n = 0;
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    cudaStream_t ownStream = nullptr;
 
-    // state (particle order) and per-step sorted copies
-    float4 *pos = nullptr, *vel = nullptr;
-    float4 *posS = nullptr, *velS = nullptr, *rho4S = nullptr, *accS = nullptr;
-    int* rowStart = nullptr;          // [9][n] neighbour-row windows recorded by the density stage
-    unsigned int* rowMask = nullptr;  // [9][n] their neighbour masks
-    SortBuffers sb{};
-    unsigned long long* scanBlock = nullptr;
-    unsigned int* status = nullptr;     // device status word
-    unsigned int* statusHost = nullptr; // pinned copy
-    float* staging = nullptr;           // device AoS staging, n*10 floats
-    std::vector<float> sdMass, sdEnergy;  // SD_MASS / SD_ENERGY columns (never touched by the step)
-
-    // boundary maps
-    float4* map4 = nullptr;
-    float* mapDist = nullptr;
-    MapDev map{};
-
-    unsigned int numTimeSteps = 0;
-    bool stepped = false;
-
-    // launch configuration
-    StepConfig cfg;
-
-    // two-scale pass (allocated on first use)
-    TwoScaleDev ts{};
-    SortBuffers subSb{};
-    unsigned long long* subScanBlock = nullptr;
-    bool tsReady = false;
-
-    // CUDA graph of one step of graphMode
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t graphExec = nullptr;
-    bool graphValid = false;
-    int graphMode = -1;
-
-    // FP64 diagnostics scratch: partial rows then the DIAG_TERMS results
-    double* diagBuf = nullptr;
-
-    // stage timing ring
-    int timingCap = 0, timingNext = 0, timingFilled = 0;
-    std::vector<cudaEvent_t> events;  // timingCap * (ST_COUNT + 1)
-};
-
-namespace {
+namespace sph {
 
 RowTables rows_of(const sph_sim* s) { return RowTables{s->sb.cellOffset, s->sb.halfOffset}; }
 
@@ -365,7 +298,7 @@ sph_status latched_status(sph_sim* s) {
     return SPH_OK;
 }
 
-}  // namespace
+}  // namespace sph
 
 extern "C" {
 

@@ -1,0 +1,111 @@
+// The simulation handle behind the C ABI and the host helpers that the
+// translation units orchestrating a step share (sph_api.cu, sph_corrector.cu).
+// Not part of the public ABI.
+#pragma once
+
+#include <string>
+#include <vector>
+
+#include "sph_internal.h"
+
+namespace sph {
+// Records a failure in the per-thread message sph_last_error() returns and
+// passes the status through (the reference's message shape, util.h:24-39).
+sph_status record_error(sph_status st, const char* file, int line, const std::string& msg);
+}  // namespace sph
+
+#define SPH_FAIL(st, msg) return sph::record_error((st), __FILE__, __LINE__, (msg))
+#define SPH_CUDA(call)                                                                   \
+    do {                                                                                 \
+        cudaError_t e_ = (call);                                                         \
+        if (e_ != cudaSuccess) {                                                         \
+            sph_status st_ = e_ == cudaErrorMemoryAllocation ? SPH_ERR_OUT_OF_MEMORY      \
+                                                             : SPH_ERR_CUDA;              \
+            return sph::record_error(st_, __FILE__, __LINE__, cudaGetErrorString(e_));    \
+        }                                                                                \
+    } while (0)
+
+namespace sph {
+
+enum Stage { ST_HASH, ST_SCAN, ST_SCATTER, ST_RANK, ST_DENSITY, ST_FORCE, ST_COUNT };
+
+template <class T>
+cudaError_t dalloc(T** p, size_t count) {
+    return cudaMalloc((void**)p, sizeof(T) * (count > 0 ? count : 1));
+}
+
+struct Corrector;  // sph_corrector.cu
+
+}  // namespace sph
+
+struct sph_sim {
+    SimulationParameters P;
+    sph_options O;
+    int n = 0;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaStream_t ownStream = nullptr;
+
+    // state (particle order) and per-step sorted copies
+    float4 *pos = nullptr, *vel = nullptr;
+    float4 *posS = nullptr, *velS = nullptr, *rho4S = nullptr, *accS = nullptr;
+    int* rowStart = nullptr;          // [9][n] neighbour-row windows recorded by the density stage
+    unsigned int* rowMask = nullptr;  // [9][n] their neighbour masks
+    sph::SortBuffers sb{};
+    unsigned long long* scanBlock = nullptr;
+    unsigned int* status = nullptr;     // device status word
+    unsigned int* statusHost = nullptr; // pinned copy
+    float* staging = nullptr;           // device AoS staging, n*10 floats
+    std::vector<float> sdMass, sdEnergy;  // SD_MASS / SD_ENERGY columns (never touched by the step)
+
+    // boundary maps
+    float4* map4 = nullptr;
+    float* mapDist = nullptr;
+    sph::MapDev map{};
+
+    unsigned int numTimeSteps = 0;
+    bool stepped = false;
+
+    // launch configuration
+    sph::StepConfig cfg;
+
+    // two-scale pass (allocated on first use)
+    sph::TwoScaleDev ts{};
+    sph::SortBuffers subSb{};
+    unsigned long long* subScanBlock = nullptr;
+    bool tsReady = false;
+
+    // CUDA graph of one step of graphMode
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graphExec = nullptr;
+    bool graphValid = false;
+    int graphMode = -1;
+
+    // learned step corrector (sph_corrector.cu; allocated on first use)
+    sph::Corrector* corr = nullptr;
+
+    // FP64 diagnostics scratch: partial rows then the DIAG_TERMS results
+    double* diagBuf = nullptr;
+
+    // stage timing ring
+    int timingCap = 0, timingNext = 0, timingFilled = 0;
+    std::vector<cudaEvent_t> events;  // timingCap * (sph::ST_COUNT + 1)
+};
+
+
+namespace sph {
+
+RowTables rows_of(const sph_sim* s);
+GridDev make_grid(const SimulationParameters& P, bool sub);
+PhysDev make_phys(const SimulationParameters& P, const sph_options& O);
+PhysDev make_sub_phys(const SimulationParameters& P, const sph_options& O);
+sph_status validate_params(const SimulationParameters* P, const sph_options* O);
+sph_status check_desc(const sph_boundary_desc* d, unsigned int dims[3]);
+void free_all(sph_sim* s);
+sph_status ensure_two_scale(sph_sim* s);
+// Enqueues one step of `mode` (no host synchronisation).
+void enqueue_step(sph_sim* s, int mode, bool timing);
+// Waits for the handle's stream and maps the latched device status.
+sph_status latched_status(sph_sim* s);
+
+}  // namespace sph
