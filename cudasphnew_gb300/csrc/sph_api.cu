@@ -128,6 +128,7 @@ sph_status check_desc(const sph_boundary_desc* d, unsigned int dims[3]) {
 }
 
 void free_all(sph_sim* s) {
+    corrector_free(s);
     if (s->graphExec) cudaGraphExecDestroy(s->graphExec);
     if (s->graph) cudaGraphDestroy(s->graph);
     for (cudaEvent_t e : s->events) cudaEventDestroy(e);
@@ -217,6 +218,46 @@ sph_status ensure_two_scale(sph_sim* s) {
 }
 
 // Enqueues one step of `mode` (no host synchronisation).
+void enqueue_coarse(sph_sim* s, const GridDev& g, const PhysDev& ph, int collide, cudaEvent_t* ev) {
+    cudaStream_t st = s->stream;
+    const int n = s->n;
+    auto mark = [&](int k) {
+        if (ev) cudaEventRecord(ev[k], st);
+    };
+    mark(ST_HASH);
+    launch_hash_count(n, s->pos, g, s->sb, s->status, st);
+    mark(ST_SCAN);
+    launch_cell_scan(g.numCells, s->sb, s->status, st);
+    mark(ST_SCATTER);
+    launch_scatter(n, s->sb, st);
+    mark(ST_RANK);
+    launch_rank_gather(n, s->sb, s->pos, s->vel, g, s->posS, s->velS, st);
+    mark(ST_DENSITY);
+    // density and forces read the sorted copies only
+    launch_density(n, s->posS, rows_of(s), g, ph, s->map, s->rho4S, s->rowStart, s->rowMask, s->cfg, st);
+    mark(ST_FORCE);
+    launch_force(n, s->posS, s->velS, s->rho4S, s->sb.workIds, rows_of(s), g, ph, s->map, collide, s->rowStart,
+                 s->rowMask, s->pos, s->vel, s->accS, s->cfg, st);
+    mark(ST_COUNT);
+}
+
+void enqueue_density_only(sph_sim* s, const float4* pos, const float4* vel) {
+    cudaStream_t st = s->stream;
+    const int n = s->n;
+    GridDev g = make_grid(s->P, false);
+    PhysDev ph = make_phys(s->P, s->O);
+    launch_hash_count(n, pos, g, s->sb, s->status, st);
+    launch_cell_scan(g.numCells, s->sb, s->status, st);
+    launch_scatter(n, s->sb, st);
+    launch_rank_gather(n, s->sb, pos, vel, g, s->posS, s->velS, st);
+    launch_density(n, s->posS, rows_of(s), g, ph, s->map, s->rho4S, s->rowStart, s->rowMask, s->cfg, st);
+}
+
+void invalidate_graphs(sph_sim* s) {
+    s->graphValid = false;
+    s->graphGen++;
+}
+
 void enqueue_step(sph_sim* s, int mode, bool timing) {
     if (mode == SPH_STEP_SUB_ONLY) {
         if (!s->tsReady) return;
@@ -245,26 +286,9 @@ void enqueue_step(sph_sim* s, int mode, bool timing) {
         s->timingNext = (s->timingNext + 1) % s->timingCap;
         s->timingFilled = std::min(s->timingFilled + 1, s->timingCap);
     }
-    auto mark = [&](int k) {
-        if (ev) cudaEventRecord(ev[k], st);
-    };
-    mark(ST_HASH);
-    launch_hash_count(n, s->pos, g, s->sb, s->status, st);
-    mark(ST_SCAN);
-    launch_cell_scan(g.numCells, s->sb, s->status, st);
-    mark(ST_SCATTER);
-    launch_scatter(n, s->sb, st);
-    mark(ST_RANK);
-    launch_rank_gather(n, s->sb, s->pos, s->vel, g, s->posS, s->velS, st);
-    mark(ST_DENSITY);
-    // density and forces read the sorted copies only
-    launch_density(n, s->posS, rows_of(s), g, ph, s->map, s->rho4S, s->rowStart, s->rowMask, s->cfg, st);
-    mark(ST_FORCE);
     // AdvanceTwoScale always runs handleCollisions (:2170)
     const int collide = twoScale ? 1 : s->O.boxCollision;
-    launch_force(n, s->posS, s->velS, s->rho4S, s->sb.workIds, rows_of(s), g, ph, s->map, collide, s->rowStart,
-                 s->rowMask, s->pos, s->vel, s->accS, s->cfg, st);
-    mark(ST_COUNT);
+    enqueue_coarse(s, g, ph, collide, ev);
     if (twoScale) {
         // computeParticleState, collect, initializeSubParticles, projectQuantities
         // (:2157-2160) from the pre-integration sorted state, which the force
@@ -456,6 +480,8 @@ sph_status sph_create(const SimulationParameters* params, const sph_options* opt
         CREATE_CUDA(dalloc(&s->map4, total));
         CREATE_CUDA(dalloc(&s->mapDist, total));
         launch_build_maps(*boundary, mdims, s->mapDist, nullptr, nullptr, s->map4, s->stream);
+        s->desc = *boundary;
+        s->hasDesc = true;
         MapDev& m = s->map;
         m.map4 = s->map4;
         m.dist = s->mapDist;
@@ -495,7 +521,7 @@ sph_status sph_bind(sph_handle s, const SimulationParameters* params) {
             params->gridDimSubParticles[a] != s->P.gridDimSubParticles[a])
             SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "grid dimensions cannot change after Init");
     s->P = *params;
-    s->graphValid = false;
+    invalidate_graphs(s);
     return SPH_OK;
 }
 
@@ -503,13 +529,14 @@ sph_status sph_set_stream(sph_handle s, void* stream) {
     if (!s) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "handle is NULL");
     SPH_CUDA(cudaStreamSynchronize(s->stream));
     s->stream = stream ? (cudaStream_t)stream : s->ownStream;
-    s->graphValid = false;
+    invalidate_graphs(s);
     return SPH_OK;
 }
 
 sph_status sph_step(sph_handle s, int mode) {
     if (!s) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "handle is NULL");
-    if (mode < SPH_STEP_PLAIN || mode > SPH_STEP_SUB_ONLY) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "unknown step mode");
+    if (mode < SPH_STEP_PLAIN || mode > SPH_STEP_LEARNED) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "unknown step mode");
+    if (mode == SPH_STEP_LEARNED) return corrector_step(s, 1, false);
     if (mode != SPH_STEP_PLAIN) {
         sph_status st = ensure_two_scale(s);
         if (st) return st;
@@ -525,8 +552,9 @@ sph_status sph_step(sph_handle s, int mode) {
 
 sph_status sph_step_many(sph_handle s, int mode, int count) {
     if (!s) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "handle is NULL");
-    if (mode < SPH_STEP_PLAIN || mode > SPH_STEP_SUB_ONLY) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "unknown step mode");
+    if (mode < SPH_STEP_PLAIN || mode > SPH_STEP_LEARNED) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "unknown step mode");
     if (count <= 0) return SPH_OK;
+    if (mode == SPH_STEP_LEARNED) return corrector_step(s, count, true);
     if (mode != SPH_STEP_PLAIN) {
         sph_status st = ensure_two_scale(s);
         if (st) return st;
@@ -864,7 +892,7 @@ sph_status sph_set_tuning(sph_handle s, const sph_tuning* t) {
     s->cfg.forceVariant = t->forceVariant;
     s->cfg.prune = t->prune ? 1 : 0;
     s->cfg.kahan = t->kahan ? 1 : 0;
-    s->graphValid = false;
+    invalidate_graphs(s);
     return SPH_OK;
 }
 
@@ -977,7 +1005,7 @@ sph_status sph_autotune(sph_handle s, int reps, sph_tuning* chosen) {
 #undef TUNE_CUDA
     cleanup();
     s->cfg = best;
-    s->graphValid = false;
+    invalidate_graphs(s);
     if (chosen) return sph_get_tuning(s, chosen);
     return SPH_OK;
 }

@@ -1,0 +1,100 @@
+// Internal declarations of the learned step corrector: the per-particle MLP
+// 24 -> 64 -> 64 -> 6 (SiLU) with BF16 weights and activations on tcgen05
+// tensor cores (FP32 accumulation in TMEM), its Adam trainer, and the
+// neighbour features it reads.  Not part of the public ABI.
+#pragma once
+
+#include "sph_internal.h"
+
+namespace sph {
+
+namespace mlp {
+
+constexpr int IN = 24;     // features
+constexpr int INP = 32;    // padded to the MMA's K granule
+constexpr int HID = 64;
+constexpr int OUT = 6;     // position and velocity correction
+constexpr int OUTP = 16;   // padded to the smallest N of an M = 128 MMA
+constexpr int TILE = 128;  // samples per CTA tile (the MMA's M)
+constexpr int TGT = 8;     // floats per stored target (6 used)
+
+// FP32 master parameters, in this order.
+constexpr int P_W1 = 0;                     // [HID][INP]
+constexpr int P_W2 = P_W1 + HID * INP;      // [HID][HID]
+constexpr int P_W3 = P_W2 + HID * HID;      // [OUTP][HID]
+constexpr int P_B1 = P_W3 + OUTP * HID;     // [HID]
+constexpr int P_B2 = P_B1 + HID;            // [HID]
+constexpr int P_B3 = P_B2 + HID;            // [OUTP]
+constexpr int NPARAM = P_B3 + OUTP;         // 7312
+constexpr int PARTIAL = NPARAM + 16;        // per-CTA gradient row (+ loss)
+
+// Normalisation block: feature mean and inverse deviation, target mean and deviation.
+constexpr int N_MUX = 0, N_ISX = IN, N_MUT = 2 * IN, N_SGT = 2 * IN + OUT, NNORM = 64;
+
+// BF16 weight image, byte offsets: the shared-memory layouts the kernels copy.
+constexpr int IMG_W1 = 0;                  // W1  [64 x 32]
+constexpr int IMG_W2 = 4096;               // W2  [64 x 64]
+constexpr int IMG_W3 = 12288;              // W3  [16 x 64]
+constexpr int IMG_W3T = 14336;             // W3^T [64 x 16]
+constexpr int IMG_W2T = 16384;             // W2^T [64 x 64]
+constexpr int IMG_BYTES = 24576;
+constexpr int IMG_FWD_BYTES = 14336;       // W1, W2, W3: what inference needs
+constexpr int NBIAS = HID + HID + OUTP;    // b1, b2, b3 (FP32)
+
+}  // namespace mlp
+
+// Device state of a corrector.
+struct MlpDev {
+    const unsigned char* image;  // IMG_BYTES
+    const float* bias;           // NBIAS
+    const float* norm;           // NNORM
+};
+
+// Features of every particle from the sorted pre-step state (after the force
+// stage of a step): fp32 [24] per particle, written at index workIds[u] when
+// `byId`, else at u.
+void launch_features(int n, const float4* posS, const float4* velS, const float4* rho4S, const float4* accS,
+                     const int* workIds, RowTables T, GridDev g, PhysDev ph, MapDev map, int boxWalls,
+                     float dtL, int byId, float* feat, cudaStream_t s);
+
+// Inference.  mode 0: adds the correction of working index u to pos/vel of
+// particle workIds[u] (and collides when `collide`); mode 1: writes the
+// correction (6 floats) of row u to `out`.
+void launch_mlp_apply(int n, const float* feat, MlpDev m, int mode, const int* workIds, float4* pos, float4* vel,
+                      PhysDev ph, int collide, float* out, unsigned int* status, cudaStream_t s);
+
+// One optimiser step's gradients: `ctas` CTAs, CTA c takes tiles
+// tileList[c * tilesPerCta + j]; tile t covers samples t*128 .. t*128+127 of
+// feat/tgt (rows >= count are padding).  Writes partial[c][PARTIAL].
+void launch_mlp_grad(int ctas, int tilesPerCta, const int* tileList, const float* feat, const float* tgt,
+                     long long count, float invScale, MlpDev m, float* partial, unsigned int* status,
+                     cudaStream_t s);
+
+// Sums the partial rows in order and applies Adam (step index t >= 1) to the
+// master weights, then rewrites the BF16 image and the FP32 biases.
+// gradOut (optional) receives the summed gradient, lossOut[0] the summed loss.
+void launch_mlp_adam(int ctas, const float* partial, float* master, float* m1, float* m2, int t, float lr,
+                     int update, unsigned char* image, float* bias, float* gradOut, float* lossOut,
+                     cudaStream_t s);
+
+// Rewrites the BF16 image and the FP32 biases from the master weights.
+void launch_mlp_pack(const float* master, unsigned char* image, float* bias, cudaStream_t s);
+
+// Per-column mean and deviation of rows of `cols` floats (stride `stride`),
+// in double precision, deterministic: out[2*c] = mean, out[2*c+1] = deviation.
+void launch_column_stats(long long rows, int cols, int stride, const float* data, double* partial, double* out,
+                         cudaStream_t s);
+
+// Training targets: tgt[id] = (x_ref - x_coarse, v_ref - v_coarse, 0, 0).
+void launch_targets(int n, const float4* refPos, const float4* refVel, const float4* pos, const float4* vel,
+                    float* tgt, cudaStream_t s);
+
+// Audit: err = max_i |rhoA_i - rhoB_i| / rhoB_i over particles (as float bits
+// in *errBits, which must start at 0); then, when err <= tol, copies
+// (srcPos, srcVel) over (pos, vel) and counts an acceptance, else a rollback.
+void launch_audit(int n, const float* rhoA, const float* rhoB, unsigned int* errBits, cudaStream_t s);
+void launch_audit_select(int n, const unsigned int* errBits, float tol, const float4* srcPos,
+                         const float4* srcVel, float4* pos, float4* vel, unsigned int* counters,
+                         cudaStream_t s);
+
+}  // namespace sph

@@ -80,6 +80,11 @@ struct sph_sim {
     cudaGraphExec_t graphExec = nullptr;
     bool graphValid = false;
     int graphMode = -1;
+    unsigned int graphGen = 0;  // bumped whenever captured graphs go stale
+
+    // the boundary description the maps were built from
+    sph_boundary_desc desc{};
+    bool hasDesc = false;
 
     // learned step corrector (sph_corrector.cu; allocated on first use)
     sph::Corrector* corr = nullptr;
@@ -105,6 +110,18 @@ void free_all(sph_sim* s);
 sph_status ensure_two_scale(sph_sim* s);
 // Enqueues one step of `mode` (no host synchronisation).
 void enqueue_step(sph_sim* s, int mode, bool timing);
+// Hash, sort, density and force + integration (+ box collision) of the
+// coarse particles with the given constants; stage events when `ev`.
+void enqueue_coarse(sph_sim* s, const GridDev& g, const PhysDev& ph, int collide, cudaEvent_t* ev);
+// Hash, sort and density of the state (pos, vel) into the handle's sorted
+// copies (posS, velS, rho4S) and tables; nothing is integrated.
+void enqueue_density_only(sph_sim* s, const float4* pos, const float4* vel);
+// Marks every captured step graph of the handle stale.
+void invalidate_graphs(sph_sim* s);
+
+// The learned step corrector (sph_corrector.cu).
+sph_status corrector_step(sph_sim* s, int count, bool useGraph);
+void corrector_free(sph_sim* s);
 // Waits for the handle's stream and maps the latched device status.
 sph_status latched_status(sph_sim* s);
 

@@ -1,0 +1,163 @@
+// Fifth-generation tensor-core (tcgen05) primitives for sm_103a, as inline
+// PTX: shared-memory matrix descriptors, the kind::f16 instruction
+// descriptor, TMEM allocation, MMA issue/commit, mbarrier waits with an
+// iteration limit, and TMEM loads.
+//
+// Operand layout used throughout: K-major, no swizzle.  A matrix of R rows and
+// K columns (16-bit elements) is stored as "core matrices" of 8 rows x 8
+// elements (8 rows of 16 bytes, 128 contiguous bytes); the core matrix of row
+// group r/8 and column group k/8 sits at (r/8)*SBO + (k/8)*LBO with
+// LBO = 128 bytes and SBO = K*16 bytes (core_off below).  One MMA with K = 16
+// consumes two core-matrix columns, so consecutive K steps advance the
+// descriptor's start address by 256 bytes.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace sph {
+namespace tc {
+
+// Byte offset of element (r, k) of an R x K operand in the layout above.
+__host__ __device__ constexpr uint32_t core_off(int r, int k, int K) {
+    return (uint32_t)((r >> 3) * (K * 16) + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2);
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// Shared-memory matrix descriptor: start address, leading-dimension byte
+// offset (K direction), stride-dimension byte offset (M/N direction), all in
+// 16-byte units; bits 46-48 hold the fixed descriptor version 0b001; base
+// offset 0, relative LBO, no swizzle.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = (uint64_t)((addr >> 4) & 0x3FFFu);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;
+    return d;
+}
+
+// Instruction descriptor of tcgen05.mma kind::f16: D in FP32 (bits 4-5 = 1),
+// A and B in BF16 (bits 7-9 = 1, 10-12 = 1), no negation, both K-major,
+// N >> 3 in bits 17-22, M >> 4 in bits 24-28.
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+// D[tmem] (+)= A[smem] * B[smem]^T, one CTA, issued by one thread.
+__device__ __forceinline__ void mma_bf16(uint32_t dTmem, uint64_t aDesc, uint64_t bDesc, uint32_t idesc,
+                                         uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dTmem),
+        "l"(aDesc), "l"(bDesc), "r"(idesc), "r"(accumulate));
+}
+
+// Arrives on `bar` once every MMA this thread issued before has completed.
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred P1;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 P1, [%1], %2;\n\t"
+        "selp.b32 %0, 1, 0, P1;\n\t}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Waits for phase `parity` of `bar` to complete; gives up after `limit` polls
+// (returns false).
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit) {
+    for (uint32_t i = 0; i < limit; i++) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if (i >= 64) __nanosleep(64);
+    }
+    return false;
+}
+
+// TMEM allocation by one full warp; the column address lands in *slot.
+__device__ __forceinline__ void tmem_alloc(uint32_t* slot, uint32_t ncols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)),
+                 "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+__device__ __forceinline__ void fence_before_sync() {
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void fence_after_sync() {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+// Makes this thread's generic-proxy shared-memory writes visible to the
+// tensor core's (async proxy) reads.
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// Block barrier that orders tcgen05 operations and shared-memory operand
+// writes across the threads of the CTA.
+__device__ __forceinline__ void cta_sync() {
+    fence_async_smem();
+    fence_before_sync();
+    __syncthreads();
+    fence_after_sync();
+}
+
+// 32 lanes x 16 consecutive 32-bit columns: thread `lane` of the warp gets
+// row (lane base + lane), columns col .. col + 15.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+        "%14, %15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+
+// TMEM address of (lane, column).
+__device__ __forceinline__ uint32_t tmem_at(uint32_t base, int lane, int col) {
+    return base + ((uint32_t)lane << 16) + (uint32_t)col;
+}
+
+// Issues the K/16 MMAs of D (+)= A * B^T for operands in the layout above:
+// A has 128 rows and K columns at aAddr, B has N rows and K columns at bAddr.
+__device__ __forceinline__ void mma_chain(uint32_t dTmem, uint32_t aAddr, uint32_t bAddr, int K, int N,
+                                          bool accumulate) {
+    const uint32_t idesc = idesc_bf16(128, N);
+    const uint32_t sbo = (uint32_t)K * 16u;
+    for (int k = 0; k < K / 16; k++) {
+        const uint64_t a = smem_desc(aAddr + 256u * k, 128u, sbo);
+        const uint64_t b = smem_desc(bAddr + 256u * k, 128u, sbo);
+        mma_bf16(dTmem, a, b, idesc, (accumulate || k > 0) ? 1u : 0u);
+    }
+}
+
+__device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
+    const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<const uint32_t*>(&v);
+}
+
+}  // namespace tc
+}  // namespace sph

@@ -16,7 +16,8 @@ from .params import BoundaryDesc, Options, SimulationParameters
 PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, "_build", "libsph_gb300.so")
 
-SPH_STEP_PLAIN, SPH_STEP_TWO_SCALE, SPH_STEP_SUB_ONLY = 0, 1, 2
+SPH_STEP_PLAIN, SPH_STEP_TWO_SCALE, SPH_STEP_SUB_ONLY, SPH_STEP_LEARNED = 0, 1, 2, 3
+CORRECTOR_FEATURES, CORRECTOR_OUTPUTS, CORRECTOR_FLOATS = 24, 6, 7372
 (FIELD_VERTEX_DATA, FIELD_SIMULATION_DATA, FIELD_VELOCITY, FIELD_ACCELERATION,
  FIELD_DENSITY, FIELD_PRESSURE, FIELD_STATE, FIELD_SUB_VERTEX_DATA, FIELD_SUB_SIMULATION_DATA,
  FIELD_SUB_IDS, FIELD_SPLIT_IDS, FIELD_BOUNDARY_IDS, FIELD_DEFAULT_IDS) = range(13)
@@ -53,6 +54,14 @@ SIGNATURES = {
     "sph_stage_times": (_i, [_vp, _vp, _vp, _i, _vp]),
     "sph_stage_name": (ctypes.c_char_p, [_i]),
     "sph_cell_tables_noalloc": (_i, [_vp, _vp, _u, _vp, _vp, _vp, _vp, _vp]),
+    "sph_corrector_default_config": (None, [_vp]),
+    "sph_corrector_train": (_i, [_vp, _vp]),
+    "sph_corrector_load": (_i, [_vp, _vp, _vp, ctypes.c_size_t]),
+    "sph_corrector_save": (_i, [_vp, _vp, ctypes.c_size_t]),
+    "sph_corrector_get_report": (_i, [_vp, _vp]),
+    "sph_corrector_predict": (_i, [_vp, _vp, _i, _vp]),
+    "sph_corrector_gradient": (_i, [_vp, _vp, _vp, _i, _vp, _vp]),
+    "sph_read_features": (_i, [_vp, _i, _vp, ctypes.c_size_t]),
     "sph_last_error": (ctypes.c_char_p, []),
     "sph_status_string": (ctypes.c_char_p, [_i]),
 }
@@ -70,6 +79,32 @@ class Diagnostics(ctypes.Structure):
     _fields_ = [("mass", ctypes.c_double), ("momentum", ctypes.c_double * 3),
                 ("kineticEnergy", ctypes.c_double), ("potentialEnergy", ctypes.c_double),
                 ("densityMean", ctypes.c_double), ("densityMaxRelError", ctypes.c_double)]
+
+
+class CorrectorConfig(ctypes.Structure):
+    """sph_corrector_config."""
+
+    _fields_ = [("trainSteps", ctypes.c_int), ("stride", ctypes.c_int), ("epochs", ctypes.c_int),
+                ("batchTiles", ctypes.c_int), ("learningRate", ctypes.c_float),
+                ("densityTolerance", ctypes.c_float), ("auditInterval", ctypes.c_int), ("seed", ctypes.c_uint)]
+
+    @classmethod
+    def default(cls, **kw) -> "CorrectorConfig":
+        c = cls()
+        load().sph_corrector_default_config(ctypes.byref(c))
+        for k, v in kw.items():
+            setattr(c, k, v)
+        return c
+
+
+class CorrectorReport(ctypes.Structure):
+    """sph_corrector_report."""
+
+    _fields_ = [("samples", ctypes.c_uint), ("optimizerSteps", ctypes.c_uint),
+                ("firstEpochLoss", ctypes.c_float), ("lastEpochLoss", ctypes.c_float),
+                ("trainMilliseconds", ctypes.c_float), ("learnedSteps", ctypes.c_uint),
+                ("audits", ctypes.c_uint), ("rollbacks", ctypes.c_uint),
+                ("lastAuditError", ctypes.c_float), ("maxAuditError", ctypes.c_float)]
 
 
 class Tuning(ctypes.Structure):
@@ -215,6 +250,48 @@ class ParticleSimulation:
         check(load().sph_get_counts(self._h, ctypes.byref(c)))
         return c
 
+    # -- learned step corrector ------------------------------------------------
+    def train_corrector(self, cfg: CorrectorConfig | None = None, **kw) -> CorrectorReport:
+        cfg = cfg or CorrectorConfig.default(**kw)
+        check(load().sph_corrector_train(self._h, ctypes.byref(cfg)))
+        return self.corrector_report()
+
+    def load_corrector(self, model: np.ndarray, cfg: CorrectorConfig | None = None, **kw) -> None:
+        cfg = cfg or CorrectorConfig.default(**kw)
+        m = np.ascontiguousarray(model, np.float32)
+        check(load().sph_corrector_load(self._h, ctypes.byref(cfg), m.ctypes.data, m.size))
+
+    def save_corrector(self) -> np.ndarray:
+        m = np.zeros(CORRECTOR_FLOATS, np.float32)
+        check(load().sph_corrector_save(self._h, m.ctypes.data, m.size))
+        return m
+
+    def corrector_report(self) -> CorrectorReport:
+        r = CorrectorReport()
+        check(load().sph_corrector_get_report(self._h, ctypes.byref(r)))
+        return r
+
+    def corrector_predict(self, features: np.ndarray) -> np.ndarray:
+        f = np.ascontiguousarray(features, np.float32).reshape(-1, CORRECTOR_FEATURES)
+        out = np.zeros((len(f), CORRECTOR_OUTPUTS), np.float32)
+        check(load().sph_corrector_predict(self._h, f.ctypes.data, len(f), out.ctypes.data))
+        return out
+
+    def corrector_gradient(self, features: np.ndarray, targets: np.ndarray):
+        f = np.ascontiguousarray(features, np.float32).reshape(-1, CORRECTOR_FEATURES)
+        t = np.zeros((len(f), 8), np.float32)
+        t[:, :CORRECTOR_OUTPUTS] = np.asarray(targets, np.float32).reshape(len(f), CORRECTOR_OUTPUTS)
+        g = np.zeros(CORRECTOR_FLOATS - 60, np.float32)
+        loss = np.zeros(1, np.float32)
+        check(load().sph_corrector_gradient(self._h, f.ctypes.data, t.ctypes.data, len(f), g.ctypes.data,
+                                            loss.ctypes.data))
+        return g, float(loss[0])
+
+    def features(self, stride: int = 4) -> np.ndarray:
+        out = np.zeros((self.n, CORRECTOR_FEATURES), np.float32)
+        check(load().sph_read_features(self._h, stride, out.ctypes.data, out.nbytes))
+        return out
+
     def diagnostics(self) -> Diagnostics:
         d = Diagnostics()
         check(load().sph_get_diagnostics(self._h, ctypes.byref(d)))
@@ -236,6 +313,10 @@ class ParticleSimulation:
         out = np.zeros(shape, dt)
         check(load().sph_read(self._h, field, _p(out), out.nbytes))
         return out
+
+    def write_state(self, positions: np.ndarray, velocities: np.ndarray) -> None:
+        self.write(FIELD_VERTEX_DATA, np.asarray(positions, np.float32).reshape(-1, 3))
+        self.write(FIELD_VELOCITY, np.asarray(velocities, np.float32).reshape(-1, 3))
 
     def write(self, field: int, data: np.ndarray) -> None:
         a = np.ascontiguousarray(data, np.float32)

@@ -136,7 +136,10 @@ typedef enum sph_status {
 typedef enum sph_step_mode {
     SPH_STEP_PLAIN = 0,     /* Advance (particle_simulation.cu:2085-2117) */
     SPH_STEP_TWO_SCALE = 1, /* AdvanceTwoScale (:2145-2182) */
-    SPH_STEP_SUB_ONLY = 2   /* AdvanceSubParticles (:2119-2143) */
+    SPH_STEP_SUB_ONLY = 2,  /* AdvanceSubParticles (:2119-2143) */
+    SPH_STEP_LEARNED = 3    /* one plain step of stride*dt plus the learned
+                               correction (no reference counterpart; needs a
+                               trained or loaded corrector, see below) */
 } sph_step_mode;
 
 /* Per-particle fields, returned in particle-index order. */
@@ -240,6 +243,75 @@ typedef struct sph_diagnostics {
     double densityMaxRelError; /* max |rho - restDensity| / restDensity */
 } sph_diagnostics;
 sph_status sph_get_diagnostics(sph_handle h, sph_diagnostics* out);
+
+/* ---------------------------------------------------------------------------
+ * Learned step corrector (no reference counterpart).
+ *
+ * A per-particle MLP, 24 neighbour features -> 64 -> 64 -> 6 with SiLU, BF16
+ * weights and activations and FP32 accumulation on the tensor cores, corrects
+ * one plain step of stride*dt (SPH_STEP_LEARNED) towards `stride` plain steps
+ * of dt.  It is trained on the device from the plain solver's own trajectory.
+ * The plain solver is the fallback and the judge: every auditInterval-th
+ * learned step is also run as `stride` plain steps from the same state, and
+ * when the largest per-particle relative density difference between the two
+ * results exceeds densityTolerance the plain result is kept (a rollback).
+ * ------------------------------------------------------------------------- */
+#define SPH_CORRECTOR_FEATURES 24
+#define SPH_CORRECTOR_OUTPUTS 6
+/* Model blob: FP32 weights W1[64][32] (input columns 24..31 zero), W2[64][64],
+ * W3[16][64] (rows 6..15 zero), b1[64], b2[64], b3[16] (6..15 zero), then the
+ * feature means[24], feature deviations[24], target means[6], target
+ * deviations[6]. */
+#define SPH_CORRECTOR_FLOATS 7372
+
+typedef struct sph_corrector_config {
+    int trainSteps;         /* plain steps of dt that generate samples (2000) */
+    int stride;             /* a learned step is stride*dt (4) */
+    int epochs;             /* passes over the samples (6) */
+    int batchTiles;         /* 128-sample tiles per Adam step (128) */
+    float learningRate;     /* Adam, decayed linearly to 1% (2e-3) */
+    float densityTolerance; /* audit threshold (0.01) */
+    int auditInterval;      /* audit every k-th learned step (16); 0: never */
+    unsigned int seed;      /* weight initialisation and sample order */
+} sph_corrector_config;
+
+typedef struct sph_corrector_report {
+    unsigned int samples;         /* training samples (particles x start states) */
+    unsigned int optimizerSteps;
+    float firstEpochLoss;         /* mean loss on standardised targets */
+    float lastEpochLoss;
+    float trainMilliseconds;      /* sample generation + training, device time */
+    unsigned int learnedSteps;    /* SPH_STEP_LEARNED steps taken */
+    unsigned int audits;
+    unsigned int rollbacks;
+    float lastAuditError;         /* max relative density difference of the last audit */
+    float maxAuditError;
+} sph_corrector_report;
+
+void sph_corrector_default_config(sph_corrector_config* cfg);
+
+/* Runs cfg->trainSteps plain steps of dt from the handle's current state (the
+ * handle advances), collects (features, correction) samples for every start
+ * state with `stride` steps after it, fits the standardisation and trains the
+ * MLP with Adam.  Deterministic for a given seed. */
+sph_status sph_corrector_train(sph_handle h, const sph_corrector_config* cfg);
+
+/* Replaces the corrector by a model blob (SPH_CORRECTOR_FLOATS floats). */
+sph_status sph_corrector_load(sph_handle h, const sph_corrector_config* cfg, const float* model, size_t count);
+sph_status sph_corrector_save(sph_handle h, float* model, size_t count);
+sph_status sph_corrector_get_report(sph_handle h, sph_corrector_report* out);
+
+/* Checking entry points: corrections (count x 6, denormalised) of given raw
+ * features (count x 24), and the loss gradient (SPH_CORRECTOR_FLOATS - 60
+ * weight floats, blob order) and summed loss of given samples (targets count
+ * x 8, first 6 used), both through the tensor-core kernels. */
+sph_status sph_corrector_predict(sph_handle h, const float* features, int count, float* corrections);
+sph_status sph_corrector_gradient(sph_handle h, const float* features, const float* targets, int count,
+                                  float* grad, float* loss);
+
+/* The corrector's input features (n x 24, particle order) of the state that
+ * entered the last step, for learned step size stride*dt. */
+sph_status sph_read_features(sph_handle h, int stride, float* dst, size_t bytes);
 
 /* Device pointer of a field in the handle's layout, for zero-copy consumers
  * (replaces the OpenGL VBO getters, :2278-2301): 0 = positions (float4[n],

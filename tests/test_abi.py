@@ -44,6 +44,11 @@ int main(void) {
     printf("sph_counts %zu\n", sizeof(sph_counts));
     printf("sph_diagnostics %zu\n", sizeof(sph_diagnostics));
     O(sph_diagnostics, kineticEnergy); O(sph_diagnostics, densityMaxRelError);
+    printf("sph_corrector_config %zu\n", sizeof(sph_corrector_config));
+    printf("sph_corrector_report %zu\n", sizeof(sph_corrector_report));
+    O(sph_corrector_config, seed); O(sph_corrector_config, densityTolerance);
+    O(sph_corrector_report, trainMilliseconds); O(sph_corrector_report, maxAuditError);
+    printf("SPH_CORRECTOR_FLOATS %d\n", SPH_CORRECTOR_FLOATS);
     O(SimulationParameters, numParticles); O(SimulationParameters, timeStep);
     O(SimulationParameters, poly6); O(SimulationParameters, laplViscSub);
     O(SimulationParameters, boxDim); O(SimulationParameters, restitution);
@@ -68,12 +73,17 @@ def test_struct_layouts_match_header():
     assert lay["sph_boundary_desc"] == ctypes.sizeof(P.BoundaryDesc)
     assert lay["sph_counts"] == ctypes.sizeof(sphmod.Counts)
     assert lay["sph_diagnostics"] == ctypes.sizeof(sphmod.Diagnostics)
+    assert lay["sph_corrector_config"] == ctypes.sizeof(sphmod.CorrectorConfig)
+    assert lay["sph_corrector_report"] == ctypes.sizeof(sphmod.CorrectorReport)
+    assert lay.pop("SPH_CORRECTOR_FLOATS") == sphmod.CORRECTOR_FLOATS
     for key, v in lay.items():
         if "." not in key:
             continue
         t, f = key.split(".")
         cls = {"SimulationParameters": P.SimulationParameters, "sph_options": P.Options,
-               "sph_boundary_desc": P.BoundaryDesc, "sph_diagnostics": sphmod.Diagnostics}[t]
+               "sph_boundary_desc": P.BoundaryDesc, "sph_diagnostics": sphmod.Diagnostics,
+               "sph_corrector_config": sphmod.CorrectorConfig,
+               "sph_corrector_report": sphmod.CorrectorReport}[t]
         assert getattr(cls, f).offset == v, key
 
 

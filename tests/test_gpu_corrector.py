@@ -1,0 +1,310 @@
+"""GPU checks of the learned step corrector (SPH_STEP_LEARNED).
+
+* The tensor-core MLP (predict and loss gradient) against a numpy
+  restatement that rounds the same operands to BF16; the remaining differences
+  come from FP32 accumulation order and the device exponential, so the bars
+  are relative (1e-3 of the output scale, 2e-2 of each gradient block's norm).
+* The neighbour features against a brute-force float64 restatement.
+* Training lowers the loss; the learned step beats the uncorrected plain step
+  of the same size against the plain trajectory.
+* The audit: with tolerance 0 every audited step is rolled back to exactly the
+  plain solver's result, with an infinite tolerance it keeps exactly the
+  learned result; CUDA-graph replay equals eager launches.
+"""
+import numpy as np
+import pytest
+
+from cudasphnew_gb300 import params as P
+from cudasphnew_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+IN, OUT, HID = 24, 6, 64
+NPARAM = 7312
+
+
+def bf16(x):
+    """Round float32 to bfloat16 (nearest even), returned as float32."""
+    x = np.ascontiguousarray(x, np.float32)
+    u = x.view(np.uint32).astype(np.uint64)
+    u = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
+    return u.astype(np.uint32).view(np.float32)
+
+
+def unpack(blob):
+    w = blob[:NPARAM]
+    W1 = w[0:2048].reshape(64, 32)
+    W2 = w[2048:6144].reshape(64, 64)
+    W3 = w[6144:7168].reshape(16, 64)
+    b1, b2, b3 = w[7168:7232], w[7232:7296], w[7296:7312]
+    s = blob[NPARAM:]
+    return W1, W2, W3, b1, b2, b3, s[:24], s[24:48], s[48:54], s[54:60]
+
+
+def random_blob(seed):
+    rng = np.random.default_rng(seed)
+    W1 = np.zeros((64, 32))
+    W1[:, :24] = rng.uniform(-1, 1, (64, 24)) / np.sqrt(24)
+    W2 = rng.uniform(-1, 1, (64, 64)) / 8
+    W3 = np.zeros((16, 64))
+    W3[:6] = rng.uniform(-1, 1, (6, 64)) / 8
+    b1, b2 = rng.normal(0, 0.1, 64), rng.normal(0, 0.1, 64)
+    b3 = np.zeros(16)
+    b3[:6] = rng.normal(0, 0.1, 6)
+    blob = np.zeros(7372, np.float32)
+    blob[:NPARAM] = np.concatenate([W1.ravel(), W2.ravel(), W3.ravel(), b1, b2, b3])
+    blob[NPARAM:NPARAM + 24] = rng.normal(0, 1, 24)
+    blob[NPARAM + 24:NPARAM + 48] = rng.uniform(0.5, 2.0, 24)
+    blob[NPARAM + 48:NPARAM + 54] = rng.normal(0, 1e-4, 6)
+    blob[NPARAM + 54:NPARAM + 60] = rng.uniform(1e-5, 1e-4, 6)
+    return blob
+
+
+def forward(blob, feats):
+    W1, W2, W3, b1, b2, b3, mux, sx, mut, st = unpack(blob)
+    isx = np.where(sx > 1e-8, np.float32(1) / sx, 0).astype(np.float32)
+    xn = bf16((feats.astype(np.float32) - mux) * isx)
+    z1 = xn.astype(np.float64) @ bf16(W1[:, :24]).astype(np.float64).T
+    a = z1 + b1
+    a1 = bf16(a / (1 + np.exp(-a)))
+    z2 = a1.astype(np.float64) @ bf16(W2).astype(np.float64).T
+    a = z2 + b2
+    a2 = bf16(a / (1 + np.exp(-a)))
+    y = a2.astype(np.float64) @ bf16(W3[:6]).astype(np.float64).T + b3[:6]
+    return dict(xn=xn, z1=z1, a1=a1, z2=z2, a2=a2, y=y, corr=mut + st * y)
+
+
+def gradient(blob, feats, targets):
+    W1, W2, W3, b1, b2, b3, mux, sx, mut, st = unpack(blob)
+    f = forward(blob, feats)
+    n = len(feats)
+    tn = (targets.astype(np.float32) - mut) / st
+    e = f["y"] - tn
+    loss = (e * e).sum()
+    dy = 2 * e / (6 * n)
+    dyb = bf16(dy).astype(np.float64)
+    dW3 = np.zeros((16, 64))
+    dW3[:6] = dyb.T @ f["a2"]
+    db3 = np.zeros(16)
+    db3[:6] = dy.sum(0)
+
+    def dsilu(a):
+        s = 1 / (1 + np.exp(-a))
+        return s * (1 + a * (1 - s))
+
+    dz2 = (dyb @ bf16(W3[:6]).astype(np.float64)) * dsilu(f["z2"] + b2)
+    dW2 = bf16(dz2).astype(np.float64).T @ f["a1"]
+    dz1 = (bf16(dz2).astype(np.float64) @ bf16(W2).astype(np.float64)) * dsilu(f["z1"] + b1)
+    dW1 = np.zeros((64, 32))
+    dW1[:, :24] = bf16(dz1).astype(np.float64).T @ f["xn"]
+    blocks = dict(W1=dW1.ravel(), W2=dW2.ravel(), W3=dW3.ravel(), b1=dz1.sum(0), b2=dz2.sum(0), b3=db3)
+    return blocks, loss
+
+
+SLICES = dict(W1=slice(0, 2048), W2=slice(2048, 6144), W3=slice(6144, 7168), b1=slice(7168, 7232),
+              b2=slice(7232, 7296), b3=slice(7296, 7312))
+
+
+def tiny():
+    return scenes.dam_break(8, 8, 8, (0, 0, 0), (0.5, 0.5, 0.5), 3, "tiny", 1)
+
+
+def small():
+    return scenes.dam_break(16, 16, 8, (0, 0, 0), (0.5, 0.5, 0.5), 5, "small", 1)
+
+
+def make(sphlib, sc, pos=None, vel=None, dt_scale=1):
+    p = P.SimulationParameters.from_buffer_copy(bytes(sc.params))
+    p.timeStep = float(np.float32(p.timeStep * dt_scale))
+    p.timeStepSubParticles = p.timeStep
+    return sphlib.ParticleSimulation(p, sc.positions if pos is None else pos,
+                                     sc.velocities if vel is None else vel, sc.options, sc.boundary)
+
+
+def density_at(sphlib, sc, pos, vel):
+    with make(sphlib, sc, pos, vel) as sim:
+        sim.Advance()
+        return sim.read(sphlib.FIELD_DENSITY)
+
+
+@pytest.mark.parametrize("count", [1, 127, 128, 300, 4099])
+def test_mlp_predict_matches_numpy(sphlib, count):
+    blob = random_blob(1)
+    rng = np.random.default_rng(count)
+    feats = rng.normal(0, 1.5, (count, IN)).astype(np.float32)
+    with make(sphlib, tiny()) as sim:
+        sim.load_corrector(blob)
+        got = sim.corrector_predict(feats)
+    ref = forward(blob, feats)["y"]
+    mut, st = blob[NPARAM + 48:NPARAM + 54], blob[NPARAM + 54:NPARAM + 60]
+    y = (got.astype(np.float64) - mut) / st  # back to the network's output space
+    assert np.isfinite(got).all()
+    assert np.abs(y - ref).max() <= 2e-3 * max(1.0, np.abs(ref).max())
+
+
+@pytest.mark.parametrize("count", [128, 1000])
+def test_mlp_gradient_matches_numpy(sphlib, count):
+    blob = random_blob(2)
+    rng = np.random.default_rng(7 + count)
+    feats = rng.normal(0, 1.5, (count, IN)).astype(np.float32)
+    tgt = (blob[NPARAM + 48:NPARAM + 54] + blob[NPARAM + 54:NPARAM + 60] *
+           rng.normal(0, 1, (count, OUT))).astype(np.float32)
+    with make(sphlib, tiny()) as sim:
+        sim.load_corrector(blob)
+        g, loss = sim.corrector_gradient(feats, tgt)
+    ref, rloss = gradient(blob, feats, tgt)
+    assert abs(loss - rloss) <= 2e-3 * rloss
+    for k, sl in SLICES.items():
+        r = ref[k]
+        err = np.linalg.norm(g[sl] - r) / max(np.linalg.norm(r), 1e-30)
+        assert err < 2e-2, (k, err)
+    # padding stays untouched: input columns 24..31, output rows 6..15
+    assert not g[SLICES["W1"]].reshape(64, 32)[:, 24:].any()
+    assert not g[SLICES["W3"]].reshape(16, 64)[6:].any()
+    assert not g[SLICES["b3"]][6:].any()
+
+
+def features_ref(sc, pos, vel, rho, acc, stride):
+    p = sc.params
+    f32 = np.float32
+    h = float(f32(p.compactSupport))
+    h2 = h * h
+    m = float(f32(p.particleMass))
+    dtL = float(f32(stride) * f32(p.timeStep))
+    x = pos.astype(np.float64)
+    v = vel.astype(np.float64)
+    d = x[:, None, :] - x[None, :, :]
+    r2 = (d * d).sum(2)
+    mask = (r2 < h2) & (r2 > 0)
+    inv = 1.0 / rho.astype(np.float64)[None, :]
+    W = np.where(mask, float(f32(p.poly6) * f32(m)) * (h2 - r2) ** 3 * inv, 0.0)
+    r = np.sqrt(np.where(mask, r2, 1.0))
+    G = np.where(mask, float(f32(m) * f32(p.gradSpiky)) * (h - r) ** 2 / r * inv, 0.0)
+    gv = G[..., None] * d
+    u = v[None, :, :] - v[:, None, :]
+    out = np.zeros((len(x), IN))
+    out[:, 0] = rho / float(f32(p.restDensity)) - 1
+    out[:, 1] = W.sum(1)
+    out[:, 2:5] = v
+    out[:, 5:8] = acc / float(f32(p.gravity))
+    out[:, 8:11] = (W[..., None] * u).sum(1)
+    out[:, 11] = dtL * (u * gv).sum(2).sum(1)
+    out[:, 12:15] = dtL * np.cross(u, gv).sum(1)
+    out[:, 15:18] = h * gv.sum(1)
+    out[:, 18] = mask.sum(1) / 32
+    c = x - np.array(p.boxCen, np.float64)
+    da = np.array(p.boxDim, np.float64) - np.abs(c)
+    k = da.argmin(1)
+    dmin = da[np.arange(len(x)), k]
+    near = dmin < 4 * h
+    out[:, 19] = np.clip(np.where(near, dmin, 4 * h), 0, 4 * h) / h
+    sgn = np.where(c[np.arange(len(x)), k] > 0, -1.0, 1.0)
+    for a in range(3):
+        out[:, 20 + a] = np.where(near & (k == a), sgn, 0.0)
+    out[:, 23] = np.sqrt((v * v).sum(1)) * dtL / h
+    return out
+
+
+def test_features_match_numpy(sphlib):
+    sc = tiny()
+    with make(sphlib, sc) as sim:
+        sim.step(count=30)
+        x0, v0 = sim.positions(), sim.velocities()
+        sim.Advance()
+        rho, acc = sim.read(sphlib.FIELD_DENSITY), sim.read(sphlib.FIELD_ACCELERATION)
+        got = sim.features(stride=4)
+    ref = features_ref(sc, x0, v0, rho, acc, 4)
+    scale = np.abs(ref).max(0) + 1e-6
+    err = np.abs(got - ref) / scale
+    assert err.max() < 1e-4, (err.max(0))
+    assert np.abs(ref[:, 11:18]).max() > 0 and ref[:, 20:23].any()
+
+
+def test_training_lowers_loss_and_corrects_the_long_step(sphlib):
+    sc = small()
+    stride, steps = 4, 200
+    with make(sphlib, sc) as sim:
+        rep = sim.train_corrector(trainSteps=steps, stride=stride, epochs=4, batchTiles=16, auditInterval=0,
+                                  seed=3)
+        ref_pos, ref_vel = sim.positions(), sim.velocities()  # plain trajectory at t = steps*dt
+        assert rep.samples == (steps - stride + 1) * sc.n
+        assert rep.optimizerSteps > 0 and rep.lastEpochLoss < rep.firstEpochLoss
+        model = sim.save_corrector()
+        # learned steps from the same start cover the same time
+        sim.write_state(sc.positions, sc.velocities)
+        sim.step(mode=sphlib.SPH_STEP_LEARNED, count=steps // stride)
+        lpos, lvel = sim.positions(), sim.velocities()
+        r = sim.corrector_report()
+        assert r.learnedSteps == steps // stride and r.audits == 0
+    with make(sphlib, sc, dt_scale=stride) as coarse:  # the uncorrected long step
+        coarse.step(count=steps // stride)
+        cpos, cvel = coarse.positions(), coarse.velocities()
+    rho_ref = density_at(sphlib, sc, ref_pos, ref_vel)
+    err_l = np.abs(density_at(sphlib, sc, lpos, lvel) - rho_ref) / rho_ref
+    err_c = np.abs(density_at(sphlib, sc, cpos, cvel) - rho_ref) / rho_ref
+    print("mean density error: learned %.3e, uncorrected %.3e; loss %.3f -> %.3f"
+          % (err_l.mean(), err_c.mean(), rep.firstEpochLoss, rep.lastEpochLoss))
+    assert np.isfinite(lpos).all()
+    assert err_l.mean() < err_c.mean()
+    assert err_l.mean() < 0.01
+    # a saved model loads back to the same predictions
+    with make(sphlib, sc) as again:
+        again.load_corrector(model)
+        f = np.random.default_rng(0).normal(0, 1, (256, IN)).astype(np.float32)
+        with make(sphlib, sc) as other:
+            other.load_corrector(model)
+            np.testing.assert_array_equal(again.corrector_predict(f), other.corrector_predict(f))
+
+
+def test_audit_rolls_back_to_the_plain_solver(sphlib):
+    sc = tiny()
+    blob = random_blob(5)
+    k, stride = 3, 4
+    with make(sphlib, sc) as sim:
+        sim.load_corrector(blob, stride=stride, auditInterval=1, densityTolerance=0.0)
+        sim.step(mode=sphlib.SPH_STEP_LEARNED, count=k)
+        pos, vel = sim.positions(), sim.velocities()
+        rep = sim.corrector_report()
+    assert rep.audits == k and rep.rollbacks == k and rep.maxAuditError > 0
+    with make(sphlib, sc) as plain:
+        plain.step(count=k * stride)
+        np.testing.assert_array_equal(pos, plain.positions())
+        np.testing.assert_array_equal(vel, plain.velocities())
+
+
+def test_audit_keeps_the_learned_result_within_tolerance(sphlib):
+    sc = tiny()
+    blob = random_blob(6)
+    outs = []
+    for interval, tol in ((1, 1e9), (0, 0.01)):
+        with make(sphlib, sc) as sim:
+            sim.load_corrector(blob, stride=4, auditInterval=interval, densityTolerance=tol)
+            sim.step(mode=sphlib.SPH_STEP_LEARNED, count=3)
+            outs.append((sim.positions(), sim.velocities(), sim.corrector_report()))
+    np.testing.assert_array_equal(outs[0][0], outs[1][0])
+    np.testing.assert_array_equal(outs[0][1], outs[1][1])
+    assert outs[0][2].audits == 3 and outs[0][2].rollbacks == 0 and outs[1][2].audits == 0
+
+
+def test_learned_graph_matches_eager(sphlib):
+    sc = tiny()
+    blob = random_blob(7)
+    outs = []
+    for graph in (False, True, True):
+        with make(sphlib, sc) as sim:
+            sim.load_corrector(blob, stride=4, auditInterval=2, densityTolerance=0.5)
+            if graph:
+                sim.step(mode=sphlib.SPH_STEP_LEARNED, count=5)
+            else:
+                for _ in range(5):
+                    sim.step(mode=sphlib.SPH_STEP_LEARNED)
+            outs.append((sim.positions(), sim.velocities()))
+    for o in outs[1:]:
+        np.testing.assert_array_equal(o[0], outs[0][0])
+        np.testing.assert_array_equal(o[1], outs[0][1])
+
+
+def test_learned_step_needs_a_corrector(sphlib):
+    with make(sphlib, tiny()) as sim:
+        with pytest.raises(sphlib.SphError):
+            sim.step(mode=sphlib.SPH_STEP_LEARNED)
