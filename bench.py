@@ -48,6 +48,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="config2")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-learned", action="store_true",
+                    help="skip the learned-corrector legs (16,384-particle scene and the 1M scene)")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the library's default launch shapes (for profiling runs)")
     return ap.parse_args()
@@ -218,6 +220,179 @@ def run_reference(args):
     print(json.dumps(out), flush=True)
 
 
+def time_steps(torch, stream, sim, mode, count):
+    """Device time (ms) of `count` graph-launched steps of `mode` on `stream`."""
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        e0.record()
+        sim.step(mode=mode, count=count)
+        e1.record()
+    torch.cuda.synchronize()
+    sim.synchronize()
+    return e0.elapsed_time(e1)
+
+
+def fp64_density(oracle, sc, pos, vel):
+    """Densities at the given positions, from the oracle's FP64 density pass."""
+    return oracle.step_plain(sc.params, sc.options, None, pos, vel, fp64=True)["rho"]
+
+
+def density_field(sc, pos, pts):
+    """sum_j m W_poly6(|x - x_j|) at the sample points `pts` (float64)."""
+    import numpy as np
+    from scipy.spatial import cKDTree
+    h = float(sc.params.compactSupport)
+    k = float(sc.params.particleMass) * float(sc.params.poly6)
+    tree = cKDTree(pos.astype(np.float64))
+    out = np.zeros(len(pts))
+    for i, lst in enumerate(tree.query_ball_point(pts, h)):
+        if lst:
+            d = pts[i] - pos[lst]
+            out[i] = k * (np.maximum(h * h - (d * d).sum(1), 0.0) ** 3).sum()
+    return out
+
+
+def density_errors(oracle, sc, ref, pos, vel, pts):
+    """Three density errors of a state against the FP64 reference state `ref`:
+    per particle (same particle index), of the density field sampled on a
+    fixed grid inside the fluid (points where the reference field exceeds
+    half the rest density), and of the mean density."""
+    import numpy as np
+    rho = fp64_density(oracle, sc, pos.astype(np.float64), vel.astype(np.float64))
+    pp = np.abs(rho - ref["rho"]) / ref["rho"]
+    f = density_field(sc, pos, pts)
+    inside = ref["field"] > 0.5 * float(sc.params.restDensity)
+    fe = np.abs(f[inside] - ref["field"][inside]) / ref["field"][inside]
+    return {"per_particle_mean": float(pp.mean()), "per_particle_max": float(pp.max()),
+            "field_mean": float(fe.mean()), "field_max": float(fe.max()),
+            "mean_density": float(abs(rho.mean() - ref["rho"].mean()) / ref["rho"].mean())}
+
+
+def learned_leg(lib, torch, stream):
+    """Learned 4x-dt corrector on the plain 16,384-particle dam break: trained on
+    2,000 plain steps of dt = 1e-4, then 500 learned steps of 4e-4 from the same
+    start, against 2,000 plain steps; density error against the FP64 oracle's
+    own trajectory at the same time."""
+    import numpy as np
+    from cudasphnew_gb300 import scenes
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle  # FP64 reference trajectory (the error measure only)
+    if not os.path.exists(oracle.LIB_PATH):
+        oracle.build()
+    oracle.set_threads(os.cpu_count() or 1)
+    sc = scenes.config1()
+    K, train_steps, learned_steps = 4, 2000, 500
+    dt = float(sc.params.timeStep)
+    x0, v0 = sc.positions, sc.velocities
+    sim = lib.ParticleSimulation(sc.params, x0, v0, sc.options, sc.boundary)
+    sim.set_stream(stream.cuda_stream)
+    cfg = lib.CorrectorConfig.default(trainSteps=train_steps, stride=K, auditInterval=16, densityTolerance=0.01)
+    t0 = time.perf_counter()
+    rep = sim.train_corrector(cfg)
+    train_wall = time.perf_counter() - t0
+    model = sim.save_corrector()
+    plain_pos, plain_vel = sim.positions(), sim.velocities()
+    # plain timing: 2,000 steps from the start (graph captured by the warm-up)
+    sim.write_state(x0, v0)
+    sim.step(count=10)
+    sim.write_state(x0, v0)
+    ms_plain = time_steps(torch, stream, sim, lib.SPH_STEP_PLAIN, train_steps)
+    # learned timing: warm-up captures the learned and the audit graph
+    sim.write_state(x0, v0)
+    sim.step(mode=lib.SPH_STEP_LEARNED, count=20)
+    before = sim.corrector_report()
+    sim.write_state(x0, v0)
+    ms_learned = time_steps(torch, stream, sim, lib.SPH_STEP_LEARNED, learned_steps)
+    after = sim.corrector_report()
+    lpos, lvel = sim.positions(), sim.velocities()
+    sim.close()
+    # the uncorrected long step, for comparison (not timed)
+    p4 = type(sc.params).from_buffer_copy(bytes(sc.params))
+    p4.timeStep = float(np.float32(dt * K))
+    p4.timeStepSubParticles = p4.timeStep
+    with lib.ParticleSimulation(p4, x0, v0, sc.options, sc.boundary) as coarse:
+        coarse.step(count=learned_steps)
+        cpos, cvel = coarse.positions(), coarse.velocities()
+    # FP64 oracle trajectory of 2,000 plain steps
+    t1 = time.perf_counter()
+    x, v = x0.astype(np.float64), v0.astype(np.float64)
+    for _ in range(train_steps):
+        r = oracle.step_plain(sc.params, sc.options, None, x, v, fp64=True)
+        x, v = r["pos"], r["vel"]
+    fp64_wall = time.perf_counter() - t1
+    h = float(sc.params.compactSupport)
+    g = np.arange(h / 2, 1.0, h)  # the unit box at spacing h
+    pts = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)
+    ref = {"rho": fp64_density(oracle, sc, x, v), "field": density_field(sc, x, pts)}
+    el = density_errors(oracle, sc, ref, lpos, lvel, pts)
+    ec = density_errors(oracle, sc, ref, cpos, cvel, pts)
+    ep = density_errors(oracle, sc, ref, plain_pos, plain_vel, pts)
+    sim_plain = train_steps * dt / (ms_plain / 1e3)
+    sim_learned = learned_steps * K * dt / (ms_learned / 1e3)
+    return {"workload": f"{sc.name}: {sc.n} particles, plain dt {dt:g} x {train_steps} steps vs learned "
+                        f"{K}x dt x {learned_steps} steps, same start and end time",
+            "unit": "simulated s / wall s",
+            "plain": sim_plain, "learned": sim_learned, "speedup": sim_learned / sim_plain,
+            "plain_ms_per_step": ms_plain / train_steps, "learned_ms_per_step": ms_learned / learned_steps,
+            "density_err_vs_fp64": {"learned_4dt": el, "uncorrected_4dt": ec, "plain_fp32_dt": ep,
+                                    "note": "against the FP64 oracle's 2,000-step trajectory at the same time; "
+                                            "per-particle and field errors include the trajectories' chaotic "
+                                            "divergence, which plain FP32 shows too"},
+            "audit_interval": cfg.auditInterval, "density_tolerance": cfg.densityTolerance,
+            "audits": after.audits - before.audits, "rollbacks": after.rollbacks - before.rollbacks,
+            "max_audit_err": after.maxAuditError,
+            "training": {"samples": rep.samples, "adam_steps": rep.optimizerSteps,
+                         "loss_first_epoch": rep.firstEpochLoss, "loss_last_epoch": rep.lastEpochLoss,
+                         "device_ms": rep.trainMilliseconds, "wall_s": train_wall},
+            "fp64_oracle_wall_s": fp64_wall,
+            "l2": "not flushed: the 16,384-particle state (~3 MB) stays L2-resident in use"}, cfg, model
+
+
+def learned_leg_1m(lib, torch, stream, model, cfg, sc, steps):
+    """The corrector trained on the 16,384-particle scene, run on the 1M obstacle
+    scene: `steps` plain steps against steps/4 learned steps from the same start;
+    density error against that plain FP32 trajectory (the FP64 oracle is too
+    slow at this size)."""
+    import numpy as np
+    K = cfg.stride
+    steps = (steps // K) * K
+    dt = float(sc.params.timeStep)
+    x0, v0 = sc.positions, sc.velocities
+    with lib.ParticleSimulation(sc.params, x0, v0, sc.options, sc.boundary) as sim:
+        sim.set_stream(stream.cuda_stream)
+        sim.load_corrector(model, cfg)
+        sim.step(count=3)
+        sim.write_state(x0, v0)
+        ms_plain = time_steps(torch, stream, sim, lib.SPH_STEP_PLAIN, steps)
+        ppos, pvel = sim.positions(), sim.velocities()
+        sim.write_state(x0, v0)
+        sim.step(mode=lib.SPH_STEP_LEARNED, count=cfg.auditInterval + 1)
+        before = sim.corrector_report()
+        sim.write_state(x0, v0)
+        ms_learned = time_steps(torch, stream, sim, lib.SPH_STEP_LEARNED, steps // K)
+        after = sim.corrector_report()
+        lpos, lvel = sim.positions(), sim.velocities()
+        # densities at both end states through the plain density pass
+        rho = []
+        for pos, vel in ((ppos, pvel), (lpos, lvel)):
+            sim.write_state(pos, vel)
+            sim.Advance()
+            rho.append(sim.read(lib.FIELD_DENSITY).astype(np.float64))
+    e = np.abs(rho[1] - rho[0]) / rho[0]
+    sim_plain = steps * dt / (ms_plain / 1e3)
+    sim_learned = steps * dt / (ms_learned / 1e3)
+    return {"workload": f"{sc.name}: {sc.n} particles, {steps} plain steps vs {steps // K} learned steps, "
+                        f"model trained on the 16,384-particle scene",
+            "unit": "simulated s / wall s", "plain": sim_plain, "learned": sim_learned,
+            "speedup": sim_learned / sim_plain,
+            "learned_particle_steps_per_s": sc.n * (steps // K) / (ms_learned / 1e3),
+            "plain_particle_steps_per_s": sc.n * steps / (ms_plain / 1e3),
+            "mean_density_err_vs_plain_fp32": float(e.mean()), "max_density_err_vs_plain_fp32": float(e.max()),
+            "audits": after.audits - before.audits, "rollbacks": after.rollbacks - before.rollbacks}
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -311,6 +486,11 @@ def run_ours(args):
     e2e_value = world * n * e2e_steps / el
     sim.close()
 
+    learned = learned_1m = None
+    if rank == 0 and not args.no_learned:
+        learned, lcfg, model = learned_leg(lib, torch, stream)
+        learned_1m = learned_leg_1m(lib, torch, stream, model, lcfg, sc, min(args.steps, 500))
+
     if rank != 0:
         return
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -334,6 +514,9 @@ def run_ours(args):
                         "algorithmic_bytes_per_launch": alg,
                         "avg_launch_us": force_avg_s * 1e6},
            "stages_us": {k: round(v[0] / v[1] * 1e3, 2) for k, v in stages.items()}}
+    if learned is not None:
+        out["learned"] = learned
+        out["learned_1m"] = learned_1m
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(sc)
     print(json.dumps(out), flush=True)

@@ -218,9 +218,12 @@ sph_status ensure_two_scale(sph_sim* s) {
 }
 
 // Enqueues one step of `mode` (no host synchronisation).
-void enqueue_coarse(sph_sim* s, const GridDev& g, const PhysDev& ph, int collide, cudaEvent_t* ev) {
+void enqueue_coarse(sph_sim* s, const GridDev& g, const PhysDev& ph, int collide, cudaEvent_t* ev,
+                    const FeatureOut* feat) {
     cudaStream_t st = s->stream;
     const int n = s->n;
+    StepConfig cfg = s->cfg;
+    if (feat) cfg.forceVariant = FORCE_PRETESTED;  // the feature form reads the density stage's masks
     auto mark = [&](int k) {
         if (ev) cudaEventRecord(ev[k], st);
     };
@@ -234,10 +237,10 @@ void enqueue_coarse(sph_sim* s, const GridDev& g, const PhysDev& ph, int collide
     launch_rank_gather(n, s->sb, s->pos, s->vel, g, s->posS, s->velS, st);
     mark(ST_DENSITY);
     // density and forces read the sorted copies only
-    launch_density(n, s->posS, rows_of(s), g, ph, s->map, s->rho4S, s->rowStart, s->rowMask, s->cfg, st);
+    launch_density(n, s->posS, rows_of(s), g, ph, s->map, s->rho4S, s->rowStart, s->rowMask, cfg, st);
     mark(ST_FORCE);
     launch_force(n, s->posS, s->velS, s->rho4S, s->sb.workIds, rows_of(s), g, ph, s->map, collide, s->rowStart,
-                 s->rowMask, s->pos, s->vel, s->accS, s->cfg, st);
+                 s->rowMask, s->pos, s->vel, s->accS, cfg, st, feat);
     mark(ST_COUNT);
 }
 

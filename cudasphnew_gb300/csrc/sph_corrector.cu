@@ -41,7 +41,7 @@ struct Corrector {
     float* norm = nullptr;
     float stats[2 * IN + 2 * OUT] = {};  // feature means, deviations, target means, deviations
     // learned step and audit scratch
-    float* feat = nullptr;  // n x 24
+    float* feat = nullptr;  // n x 24, particle order: the last learned step's features
     float4 *savePos = nullptr, *saveVel = nullptr, *lPos = nullptr, *lVel = nullptr;
     float *rhoA = nullptr, *rhoB = nullptr;
     unsigned int* errBits = nullptr;
@@ -158,9 +158,8 @@ void enqueue_learned(sph_sim* s, Corrector* C) {
     const int K = C->cfg.stride;
     GridDev g = make_grid(s->P, false);
     PhysDev ph = learned_phys(s, K);
-    enqueue_coarse(s, g, ph, s->O.boxCollision, nullptr);
-    launch_features(s->n, s->posS, s->velS, s->rho4S, s->accS, s->sb.workIds, rows_of(s), g, ph, s->map,
-                    s->O.boxCollision, ph.dt, 0, C->feat, s->stream);
+    const FeatureOut fo{C->feat, 1, s->O.boxCollision, ph.dt};
+    enqueue_coarse(s, g, ph, s->O.boxCollision, nullptr, &fo);
     launch_mlp_apply(s->n, C->feat, mdev(C), 0, s->sb.workIds, s->pos, s->vel, ph, s->O.boxCollision, nullptr,
                      s->status, s->stream);
 }
@@ -350,9 +349,8 @@ sph_status sph_corrector_train(sph_handle s, const sph_corrector_config* cfg) {
             const float4* start = ring + (size_t)2 * (k % (K + 1)) * n;
             TRAIN_CUDA(cudaMemcpyAsync(sh->pos, start, bytes, cudaMemcpyDeviceToDevice, q));
             TRAIN_CUDA(cudaMemcpyAsync(sh->vel, start + n, bytes, cudaMemcpyDeviceToDevice, q));
-            enqueue_coarse(sh, g, ph4, s->O.boxCollision, nullptr);
-            launch_features(n, sh->posS, sh->velS, sh->rho4S, sh->accS, sh->sb.workIds, rows_of(sh), g, ph4, sh->map,
-                            s->O.boxCollision, ph4.dt, 1, feat + (size_t)k * n * IN, q);
+            const FeatureOut fo{feat + (size_t)k * n * IN, 1, s->O.boxCollision, ph4.dt};
+            enqueue_coarse(sh, g, ph4, s->O.boxCollision, nullptr, &fo);
             launch_targets(n, s->pos, s->vel, sh->pos, sh->vel, tgt + (size_t)k * n * TGT, q);
         }
         if (i < cfg->trainSteps) TRAIN_ST(sph_step_many(s, SPH_STEP_PLAIN, 1));
@@ -576,22 +574,12 @@ sph_status sph_corrector_gradient(sph_handle s, const float* features, const flo
     return latched_status(s);
 }
 
-sph_status sph_read_features(sph_handle s, int stride, float* dst, size_t bytes) {
+sph_status sph_read_features(sph_handle s, float* dst, size_t bytes) {
     if (!s || !dst) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "NULL argument");
-    if (stride < 1) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "stride must be >= 1");
-    if (!s->stepped) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "no step has run yet");
+    if (!s->corr || s->corr->rep.learnedSteps == 0) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "no learned step has run");
     const size_t need = sizeof(float) * (size_t)s->n * IN;
     if (bytes < need) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "destination too small");
-    float* f = nullptr;
-    SPH_CUDA(dalloc(&f, (size_t)s->n * IN));
-    GridDev g = make_grid(s->P, false);
-    PhysDev ph = learned_phys(s, stride);
-    launch_features(s->n, s->posS, s->velS, s->rho4S, s->accS, s->sb.workIds, rows_of(s), g, ph, s->map,
-                    s->O.boxCollision, ph.dt, 1, f, s->stream);
-    cudaError_t e = cudaMemcpyAsync(dst, f, need, cudaMemcpyDeviceToHost, s->stream);
-    cudaStreamSynchronize(s->stream);
-    cudaFree(f);
-    SPH_CUDA(e);
+    SPH_CUDA(cudaMemcpyAsync(dst, s->corr->feat, need, cudaMemcpyDeviceToHost, s->stream));
     return latched_status(s);
 }
 

@@ -1,7 +1,8 @@
 // Internal declarations of the learned step corrector: the per-particle MLP
 // 24 -> 64 -> 64 -> 6 (SiLU) with BF16 weights and activations on tcgen05
-// tensor cores (FP32 accumulation in TMEM), its Adam trainer, and the
-// neighbour features it reads.  Not part of the public ABI.
+// tensor cores (FP32 accumulation in TMEM) and its Adam trainer.  The
+// features it reads are recorded by the force stage (write_features,
+// sph_step.cu).  Not part of the public ABI.
 #pragma once
 
 #include "sph_internal.h"
@@ -50,16 +51,10 @@ struct MlpDev {
     const float* norm;           // NNORM
 };
 
-// Features of every particle from the sorted pre-step state (after the force
-// stage of a step): fp32 [24] per particle, written at index workIds[u] when
-// `byId`, else at u.
-void launch_features(int n, const float4* posS, const float4* velS, const float4* rho4S, const float4* accS,
-                     const int* workIds, RowTables T, GridDev g, PhysDev ph, MapDev map, int boxWalls,
-                     float dtL, int byId, float* feat, cudaStream_t s);
-
-// Inference.  mode 0: adds the correction of working index u to pos/vel of
-// particle workIds[u] (and collides when `collide`); mode 1: writes the
-// correction (6 floats) of row u to `out`.
+// Inference over rows u < n.  mode 0: the features of particle id =
+// workIds[u] (rows of `feat` in particle order), whose correction is added to
+// pos/vel[id] (then collided when `collide`); mode 1: feature row u, and the
+// correction (6 floats) is written to out[u].
 void launch_mlp_apply(int n, const float* feat, MlpDev m, int mode, const int* workIds, float4* pos, float4* vel,
                       PhysDev ph, int collide, float* out, unsigned int* status, cudaStream_t s);
 

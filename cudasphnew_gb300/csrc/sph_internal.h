@@ -133,10 +133,18 @@ void launch_rank_gather(int n, SortBuffers sb, const float4* pos, const float4* 
 void launch_density(int n, const float4* posS, RowTables T, GridDev g, PhysDev ph, MapDev map,
                     float4* rho4S, int* rowStart, unsigned int* rowMask, const StepConfig& cfg,
                     cudaStream_t s);
+// Learned-step features recorded by the force stage (24 floats per particle
+// at index workIds[i] when byId, else i; see write_features in sph_step.cu).
+struct FeatureOut {
+    float* feat;
+    int byId;
+    int boxWalls;
+    float dtL;
+};
 void launch_force(int n, const float4* posS, const float4* velS, const float4* rho4S,
                   const int* workIds, RowTables T, GridDev g, PhysDev ph, MapDev map, int collide,
                   const int* rowStart, const unsigned int* rowMask, float4* pos, float4* vel,
-                  float4* accS, const StepConfig& cfg, cudaStream_t s);
+                  float4* accS, const StepConfig& cfg, cudaStream_t s, const FeatureOut* feat = nullptr);
 void launch_unpermute(int n, const int* sortedIds, const float4* srcS, int comp, float* dst,
                       int stride, int offset, cudaStream_t s);
 void launch_cell_tables(int numCells, const int* cellOffset, int* start, int* end, cudaStream_t s);

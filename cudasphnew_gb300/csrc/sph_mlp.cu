@@ -15,6 +15,8 @@
 // is the transposed gradient written to shared memory; rows beyond the layer
 // width are ignored), so a CTA writes one gradient row per optimiser step and
 // Adam sums the rows in a fixed order: training is deterministic.
+#include <cmath>
+
 #include "sph_corrector.h"
 #include "sph_device.cuh"
 #include "sph_tc.cuh"
@@ -28,7 +30,9 @@ using namespace tc;
 
 constexpr uint32_t WAIT_LIMIT = 1u << 22;
 
-__device__ __forceinline__ float sigmoid(float z) { return 1.f / (1.f + __expf(-z)); }
+// 1 / (1 + e^-z); for very negative z the denominator overflows to infinity
+// and the fast division returns 0.
+__device__ __forceinline__ float sigmoid(float z) { return __fdividef(1.f, 1.f + __expf(-z)); }
 
 __device__ __forceinline__ void store_bf16(unsigned char* base, uint32_t off, float v) {
     *reinterpret_cast<__nv_bfloat16*>(base + off) = __float2bfloat16_rn(v);
@@ -99,11 +103,12 @@ constexpr int A_H2 = A_H1 + 16384;      // 128 x 64
 constexpr int A_BIAS = A_H2 + 16384;    // NBIAS floats
 constexpr int A_NORM = A_BIAS + 4 * NBIAS;
 constexpr int A_BAR = A_NORM + 4 * NNORM;
-constexpr int A_BYTES = A_BAR + 16;
-// Requested dynamic shared memory: at most two CTAs per SM, so the two
-// 256-column TMEM allocations always fit the SM's 512 columns.
-constexpr int A_SMEM = 100 * 1024;
-static_assert(A_BYTES <= A_SMEM, "inference shared memory");
+constexpr int A_SMEM = A_BAR + 16;
+// Three CTAs fit an SM's shared memory; their 128-column TMEM allocations
+// (3 x 128 <= 512) always fit beside each other.
+constexpr int A_CTAS_PER_SM = 3;
+constexpr int A_TMEM_COLS = 128;  // D1 at 0, D2 at 64, D3 reuses D1's columns
+static_assert(A_CTAS_PER_SM * A_TMEM_COLS <= 512, "inference TMEM");
 
 // bias + SiLU of 64 accumulator columns at `col`, as BF16 row t of `dst` (K = 64).
 __device__ __forceinline__ void hidden_layer_out(uint32_t tbase, int warp, int col, const float* bias,
@@ -141,7 +146,7 @@ __global__ void __launch_bounds__(TILE, 1)
         mbar_init(bar, 1);
         sOk = 1;
     }
-    if (warp == 0) tmem_alloc(slot, 256);
+    if (warp == 0) tmem_alloc(slot, A_TMEM_COLS);
     cta_sync();
     const uint32_t tbase = *slot;
     const uint32_t sW = smem_u32(sm + A_W);
@@ -150,9 +155,10 @@ __global__ void __launch_bounds__(TILE, 1)
     for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
         const long long u = (long long)tile * TILE + t;
         const bool valid = u < n;
+        const long long row = (mode == 0 && valid) ? (long long)workIds[u] : u;
         {
             float f[INP];
-            load_features(feat, u, valid, sNorm, f);
+            load_features(feat, row, valid, sNorm, f);
 #pragma unroll
             for (int c = 0; c < INP / 8; c++) store_row8(sm + A_X, t, 8 * c, INP, f + 8 * c);
         }
@@ -165,17 +171,17 @@ __global__ void __launch_bounds__(TILE, 1)
         if (!commit_and_wait(bar, phase, &sOk, t)) break;
         hidden_layer_out(tbase, warp, 64, sBias + HID, sm + A_H2, t);
         cta_sync();
-        if (t == 0) mma_chain(tbase + 128, smem_u32(sm + A_H2), sW + IMG_W3, HID, OUTP, false);
+        if (t == 0) mma_chain(tbase + 0, smem_u32(sm + A_H2), sW + IMG_W3, HID, OUTP, false);
         if (!commit_and_wait(bar, phase, &sOk, t)) break;
         float y[16];
-        tmem_ld16(tmem_at(tbase, 32 * warp, 128), y);
+        tmem_ld16(tmem_at(tbase, 32 * warp, 0), y);
         if (valid) {
             float c[OUT];
 #pragma unroll
             for (int o = 0; o < OUT; o++)
                 c[o] = sNorm[N_MUT + o] + sNorm[N_SGT + o] * (y[o] + sBias[2 * HID + o]);
             if (mode == 0) {
-                const int id = workIds[u];
+                const int id = (int)row;
                 const float4 p = pos[id], w = vel[id];
                 float3 x = make_float3(p.x + c[0], p.y + c[1], p.z + c[2]);
                 float3 v = make_float3(w.x + c[3], w.y + c[4], w.z + c[5]);
@@ -191,7 +197,7 @@ __global__ void __launch_bounds__(TILE, 1)
     cta_sync();
     if (!sOk) drain(bar, phase, t, status);
     cta_sync();
-    if (warp == 0) tmem_dealloc(tbase, 256);
+    if (warp == 0) tmem_dealloc(tbase, A_TMEM_COLS);
 }
 
 // ---------------------------------------------------------------------------
@@ -560,7 +566,7 @@ void launch_mlp_apply(int n, const float* feat, MlpDev m, int mode, const int* w
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int grid = tiles < 2 * sms ? tiles : 2 * sms;
+    const int grid = tiles < A_CTAS_PER_SM * sms ? tiles : A_CTAS_PER_SM * sms;
     if (grid > 0)
         k_mlp_apply<<<grid, TILE, A_SMEM, s>>>(n, feat, m, mode, workIds, pos, vel, ph, collide, out, status);
 }

@@ -111,8 +111,10 @@ sph_status ensure_two_scale(sph_sim* s);
 // Enqueues one step of `mode` (no host synchronisation).
 void enqueue_step(sph_sim* s, int mode, bool timing);
 // Hash, sort, density and force + integration (+ box collision) of the
-// coarse particles with the given constants; stage events when `ev`.
-void enqueue_coarse(sph_sim* s, const GridDev& g, const PhysDev& ph, int collide, cudaEvent_t* ev);
+// coarse particles with the given constants; stage events when `ev`; the
+// force stage also records the corrector's features when `feat`.
+void enqueue_coarse(sph_sim* s, const GridDev& g, const PhysDev& ph, int collide, cudaEvent_t* ev,
+                    const FeatureOut* feat = nullptr);
 // Hash, sort and density of the state (pos, vel) into the handle's sorted
 // copies (posS, velS, rho4S) and tables; nothing is integrated.
 void enqueue_density_only(sph_sim* s, const float4* pos, const float4* vel);

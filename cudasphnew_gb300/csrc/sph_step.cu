@@ -120,6 +120,44 @@ struct RowSums {
     }
 };
 
+// Neighbour sums of the learned corrector's input features (FEAT forms
+// only; the scale factors poly6*m and m*gradSpiky are applied once at the end).
+struct FeatSums {
+    float shep = 0.f, m1[3] = {0.f, 0.f, 0.f}, div = 0.f, curl[3] = {0.f, 0.f, 0.f}, cg[3] = {0.f, 0.f, 0.f};
+    float cnt = 0.f;
+    __device__ __forceinline__ void add(const PhysDev& ph, float4 xi, float4 vi, float4 xj, float4 vj, float4 rj) {
+        const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
+        const float r2 = dist2(xi, xj);
+        const float rinv = rsqrtf(r2);
+        const float hr = ph.h - r2 * rinv;
+        const float q = ph.h2 - r2;
+        const float w = q * q * q * rj.w;          // W_ij / (poly6 m) * m/rho_j
+        const float gs = hr * hr * rinv * rj.w;    // |gradW_ij| / (m gradSpiky) * m/rho_j / r
+        const float ux = vj.x - vi.x, uy = vj.y - vi.y, uz = vj.z - vi.z;
+        const float ex = gs * dx, ey = gs * dy, ez = gs * dz;
+        shep += w;
+        m1[0] = fmaf(w, ux, m1[0]);
+        m1[1] = fmaf(w, uy, m1[1]);
+        m1[2] = fmaf(w, uz, m1[2]);
+        div += ux * ex + uy * ey + uz * ez;
+        curl[0] += uy * ez - uz * ey;
+        curl[1] += uz * ex - ux * ez;
+        curl[2] += ux * ey - uy * ex;
+        cg[0] += ex;
+        cg[1] += ey;
+        cg[2] += ez;
+        cnt += 1.f;
+    }
+};
+
+// Where the force stage writes the features: feat[(byId ? workIds[i] : i) * 24].
+struct FeatOut {
+    float* feat;
+    int byId;
+    int boxWalls;
+    float dtL;
+};
+
 template <bool KAHAN, bool TENSION>
 struct ForceTotals {
     float fp[3] = {0.f, 0.f, 0.f}, cp[3] = {0.f, 0.f, 0.f};
@@ -142,16 +180,65 @@ struct ForceTotals {
     }
 };
 
+// The 24 input features of the learned step corrector:
+//   0 rho/rho0 - 1;  1 Shepard sum sum_j (m/rho_j) W_ij;  2-4 v;  5-7 a/g;
+//   8-10 sum_j (m/rho_j) W_ij (v_j - v_i);  11 dtL sum_j (m/rho_j)(v_j - v_i).gradW_ij;
+//   12-14 dtL sum_j (m/rho_j)(v_j - v_i) x gradW_ij;  15-17 h sum_j (m/rho_j) gradW_ij;
+//   18 neighbours/32;  19 wall distance/h (box walls and boundary map, capped at 4);
+//   20-22 unit wall normal into the fluid;  23 |v| dtL/h.
+// W is poly6, gradW the spiky gradient, sums over neighbours within h of
+// the pre-step state.  No reference counterpart.
+__device__ __forceinline__ void write_features(const FeatSums& fs, const FeatOut& fo, int i, int id, float4 xi,
+                                               float4 vi, float4 ri, const float* acc, float mapDist,
+                                               const float* mapN, const PhysDev& ph) {
+    const float h = ph.h;
+    float dw = 4.f * h, nx = 0.f, ny = 0.f, nz = 0.f;
+    if (fo.boxWalls) {
+        const float c[3] = {xi.x - ph.boxCen[0], xi.y - ph.boxCen[1], xi.z - ph.boxCen[2]};
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            const float da = ph.boxDim[a] - fabsf(c[a]);
+            if (da < dw) {
+                dw = da;
+                const float sg = c[a] > 0.f ? -1.f : 1.f;
+                nx = a == 0 ? sg : 0.f;
+                ny = a == 1 ? sg : 0.f;
+                nz = a == 2 ? sg : 0.f;
+            }
+        }
+    }
+    if (mapDist < dw) {
+        dw = mapDist;
+        nx = mapN[0];
+        ny = mapN[1];
+        nz = mapN[2];
+    }
+    dw = fminf(fmaxf(dw, 0.f), 4.f * h);
+    const float gInv = ph.gravity != 0.f ? 1.f / ph.gravity : 1.f;
+    const float gw = -ph.pressCoef;  // m gradSpiky
+    const float kd = gw * fo.dtL;
+    const float vn = sqrtf(vi.x * vi.x + vi.y * vi.y + vi.z * vi.z);
+    float4* dst = reinterpret_cast<float4*>(fo.feat + (size_t)(fo.byId ? id : i) * 24);
+    dst[0] = make_float4(ri.x / ph.restDensity - 1.f, ph.poly6m * fs.shep, vi.x, vi.y);
+    dst[1] = make_float4(vi.z, acc[0] * gInv, acc[1] * gInv, acc[2] * gInv);
+    dst[2] = make_float4(ph.poly6m * fs.m1[0], ph.poly6m * fs.m1[1], ph.poly6m * fs.m1[2], kd * fs.div);
+    dst[3] = make_float4(kd * fs.curl[0], kd * fs.curl[1], kd * fs.curl[2], gw * h * fs.cg[0]);
+    dst[4] = make_float4(gw * h * fs.cg[1], gw * h * fs.cg[2], fs.cnt * (1.f / 32.f), dw / h);
+    dst[5] = make_float4(nx, ny, nz, vn * fo.dtL / h);
+}
+
 // Wall terms, surface tension, a = F/rho - g, symplectic Euler, box
 // collision, and the write-back (compute_particle_acceleration_ifsurf
 // :407-473, integrate_euler :632-665, collision_handling :742-834).  The wall
 // terms follow the reference's operation order exactly.
-template <bool KAHAN, bool TENSION>
+template <bool KAHAN, bool TENSION, bool FEAT>
 __device__ __forceinline__ void force_epilogue(const ForceTotals<KAHAN, TENSION>& A, int i, float4 xi,
                                                float4 vi, float4 ri, const PhysDev& ph, const MapDev& map,
                                                int collideFlag, const int* __restrict__ workIds,
                                                float4* __restrict__ pos, float4* __restrict__ vel,
-                                               float4* __restrict__ accS) {
+                                               float4* __restrict__ accS, const FeatSums& fs,
+                                               const FeatOut& fo) {
+    float mapDist = 1e30f, mapN[3] = {0.f, 0.f, 0.f};  // learned features only
     const float rho = ri.x;
     const float pc = ph.pressCoef * rho;
     float force[3];
@@ -167,6 +254,7 @@ __device__ __forceinline__ void force_epilogue(const ForceTotals<KAHAN, TENSION>
         map_uvw(map, xi, uvw);
         const float4 s = tri_vec(map, uvw[0], uvw[1], uvw[2]);
         const float distWall = -s.x;
+        if (FEAT) mapDist = distWall;
         if (distWall < map.restDistance) {
             tension = false;
             const float coeff = rho / (ph.dtCollide * ph.dtCollide) * (map.restDistance - distWall);
@@ -183,6 +271,14 @@ __device__ __forceinline__ void force_epilogue(const ForceTotals<KAHAN, TENSION>
             force[0] -= coeff * gN[0];
             force[1] -= coeff * gN[1];
             force[2] -= coeff * gN[2];
+            if (FEAT) {
+                const float gn = sqrtf(gN[0] * gN[0] + gN[1] * gN[1] + gN[2] * gN[2]);
+                if (gn > 0.f) {
+                    mapN[0] = -gN[0] / gn;
+                    mapN[1] = -gN[1] / gn;
+                    mapN[2] = -gN[2] / gn;
+                }
+            }
             force[0] -= vi.x * s.z;
             force[1] -= vi.y * s.z;
             force[2] -= vi.z * s.z;
@@ -209,6 +305,7 @@ __device__ __forceinline__ void force_epilogue(const ForceTotals<KAHAN, TENSION>
     pos[id] = make_float4(x.x, x.y, x.z, 0.f);
     vel[id] = make_float4(v.x, v.y, v.z, 0.f);
     accS[i] = make_float4(acc[0], acc[1], acc[2], 0.f);
+    if (FEAT) write_features(fs, fo, i, id, xi, vi, ri, acc, mapDist, mapN, ph);
 }
 
 struct ForceArgs {
@@ -227,9 +324,10 @@ struct ForceArgs {
     float4* pos;
     float4* vel;
     float4* accS;
+    FeatOut fo;
 };
 
-template <bool KAHAN, bool TENSION, int FORM>
+template <bool KAHAN, bool TENSION, int FORM, bool FEAT>
 __global__ void __launch_bounds__(256, 2) k_force(ForceArgs F) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= F.n) return;
@@ -240,18 +338,25 @@ __global__ void __launch_bounds__(256, 2) k_force(ForceArgs F) {
     Stencil st;
     if (FORM != FORCE_PRETESTED) st = stencil(xi, F.ph.h, F.g);
     ForceTotals<KAHAN, TENSION> A;
+    FeatSums fs;
     auto direct = [&](RowSums<TENSION>& R, int s, int e) {
         for (int t = s; t < e; t++) {
             const float4 xj = __ldg(F.posS + t);
             const float r2 = dist2(xi, xj);
-            if (r2 <= h2 && r2 > 0.f) R.add(F.ph, xi, vi, ri.z, xj, __ldg(F.velS + t), __ldg(F.rho4S + t));
+            if (r2 <= h2 && r2 > 0.f) {
+                const float4 vj = __ldg(F.velS + t), rj = __ldg(F.rho4S + t);
+                R.add(F.ph, xi, vi, ri.z, xj, vj, rj);
+                if (FEAT) fs.add(F.ph, xi, vi, xj, vj, rj);
+            }
         }
     };
     auto bits = [&](RowSums<TENSION>& R, int base, unsigned int m) {
         while (m) {
             const int t = base + __ffs(m) - 1;
             m &= m - 1u;
-            R.add(F.ph, xi, vi, ri.z, __ldg(F.posS + t), __ldg(F.velS + t), __ldg(F.rho4S + t));
+            const float4 xj = __ldg(F.posS + t), vj = __ldg(F.velS + t), rj = __ldg(F.rho4S + t);
+            R.add(F.ph, xi, vi, ri.z, xj, vj, rj);
+            if (FEAT) fs.add(F.ph, xi, vi, xj, vj, rj);
         }
     };
 #pragma unroll
@@ -282,7 +387,8 @@ __global__ void __launch_bounds__(256, 2) k_force(ForceArgs F) {
         }
         A.add(R);
     }
-    force_epilogue(A, i, xi, vi, ri, F.ph, F.map, F.collide, F.workIds, F.pos, F.vel, F.accS);
+    force_epilogue<KAHAN, TENSION, FEAT>(A, i, xi, vi, ri, F.ph, F.map, F.collide, F.workIds, F.pos, F.vel,
+                                         F.accS, fs, F.fo);
 }
 
 // ---------------------------------------------------------------------------
@@ -308,18 +414,28 @@ template <bool KAHAN, bool TENSION>
 static void force_dispatch(const ForceArgs& F, const StepConfig& cfg, cudaStream_t s) {
     const int bs = cfg.forceBlock > 0 ? cfg.forceBlock : 128;
     const int grid = (F.n + bs - 1) / bs;
-    if (cfg.forceVariant == FORCE_PRETESTED) k_force<KAHAN, TENSION, FORCE_PRETESTED><<<grid, bs, 0, s>>>(F);
-    else if (cfg.forceVariant == FORCE_MASK) k_force<KAHAN, TENSION, FORCE_MASK><<<grid, bs, 0, s>>>(F);
-    else k_force<KAHAN, TENSION, FORCE_DIRECT><<<grid, bs, 0, s>>>(F);
+    if (F.fo.feat) {
+        // the learned step's force stage records the corrector's features; the
+        // density stage has recorded the neighbour masks (pretested form)
+        k_force<KAHAN, TENSION, FORCE_PRETESTED, true><<<grid, bs, 0, s>>>(F);
+    } else if (cfg.forceVariant == FORCE_PRETESTED) {
+        k_force<KAHAN, TENSION, FORCE_PRETESTED, false><<<grid, bs, 0, s>>>(F);
+    } else if (cfg.forceVariant == FORCE_MASK) {
+        k_force<KAHAN, TENSION, FORCE_MASK, false><<<grid, bs, 0, s>>>(F);
+    } else {
+        k_force<KAHAN, TENSION, FORCE_DIRECT, false><<<grid, bs, 0, s>>>(F);
+    }
 }
 
 void launch_force(int n, const float4* posS, const float4* velS, const float4* rho4S, const int* workIds,
                   RowTables T, GridDev g, PhysDev ph, MapDev map, int collide, const int* rowStart,
                   const unsigned int* rowMask, float4* pos, float4* vel, float4* accS, const StepConfig& cfg,
-                  cudaStream_t s) {
+                  cudaStream_t s, const FeatureOut* feat) {
     if (n <= 0) return;
+    FeatOut fo{nullptr, 0, 0, 0.f};
+    if (feat) fo = FeatOut{feat->feat, feat->byId, feat->boxWalls, feat->dtL};
     ForceArgs F{n,  posS, velS, rho4S, workIds, T, g, ph, map, collide, cfg.prune,
-                RowMasks{const_cast<int*>(rowStart), const_cast<unsigned int*>(rowMask)}, pos, vel, accS};
+                RowMasks{const_cast<int*>(rowStart), const_cast<unsigned int*>(rowMask)}, pos, vel, accS, fo};
     const bool tension = ph.tension != 0.0f;
     if (cfg.kahan) {
         if (tension) force_dispatch<true, true>(F, cfg, s);

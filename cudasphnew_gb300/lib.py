@@ -61,7 +61,7 @@ SIGNATURES = {
     "sph_corrector_get_report": (_i, [_vp, _vp]),
     "sph_corrector_predict": (_i, [_vp, _vp, _i, _vp]),
     "sph_corrector_gradient": (_i, [_vp, _vp, _vp, _i, _vp, _vp]),
-    "sph_read_features": (_i, [_vp, _i, _vp, ctypes.c_size_t]),
+    "sph_read_features": (_i, [_vp, _vp, ctypes.c_size_t]),
     "sph_last_error": (ctypes.c_char_p, []),
     "sph_status_string": (ctypes.c_char_p, [_i]),
 }
@@ -287,9 +287,10 @@ class ParticleSimulation:
                                             loss.ctypes.data))
         return g, float(loss[0])
 
-    def features(self, stride: int = 4) -> np.ndarray:
+    def features(self) -> np.ndarray:
+        """Features the last learned step computed (particle order)."""
         out = np.zeros((self.n, CORRECTOR_FEATURES), np.float32)
-        check(load().sph_read_features(self._h, stride, out.ctypes.data, out.nbytes))
+        check(load().sph_read_features(self._h, out.ctypes.data, out.nbytes))
         return out
 
     def diagnostics(self) -> Diagnostics:

@@ -309,9 +309,9 @@ sph_status sph_corrector_predict(sph_handle h, const float* features, int count,
 sph_status sph_corrector_gradient(sph_handle h, const float* features, const float* targets, int count,
                                   float* grad, float* loss);
 
-/* The corrector's input features (n x 24, particle order) of the state that
- * entered the last step, for learned step size stride*dt. */
-sph_status sph_read_features(sph_handle h, int stride, float* dst, size_t bytes);
+/* The corrector's input features (n x 24, particle order) that the last
+ * SPH_STEP_LEARNED step computed from the state it started from. */
+sph_status sph_read_features(sph_handle h, float* dst, size_t bytes);
 
 /* Device pointer of a field in the handle's layout, for zero-copy consumers
  * (replaces the OpenGL VBO getters, :2278-2301): 0 = positions (float4[n],

@@ -4,7 +4,8 @@
   restatement that rounds the same operands to BF16; the remaining differences
   come from FP32 accumulation order and the device exponential, so the bars
   are relative (1e-3 of the output scale, 2e-2 of each gradient block's norm).
-* The neighbour features against a brute-force float64 restatement.
+* The neighbour features (recorded by the learned step's force stage)
+  against a brute-force float64 restatement.
 * Training lowers the loss; the learned step beats the uncorrected plain step
   of the same size against the plain trajectory.
 * The audit: with tolerance 0 every audited step is rolled back to exactly the
@@ -175,7 +176,7 @@ def features_ref(sc, pos, vel, rho, acc, stride):
     v = vel.astype(np.float64)
     d = x[:, None, :] - x[None, :, :]
     r2 = (d * d).sum(2)
-    mask = (r2 < h2) & (r2 > 0)
+    mask = (r2 <= h2) & (r2 > 0)
     inv = 1.0 / rho.astype(np.float64)[None, :]
     W = np.where(mask, float(f32(p.poly6) * f32(m)) * (h2 - r2) ** 3 * inv, 0.0)
     r = np.sqrt(np.where(mask, r2, 1.0))
@@ -206,13 +207,16 @@ def features_ref(sc, pos, vel, rho, acc, stride):
 
 
 def test_features_match_numpy(sphlib):
+    """The features the learned step's force stage records, against a
+    brute-force restatement from the state the step started from."""
     sc = tiny()
     with make(sphlib, sc) as sim:
         sim.step(count=30)
         x0, v0 = sim.positions(), sim.velocities()
-        sim.Advance()
+        sim.load_corrector(random_blob(4), stride=4, auditInterval=0)
+        sim.step(mode=sphlib.SPH_STEP_LEARNED)
         rho, acc = sim.read(sphlib.FIELD_DENSITY), sim.read(sphlib.FIELD_ACCELERATION)
-        got = sim.features(stride=4)
+        got = sim.features()
     ref = features_ref(sc, x0, v0, rho, acc, 4)
     scale = np.abs(ref).max(0) + 1e-6
     err = np.abs(got - ref) / scale
