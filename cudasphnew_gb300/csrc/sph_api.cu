@@ -44,7 +44,7 @@ sph_status record_error(sph_status st, const char* file, int line, const std::st
 
 namespace sph {
 
-RowTables rows_of(const sph_sim* s) { return RowTables{s->sb.cellOffset, s->sb.halfOffset}; }
+RowTables rows_of(const sph_sim* s) { return RowTables{s->sb.cellOffset, s->sb.halfOffset, s->sb.scenes}; }
 
 GridDev make_grid(const SimulationParameters& P, bool sub) {
     GridDev g;
@@ -54,6 +54,7 @@ GridDev make_grid(const SimulationParameters& P, bool sub) {
     }
     g.spacing = sub ? P.gridSpacingSubParticles : P.gridSpacing;
     g.numCells = g.dim[0] * g.dim[1] * g.dim[2];
+    g.cellBase = 0;
     return g;
 }
 
@@ -135,7 +136,8 @@ void free_all(sph_sim* s) {
     void* ptrs[] = {s->pos, s->vel, s->posS, s->velS, s->rho4S, s->accS, s->sb.cnt, s->sb.cellOffset,
                     s->sb.keySlot, s->sb.tmpIds, s->sb.sortedHash, s->sb.sortedIds, s->sb.workIds,
                     s->sb.xS, s->sb.halfOffset, s->scanBlock,
-                    s->status, s->staging, s->map4, s->mapDist, s->rowStart, s->rowMask, s->diagBuf};
+                    s->status, s->staging, s->map4, s->mapDist, s->rowStart, s->rowMask, s->diagBuf,
+                    s->scenesDev};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     void* tsPtrs[] = {s->ts.state,     s->ts.blockCounts, s->ts.blockOffsets, s->ts.counts,
@@ -247,7 +249,7 @@ void enqueue_coarse(sph_sim* s, const GridDev& g, const PhysDev& ph, int collide
 void enqueue_density_only(sph_sim* s, const float4* pos, const float4* vel) {
     cudaStream_t st = s->stream;
     const int n = s->n;
-    GridDev g = make_grid(s->P, false);
+    GridDev g = grid_of(s);
     PhysDev ph = make_phys(s->P, s->O);
     launch_hash_count(n, pos, g, s->sb, s->status, st);
     launch_cell_scan(g.numCells, s->sb, s->status, st);
@@ -281,7 +283,7 @@ void enqueue_step(sph_sim* s, int mode, bool timing) {
     const bool twoScale = mode == SPH_STEP_TWO_SCALE;
     cudaStream_t st = s->stream;
     const int n = s->n;
-    GridDev g = make_grid(s->P, false);
+    GridDev g = grid_of(s);
     PhysDev ph = make_phys(s->P, s->O);
     cudaEvent_t* ev = nullptr;
     if (timing) {
@@ -311,6 +313,70 @@ void enqueue_step(sph_sim* s, int mode, bool timing) {
         launch_ts_sub_force(sg, sph, s->ts, cap, st);
         launch_ts_sub_integrate(sph, s->ts, cap, st);
     }
+}
+
+sph_status alloc_handle(sph_sim* s, int n, long long C) {
+    s->n = n;
+    s->numCellsTotal = C;
+    const long long tiles = (C + 1 + SCAN_TILE - 1) / SCAN_TILE;
+    SPH_CUDA(cudaGetDevice(&s->device));
+    SPH_CUDA(cudaStreamCreateWithFlags(&s->ownStream, cudaStreamNonBlocking));
+    s->stream = s->ownStream;
+    SPH_CUDA(dalloc(&s->pos, n));
+    SPH_CUDA(dalloc(&s->vel, n));
+    SPH_CUDA(dalloc(&s->posS, n));
+    SPH_CUDA(dalloc(&s->velS, n));
+    SPH_CUDA(dalloc(&s->rho4S, n));
+    SPH_CUDA(dalloc(&s->accS, n));
+    SPH_CUDA(dalloc(&s->rowStart, (size_t)9 * n));
+    SPH_CUDA(dalloc(&s->rowMask, (size_t)9 * n));
+    SPH_CUDA(dalloc(&s->sb.cnt, (size_t)C + 1 + SCAN_TILE));
+    SPH_CUDA(dalloc(&s->sb.cellOffset, (size_t)C + 1 + SCAN_TILE));
+    SPH_CUDA(dalloc(&s->sb.keySlot, n));
+    SPH_CUDA(dalloc(&s->sb.tmpIds, n));
+    SPH_CUDA(dalloc(&s->sb.sortedHash, n));
+    SPH_CUDA(dalloc(&s->sb.sortedIds, n));
+    SPH_CUDA(dalloc(&s->sb.workIds, n));
+    SPH_CUDA(dalloc(&s->sb.xS, n));
+    SPH_CUDA(dalloc(&s->sb.halfOffset, (size_t)C + 1));
+    SPH_CUDA(cudaMemsetAsync(s->sb.halfOffset, 0, sizeof(int) * ((size_t)C + 1), s->stream));
+    SPH_CUDA(dalloc(&s->scanBlock, (size_t)tiles + 2));
+    s->sb.tileCounter = reinterpret_cast<unsigned int*>(s->scanBlock);
+    s->sb.scanFlags = s->scanBlock + 2;
+    s->sb.maxTiles = (int)tiles;
+    SPH_CUDA(dalloc(&s->status, 1));
+    SPH_CUDA(cudaMallocHost((void**)&s->statusHost, sizeof(unsigned int)));
+    SPH_CUDA(dalloc(&s->staging, (size_t)n * 10));
+    SPH_CUDA(cudaMemsetAsync(s->sb.cnt, 0, sizeof(int) * ((size_t)C + 1 + SCAN_TILE), s->stream));
+    SPH_CUDA(cudaMemsetAsync(s->status, 0, sizeof(unsigned int), s->stream));
+    SPH_CUDA(cudaMemsetAsync(s->vel, 0, sizeof(float4) * n, s->stream));
+    SPH_CUDA(cudaMemsetAsync(s->rho4S, 0, sizeof(float4) * n, s->stream));
+    SPH_CUDA(cudaMemsetAsync(s->accS, 0, sizeof(float4) * n, s->stream));
+    s->sdMass.assign(n, 0.0f);
+    s->sdEnergy.assign(n, 0.0f);
+    return SPH_OK;
+}
+
+MapDev map_of(const sph_boundary_desc& d, const unsigned int dims[3], const float4* map4, const float* dist) {
+    MapDev m{};
+    m.map4 = map4;
+    m.dist = dist;
+    for (int a = 0; a < 3; a++) {
+        m.origin[a] = d.gridStart[a];
+        m.dims[a] = (int)dims[a];
+        m.dimsf[a] = (float)dims[a];
+        m.length[a] = (float)(dims[a] - 1) * d.gridSpacing;
+        m.du[a] = d.gridSpacing / m.length[a];
+    }
+    m.restDistance = d.restDistance;
+    m.present = 1;
+    return m;
+}
+
+GridDev grid_of(const sph_sim* s) {
+    GridDev g = make_grid(s->P, false);
+    g.numCells = (int)s->numCellsTotal;
+    return g;
 }
 
 sph_status latched_status(sph_sim* s) {
@@ -412,10 +478,14 @@ sph_status sph_create(const SimulationParameters* params, const sph_options* opt
     s->P = *params;
     if (opts) s->O = *opts;
     else sph_default_options(&s->O);
-    s->n = (int)params->numParticles;
-    const int n = s->n;
-    const int C = params->gridDim[0] * params->gridDim[1] * params->gridDim[2];
-    const int tiles = (C + 1 + SCAN_TILE - 1) / SCAN_TILE;
+    const int n = (int)params->numParticles;
+    const long long C = (long long)params->gridDim[0] * params->gridDim[1] * params->gridDim[2];
+    st = alloc_handle(s, n, C);
+    if (st) {
+        free_all(s);
+        delete s;
+        return st;
+    }
 
 #define CREATE_CUDA(call)                                                  \
     do {                                                                   \
@@ -428,46 +498,10 @@ sph_status sph_create(const SimulationParameters* params, const sph_options* opt
         }                                                                  \
     } while (0)
 
-    CREATE_CUDA(cudaGetDevice(&s->device));
-    CREATE_CUDA(cudaStreamCreateWithFlags(&s->ownStream, cudaStreamNonBlocking));
-    s->stream = s->ownStream;
-    CREATE_CUDA(dalloc(&s->pos, n));
-    CREATE_CUDA(dalloc(&s->vel, n));
-    CREATE_CUDA(dalloc(&s->posS, n));
-    CREATE_CUDA(dalloc(&s->velS, n));
-    CREATE_CUDA(dalloc(&s->rho4S, n));
-    CREATE_CUDA(dalloc(&s->accS, n));
-    CREATE_CUDA(dalloc(&s->rowStart, (size_t)9 * n));
-    CREATE_CUDA(dalloc(&s->rowMask, (size_t)9 * n));
-    CREATE_CUDA(dalloc(&s->sb.cnt, (size_t)C + 1 + SCAN_TILE));
-    CREATE_CUDA(dalloc(&s->sb.cellOffset, (size_t)C + 1 + SCAN_TILE));
-    CREATE_CUDA(dalloc(&s->sb.keySlot, n));
-    CREATE_CUDA(dalloc(&s->sb.tmpIds, n));
-    CREATE_CUDA(dalloc(&s->sb.sortedHash, n));
-    CREATE_CUDA(dalloc(&s->sb.sortedIds, n));
-    CREATE_CUDA(dalloc(&s->sb.workIds, n));
-    CREATE_CUDA(dalloc(&s->sb.xS, n));
-    CREATE_CUDA(dalloc(&s->sb.halfOffset, (size_t)C + 1));
-    CREATE_CUDA(cudaMemsetAsync(s->sb.halfOffset, 0, sizeof(int) * ((size_t)C + 1), s->stream));
-    CREATE_CUDA(dalloc(&s->scanBlock, (size_t)tiles + 2));
-    s->sb.tileCounter = reinterpret_cast<unsigned int*>(s->scanBlock);
-    s->sb.scanFlags = s->scanBlock + 2;
-    s->sb.maxTiles = tiles;
-    CREATE_CUDA(dalloc(&s->status, 1));
-    CREATE_CUDA(cudaMallocHost((void**)&s->statusHost, sizeof(unsigned int)));
-    CREATE_CUDA(dalloc(&s->staging, (size_t)n * 10));
-    CREATE_CUDA(cudaMemsetAsync(s->sb.cnt, 0, sizeof(int) * ((size_t)C + 1 + SCAN_TILE), s->stream));
-    CREATE_CUDA(cudaMemsetAsync(s->status, 0, sizeof(unsigned int), s->stream));
-    CREATE_CUDA(cudaMemsetAsync(s->vel, 0, sizeof(float4) * n, s->stream));
-    CREATE_CUDA(cudaMemsetAsync(s->rho4S, 0, sizeof(float4) * n, s->stream));
-    CREATE_CUDA(cudaMemsetAsync(s->accS, 0, sizeof(float4) * n, s->stream));
-
     // initial state: VD positions, SD velocities
     CREATE_CUDA(cudaMemcpyAsync(s->staging, vertexData, sizeof(float) * 3 * (size_t)n,
                                 cudaMemcpyHostToDevice, s->stream));
     launch_unpack_aos(s->staging, 3, 0, n, s->pos, s->stream);
-    s->sdMass.assign(n, 0.0f);
-    s->sdEnergy.assign(n, 0.0f);
     if (simulationData) {
         CREATE_CUDA(cudaStreamSynchronize(s->stream));
         CREATE_CUDA(cudaMemcpyAsync(s->staging, simulationData, sizeof(float) * 10 * (size_t)n,
@@ -485,18 +519,7 @@ sph_status sph_create(const SimulationParameters* params, const sph_options* opt
         launch_build_maps(*boundary, mdims, s->mapDist, nullptr, nullptr, s->map4, s->stream);
         s->desc = *boundary;
         s->hasDesc = true;
-        MapDev& m = s->map;
-        m.map4 = s->map4;
-        m.dist = s->mapDist;
-        for (int a = 0; a < 3; a++) {
-            m.origin[a] = boundary->gridStart[a];
-            m.dims[a] = (int)mdims[a];
-            m.dimsf[a] = (float)mdims[a];
-            m.length[a] = (float)(mdims[a] - 1) * boundary->gridSpacing;
-            m.du[a] = boundary->gridSpacing / m.length[a];
-        }
-        m.restDistance = boundary->restDistance;
-        m.present = 1;
+        s->map = map_of(*boundary, mdims, s->map4, s->mapDist);
     }
     CREATE_CUDA(cudaGetLastError());
     CREATE_CUDA(cudaStreamSynchronize(s->stream));
@@ -515,6 +538,7 @@ sph_status sph_destroy(sph_handle s) {
 
 sph_status sph_bind(sph_handle s, const SimulationParameters* params) {
     if (!s) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "handle is NULL");
+    if (s->numScenes > 1) SPH_FAIL(SPH_ERR_NOT_SUPPORTED, "batched handles keep their scenes' parameters");
     sph_status st = validate_params(params, &s->O);
     if (st) return st;
     if (params->numParticles != s->P.numParticles)
@@ -539,6 +563,8 @@ sph_status sph_set_stream(sph_handle s, void* stream) {
 sph_status sph_step(sph_handle s, int mode) {
     if (!s) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "handle is NULL");
     if (mode < SPH_STEP_PLAIN || mode > SPH_STEP_LEARNED) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "unknown step mode");
+    if (s->numScenes > 1 && mode != SPH_STEP_PLAIN)
+        SPH_FAIL(SPH_ERR_NOT_SUPPORTED, "batched handles take plain steps only");
     if (mode == SPH_STEP_LEARNED) return corrector_step(s, 1, false);
     if (mode != SPH_STEP_PLAIN) {
         sph_status st = ensure_two_scale(s);
@@ -557,6 +583,8 @@ sph_status sph_step_many(sph_handle s, int mode, int count) {
     if (!s) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "handle is NULL");
     if (mode < SPH_STEP_PLAIN || mode > SPH_STEP_LEARNED) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "unknown step mode");
     if (count <= 0) return SPH_OK;
+    if (s->numScenes > 1 && mode != SPH_STEP_PLAIN)
+        SPH_FAIL(SPH_ERR_NOT_SUPPORTED, "batched handles take plain steps only");
     if (mode == SPH_STEP_LEARNED) return corrector_step(s, count, true);
     if (mode != SPH_STEP_PLAIN) {
         sph_status st = ensure_two_scale(s);
@@ -729,6 +757,9 @@ sph_status sph_write(sph_handle s, int field, const void* src, size_t bytes) {
             if (bytes < sizeof(float) * 3 * (size_t)n) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "source too small");
             SPH_CUDA(cudaMemcpyAsync(s->staging, src, sizeof(float) * 3 * (size_t)n, cudaMemcpyHostToDevice, q));
             launch_unpack_aos(s->staging, 3, 0, n, field == SPH_FIELD_VERTEX_DATA ? s->pos : s->vel, q);
+            if (field == SPH_FIELD_VERTEX_DATA && s->numScenes > 1)  // restore the scene index lanes
+                for (int k = 0; k < s->numScenes; k++)
+                    launch_set_scene(s->pos + s->sceneStart[k], (int)(s->sceneStart[k + 1] - s->sceneStart[k]), k, q);
             break;
         case SPH_FIELD_SIMULATION_DATA:
             if (bytes < sizeof(float) * 10 * (size_t)n) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "source too small");
@@ -783,7 +814,7 @@ sph_status sph_read_cells(sph_handle s, int level, int* sortedHash, int* sortedI
         return SPH_OK;
     }
     const int n = s->n;
-    const int C = s->P.gridDim[0] * s->P.gridDim[1] * s->P.gridDim[2];
+    const int C = (int)s->numCellsTotal;
     cudaStream_t q = s->stream;
     if (sortedHash)
         SPH_CUDA(cudaMemcpyAsync(sortedHash, s->sb.sortedHash, sizeof(int) * n, cudaMemcpyDeviceToHost, q));
@@ -820,7 +851,7 @@ sph_status sph_get_counts(sph_handle s, sph_counts* out) {
     out->numParticlesDefault = (unsigned int)c[2];
     out->numSubParticles = (unsigned int)c[3];
     out->numTimeSteps = s->numTimeSteps;
-    out->numCells = (unsigned int)(s->P.gridDim[0] * s->P.gridDim[1] * s->P.gridDim[2]);
+    out->numCells = (unsigned int)s->numCellsTotal;
     out->numSubCells = (unsigned int)(s->P.gridDimSubParticles[0] * s->P.gridDimSubParticles[1] *
                                       s->P.gridDimSubParticles[2]);
     return SPH_OK;
@@ -828,6 +859,7 @@ sph_status sph_get_counts(sph_handle s, sph_counts* out) {
 
 sph_status sph_get_diagnostics(sph_handle s, sph_diagnostics* out) {
     if (!s || !out) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (s->numScenes > 1) SPH_FAIL(SPH_ERR_NOT_SUPPORTED, "diagnostics are per scene: not for batched handles");
     const int rows = diag_partial_rows();
     if (!s->diagBuf) SPH_CUDA(dalloc(&s->diagBuf, (size_t)(rows + 1) * DIAG_TERMS));
     double* res = s->diagBuf + (size_t)rows * DIAG_TERMS;
@@ -903,7 +935,7 @@ sph_status sph_autotune(sph_handle s, int reps, sph_tuning* chosen) {
     if (!s) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "handle is NULL");
     reps = std::max(reps, 1);
     const int n = s->n;
-    const int C = s->P.gridDim[0] * s->P.gridDim[1] * s->P.gridDim[2];
+    const int C = (int)s->numCellsTotal;
     cudaStream_t st = s->stream;
     SPH_CUDA(cudaStreamSynchronize(st));
     // keep the last step's sorted data (read-back) and write forces to scratch
@@ -940,7 +972,7 @@ sph_status sph_autotune(sph_handle s, int reps, sph_tuning* chosen) {
     TUNE_CUDA(cudaMalloc((void**)&scratch, sizeof(float4) * 3 * (size_t)n));
     TUNE_CUDA(cudaEventCreate(&e0));
     TUNE_CUDA(cudaEventCreate(&e1));
-    GridDev g = make_grid(s->P, false);
+    GridDev g = grid_of(s);
     PhysDev ph = make_phys(s->P, s->O);
     auto sortStages = [&]() {
         launch_hash_count(n, s->pos, g, s->sb, s->status, st);

@@ -103,6 +103,7 @@ void free_graphs(Corrector* C) {
 }
 
 sph_status ensure_corrector(sph_sim* s) {
+    if (s->numScenes > 1) SPH_FAIL(SPH_ERR_NOT_SUPPORTED, "batched handles take plain steps only");
     if (s->corr) return SPH_OK;
     Corrector* C = new Corrector();
     s->corr = C;
@@ -156,7 +157,7 @@ void upload_norm(sph_sim* s, Corrector* C) {
 // The learned step: a plain step of stride*dt, then features and correction.
 void enqueue_learned(sph_sim* s, Corrector* C) {
     const int K = C->cfg.stride;
-    GridDev g = make_grid(s->P, false);
+    GridDev g = grid_of(s);
     PhysDev ph = learned_phys(s, K);
     const FeatureOut fo{C->feat, 1, s->O.boxCollision, ph.dt};
     enqueue_coarse(s, g, ph, s->O.boxCollision, nullptr, &fo);
@@ -337,7 +338,7 @@ sph_status sph_corrector_train(sph_handle s, const sph_corrector_config* cfg) {
     TRAIN_ST(sph_set_stream(sh, q));
     sh->cfg = s->cfg;
     TRAIN_CUDA(cudaEventRecord(e0, q));
-    const GridDev g = make_grid(s->P, false);
+    const GridDev g = grid_of(s);
     const PhysDev ph4 = learned_phys(s, K);
     const size_t bytes = sizeof(float4) * (size_t)n;
     for (int i = 0; i <= cfg->trainSteps; i++) {

@@ -25,7 +25,7 @@ __device__ __forceinline__ int particle_hash(float4 p, const GridDev& g, bool* o
         *outside = true;
         h = min(max(h, 0), g.numCells - 1);
     }
-    return h;
+    return g.cellBase + h;
 }
 
 // compute_grid_coordinate (particle_simulation.cu:1238-1258): the (unsigned)
@@ -164,7 +164,7 @@ __device__ __forceinline__ void row_range(float4 xi, const Stencil& st, float h,
     s = e = 0;
     const int z = st.z0 + r / 3, y = st.y0 + r % 3;
     if (z > st.z1 || y > st.y1) return;
-    const int row = g.dim[0] * (g.dim[1] * z + y);
+    const int row = g.cellBase + g.dim[0] * (g.dim[1] * z + y);
     if (!window) {
         s = __ldg(T.cellOffset + row + st.x0);
         e = __ldg(T.cellOffset + row + st.x1 + 1);

@@ -22,6 +22,7 @@ struct GridDev {
     float spacing;
     int dim[3];
     int numCells;
+    int cellBase;  // first global cell index of this grid (batched scenes; else 0)
 };
 
 // Trilinear boundary maps: map4 = (signed distance, wall density, wall
@@ -56,6 +57,15 @@ struct PhysDev {
     float boxCen[3], boxDim[3], restitution;
 };
 
+// One scene of a batched handle: its own cell grid (at cellBase in the
+// concatenated cell space), physical constants, walls and boundary maps.  A
+// particle's scene index travels in the .w lane of its position.
+struct SceneDev {
+    GridDev g;
+    PhysDev ph;
+    MapDev map;
+};
+
 // Scratch of the counting sort + cell scan.
 struct SortBuffers {
     int* cnt;                 // [C+1] per-cell counters (kept zero between steps)
@@ -71,6 +81,7 @@ struct SortBuffers {
     unsigned long long* scanFlags;  // decoupled look-back tile states
     unsigned int* tileCounter;
     int maxTiles;
+    const SceneDev* scenes;   // batched handles: per-scene grids (else NULL)
 };
 
 // Two-scale state (AdvanceTwoScale): particle states, the three-way lists,
@@ -102,6 +113,7 @@ struct TwoScaleDev {
 struct RowTables {
     const int* cellOffset;  // [C+1]
     const int* halfOffset;  // [C+1], valid for occupied cells
+    const SceneDev* scenes; // batched handles: per-scene grids, constants, maps (else NULL)
 };
 
 // Launch configuration of the step (chosen per handle; see the autotuner).
@@ -123,6 +135,8 @@ constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
 // Launch wrappers (sph_kernels.cu)
 // ---------------------------------------------------------------------------
 void launch_unpack_aos(const float* aos, int stride, int offset, int n, float4* out, cudaStream_t s);
+// pos[i].w = scene index `sid` (as integer bits) for i < count.
+void launch_set_scene(float4* pos, int count, int sid, cudaStream_t s);
 void launch_pack_aos(const float4* in, int n, float* aos, int stride, int offset, cudaStream_t s);
 void launch_hash_count(int n, const float4* pos, GridDev g, SortBuffers sb, unsigned int* status,
                        cudaStream_t s);

@@ -186,7 +186,7 @@ __global__ void __launch_bounds__(TILE, 1)
                 float3 x = make_float3(p.x + c[0], p.y + c[1], p.z + c[2]);
                 float3 v = make_float3(w.x + c[3], w.y + c[4], w.z + c[5]);
                 if (collideFlag) collide(ph, x, v);
-                pos[id] = make_float4(x.x, x.y, x.z, 0.f);
+                pos[id] = make_float4(x.x, x.y, x.z, p.w);
                 vel[id] = make_float4(v.x, v.y, v.z, 0.f);
             } else {
 #pragma unroll

@@ -203,6 +203,7 @@ extern "C" sph_status sph_cell_tables_noalloc(const SimulationParameters* params
     }
     g.spacing = params->gridSpacing;
     g.numCells = g.dim[0] * g.dim[1] * g.dim[2];
+    g.cellBase = 0;
     const NaView v = na_view(base);
     const int total = g.numCells + 1;
     const int nn = (int)n;

@@ -86,6 +86,14 @@ struct sph_sim {
     sph_boundary_desc desc{};
     bool hasDesc = false;
 
+    // cells owned by the handle: the grid's, or the sum over batched scenes
+    long long numCellsTotal = 0;
+    // batched scenes (sph_create_batch): count, first particle and first cell
+    // of each scene (numScenes + 1 entries) and the device scene table
+    int numScenes = 1;
+    std::vector<unsigned int> sceneStart, sceneCell;
+    sph::SceneDev* scenesDev = nullptr;
+
     // learned step corrector (sph_corrector.cu; allocated on first use)
     sph::Corrector* corr = nullptr;
 
@@ -126,5 +134,13 @@ sph_status corrector_step(sph_sim* s, int count, bool useGraph);
 void corrector_free(sph_sim* s);
 // Waits for the handle's stream and maps the latched device status.
 sph_status latched_status(sph_sim* s);
+// Allocates the device state of n particles over C cells (zeroed counters,
+// velocities and per-step outputs) and the handle's stream.
+sph_status alloc_handle(sph_sim* s, int n, long long C);
+// Texture metadata of boundary maps built from `d` on a dims^3 grid.
+MapDev map_of(const sph_boundary_desc& d, const unsigned int dims[3], const float4* map4, const float* dist);
+// The coarse grid of the handle with numCells = all cells it owns (the sum
+// over the scenes of a batched handle).
+GridDev grid_of(const sph_sim* s);
 
 }  // namespace sph

@@ -20,6 +20,15 @@ namespace sph {
 // ---------------------------------------------------------------------------
 // AoS <-> float4 conversion (VD/SD layouts of particle_simulation.h:17-41)
 // ---------------------------------------------------------------------------
+__global__ void k_set_scene(float4* __restrict__ pos, int count, int sid) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < count) pos[i].w = __int_as_float(sid);
+}
+
+void launch_set_scene(float4* pos, int count, int sid, cudaStream_t s) {
+    if (count > 0) k_set_scene<<<(count + 255) / 256, 256, 0, s>>>(pos, count, sid);
+}
+
 __global__ void k_unpack_aos(const float* __restrict__ aos, int stride, int offset, int n,
                              float4* __restrict__ out) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -52,11 +61,15 @@ void launch_pack_aos(const float4* in, int n, float* aos, int stride, int offset
 // ---------------------------------------------------------------------------
 // Stage 1: hash + per-cell arrival slot
 // ---------------------------------------------------------------------------
-__global__ void k_hash_count(int n, const float4* __restrict__ pos, GridDev g, int* __restrict__ cnt,
-                             int2* __restrict__ keySlot, unsigned int* status) {
+// With BATCH the particle's scene (pos.w) supplies its grid, whose cells
+// start at that scene's cellBase in the concatenated cell space.
+template <bool BATCH>
+__global__ void k_hash_count(int n, const float4* __restrict__ pos, GridDev g_, const SceneDev* __restrict__ scenes,
+                             int* __restrict__ cnt, int2* __restrict__ keySlot, unsigned int* status) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float4 p = pos[i];
+    const GridDev& g = BATCH ? scenes[__float_as_int(p.w)].g : g_;
     bool outside = false;
     if (!(isfinite(p.x) && isfinite(p.y) && isfinite(p.z))) {
         atomicOr(status, STATUS_NON_FINITE);
@@ -71,7 +84,10 @@ __global__ void k_hash_count(int n, const float4* __restrict__ pos, GridDev g, i
 void launch_hash_count(int n, const float4* pos, GridDev g, SortBuffers sb, unsigned int* status,
                        cudaStream_t s) {
     if (n <= 0) return;
-    k_hash_count<<<(n + 255) / 256, 256, 0, s>>>(n, pos, g, sb.cnt, sb.keySlot, status);
+    if (sb.scenes)
+        k_hash_count<true><<<(n + 255) / 256, 256, 0, s>>>(n, pos, g, sb.scenes, sb.cnt, sb.keySlot, status);
+    else
+        k_hash_count<false><<<(n + 255) / 256, 256, 0, s>>>(n, pos, g, nullptr, sb.cnt, sb.keySlot, status);
 }
 
 // ---------------------------------------------------------------------------
@@ -249,10 +265,11 @@ __device__ __forceinline__ unsigned int ordered_bits(float x) {
 // The same pass records, per cell, where its upper x-half starts in the
 // working order (halfOffset[c] = first index with x >= the cell's mid-plane),
 // so a neighbour search can cut a row at half-cell granularity from a table.
+template <bool BATCH>
 __global__ void k_rank_gather(int n, const int* __restrict__ sortedHash, const int* __restrict__ cellOffset,
                               const int* __restrict__ tmpIds, const float4* __restrict__ pos,
-                              const float4* __restrict__ vel, GridDev g, int* __restrict__ sortedIds,
-                              int* __restrict__ workIds, int* __restrict__ halfOffset,
+                              const float4* __restrict__ vel, GridDev g_, const SceneDev* __restrict__ scenes,
+                              int* __restrict__ sortedIds, int* __restrict__ workIds, int* __restrict__ halfOffset,
                               float4* __restrict__ posS, float4* __restrict__ velS, float* __restrict__ xS) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
@@ -260,8 +277,9 @@ __global__ void k_rank_gather(int n, const int* __restrict__ sortedHash, const i
     int s = __ldg(cellOffset + c), e = __ldg(cellOffset + c + 1);
     int my = tmpIds[k];
     float4 p = __ldg(pos + my);
+    const GridDev& g = BATCH ? scenes[__float_as_int(p.w)].g : g_;
     unsigned int key = ordered_bits(p.x);
-    const float mid = g.origin[0] + ((float)(c % g.dim[0]) + 0.5f) * g.spacing;
+    const float mid = g.origin[0] + ((float)((c - g.cellBase) % g.dim[0]) + 0.5f) * g.spacing;
     int rId = 0, rX = 0, below = 0;
     for (int t = s; t < e; t++) {
         int o = __ldg(tmpIds + t);
@@ -282,8 +300,14 @@ __global__ void k_rank_gather(int n, const int* __restrict__ sortedHash, const i
 void launch_rank_gather(int n, SortBuffers sb, const float4* pos, const float4* vel, GridDev g, float4* posS,
                         float4* velS, cudaStream_t s) {
     if (n <= 0) return;
-    k_rank_gather<<<(n + 255) / 256, 256, 0, s>>>(n, sb.sortedHash, sb.cellOffset, sb.tmpIds, pos, vel, g,
-                                                  sb.sortedIds, sb.workIds, sb.halfOffset, posS, velS, sb.xS);
+    if (sb.scenes)
+        k_rank_gather<true><<<(n + 255) / 256, 256, 0, s>>>(n, sb.sortedHash, sb.cellOffset, sb.tmpIds, pos, vel, g,
+                                                            sb.scenes, sb.sortedIds, sb.workIds, sb.halfOffset, posS,
+                                                            velS, sb.xS);
+    else
+        k_rank_gather<false><<<(n + 255) / 256, 256, 0, s>>>(n, sb.sortedHash, sb.cellOffset, sb.tmpIds, pos, vel,
+                                                             g, nullptr, sb.sortedIds, sb.workIds, sb.halfOffset,
+                                                             posS, velS, sb.xS);
 }
 
 // ---------------------------------------------------------------------------

@@ -33,13 +33,18 @@ struct RowMasks {
     unsigned int* mask;  // [9][n] neighbour bits relative to start, or the window end
 };
 
-template <bool KAHAN, bool EMIT>
+template <bool KAHAN, bool EMIT, bool BATCH>
 __global__ void __launch_bounds__(256)
-k_density(int n, const float4* __restrict__ posS, RowTables T, GridDev g, PhysDev ph, MapDev map, int window,
+k_density(int n, const float4* __restrict__ posS, RowTables T, GridDev g_, PhysDev ph_, MapDev map_, int window,
           float4* __restrict__ rho4S, RowMasks M) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float4 xi = posS[i];
+    // batched handles: the particle's own scene supplies grid, constants and maps
+    const SceneDev* S = BATCH ? T.scenes + __float_as_int(xi.w) : nullptr;
+    const GridDev& g = BATCH ? S->g : g_;
+    const PhysDev& ph = BATCH ? S->ph : ph_;
+    const MapDev& map = BATCH ? S->map : map_;
     const Stencil st = stencil(xi, ph.h, g);
     const float h2 = ph.h2;
     float sum = 0.f, comp = 0.f;
@@ -302,7 +307,7 @@ __device__ __forceinline__ void force_epilogue(const ForceTotals<KAHAN, TENSION>
     float3 x = make_float3(xi.x + ph.dt * v.x, xi.y + ph.dt * v.y, xi.z + ph.dt * v.z);
     if (collideFlag) collide(ph, x, v);
     const int id = workIds[i];
-    pos[id] = make_float4(x.x, x.y, x.z, 0.f);
+    pos[id] = make_float4(x.x, x.y, x.z, xi.w);  // .w: the scene index of batched handles
     vel[id] = make_float4(v.x, v.y, v.z, 0.f);
     accS[i] = make_float4(acc[0], acc[1], acc[2], 0.f);
     if (FEAT) write_features(fs, fo, i, id, xi, vi, ri, acc, mapDist, mapN, ph);
@@ -327,16 +332,20 @@ struct ForceArgs {
     FeatOut fo;
 };
 
-template <bool KAHAN, bool TENSION, int FORM, bool FEAT>
+template <bool KAHAN, bool TENSION, int FORM, bool FEAT, bool BATCH>
 __global__ void __launch_bounds__(256, 2) k_force(ForceArgs F) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= F.n) return;
     const float4 xi = F.posS[i];
     const float4 vi = F.velS[i];
     const float4 ri = F.rho4S[i];
-    const float h2 = F.ph.h2;
+    const SceneDev* S = BATCH ? F.T.scenes + __float_as_int(xi.w) : nullptr;
+    const GridDev& g = BATCH ? S->g : F.g;
+    const PhysDev& ph = BATCH ? S->ph : F.ph;
+    const MapDev& map = BATCH ? S->map : F.map;
+    const float h2 = ph.h2;
     Stencil st;
-    if (FORM != FORCE_PRETESTED) st = stencil(xi, F.ph.h, F.g);
+    if (FORM != FORCE_PRETESTED) st = stencil(xi, ph.h, g);
     ForceTotals<KAHAN, TENSION> A;
     FeatSums fs;
     auto direct = [&](RowSums<TENSION>& R, int s, int e) {
@@ -345,8 +354,8 @@ __global__ void __launch_bounds__(256, 2) k_force(ForceArgs F) {
             const float r2 = dist2(xi, xj);
             if (r2 <= h2 && r2 > 0.f) {
                 const float4 vj = __ldg(F.velS + t), rj = __ldg(F.rho4S + t);
-                R.add(F.ph, xi, vi, ri.z, xj, vj, rj);
-                if (FEAT) fs.add(F.ph, xi, vi, xj, vj, rj);
+                R.add(ph, xi, vi, ri.z, xj, vj, rj);
+                if (FEAT) fs.add(ph, xi, vi, xj, vj, rj);
             }
         }
     };
@@ -355,8 +364,8 @@ __global__ void __launch_bounds__(256, 2) k_force(ForceArgs F) {
             const int t = base + __ffs(m) - 1;
             m &= m - 1u;
             const float4 xj = __ldg(F.posS + t), vj = __ldg(F.velS + t), rj = __ldg(F.rho4S + t);
-            R.add(F.ph, xi, vi, ri.z, xj, vj, rj);
-            if (FEAT) fs.add(F.ph, xi, vi, xj, vj, rj);
+            R.add(ph, xi, vi, ri.z, xj, vj, rj);
+            if (FEAT) fs.add(ph, xi, vi, xj, vj, rj);
         }
     };
 #pragma unroll
@@ -370,7 +379,7 @@ __global__ void __launch_bounds__(256, 2) k_force(ForceArgs F) {
             else bits(R, sv, m);
         } else {
             int s, e;
-            row_range(xi, st, F.ph.h, F.g, F.T, F.window != 0, r, s, e);
+            row_range(xi, st, ph.h, g, F.T, F.window != 0, r, s, e);
             if (FORM == FORCE_DIRECT) {
                 direct(R, s, e);
             } else {
@@ -387,7 +396,7 @@ __global__ void __launch_bounds__(256, 2) k_force(ForceArgs F) {
         }
         A.add(R);
     }
-    force_epilogue<KAHAN, TENSION, FEAT>(A, i, xi, vi, ri, F.ph, F.map, F.collide, F.workIds, F.pos, F.vel,
+    force_epilogue<KAHAN, TENSION, FEAT>(A, i, xi, vi, ri, ph, map, F.collide, F.workIds, F.pos, F.vel,
                                          F.accS, fs, F.fo);
 }
 
@@ -401,29 +410,49 @@ void launch_density(int n, const float4* posS, RowTables T, GridDev g, PhysDev p
     const int grid = (n + bs - 1) / bs;
     const RowMasks M{rowStart, rowMask};
     const bool emit = cfg.forceVariant == FORCE_PRETESTED;
-    if (cfg.kahan) {
-        if (emit) k_density<true, true><<<grid, bs, 0, s>>>(n, posS, T, g, ph, map, cfg.prune, rho4S, M);
-        else k_density<true, false><<<grid, bs, 0, s>>>(n, posS, T, g, ph, map, cfg.prune, rho4S, M);
+#define SPH_DENSITY(K, E, B) k_density<K, E, B><<<grid, bs, 0, s>>>(n, posS, T, g, ph, map, cfg.prune, rho4S, M)
+    if (T.scenes) {
+        if (cfg.kahan) {
+            if (emit) SPH_DENSITY(true, true, true);
+            else SPH_DENSITY(true, false, true);
+        } else {
+            if (emit) SPH_DENSITY(false, true, true);
+            else SPH_DENSITY(false, false, true);
+        }
     } else {
-        if (emit) k_density<false, true><<<grid, bs, 0, s>>>(n, posS, T, g, ph, map, cfg.prune, rho4S, M);
-        else k_density<false, false><<<grid, bs, 0, s>>>(n, posS, T, g, ph, map, cfg.prune, rho4S, M);
+        if (cfg.kahan) {
+            if (emit) SPH_DENSITY(true, true, false);
+            else SPH_DENSITY(true, false, false);
+        } else {
+            if (emit) SPH_DENSITY(false, true, false);
+            else SPH_DENSITY(false, false, false);
+        }
     }
+#undef SPH_DENSITY
 }
 
 template <bool KAHAN, bool TENSION>
 static void force_dispatch(const ForceArgs& F, const StepConfig& cfg, cudaStream_t s) {
     const int bs = cfg.forceBlock > 0 ? cfg.forceBlock : 128;
     const int grid = (F.n + bs - 1) / bs;
-    if (F.fo.feat) {
+    if (F.T.scenes) {
+        // batched scenes (plain steps only; no feature recording)
+        if (cfg.forceVariant == FORCE_PRETESTED)
+            k_force<KAHAN, TENSION, FORCE_PRETESTED, false, true><<<grid, bs, 0, s>>>(F);
+        else if (cfg.forceVariant == FORCE_MASK)
+            k_force<KAHAN, TENSION, FORCE_MASK, false, true><<<grid, bs, 0, s>>>(F);
+        else
+            k_force<KAHAN, TENSION, FORCE_DIRECT, false, true><<<grid, bs, 0, s>>>(F);
+    } else if (F.fo.feat) {
         // the learned step's force stage records the corrector's features; the
         // density stage has recorded the neighbour masks (pretested form)
-        k_force<KAHAN, TENSION, FORCE_PRETESTED, true><<<grid, bs, 0, s>>>(F);
+        k_force<KAHAN, TENSION, FORCE_PRETESTED, true, false><<<grid, bs, 0, s>>>(F);
     } else if (cfg.forceVariant == FORCE_PRETESTED) {
-        k_force<KAHAN, TENSION, FORCE_PRETESTED, false><<<grid, bs, 0, s>>>(F);
+        k_force<KAHAN, TENSION, FORCE_PRETESTED, false, false><<<grid, bs, 0, s>>>(F);
     } else if (cfg.forceVariant == FORCE_MASK) {
-        k_force<KAHAN, TENSION, FORCE_MASK, false><<<grid, bs, 0, s>>>(F);
+        k_force<KAHAN, TENSION, FORCE_MASK, false, false><<<grid, bs, 0, s>>>(F);
     } else {
-        k_force<KAHAN, TENSION, FORCE_DIRECT, false><<<grid, bs, 0, s>>>(F);
+        k_force<KAHAN, TENSION, FORCE_DIRECT, false, false><<<grid, bs, 0, s>>>(F);
     }
 }
 

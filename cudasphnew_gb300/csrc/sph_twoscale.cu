@@ -259,7 +259,7 @@ __global__ void k_ts_merge(int n, float4* __restrict__ posS, float4* __restrict_
     float3 v = make_float3(vm.x + ph.dt * a.x, vm.y + ph.dt * a.y, vm.z + ph.dt * a.z);
     float3 x = make_float3(xm.x + ph.dt * v.x, xm.y + ph.dt * v.y, xm.z + ph.dt * v.z);
     if (collideFlag) collide(ph, x, v);
-    pos[id] = make_float4(x.x, x.y, x.z, 0.f);
+    pos[id] = make_float4(x.x, x.y, x.z, x0.w);
     vel[id] = make_float4(v.x, v.y, v.z, 0.f);
 }
 

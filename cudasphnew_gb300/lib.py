@@ -33,6 +33,8 @@ _i = ctypes.c_int
 SIGNATURES = {
     "sph_default_options": (None, [_vp]),
     "sph_create": (_i, [_vp, _vp, _vp, _vp, _vp, _vp]),
+    "sph_create_batch": (_i, [_vp, _i, _vp, _vp]),
+    "sph_batch_info": (_i, [_vp, _vp, _vp, _vp]),
     "sph_destroy": (_i, [_vp]),
     "sph_bind": (_i, [_vp, _vp]),
     "sph_set_stream": (_i, [_vp, _vp]),
@@ -161,6 +163,12 @@ def boundary_maps(desc: BoundaryDesc):
     return tuple(out)
 
 
+class Scene(ctypes.Structure):
+    """sph_scene: one scene of a batched handle."""
+
+    _fields_ = [("params", _vp), ("vertexData", _vp), ("simulationData", _vp), ("boundary", _vp)]
+
+
 class ParticleSimulation:
     """Headless ``ParticleSimulation``: Init + Bind happen in the constructor
     (sph_create); the OpenGL buffer getters are replaced by device pointers
@@ -186,6 +194,45 @@ class ParticleSimulation:
                            None if sd is None else _p(sd),
                            None if boundary is None else ctypes.byref(boundary), ctypes.byref(h)))
         self._h = h
+
+    @classmethod
+    def batch(cls, scenes, options: Options | None = None) -> "ParticleSimulation":
+        """A batched handle over `scenes` (objects with params, positions,
+        velocities, boundary): sph_create_batch.  Fields read back scene after
+        scene; `scene_ranges()` gives each scene's particle range."""
+        L = load()
+        self = cls.__new__(cls)
+        keep = []
+        arr = (Scene * len(scenes))()
+        for k, sc in enumerate(scenes):
+            n = int(sc.params.numParticles)
+            vd = np.ascontiguousarray(sc.positions, np.float32).reshape(n, 3)
+            sd = np.zeros((n, 10), np.float32)
+            sd[:, 6:9] = np.asarray(sc.velocities, np.float32).reshape(n, 3)
+            keep += [vd, sd]
+            arr[k].params = ctypes.addressof(sc.params)
+            arr[k].vertexData = vd.ctypes.data
+            arr[k].simulationData = sd.ctypes.data
+            arr[k].boundary = ctypes.addressof(sc.boundary) if sc.boundary is not None else None
+        self.options = options if options is not None else Options()
+        if options is None:
+            L.sph_default_options(ctypes.byref(self.options))
+        self._params = scenes[0].params
+        self.n = sum(int(sc.params.numParticles) for sc in scenes)
+        h = ctypes.c_void_p()
+        check(L.sph_create_batch(arr, len(scenes), ctypes.byref(self.options), ctypes.byref(h)))
+        self._h = h
+        return self
+
+    def scene_ranges(self):
+        """(first particle, first cell) arrays of numScenes + 1 entries."""
+        L = load()
+        k = ctypes.c_int()
+        check(L.sph_batch_info(self._h, ctypes.byref(k), None, None))
+        fp = np.zeros(k.value + 1, np.uint32)
+        fc = np.zeros(k.value + 1, np.uint32)
+        check(L.sph_batch_info(self._h, None, fp.ctypes.data, fc.ctypes.data))
+        return fp, fc
 
     # -- lifetime ----------------------------------------------------------
     def close(self) -> None:

@@ -287,3 +287,18 @@ def obstacle_boundary(p: SimulationParameters, grid_start, n_nodes: int, shapes)
         for a, v in enumerate(vals):
             d.shapes[i].p[a] = v
     return d
+
+
+def sphere_boundary(p: SimulationParameters, centre, radius: float, n_nodes: int = 64) -> BoundaryDesc:
+    """Boundary maps of a solid sphere on an ``n_nodes``^3 grid centred on it,
+    reaching 2h beyond its surface (pitch max(h/4, 2(r + 2h)/(n_nodes - 1)))."""
+    h = float(np.float32(p.compactSupport))
+    half = radius + 2.0 * h
+    pitch = max(h / 4.0, 2.0 * half / (n_nodes - 1))
+    sp = np.float32(pitch)
+    d = obstacle_boundary(p, [c - half for c in centre], n_nodes, [(SHAPE_SPHERE, (*centre, radius))])
+    for a in range(3):
+        d.gridEnd[a] = _f32(np.float32(d.gridStart[a]) + sp * np.float32(n_nodes - 1 + 0.5))
+    d.gridSpacing = float(sp)
+    return d
+

@@ -133,3 +133,41 @@ def two_scale(nb=64, region=(0.4, 0.6), box=1.0, seed=3, name="two_scale_262k") 
 
 def config3() -> Scene:
     return two_scale()
+
+
+def batched_scene(n: int, frac: float, seed: int, name: str) -> Scene:
+    """One scene of the batched workload: a cube lattice block of n particles
+    (pitch h/2, x fastest, jittered like the other scenes) in the corner of a
+    box of side 2.5x the block side, and a solid sphere of radius frac x box
+    side at the box centre on a 64^3 boundary map.  Lattice nodes inside the
+    sphere (+ h/2) are dropped and the lattice grows until it holds n."""
+    m = int(math.ceil(n ** (1.0 / 3.0) - 1e-9))
+    while True:
+        side = 2.5 * m * P.SPACING
+        r = frac * side
+        c = (0.5 * side, 0.5 * side, 0.5 * side)
+        pos = lattice_block(m, m, m, (0.0, 0.0, 0.0), P.SPACING, seed, 0.01 * P.H)
+        keep = np.linalg.norm(pos.astype(np.float64) - np.asarray(c), axis=1) > r + 0.5 * P.H
+        if keep.sum() >= n:
+            pos = pos[keep][:n]
+            break
+        m += 1
+    p = P.dam_break_params((0.0, 0.0, 0.0), (side, side, side), n)
+    o = P.default_options(gravity_axis=2, box_collision=True)
+    return Scene(name, p, o, pos, np.zeros_like(pos), P.sphere_boundary(p, c, r), 200)
+
+
+def batch_sizes(count: int = 64, seed: int = 4, lo: int = 4096, hi: int = 262144):
+    """Particle counts log-uniform in [lo, hi] and sphere radii (as fractions
+    of the box side) uniform in [0.05, 0.2], from SplitMix64."""
+    u = uniform(seed, np.arange(2 * count, dtype=np.uint64)).reshape(count, 2)
+    ns = np.rint(np.exp(np.log(lo) + u[:, 0] * (np.log(hi) - np.log(lo)))).astype(np.int64)
+    return [int(v) for v in ns], [float(0.05 + 0.15 * v) for v in u[:, 1]]
+
+
+def config4(count: int = 64, seed: int = 4):
+    """The batched workload: `count` independent dam breaks (about 4M
+    particles for 64 scenes), each with its own seeded sphere obstacle."""
+    ns, fr = batch_sizes(count, seed)
+    return [batched_scene(n, f, seed * 1000 + k, f"batch_{k}") for k, (n, f) in enumerate(zip(ns, fr))]
+

@@ -186,6 +186,29 @@ sph_status sph_create(const SimulationParameters* params, const sph_options* opt
                       const float* vertexData, const float* simulationData,
                       const sph_boundary_desc* boundary, sph_handle* out);
 
+/* Batched scenes (no reference counterpart): many independent simulations
+ * in one handle, each with its own parameters, particles and (optional)
+ * boundary maps.  Every stage of a plain step is one launch over all scenes;
+ * the particles of all scenes share one sort over the concatenation of the
+ * scenes' cell grids, each scene's cells at its own offset, so a scene's
+ * results are bit-identical to running it alone.  Per-particle fields are
+ * read and written scene after scene (sph_batch_info gives the ranges).
+ * Batched handles take SPH_STEP_PLAIN steps only; sph_bind, the two-scale
+ * and learned modes and sph_get_diagnostics answer SPH_ERR_NOT_SUPPORTED.
+ * All scenes use the same sph_options (gravity axis, box collision). */
+typedef struct sph_scene {
+    const SimulationParameters* params; /* numParticles = this scene's count */
+    const float* vertexData;            /* float[n*3] */
+    const float* simulationData;        /* float[n*10] or NULL */
+    const sph_boundary_desc* boundary;  /* or NULL */
+} sph_scene;
+sph_status sph_create_batch(const sph_scene* scenes, int numScenes, const sph_options* opts,
+                            sph_handle* out);
+/* Scene k owns particles [firstParticle[k], firstParticle[k+1]) and cells
+ * [firstCell[k], firstCell[k+1]) of the handle; either array may be NULL
+ * (else numScenes + 1 entries). */
+sph_status sph_batch_info(sph_handle h, int* numScenes, unsigned int* firstParticle, unsigned int* firstCell);
+
 /* ~ParticleSimulation (:1691-1743). */
 sph_status sph_destroy(sph_handle h);
 
