@@ -48,6 +48,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="config2")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true",
+                    help="skip the 64-scene batched leg")
     ap.add_argument("--no-learned", action="store_true",
                     help="skip the learned-corrector legs (16,384-particle scene and the 1M scene)")
     ap.add_argument("--no-autotune", action="store_true",
@@ -393,6 +395,51 @@ def learned_leg_1m(lib, torch, stream, model, cfg, sc, steps):
             "audits": after.audits - before.audits, "rollbacks": after.rollbacks - before.rollbacks}
 
 
+def batched_leg(lib, torch, stream, steps=200):
+    """The 64-scene batched workload (about 4.4M particles, seeded sizes and
+    sphere obstacles): one handle, one launch per stage, one CUDA graph per
+    step, autotuned; beside it the same scenes as 64 separate handles stepped
+    one after another (each with its own graph)."""
+    from cudasphnew_gb300 import scenes
+    scs = scenes.config4()
+    n = sum(sc.n for sc in scs)
+    with lib.ParticleSimulation.batch(scs, scs[0].options) as sim:
+        sim.set_stream(stream.cuda_stream)
+        sim.step(count=3)
+        tuning = sim.autotune(reps=3).as_dict()
+        sim.step(count=3)
+        ms = time_steps(torch, stream, sim, lib.SPH_STEP_PLAIN, steps)
+        cells = int(sim.scene_ranges()[1][-1])
+    # the same scenes without batching, a bounded number of steps each
+    k = max(steps // 10, 5)
+    sims = [lib.ParticleSimulation(sc.params, sc.positions, sc.velocities, sc.options, sc.boundary) for sc in scs]
+    try:
+        for x in sims:
+            x.set_stream(stream.cuda_stream)
+            x.step(count=3)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
+            e0.record()
+            for _ in range(k):
+                for x in sims:
+                    x.step(count=1)
+            e1.record()
+        torch.cuda.synchronize()
+        ms_sep = e0.elapsed_time(e1)
+    finally:
+        for x in sims:
+            x.close()
+    return {"workload": f"{len(scs)} dam breaks, {n} particles (log-uniform 4,096..262,144 per scene), "
+                        f"{cells} cells, one 64^3 sphere map each",
+            "unit": UNIT, "steps": steps, "value": n * steps / (ms / 1e3), "ms_per_step": ms / steps,
+            "launches_per_step": 6, "graph": "one CUDA graph launch per step", "tuning": tuning,
+            "separate_handles": {"value": n * k / (ms_sep / 1e3), "ms_per_step": ms_sep / k, "steps": k,
+                                 "launches_per_step": 6 * len(scs)},
+            "l2": "no flush: working set of the 4.4M-particle batch far exceeds L2"}
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -486,6 +533,9 @@ def run_ours(args):
     e2e_value = world * n * e2e_steps / el
     sim.close()
 
+    batched = None
+    if rank == 0 and not args.no_batched:
+        batched = batched_leg(lib, torch, stream)
     learned = learned_1m = None
     if rank == 0 and not args.no_learned:
         learned, lcfg, model = learned_leg(lib, torch, stream)
@@ -514,6 +564,8 @@ def run_ours(args):
                         "algorithmic_bytes_per_launch": alg,
                         "avg_launch_us": force_avg_s * 1e6},
            "stages_us": {k: round(v[0] / v[1] * 1e3, 2) for k, v in stages.items()}}
+    if batched is not None:
+        out["batched"] = batched
     if learned is not None:
         out["learned"] = learned
         out["learned_1m"] = learned_1m
