@@ -981,9 +981,10 @@ sph_status sph_autotune(sph_handle s, int reps, sph_tuning* chosen) {
         launch_rank_gather(n, s->sb, s->pos, s->vel, g, s->posS, s->velS, st);
     };
     // each candidate is timed in step context: the sort stages run before
-    // every timed launch, so caches hold what they hold in a real step
+    // every timed launch, so caches hold what they hold in a real step; the
+    // fastest of the repeats counts (the least disturbed one)
     auto timeit = [&](auto&& before, auto&& launch) -> float {
-        float total = 0.f;
+        float fastest = 3.0e38f;
         for (int r = 0; r < reps + 1; r++) {
             before();
             cudaEventRecord(e0, st);
@@ -992,13 +993,32 @@ sph_status sph_autotune(sph_handle s, int reps, sph_tuning* chosen) {
             cudaEventSynchronize(e1);
             float ms = 0.f;
             cudaEventElapsedTime(&ms, e0, e1);
-            if (r > 0) total += ms;  // the first launch warms up
+            if (r > 0) fastest = std::min(fastest, ms);  // the first launch warms up
         }
-        return total / reps;
+        return fastest;
     };
     const int blocks[3] = {64, 128, 256};
-    StepConfig best = s->cfg;
-    float bestTotal = 3.0e38f;
+    // the configuration in use is kept unless a candidate beats it by 2 %
+    const StepConfig current = s->cfg;
+    auto stepTime = [&](const StepConfig& c) {
+        const float d = timeit(sortStages, [&] {
+            launch_density(n, s->posS, rows_of(s), g, ph, s->map, s->rho4S, s->rowStart, s->rowMask, c, st);
+        });
+        const float f = timeit(
+            [&] {
+                sortStages();
+                launch_density(n, s->posS, rows_of(s), g, ph, s->map, s->rho4S, s->rowStart, s->rowMask, c, st);
+            },
+            [&] {
+                launch_force(n, s->posS, s->velS, s->rho4S, s->sb.workIds, rows_of(s), g, ph, s->map,
+                             s->O.boxCollision, s->rowStart, s->rowMask, scratch, scratch + n,
+                             scratch + 2 * (size_t)n, c, st);
+            });
+        return d + f;
+    };
+    const float currentTotal = stepTime(current);
+    StepConfig best = current;
+    float bestTotal = currentTotal;
     for (int prune = 0; prune <= 1; prune++)
         for (int v = FORCE_DIRECT; v <= FORCE_PRETESTED; v++) {
             StepConfig c = s->cfg;
@@ -1034,6 +1054,7 @@ sph_status sph_autotune(sph_handle s, int reps, sph_tuning* chosen) {
                 }
             }
         }
+    if (bestTotal > 0.98f * currentTotal) best = current;
     TUNE_CUDA(cudaGetLastError());
     for (auto& b : bufs) TUNE_CUDA(cudaMemcpyAsync(b.dst, b.save, b.bytes, cudaMemcpyDeviceToDevice, st));
     TUNE_CUDA(cudaStreamSynchronize(st));

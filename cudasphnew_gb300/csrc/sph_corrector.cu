@@ -39,7 +39,7 @@ struct Corrector {
     unsigned char* image = nullptr;
     float* bias = nullptr;
     float* norm = nullptr;
-    float stats[2 * IN + 2 * OUT] = {};  // feature means, deviations, target means, deviations
+    float stats[NSTATS] = {};  // feature means, deviations; target means, deviations, scales
     // learned step and audit scratch
     float* feat = nullptr;  // n x 24, particle order: the last learned step's features
     float4 *savePos = nullptr, *saveVel = nullptr, *lPos = nullptr, *lVel = nullptr;
@@ -89,6 +89,7 @@ sph_status check_config(const sph_corrector_config* c) {
     if (c->stride < 1 || c->stride > 64) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "stride must be in [1, 64]");
     if (c->auditInterval < 0) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "auditInterval must be >= 0");
     if (!(c->densityTolerance >= 0.0f)) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "densityTolerance must be >= 0");
+    if (!(c->targetScale >= 0.0f)) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "targetScale must be >= 0");
     return SPH_OK;
 }
 
@@ -150,6 +151,7 @@ void upload_norm(sph_sim* s, Corrector* C) {
         h[N_MUT + o] = C->stats[2 * IN + o];
         const float sd = C->stats[2 * IN + OUT + o];
         h[N_SGT + o] = sd > 0.0f ? sd : 1.0f;
+        h[N_SCL + o] = C->stats[2 * IN + 2 * OUT + o];
     }
     cudaMemcpyAsync(C->norm, h, sizeof(h), cudaMemcpyHostToDevice, s->stream);
 }
@@ -268,6 +270,7 @@ void sph_corrector_default_config(sph_corrector_config* c) {
     c->densityTolerance = 0.01f;
     c->auditInterval = 16;
     c->seed = 1;
+    c->targetScale = 0.0f;
 }
 
 sph_status sph_corrector_train(sph_handle s, const sph_corrector_config* cfg) {
@@ -372,12 +375,25 @@ sph_status sph_corrector_train(sph_handle s, const sph_corrector_config* cfg) {
             C->stats[k] = (float)h[2 * k];
             C->stats[IN + k] = (float)h[2 * k + 1];
         }
+        // targets: with targetScale > 0 the network predicts asinh(t/s), s a
+        // fraction of each component's deviation (s = 0: t itself)
         launch_column_stats(rows, OUT, TGT, tgt, statP, statOut, q);
         TRAIN_CUDA(cudaMemcpyAsync(h, statOut, sizeof(double) * 2 * OUT, cudaMemcpyDeviceToHost, q));
         TRAIN_CUDA(cudaStreamSynchronize(q));
+        TargetScales sc{};
+        for (int o = 0; o < OUT; o++) sc.s[o] = (float)((double)cfg->targetScale * h[2 * o + 1]);
+        float* ttmp = nullptr;
+        TRAIN_CUDA(dalloc(&ttmp, (size_t)rows * TGT));
+        launch_target_transform(rows, tgt, sc, ttmp, q);
+        launch_column_stats(rows, OUT, TGT, ttmp, statP, statOut, q);
+        cudaError_t e = cudaMemcpyAsync(h, statOut, sizeof(double) * 2 * OUT, cudaMemcpyDeviceToHost, q);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(q);
+        cudaFree(ttmp);
+        TRAIN_CUDA(e);
         for (int o = 0; o < OUT; o++) {
             C->stats[2 * IN + o] = (float)h[2 * o];
             C->stats[2 * IN + OUT + o] = (float)h[2 * o + 1];
+            C->stats[2 * IN + 2 * OUT + o] = sc.s[o];
         }
         upload_norm(s, C);
     }

@@ -29,8 +29,12 @@ constexpr int P_B3 = P_B2 + HID;            // [OUTP]
 constexpr int NPARAM = P_B3 + OUTP;         // 7312
 constexpr int PARTIAL = NPARAM + 16;        // per-CTA gradient row (+ loss)
 
-// Normalisation block: feature mean and inverse deviation, target mean and deviation.
-constexpr int N_MUX = 0, N_ISX = IN, N_MUT = 2 * IN, N_SGT = 2 * IN + OUT, NNORM = 64;
+// Normalisation block: feature mean and inverse deviation, target mean and
+// deviation, target scale.  With a scale s > 0 the network predicts the
+// compressed target asinh(t/s) (standardised), so small and large corrections
+// weigh alike; the correction is s*sinh(prediction).  s <= 0: t itself.
+constexpr int N_MUX = 0, N_ISX = IN, N_MUT = 2 * IN, N_SGT = 2 * IN + OUT, N_SCL = 2 * IN + 2 * OUT, NNORM = 72;
+constexpr int NSTATS = 2 * IN + 3 * OUT;  // host-side blob tail: means, deviations, scales
 
 // BF16 weight image, byte offsets: the shared-memory layouts the kernels copy.
 constexpr int IMG_W1 = 0;                  // W1  [64 x 32]
@@ -79,6 +83,13 @@ void launch_mlp_pack(const float* master, unsigned char* image, float* bias, cud
 // in double precision, deterministic: out[2*c] = mean, out[2*c+1] = deviation.
 void launch_column_stats(long long rows, int cols, int stride, const float* data, double* partial, double* out,
                          cudaStream_t s);
+
+// out[r] = asinh(tgt[r][o] / scale[o]) for the 6 components of `rows` targets
+// (stride TGT in and out; a scale <= 0 copies the component).
+struct TargetScales {
+    float s[mlp::OUT];
+};
+void launch_target_transform(long long rows, const float* tgt, TargetScales sc, float* out, cudaStream_t s);
 
 // Training targets: tgt[id] = (x_ref - x_coarse, v_ref - v_coarse, 0, 0).
 void launch_targets(int n, const float4* refPos, const float4* refVel, const float4* pos, const float4* vel,

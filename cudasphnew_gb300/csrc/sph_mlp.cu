@@ -29,6 +29,7 @@ using namespace mlp;
 using namespace tc;
 
 constexpr uint32_t WAIT_LIMIT = 1u << 22;
+constexpr float ASINH_1000 = 7.6009027f;  // asinh(1000) = ln(1000 + sqrt(1000001))
 
 // 1 / (1 + e^-z); for very negative z the denominator overflows to infinity
 // and the fast division returns 0.
@@ -178,8 +179,13 @@ __global__ void __launch_bounds__(TILE, 1)
         if (valid) {
             float c[OUT];
 #pragma unroll
-            for (int o = 0; o < OUT; o++)
+            for (int o = 0; o < OUT; o++) {
                 c[o] = sNorm[N_MUT + o] + sNorm[N_SGT + o] * (y[o] + sBias[2 * HID + o]);
+                const float sc = sNorm[N_SCL + o];
+                // |correction| <= 1000 s (50 target deviations): sinh grows
+                // exponentially, so an out-of-range prediction is cut there
+                if (sc > 0.f) c[o] = sc * sinhf(fminf(fmaxf(c[o], -ASINH_1000), ASINH_1000));
+            }
             if (mode == 0) {
                 const int id = (int)row;
                 const float4 p = pos[id], w = vel[id];
@@ -283,8 +289,12 @@ __global__ void __launch_bounds__(TILE, 1)
 #pragma unroll
             for (int k = 0; k < INP; k++) store_bf16(sm + G_XT, core_off(k, t, TILE), f[k]);
 #pragma unroll
-            for (int o = 0; o < OUT; o++)
-                tn[o] = valid ? (tgt[row * TGT + o] - sNorm[N_MUT + o]) / sNorm[N_SGT + o] : 0.f;
+            for (int o = 0; o < OUT; o++) {
+                float tv = valid ? tgt[row * TGT + o] : 0.f;
+                const float sc = sNorm[N_SCL + o];
+                if (sc > 0.f) tv = asinhf(tv / sc);
+                tn[o] = valid ? (tv - sNorm[N_MUT + o]) / sNorm[N_SGT + o] : 0.f;
+            }
         }
         cta_sync();
         // forward
@@ -511,6 +521,17 @@ __global__ void k_stats_final(long long rows, int cols, int blocks, const double
     out[2 * c + 1] = sqrt(var);
 }
 
+__global__ void k_target_transform(long long rows, const float* __restrict__ tgt, TargetScales sc,
+                                   float* __restrict__ out) {
+    const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= rows) return;
+#pragma unroll
+    for (int o = 0; o < OUT; o++) {
+        const float t = tgt[r * TGT + o];
+        out[r * TGT + o] = sc.s[o] > 0.f ? asinhf(t / sc.s[o]) : t;
+    }
+}
+
 __global__ void k_targets(int n, const float4* __restrict__ refPos, const float4* __restrict__ refVel,
                           const float4* __restrict__ pos, const float4* __restrict__ vel, float* __restrict__ tgt) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -599,6 +620,10 @@ void launch_column_stats(long long rows, int cols, int stride, const float* data
                          cudaStream_t s) {
     k_stats_partial<<<ST_BLOCKS, ST_THREADS, 0, s>>>(rows, cols, stride, data, partial);
     k_stats_final<<<1, 32, 0, s>>>(rows, cols, ST_BLOCKS, partial, out);
+}
+
+void launch_target_transform(long long rows, const float* tgt, TargetScales sc, float* out, cudaStream_t s) {
+    if (rows > 0) k_target_transform<<<(unsigned int)((rows + 255) / 256), 256, 0, s>>>(rows, tgt, sc, out);
 }
 
 void launch_targets(int n, const float4* refPos, const float4* refVel, const float4* pos, const float4* vel,

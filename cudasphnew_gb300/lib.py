@@ -17,7 +17,7 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, "_build", "libsph_gb300.so")
 
 SPH_STEP_PLAIN, SPH_STEP_TWO_SCALE, SPH_STEP_SUB_ONLY, SPH_STEP_LEARNED = 0, 1, 2, 3
-CORRECTOR_FEATURES, CORRECTOR_OUTPUTS, CORRECTOR_FLOATS = 24, 6, 7372
+CORRECTOR_FEATURES, CORRECTOR_OUTPUTS, CORRECTOR_WEIGHTS, CORRECTOR_FLOATS = 24, 6, 7312, 7378
 (FIELD_VERTEX_DATA, FIELD_SIMULATION_DATA, FIELD_VELOCITY, FIELD_ACCELERATION,
  FIELD_DENSITY, FIELD_PRESSURE, FIELD_STATE, FIELD_SUB_VERTEX_DATA, FIELD_SUB_SIMULATION_DATA,
  FIELD_SUB_IDS, FIELD_SPLIT_IDS, FIELD_BOUNDARY_IDS, FIELD_DEFAULT_IDS) = range(13)
@@ -88,7 +88,8 @@ class CorrectorConfig(ctypes.Structure):
 
     _fields_ = [("trainSteps", ctypes.c_int), ("stride", ctypes.c_int), ("epochs", ctypes.c_int),
                 ("batchTiles", ctypes.c_int), ("learningRate", ctypes.c_float),
-                ("densityTolerance", ctypes.c_float), ("auditInterval", ctypes.c_int), ("seed", ctypes.c_uint)]
+                ("densityTolerance", ctypes.c_float), ("auditInterval", ctypes.c_int), ("seed", ctypes.c_uint),
+                ("targetScale", ctypes.c_float)]
 
     @classmethod
     def default(cls, **kw) -> "CorrectorConfig":
@@ -328,7 +329,7 @@ class ParticleSimulation:
         f = np.ascontiguousarray(features, np.float32).reshape(-1, CORRECTOR_FEATURES)
         t = np.zeros((len(f), 8), np.float32)
         t[:, :CORRECTOR_OUTPUTS] = np.asarray(targets, np.float32).reshape(len(f), CORRECTOR_OUTPUTS)
-        g = np.zeros(CORRECTOR_FLOATS - 60, np.float32)
+        g = np.zeros(CORRECTOR_WEIGHTS, np.float32)
         loss = np.zeros(1, np.float32)
         check(load().sph_corrector_gradient(self._h, f.ctypes.data, t.ctypes.data, len(f), g.ctypes.data,
                                             loss.ctypes.data))

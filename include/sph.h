@@ -282,10 +282,14 @@ sph_status sph_get_diagnostics(sph_handle h, sph_diagnostics* out);
 #define SPH_CORRECTOR_FEATURES 24
 #define SPH_CORRECTOR_OUTPUTS 6
 /* Model blob: FP32 weights W1[64][32] (input columns 24..31 zero), W2[64][64],
- * W3[16][64] (rows 6..15 zero), b1[64], b2[64], b3[16] (6..15 zero), then the
- * feature means[24], feature deviations[24], target means[6], target
- * deviations[6]. */
-#define SPH_CORRECTOR_FLOATS 7372
+ * W3[16][64] (rows 6..15 zero), b1[64], b2[64], b3[16] (6..15 zero) -- the
+ * first SPH_CORRECTOR_WEIGHTS floats -- then the feature means[24], feature
+ * deviations[24], and per output the target mean[6], deviation[6] and scale[6].
+ * With a scale s > 0 the network's standardised output y gives the correction
+ * s*sinh(mean + deviation*y) (the targets were compressed as asinh(t/s));
+ * s <= 0 gives mean + deviation*y. */
+#define SPH_CORRECTOR_WEIGHTS 7312
+#define SPH_CORRECTOR_FLOATS 7378
 
 typedef struct sph_corrector_config {
     int trainSteps;         /* plain steps of dt that generate samples (2000) */
@@ -296,6 +300,9 @@ typedef struct sph_corrector_config {
     float densityTolerance; /* audit threshold (0.01) */
     int auditInterval;      /* audit every k-th learned step (16); 0: never */
     unsigned int seed;      /* weight initialisation and sample order */
+    float targetScale;      /* > 0: train on asinh(t/s) with s = targetScale x the
+                               target's deviation (compresses the heavy tail of
+                               the corrections); 0: on t itself (default) */
 } sph_corrector_config;
 
 typedef struct sph_corrector_report {
@@ -325,8 +332,8 @@ sph_status sph_corrector_save(sph_handle h, float* model, size_t count);
 sph_status sph_corrector_get_report(sph_handle h, sph_corrector_report* out);
 
 /* Checking entry points: corrections (count x 6, denormalised) of given raw
- * features (count x 24), and the loss gradient (SPH_CORRECTOR_FLOATS - 60
- * weight floats, blob order) and summed loss of given samples (targets count
+ * features (count x 24), and the loss gradient (SPH_CORRECTOR_WEIGHTS floats,
+ * blob order) and summed loss of given samples (targets count
  * x 8, first 6 used), both through the tensor-core kernels. */
 sph_status sph_corrector_predict(sph_handle h, const float* features, int count, float* corrections);
 sph_status sph_corrector_gradient(sph_handle h, const float* features, const float* targets, int count,

@@ -49,6 +49,7 @@ int main(void) {
     O(sph_corrector_config, seed); O(sph_corrector_config, densityTolerance);
     O(sph_corrector_report, trainMilliseconds); O(sph_corrector_report, maxAuditError);
     printf("SPH_CORRECTOR_FLOATS %d\n", SPH_CORRECTOR_FLOATS);
+    printf("SPH_CORRECTOR_WEIGHTS %d\n", SPH_CORRECTOR_WEIGHTS);
     O(SimulationParameters, numParticles); O(SimulationParameters, timeStep);
     O(SimulationParameters, poly6); O(SimulationParameters, laplViscSub);
     O(SimulationParameters, boxDim); O(SimulationParameters, restitution);
@@ -76,6 +77,7 @@ def test_struct_layouts_match_header():
     assert lay["sph_corrector_config"] == ctypes.sizeof(sphmod.CorrectorConfig)
     assert lay["sph_corrector_report"] == ctypes.sizeof(sphmod.CorrectorReport)
     assert lay.pop("SPH_CORRECTOR_FLOATS") == sphmod.CORRECTOR_FLOATS
+    assert lay.pop("SPH_CORRECTOR_WEIGHTS") == sphmod.CORRECTOR_WEIGHTS
     for key, v in lay.items():
         if "." not in key:
             continue

@@ -42,6 +42,22 @@ def unpack(blob):
     return W1, W2, W3, b1, b2, b3, s[:24], s[24:48], s[48:54], s[54:60]
 
 
+def target_scales(blob):
+    return blob[NPARAM + 60:NPARAM + 66].astype(np.float64)
+
+
+def decode(blob, y):
+    """Correction from the network's standardised output (targetScale aware)."""
+    mut, st, sc = blob[NPARAM + 48:NPARAM + 54], blob[NPARAM + 54:NPARAM + 60], target_scales(blob)
+    a = mut + st * y
+    return np.where(sc > 0, sc * np.sinh(np.clip(a, -np.arcsinh(1000), np.arcsinh(1000))), a)
+
+
+def encode(blob, t):
+    sc = target_scales(blob)
+    return np.where(sc > 0, np.arcsinh(t / np.where(sc > 0, sc, 1)), t)
+
+
 def random_blob(seed):
     rng = np.random.default_rng(seed)
     W1 = np.zeros((64, 32))
@@ -52,7 +68,7 @@ def random_blob(seed):
     b1, b2 = rng.normal(0, 0.1, 64), rng.normal(0, 0.1, 64)
     b3 = np.zeros(16)
     b3[:6] = rng.normal(0, 0.1, 6)
-    blob = np.zeros(7372, np.float32)
+    blob = np.zeros(7378, np.float32)  # target scales 0: corrections used as the network gives them
     blob[:NPARAM] = np.concatenate([W1.ravel(), W2.ravel(), W3.ravel(), b1, b2, b3])
     blob[NPARAM:NPARAM + 24] = rng.normal(0, 1, 24)
     blob[NPARAM + 24:NPARAM + 48] = rng.uniform(0.5, 2.0, 24)
@@ -79,7 +95,7 @@ def gradient(blob, feats, targets):
     W1, W2, W3, b1, b2, b3, mux, sx, mut, st = unpack(blob)
     f = forward(blob, feats)
     n = len(feats)
-    tn = (targets.astype(np.float32) - mut) / st
+    tn = (encode(blob, targets.astype(np.float32).astype(np.float64)) - mut) / st
     e = f["y"] - tn
     loss = (e * e).sum()
     dy = 2 * e / (6 * n)
@@ -128,9 +144,19 @@ def density_at(sphlib, sc, pos, vel):
         return sim.read(sphlib.FIELD_DENSITY)
 
 
+def scaled_blob(seed):
+    """A blob whose targets were compressed: corrections s*sinh(mean + dev*y)."""
+    blob = random_blob(seed)
+    blob[NPARAM + 48:NPARAM + 54] = np.random.default_rng(seed).normal(0, 0.3, 6)
+    blob[NPARAM + 54:NPARAM + 60] = 1.5
+    blob[NPARAM + 60:NPARAM + 66] = np.linspace(1e-6, 6e-6, 6)
+    return blob
+
+
 @pytest.mark.parametrize("count", [1, 127, 128, 300, 4099])
-def test_mlp_predict_matches_numpy(sphlib, count):
-    blob = random_blob(1)
+@pytest.mark.parametrize("scaled", [False, True])
+def test_mlp_predict_matches_numpy(sphlib, count, scaled):
+    blob = scaled_blob(1) if scaled else random_blob(1)
     rng = np.random.default_rng(count)
     feats = rng.normal(0, 1.5, (count, IN)).astype(np.float32)
     with make(sphlib, tiny()) as sim:
@@ -138,18 +164,20 @@ def test_mlp_predict_matches_numpy(sphlib, count):
         got = sim.corrector_predict(feats)
     ref = forward(blob, feats)["y"]
     mut, st = blob[NPARAM + 48:NPARAM + 54], blob[NPARAM + 54:NPARAM + 60]
-    y = (got.astype(np.float64) - mut) / st  # back to the network's output space
+    y = (encode(blob, got.astype(np.float64)) - mut) / st  # back to the network's output space
     assert np.isfinite(got).all()
     assert np.abs(y - ref).max() <= 2e-3 * max(1.0, np.abs(ref).max())
+    if scaled:  # and through the decoding itself
+        np.testing.assert_allclose(got, decode(blob, ref), rtol=2e-2, atol=1e-9)
 
 
 @pytest.mark.parametrize("count", [128, 1000])
-def test_mlp_gradient_matches_numpy(sphlib, count):
-    blob = random_blob(2)
+@pytest.mark.parametrize("scaled", [False, True])
+def test_mlp_gradient_matches_numpy(sphlib, count, scaled):
+    blob = scaled_blob(2) if scaled else random_blob(2)
     rng = np.random.default_rng(7 + count)
     feats = rng.normal(0, 1.5, (count, IN)).astype(np.float32)
-    tgt = (blob[NPARAM + 48:NPARAM + 54] + blob[NPARAM + 54:NPARAM + 60] *
-           rng.normal(0, 1, (count, OUT))).astype(np.float32)
+    tgt = decode(blob, rng.normal(0, 1, (count, OUT))).astype(np.float32)
     with make(sphlib, tiny()) as sim:
         sim.load_corrector(blob)
         g, loss = sim.corrector_gradient(feats, tgt)
