@@ -49,7 +49,7 @@ def parse():
     ap.add_argument("--config", default="config2")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true",
-                    help="skip the 64-scene batched leg")
+                    help="skip the 64-scene batched leg and the two-scale leg")
     ap.add_argument("--no-learned", action="store_true",
                     help="skip the learned-corrector legs (16,384-particle scene and the 1M scene)")
     ap.add_argument("--no-autotune", action="store_true",
@@ -440,6 +440,26 @@ def batched_leg(lib, torch, stream, steps=200):
             "l2": "no flush: working set of the 4.4M-particle batch far exceeds L2"}
 
 
+def two_scale_leg(lib, torch, stream, steps=500):
+    """The 262,144-particle two-scale run (AdvanceTwoScale with persistent
+    children and merge-back), against the plain step of the same scene."""
+    from cudasphnew_gb300 import scenes
+    sc = scenes.config3()
+    with lib.ParticleSimulation(sc.params, sc.positions, sc.velocities, sc.options, sc.boundary) as sim:
+        sim.set_stream(stream.cuda_stream)
+        sim.step(mode=lib.SPH_STEP_TWO_SCALE, count=5)
+        ms = time_steps(torch, stream, sim, lib.SPH_STEP_TWO_SCALE, steps)
+        c = sim.counts()
+        ms_plain = time_steps(torch, stream, sim, lib.SPH_STEP_PLAIN, steps)
+    return {"workload": f"{sc.name}: {sc.n} coarse particles, split region [0.4, 0.6]^3, children merged back "
+                        f"on exit", "unit": UNIT, "steps": steps,
+            "value": sc.n * steps / (ms / 1e3), "ms_per_step": ms / steps,
+            "children_at_end": c.numSubParticles, "split_at_end": c.numParticlesSplit,
+            "boundary_at_end": c.numParticlesBoundary,
+            "plain_ms_per_step": ms_plain / steps,
+            "graph": "one CUDA graph launch per step; counts stay on the device"}
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -533,9 +553,10 @@ def run_ours(args):
     e2e_value = world * n * e2e_steps / el
     sim.close()
 
-    batched = None
+    batched = two_scale = None
     if rank == 0 and not args.no_batched:
         batched = batched_leg(lib, torch, stream)
+        two_scale = two_scale_leg(lib, torch, stream)
     learned = learned_1m = None
     if rank == 0 and not args.no_learned:
         learned, lcfg, model = learned_leg(lib, torch, stream)
@@ -566,6 +587,7 @@ def run_ours(args):
            "stages_us": {k: round(v[0] / v[1] * 1e3, 2) for k, v in stages.items()}}
     if batched is not None:
         out["batched"] = batched
+        out["two_scale"] = two_scale
     if learned is not None:
         out["learned"] = learned
         out["learned_1m"] = learned_1m

@@ -111,8 +111,16 @@ sph_status check_desc(const sph_boundary_desc* d, unsigned int dims[3]) {
         SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "numShapes must be in [1, 8]");
     for (int i = 0; i < d->numShapes; i++) {
         int k = d->shapes[i].kind;
-        if (k != SPH_SHAPE_SPHERE && k != SPH_SHAPE_CONE && k != SPH_SHAPE_BOX)
+        if (k != SPH_SHAPE_SPHERE && k != SPH_SHAPE_CONE && k != SPH_SHAPE_BOX && k != SPH_SHAPE_MESH)
             SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "unknown shape kind");
+        if (k == SPH_SHAPE_MESH) {
+            const float g = d->shapes[i].p[0];
+            if (!d->sdfGrids || !(g >= 0.0f) || g >= (float)d->numSdfGrids || g != (float)(int)g)
+                SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "a mesh shape names no grid of sdfGrids");
+            const sph_sdf_grid& G = d->sdfGrids[(int)g];
+            if (!G.distance || G.dims[0] == 0 || G.dims[1] == 0 || G.dims[2] == 0 || !(G.dx > 0.0f))
+                SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "empty signed distance grid");
+        }
     }
     if (!(d->gridSpacing > 0.0f) || !(d->particleSpacing > 0.0f) || !(d->compactSupport > 0.0f))
         SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "boundary spacings must be positive");
@@ -448,8 +456,7 @@ sph_status sph_boundary_maps(const sph_boundary_desc* desc, float* distance, flo
         if (v) cudaFree(v);
         SPH_FAIL(SPH_ERR_OUT_OF_MEMORY, "boundary map allocation failed");
     }
-    launch_build_maps(*desc, dims, d, r, v, nullptr, 0);
-    cudaError_t e = cudaGetLastError();
+    cudaError_t e = launch_build_maps(*desc, dims, d, r, v, nullptr, 0);
     if (e == cudaSuccess && distance) e = cudaMemcpy(distance, d, total * 4, cudaMemcpyDeviceToHost);
     if (e == cudaSuccess && density) e = cudaMemcpy(density, r, total * 4, cudaMemcpyDeviceToHost);
     if (e == cudaSuccess && viscosity) e = cudaMemcpy(viscosity, v, total * 4, cudaMemcpyDeviceToHost);
@@ -516,9 +523,7 @@ sph_status sph_create(const SimulationParameters* params, const sph_options* opt
         size_t total = (size_t)mdims[0] * mdims[1] * mdims[2];
         CREATE_CUDA(dalloc(&s->map4, total));
         CREATE_CUDA(dalloc(&s->mapDist, total));
-        launch_build_maps(*boundary, mdims, s->mapDist, nullptr, nullptr, s->map4, s->stream);
-        s->desc = *boundary;
-        s->hasDesc = true;
+        CREATE_CUDA(launch_build_maps(*boundary, mdims, s->mapDist, nullptr, nullptr, s->map4, s->stream));
         s->map = map_of(*boundary, mdims, s->map4, s->mapDist);
     }
     CREATE_CUDA(cudaGetLastError());

@@ -97,7 +97,7 @@ sph_status sph_create_batch(const sph_scene* scenes, int numScenes, const sph_op
         d.map = MapDev{};
         if (sc.boundary) {
             const unsigned int* dk = &dims[(size_t)3 * k];
-            launch_build_maps(*sc.boundary, dk, s->mapDist + mOff, nullptr, nullptr, s->map4 + mOff, q);
+            BATCH_CUDA(launch_build_maps(*sc.boundary, dk, s->mapDist + mOff, nullptr, nullptr, s->map4 + mOff, q));
             d.map = map_of(*sc.boundary, dk, s->map4 + mOff, s->mapDist + mOff);
             mOff += (size_t)dk[0] * dk[1] * dk[2];
         }

@@ -336,8 +336,9 @@ sph_status sph_corrector_train(sph_handle s, const sph_corrector_config* cfg) {
     {
         std::vector<float> host((size_t)n * 3);
         TRAIN_ST(sph_read(s, SPH_FIELD_VERTEX_DATA, host.data(), host.size() * sizeof(float)));
-        TRAIN_ST(sph_create(&s->P, &s->O, host.data(), nullptr, s->hasDesc ? &s->desc : nullptr, &sh));
+        TRAIN_ST(sph_create(&s->P, &s->O, host.data(), nullptr, nullptr, &sh));
     }
+    sh->map = s->map;  // the shadow reads the handle's boundary maps (it owns none)
     TRAIN_ST(sph_set_stream(sh, q));
     sh->cfg = s->cfg;
     TRAIN_CUDA(cudaEventRecord(e0, q));

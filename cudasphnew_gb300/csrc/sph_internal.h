@@ -190,7 +190,9 @@ void launch_diagnostics(int n, const float4* pos, const float4* vel, const float
                         cudaStream_t s);
 
 // Boundary maps.
-void launch_build_maps(const sph_boundary_desc& d, const unsigned int dims[3], float* dist,
-                       float* dens, float* visc, float4* map4, cudaStream_t s);
+// Builds the maps of `d` (grid solids are uploaded for the build and freed
+// after it, synchronising `s`).
+cudaError_t launch_build_maps(const sph_boundary_desc& d, const unsigned int dims[3], float* dist,
+                              float* dens, float* visc, float4* map4, cudaStream_t s);
 
 }  // namespace sph

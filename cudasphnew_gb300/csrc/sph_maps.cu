@@ -27,7 +27,39 @@ struct MapArgs {
     int boxIndex;
     float latStart[3];       // ghost lattice origin and last index per axis
     unsigned int latMax[3];
+    // SPH_SHAPE_MESH solids: the signed distance grid of shape slot i
+    const float* grid[8];
+    float gridOrigin[8][3];
+    float gridDx[8];
+    unsigned int gridDims[8][3];
 };
+
+// Trilinear signed distance of a grid solid (negative inside); no solid
+// outside the grid's box.
+__device__ double grid_sdf(const MapArgs& A, int s, const double* x) {
+    double w[3];
+    size_t i0[3];
+    for (int a = 0; a < 3; a++) {
+        const unsigned int n = A.gridDims[s][a];
+        const double u = (x[a] - (double)A.gridOrigin[s][a]) / (double)A.gridDx[s];
+        if (!(u >= 0.0) || u > (double)(n - 1)) return 1e30;
+        const double f = n > 1 ? fmin(floor(u), (double)(n - 2)) : 0.0;
+        i0[a] = (size_t)f;
+        w[a] = n > 1 ? u - f : 0.0;
+    }
+    const unsigned int* d = A.gridDims[s];
+    auto at = [&](int di, int dj, int dk) {
+        const size_t ii = i0[0] + (d[0] > 1 ? di : 0), jj = i0[1] + (d[1] > 1 ? dj : 0),
+                     kk = i0[2] + (d[2] > 1 ? dk : 0);
+        return (double)A.grid[s][ii + (size_t)d[0] * (jj + (size_t)d[1] * kk)];
+    };
+    const double c00 = at(0, 0, 0) + w[0] * (at(1, 0, 0) - at(0, 0, 0));
+    const double c10 = at(0, 1, 0) + w[0] * (at(1, 1, 0) - at(0, 1, 0));
+    const double c01 = at(0, 0, 1) + w[0] * (at(1, 0, 1) - at(0, 0, 1));
+    const double c11 = at(0, 1, 1) + w[0] * (at(1, 1, 1) - at(0, 1, 1));
+    const double c0 = c00 + w[1] * (c10 - c00), c1 = c01 + w[1] * (c11 - c01);
+    return c0 + w[2] * (c1 - c0);
+}
 
 // computeSignedDistancePoint3Box3 (SphInComplexShapes.cpp:714-747), axis-aligned.
 __device__ float box_signed_distance(const float* pos, const float* c, const float* e) {
@@ -86,6 +118,8 @@ __device__ float solid_distance(const MapArgs& A, const float* xf) {
             d = sqrt(dx * dx + dy * dy + dz * dz) - S.p[3];
         } else if (S.kind == SPH_SHAPE_CONE) {
             d = cone_sdf(x, S.p);
+        } else if (S.kind == SPH_SHAPE_MESH) {
+            d = grid_sdf(A, i, x);
         } else {
             d = -(double)box_signed_distance(xf, S.p, S.p + 3);
         }
@@ -164,9 +198,9 @@ __global__ void k_build_maps(MapArgs A, float* dist, float* dens, float* visc, f
 
 }  // namespace
 
-void launch_build_maps(const sph_boundary_desc& D, const unsigned int dims[3], float* dist, float* dens,
-                       float* visc, float4* map4, cudaStream_t s) {
-    MapArgs A;
+cudaError_t launch_build_maps(const sph_boundary_desc& D, const unsigned int dims[3], float* dist, float* dens,
+                              float* visc, float4* map4, cudaStream_t s) {
+    MapArgs A{};
     for (int a = 0; a < 3; a++) {
         A.start[a] = D.gridStart[a];
         A.dims[a] = dims[a];
@@ -205,8 +239,36 @@ void launch_build_maps(const sph_boundary_desc& D, const unsigned int dims[3], f
         }
     }
     size_t total = (size_t)dims[0] * dims[1] * dims[2];
-    if (total == 0) return;
-    k_build_maps<<<(unsigned int)((total + 127) / 128), 128, 0, s>>>(A, dist, dens, visc, map4);
+    if (total == 0) return cudaSuccess;
+    // grid solids: device copies of their distances for the build
+    float* devGrid[8] = {};
+    cudaError_t e = cudaSuccess;
+    for (int i = 0; i < D.numShapes && i < 8 && e == cudaSuccess; i++) {
+        if (D.shapes[i].kind != SPH_SHAPE_MESH) continue;
+        const sph_sdf_grid& G = D.sdfGrids[(int)D.shapes[i].p[0]];
+        const size_t nodes = (size_t)G.dims[0] * G.dims[1] * G.dims[2];
+        e = cudaMalloc((void**)&devGrid[i], sizeof(float) * nodes);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(devGrid[i], G.distance, sizeof(float) * nodes, cudaMemcpyHostToDevice, s);
+        A.grid[i] = devGrid[i];
+        A.gridDx[i] = G.dx;
+        for (int a = 0; a < 3; a++) {
+            A.gridOrigin[i][a] = G.origin[a];
+            A.gridDims[i][a] = G.dims[a];
+        }
+    }
+    if (e == cudaSuccess) {
+        k_build_maps<<<(unsigned int)((total + 127) / 128), 128, 0, s>>>(A, dist, dens, visc, map4);
+        e = cudaGetLastError();
+    }
+    bool any = false;
+    for (float* g : devGrid) any = any || g;
+    if (any) {
+        const cudaError_t w = cudaStreamSynchronize(s);  // the grids are freed after the build
+        if (e == cudaSuccess) e = w;
+        for (float* g : devGrid)
+            if (g) cudaFree(g);
+    }
+    return e;
 }
 
 }  // namespace sph

@@ -82,9 +82,6 @@ struct sph_sim {
     int graphMode = -1;
     unsigned int graphGen = 0;  // bumped whenever captured graphs go stale
 
-    // the boundary description the maps were built from
-    sph_boundary_desc desc{};
-    bool hasDesc = false;
 
     // cells owned by the handle: the grid's, or the sum over batched scenes
     long long numCellsTotal = 0;

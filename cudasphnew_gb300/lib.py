@@ -11,7 +11,7 @@ import os
 
 import numpy as np
 
-from .params import BoundaryDesc, Options, SimulationParameters
+from .params import BoundaryDesc, Options, SdfGrid, SimulationParameters
 
 PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, "_build", "libsph_gb300.so")
@@ -64,6 +64,13 @@ SIGNATURES = {
     "sph_corrector_predict": (_i, [_vp, _vp, _i, _vp]),
     "sph_corrector_gradient": (_i, [_vp, _vp, _vp, _i, _vp, _vp]),
     "sph_read_features": (_i, [_vp, _vp, ctypes.c_size_t]),
+    "sph_obj_load": (_i, [ctypes.c_char_p, _vp]),
+    "sph_mesh_free": (None, [_vp]),
+    "sph_sdf_from_mesh": (_i, [_vp, ctypes.c_float, ctypes.c_float, ctypes.c_float, _vp]),
+    "sph_sdf_from_mesh_on_grid": (_i, [_vp, _vp, ctypes.c_float, _vp, ctypes.c_float, ctypes.c_float, _vp]),
+    "sph_sdf_save": (_i, [_vp, ctypes.c_char_p]),
+    "sph_sdf_load": (_i, [ctypes.c_char_p, _vp]),
+    "sph_sdf_free": (None, [_vp]),
     "sph_last_error": (ctypes.c_char_p, []),
     "sph_status_string": (ctypes.c_char_p, [_i]),
 }
@@ -162,6 +169,102 @@ def boundary_maps(desc: BoundaryDesc):
     out = [np.zeros(shape, np.float32) for _ in range(3)]
     check(L.sph_boundary_maps(ctypes.byref(desc), *[_p(a) for a in out]))
     return tuple(out)
+
+
+class Mesh(ctypes.Structure):
+    """sph_mesh: triangle mesh (0-based faces)."""
+
+    _fields_ = [("vertices", ctypes.POINTER(ctypes.c_float)), ("numVertices", ctypes.c_uint),
+                ("faces", ctypes.POINTER(ctypes.c_uint)), ("numFaces", ctypes.c_uint)]
+
+
+def load_obj(path: str):
+    """sph_obj_load: (vertices float32 [nv, 3], faces uint32 [nf, 3])."""
+    L = load()
+    m = Mesh()
+    check(L.sph_obj_load(path.encode(), ctypes.byref(m)))
+    try:
+        v = np.ctypeslib.as_array(m.vertices, (m.numVertices, 3)).copy()
+        f = np.ctypeslib.as_array(m.faces, (m.numFaces, 3)).copy()
+    finally:
+        L.sph_mesh_free(ctypes.byref(m))
+    return v, f
+
+
+def _grid_arrays(g: SdfGrid):
+    n = int(g.dims[0]) * int(g.dims[1]) * int(g.dims[2])
+    shape = (int(g.dims[2]), int(g.dims[1]), int(g.dims[0]))
+    d = np.ctypeslib.as_array(g.distance, (n,)).copy().reshape(shape)
+    nrm = np.ctypeslib.as_array(g.normal, (3 * n,)).copy().reshape(shape + (3,)) if g.normal else None
+    return d, nrm
+
+
+class SignedDistanceGrid:
+    """A signed distance grid (host copy): distance[k, j, i] (negative inside),
+    normal[k, j, i, 3], origin, dx, restDistance, compactSupport, maxDist."""
+
+    def __init__(self, g: SdfGrid):
+        self.origin = np.array(g.origin[:], np.float32)
+        self.dx = float(g.dx)
+        self.restDistance, self.compactSupport, self.maxDist = (float(g.restDistance), float(g.compactSupport),
+                                                                float(g.maxDist))
+        self.distance, self.normal = _grid_arrays(g)
+
+    @property
+    def dims(self):
+        return tuple(int(v) for v in self.distance.shape[::-1])
+
+    def struct(self) -> SdfGrid:
+        """An sph_sdf_grid viewing this object's arrays (keep the object alive)."""
+        g = SdfGrid()
+        for a in range(3):
+            g.origin[a] = float(self.origin[a])
+            g.dims[a] = self.dims[a]
+        g.dx, g.restDistance, g.compactSupport, g.maxDist = self.dx, self.restDistance, self.compactSupport, \
+            self.maxDist
+        self._d = np.ascontiguousarray(self.distance, np.float32)
+        g.distance = self._d.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+        if self.normal is not None:
+            self._n = np.ascontiguousarray(self.normal, np.float32)
+            g.normal = self._n.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+        return g
+
+    @classmethod
+    def _take(cls, g: SdfGrid) -> "SignedDistanceGrid":
+        try:
+            return cls(g)
+        finally:
+            load().sph_sdf_free(ctypes.byref(g))
+
+    @classmethod
+    def from_mesh(cls, vertices, faces, rest_distance: float, compact_support: float, dx: float,
+                  origin=None, dims=None) -> "SignedDistanceGrid":
+        """sph_sdf_from_mesh (or _on_grid when origin and dims are given)."""
+        L = load()
+        v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 3)
+        f = np.ascontiguousarray(faces, np.uint32).reshape(-1, 3)
+        m = Mesh(v.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), len(v),
+                 f.ctypes.data_as(ctypes.POINTER(ctypes.c_uint)), len(f))
+        g = SdfGrid()
+        if origin is None:
+            check(L.sph_sdf_from_mesh(ctypes.byref(m), rest_distance, compact_support, dx, ctypes.byref(g)))
+        else:
+            o = (ctypes.c_float * 3)(*origin)
+            dm = (ctypes.c_uint * 3)(*dims)
+            check(L.sph_sdf_from_mesh_on_grid(ctypes.byref(m), o, dx, dm, rest_distance, compact_support,
+                                              ctypes.byref(g)))
+        return cls._take(g)
+
+    @classmethod
+    def load_file(cls, path: str) -> "SignedDistanceGrid":
+        """sph_sdf_load: the reference's boundary-map text file."""
+        g = SdfGrid()
+        check(load().sph_sdf_load(path.encode(), ctypes.byref(g)))
+        return cls._take(g)
+
+    def save(self, path: str) -> None:
+        g = self.struct()
+        check(load().sph_sdf_save(ctypes.byref(g), path.encode()))
 
 
 class Scene(ctypes.Structure):

@@ -89,6 +89,16 @@ class Shape(ctypes.Structure):
 SHAPE_SPHERE = 1
 SHAPE_CONE = 2
 SHAPE_BOX = 3
+SHAPE_MESH = 4
+
+
+class SdfGrid(ctypes.Structure):
+    """sph_sdf_grid: a signed distance grid (negative inside), x fastest."""
+
+    _fields_ = [("origin", F3), ("dx", ctypes.c_float), ("dims", ctypes.c_uint * 3),
+                ("restDistance", ctypes.c_float), ("compactSupport", ctypes.c_float),
+                ("maxDist", ctypes.c_float), ("distance", ctypes.POINTER(ctypes.c_float)),
+                ("normal", ctypes.POINTER(ctypes.c_float))]
 
 
 class BoundaryDesc(ctypes.Structure):
@@ -106,6 +116,8 @@ class BoundaryDesc(ctypes.Structure):
         ("particleSpacing", ctypes.c_float),
         ("numShapes", ctypes.c_int),
         ("shapes", Shape * 8),
+        ("sdfGrids", ctypes.c_void_p),
+        ("numSdfGrids", ctypes.c_int),
     ]
 
     def dims(self):

@@ -132,7 +132,11 @@ def two_scale(nb=64, region=(0.4, 0.6), box=1.0, seed=3, name="two_scale_262k") 
 
 
 def config3() -> Scene:
-    return two_scale()
+    """The 262,144-particle two-scale run: split region [0.4, 0.6]^3, children
+    kept while their parent stays split and merged back on exit (childMode 1)."""
+    sc = two_scale()
+    sc.options.childMode = 1
+    return sc
 
 
 def batched_scene(n: int, frac: float, seed: int, name: str) -> Scene:

@@ -96,9 +96,30 @@ typedef struct sph_options {
 enum {
     SPH_SHAPE_SPHERE = 1, /* p = (cx, cy, cz, r): solid sphere */
     SPH_SHAPE_CONE = 2,   /* p = (bx, by, bz, R, H): solid cone on its base, axis +z */
-    SPH_SHAPE_BOX = 3     /* p = (cx, cy, cz, ex, ey, ez): container, fluid inside
+    SPH_SHAPE_BOX = 3,    /* p = (cx, cy, cz, ex, ey, ez): container, fluid inside
                              (SetBox, SphInComplexShapes.cpp:203-313) */
+    SPH_SHAPE_MESH = 4    /* p[0] = index into sph_boundary_desc.sdfGrids: a solid
+                             given by a signed distance grid (negative inside),
+                             e.g. from sph_sdf_from_mesh; read trilinearly, no
+                             solid outside the grid's box */
 };
+
+/* A signed distance grid (BoundaryMap, boundary_map.h:35-122): nodes
+ * origin + (i, j, k)*dx, x fastest; distance negative inside the solid.
+ * Nodes within maxDist = max(restDistance, compactSupport) of the surface
+ * hold the exact distance and a unit normal (node minus closest surface
+ * point); the others hold +-maxDist and a zero normal (a grid read from the
+ * reference's text format holds +restDistance there, as its Load does). */
+typedef struct sph_sdf_grid {
+    float origin[3];
+    float dx;
+    unsigned int dims[3];
+    float restDistance;
+    float compactSupport;
+    float maxDist;
+    float* distance;    /* float[dims[0]*dims[1]*dims[2]] */
+    float* normal;      /* float[3*dims product], or NULL */
+} sph_sdf_grid;
 
 typedef struct sph_shape {
     int kind;
@@ -120,6 +141,9 @@ typedef struct sph_boundary_desc {
     float particleSpacing;
     int numShapes;
     sph_shape shapes[8];
+    const sph_sdf_grid* sdfGrids; /* the grids of SPH_SHAPE_MESH solids (host
+                                     memory, read during sph_create only) */
+    int numSdfGrids;
 } sph_boundary_desc;
 
 typedef enum sph_status {
@@ -249,6 +273,40 @@ sph_status sph_read_cells(sph_handle h, int level, int* sortedHash, int* sortedI
 
 /* Particle counts (GetNumParticles*, GetNumSubParticles*, GetNumTimesSteps). */
 sph_status sph_get_counts(sph_handle h, sph_counts* out);
+
+/* ---------------------------------------------------------------------------
+ * Meshes and signed distance grids (BoundaryMap, PointInMeshTest).
+ * ------------------------------------------------------------------------- */
+typedef struct sph_mesh {
+    float* vertices;        /* float[numVertices*3] */
+    unsigned int numVertices;
+    unsigned int* faces;    /* uint[numFaces*3], 0-based vertex indices */
+    unsigned int numFaces;
+} sph_mesh;
+
+/* Reads the `v` and `f` records of a Wavefront OBJ file (TriangleMesh,
+ * triangle_mesh.cpp:16-37): f entries may be "i", "i/t", "i//n" or "i/t/n",
+ * 1-based or negative (relative); polygons are split into triangle fans.
+ * The arrays are malloc'ed: free them with sph_mesh_free. */
+sph_status sph_obj_load(const char* path, sph_mesh* out);
+void sph_mesh_free(sph_mesh* mesh);
+
+/* BoundaryMap(config) + AddCanvas(mesh) (boundary_map.cpp:25-95, 351-470) on
+ * the GPU: a grid over the mesh's bounding box, ceil(extent/dx) + 1 nodes per
+ * axis.  sph_sdf_from_mesh_on_grid takes the grid (origin, dx, dims) from
+ * the caller instead, e.g. the bounding box grown by a margin so that the
+ * grid can serve as an SPH_SHAPE_MESH solid.  The arrays are malloc'ed: free
+ * them with sph_sdf_free. */
+sph_status sph_sdf_from_mesh(const sph_mesh* mesh, float restDistance, float compactSupport, float dx,
+                             sph_sdf_grid* out);
+sph_status sph_sdf_from_mesh_on_grid(const sph_mesh* mesh, const float origin[3], float dx,
+                                     const unsigned int dims[3], float restDistance,
+                                     float compactSupport, sph_sdf_grid* out);
+/* The reference's boundary-map text file (BoundaryMap::Save / Load,
+ * boundary_map.cpp:161-287): the band's nodes only, one value per line. */
+sph_status sph_sdf_save(const sph_sdf_grid* grid, const char* path);
+sph_status sph_sdf_load(const char* path, sph_sdf_grid* out);
+void sph_sdf_free(sph_sdf_grid* grid);
 
 /* FP64 conservation diagnostics of the coarse particles (no reference
  * counterpart; the reference's SD_ENERGY column, particle_simulation.h:40, is

@@ -276,3 +276,20 @@ class TwoScale:
         rc = fn(self._h, ctypes.byref(p), ctypes.byref(o), *[_ptr(a) for a in arrs], *[_ptr(a) for a in ints])
         if rc:
             raise ValueError(f"oracle two-scale part failed ({rc})")
+
+
+def mesh_sdf(vertices, faces, origin, dx, dims, max_dist):
+    """The oracle's mesh signed distance grid: (distance [k, j, i], normal [k, j, i, 3])."""
+    L = lib()
+    fn = L.orc_mesh_sdf
+    fn.restype = None
+    fn.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_float,
+                   ctypes.c_void_p, ctypes.c_float, ctypes.c_void_p, ctypes.c_void_p]
+    v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 3)
+    f = np.ascontiguousarray(faces, np.uint32).reshape(-1, 3)
+    o = np.ascontiguousarray(origin, np.float32)
+    d = np.ascontiguousarray(dims, np.uint32)
+    dist = np.zeros((int(d[2]), int(d[1]), int(d[0])), np.float32)
+    nrm = np.zeros(dist.shape + (3,), np.float32)
+    fn(_ptr(v), len(v), _ptr(f), len(f), _ptr(o), float(dx), _ptr(d), float(max_dist), _ptr(dist), _ptr(nrm))
+    return dist, nrm

@@ -1226,3 +1226,110 @@ void orc_ts_get(void* h, int fp64, int what, void* dst) {
 }
 
 }  // extern "C"
+
+// =============================================================================
+//  Mesh signed distance grid (BoundaryMap::computeSignedDistanceField,
+//  boundary_map.cpp:351-470; PointInMeshTest::isContained,
+//  point_in_mesh_test.cpp:31-120), brute force in double precision.  The
+//  closest point is found here by projecting onto the triangle's plane when
+//  the projection falls inside the triangle, else on the nearest of the three
+//  edges; the sign is the parity of the crossings of the ray o + t (0.3137 dx,
+//  0.2718 dx, max(mesh height, dx)), t > 0, with every triangle, solved by
+//  Cramer's rule.  Nodes outside the mesh's bounding box are outside.
+// =============================================================================
+namespace {
+
+struct V3 {
+    double x, y, z;
+};
+inline V3 operator-(V3 a, V3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline V3 operator+(V3 a, V3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+inline V3 operator*(double s, V3 a) { return {s * a.x, s * a.y, s * a.z}; }
+inline double dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline V3 cross(V3 a, V3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+
+V3 closest_on_segment(V3 p, V3 a, V3 b) {
+    V3 ab = b - a;
+    double l2 = dot(ab, ab);
+    double t = l2 > 0.0 ? dot(p - a, ab) / l2 : 0.0;
+    t = std::min(1.0, std::max(0.0, t));
+    return a + t * ab;
+}
+
+V3 closest_on_triangle_oracle(V3 p, V3 a, V3 b, V3 c) {
+    V3 nrm = cross(b - a, c - a);
+    double n2 = dot(nrm, nrm);
+    if (n2 > 0.0) {
+        V3 q = p - (dot(p - a, nrm) / n2) * nrm;  // projection onto the plane
+        // inside test by the signs of the sub-triangle normals
+        double s0 = dot(cross(b - a, q - a), nrm), s1 = dot(cross(c - b, q - b), nrm),
+               s2 = dot(cross(a - c, q - c), nrm);
+        if (s0 >= 0.0 && s1 >= 0.0 && s2 >= 0.0) return q;
+    }
+    V3 best = closest_on_segment(p, a, b);
+    for (V3 cand : {closest_on_segment(p, b, c), closest_on_segment(p, c, a)})
+        if (dot(p - cand, p - cand) < dot(p - best, p - best)) best = cand;
+    return best;
+}
+
+bool ray_hits_oracle(V3 o, V3 d, V3 a, V3 b, V3 c) {
+    // o + t d = a + u (b - a) + v (c - a): 3x3 system in (t, u, v)
+    V3 e1 = b - a, e2 = c - a, r = o - a;
+    V3 m0 = {-d.x, -d.y, -d.z};
+    double det = dot(m0, cross(e1, e2));
+    if (det == 0.0) return false;
+    double t = dot(r, cross(e1, e2)) / det;
+    double u = dot(m0, cross(r, e2)) / det;
+    double v = dot(m0, cross(e1, r)) / det;
+    return t > 0.0 && u >= 0.0 && v >= 0.0 && u + v <= 1.0;
+}
+
+}  // namespace
+
+extern "C" void orc_mesh_sdf(const float* verts, int nv, const unsigned int* faces, int nf, const float* origin,
+                             float dx, const unsigned int* dims, float maxDist, float* dist, float* normal) {
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int i = 0; i < nv; i++)
+        for (int a = 0; a < 3; a++) {
+            lo[a] = std::min(lo[a], (double)verts[3 * i + a]);
+            hi[a] = std::max(hi[a], (double)verts[3 * i + a]);
+        }
+    const V3 ray = {0.3137 * dx, 0.2718 * dx, std::max(hi[2] - lo[2], (double)dx)};
+    auto vert = [&](unsigned int k) { return V3{verts[3 * k], verts[3 * k + 1], verts[3 * k + 2]}; };
+    const size_t n = (size_t)dims[0] * dims[1] * dims[2];
+    for (size_t id = 0; id < n; id++) {
+        const unsigned int i = (unsigned int)(id % dims[0]), j = (unsigned int)((id / dims[0]) % dims[1]),
+                           k = (unsigned int)(id / ((size_t)dims[0] * dims[1]));
+        const float xf[3] = {origin[0] + (float)i * dx, origin[1] + (float)j * dx, origin[2] + (float)k * dx};
+        const V3 x = {xf[0], xf[1], xf[2]};
+        double best = 1e300;
+        V3 q = {0, 0, 0};
+        for (int f = 0; f < nf; f++) {
+            V3 c = closest_on_triangle_oracle(x, vert(faces[3 * f]), vert(faces[3 * f + 1]), vert(faces[3 * f + 2]));
+            double d = std::sqrt(dot(x - c, x - c));
+            if (d < best) {
+                best = d;
+                q = c;
+            }
+        }
+        const bool band = best <= (double)maxDist;
+        bool inside = false;
+        if (x.x >= lo[0] && x.x <= hi[0] && x.y >= lo[1] && x.y <= hi[1] && x.z >= lo[2] && x.z <= hi[2]) {
+            unsigned int cnt = 0;
+            for (int f = 0; f < nf; f++)
+                cnt += ray_hits_oracle(x, ray, vert(faces[3 * f]), vert(faces[3 * f + 1]), vert(faces[3 * f + 2]));
+            inside = cnt & 1u;
+        }
+        const double mag = band ? best : (double)maxDist;
+        dist[id] = (float)(inside ? -mag : mag);
+        if (normal) {
+            for (int a = 0; a < 3; a++) normal[3 * id + a] = 0.0f;
+            if (band && best > 0.0) {
+                V3 r = (1.0 / best) * (x - q);
+                normal[3 * id] = (float)r.x;
+                normal[3 * id + 1] = (float)r.y;
+                normal[3 * id + 2] = (float)r.z;
+            }
+        }
+    }
+}
