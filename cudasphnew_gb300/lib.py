@@ -71,6 +71,7 @@ SIGNATURES = {
     "sph_sdf_save": (_i, [_vp, ctypes.c_char_p]),
     "sph_sdf_load": (_i, [ctypes.c_char_p, _vp]),
     "sph_sdf_free": (None, [_vp]),
+    "sph_surface_particles": (_i, [_vp, _vp]),
     "sph_last_error": (ctypes.c_char_p, []),
     "sph_status_string": (ctypes.c_char_p, [_i]),
 }
@@ -442,6 +443,12 @@ class ParticleSimulation:
         """Features the last learned step computed (particle order)."""
         out = np.zeros((self.n, CORRECTOR_FEATURES), np.float32)
         check(load().sph_read_features(self._h, out.ctypes.data, out.nbytes))
+        return out
+
+    def surface_particles(self) -> np.ndarray:
+        """CreateIsParticleSurfaceList: 1 for surface particles (particle order)."""
+        out = np.zeros(self.n, np.int32)
+        check(load().sph_surface_particles(self._h, out.ctypes.data))
         return out
 
     def diagnostics(self) -> Diagnostics:

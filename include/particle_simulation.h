@@ -264,12 +264,19 @@ public:
         return sim;
     }
 
-    // The reference never fills its surface list (:1819-1851); this keeps the
-    // call shape and returns all zeros.
+    // Surface particles of the state that entered the last step (:1819-1839;
+    // the reference never fills its list): fewer than nPartTresh neighbours
+    // or a neighbour centre of mass farther than cmDistanceThresh * h.  All
+    // zeros before the first step.
     static int* CreateIsParticleSurfaceList(const ParticleSimulation* sim) {
-        int* list = new int[sim->mParameters.numParticles];
-        std::memset(list, 0, sizeof(int) * sim->mParameters.numParticles);
-        std::printf("%d of %d extracted\n", 0, sim->mParameters.numParticles);
+        const unsigned int n = sim->mParameters.numParticles;
+        int* list = new int[n];
+        std::memset(list, 0, sizeof(int) * n);
+        if (sim->mHandle && sim->counts().numTimeSteps > 0)
+            check(sph_surface_particles(sim->mHandle, list), __FILE__, __LINE__);
+        int extracted = 0;
+        for (unsigned int i = 0; i < n; i++) extracted += list[i];
+        std::printf("%d of %d extracted\n", extracted, n);
         return list;
     }
 

@@ -401,6 +401,14 @@ sph_status sph_corrector_gradient(sph_handle h, const float* features, const flo
  * SPH_STEP_LEARNED step computed from the state it started from. */
 sph_status sph_read_features(sph_handle h, float* dst, size_t bytes);
 
+/* CreateIsParticleSurfaceList (particle_simulation.cu:1818-1839): flags[i] =
+ * 1 when particle i, in the state that entered the last step, has fewer
+ * than nPartTresh neighbours within compactSupport or its neighbours'
+ * centre of mass lies farther than cmDistanceThresh * compactSupport from
+ * it (the thresholds of SimulationParameters; the reference never fills its
+ * list).  int[n], particle order. */
+sph_status sph_surface_particles(sph_handle h, int* flags);
+
 /* Device pointer of a field in the handle's layout, for zero-copy consumers
  * (replaces the OpenGL VBO getters, :2278-2301): 0 = positions (float4[n],
  * particle order), 1 = velocities (float4[n]). */

@@ -337,3 +337,26 @@ def test_fp64_diagnostics(sphlib):
         abs(d.densityMaxRelError - np.abs(rho - rest).max() / rest) <= 1e-15
     # the dam break falls: the potential energy drops and kinetic energy appears
     assert d.kineticEnergy > 0.0
+
+
+def test_surface_particles(sphlib):
+    """CreateIsParticleSurfaceList: fewer than nPartTresh neighbours within h,
+    or a neighbour centre of mass farther than cmDistanceThresh * h, in the
+    state that entered the last step (brute force in float64)."""
+    sc = scenes.dam_break(12, 12, 8, (0, 0, 0), (0.5, 0.5, 0.5), 3, "surface", 1)
+    with sphlib.ParticleSimulation(sc.params, sc.positions, sc.velocities, sc.options) as sim:
+        sim.step(count=5)
+        x = sim.positions().astype(np.float64)
+        sim.Advance()
+        flags = sim.surface_particles()
+    h = float(np.float32(sc.params.compactSupport))
+    d = x[:, None, :] - x[None, :, :]
+    r2 = (d * d).sum(2)
+    nb = (r2 <= h * h) & ~np.eye(len(x), dtype=bool)
+    cnt = nb.sum(1)
+    cm = (nb[..., None] * x[None]).sum(1) / np.maximum(cnt, 1)[:, None]
+    off = np.linalg.norm(cm - x, axis=1)
+    ref = (cnt < sc.params.nPartTresh) | ((cnt > 0) & (off > sc.params.cmDistanceThresh * h))
+    # the GPU tests r^2 in float: a pair exactly at h may count differently
+    assert (flags != ref).sum() <= 2
+    assert 0 < flags.sum() < len(flags)
