@@ -43,6 +43,23 @@ inline int stride_grid(long long work, int bs) {
     return (int)(g < 1 ? 1 : (g > 4096 ? 4096 : g));
 }
 
+// The neighbour loops of the two-scale pass run over few particles (a few
+// thousand split parents, tens of thousands of children), so each particle
+// gets a group of TS_G lanes that stride through its candidates; the
+// group's partial sums are combined by a fixed shuffle tree, so results do
+// not depend on scheduling.  Groups are aligned to TS_G lanes of a warp and
+// all lanes of a group take the same branches.
+constexpr int TS_G = 8;
+
+__device__ __forceinline__ unsigned int group_mask() { return 0xFFu << (threadIdx.x & 24u); }
+
+__device__ __forceinline__ float group_sum(float v, unsigned int m) {
+    v += __shfl_xor_sync(m, v, 4);
+    v += __shfl_xor_sync(m, v, 2);
+    v += __shfl_xor_sync(m, v, 1);
+    return v;
+}
+
 // ---------------------------------------------------------------------------
 // shift_state + find_split_particles (:730-740, 932-952)
 // ---------------------------------------------------------------------------
@@ -61,8 +78,10 @@ __global__ void k_ts_state(int n, const float4* __restrict__ posS, const int* __
 // itself included, with a word-wide atomic OR.
 __global__ void k_ts_mark(int n, const float4* __restrict__ posS, const int* __restrict__ workIds,
                           const int* __restrict__ cellOffset, GridDev g, float h, TwoScaleDev T) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
+    const long long gid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) / TS_G;
+    const int lane = threadIdx.x & (TS_G - 1);
+    if (gid >= n) return;
+    const int k = (int)gid;
     const float4 xs = posS[k];
     if (!in_region(T, xs)) return;
     const Stencil st = stencil(xs, h, g);
@@ -72,7 +91,7 @@ __global__ void k_ts_mark(int n, const float4* __restrict__ posS, const int* __r
         for (int y = st.y0; y <= st.y1; y++) {
             const int row = g.dim[0] * (g.dim[1] * z + y);
             const int s = __ldg(cellOffset + row + st.x0), e = __ldg(cellOffset + row + st.x1 + 1);
-            for (int t = s; t < e; t++) {
+            for (int t = s + lane; t < e; t += TS_G) {
                 if (ref_r2(xs, __ldg(posS + t)) <= h2) {
                     const int v = workIds[t];
                     atomicOr(words + (v >> 2), 2u << (8 * (v & 3)));
@@ -276,7 +295,10 @@ __global__ void k_ts_project(const float4* __restrict__ coarsePos, const int* __
     const int nSplit = T.counts[0];
     const int nSub = T.counts[3];
     const float hs2 = __fmul_rn(hs, hs);
-    for (int idx = 8 * nSplit + blockIdx.x * blockDim.x + threadIdx.x; idx < nSub; idx += gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & (TS_G - 1);
+    const unsigned int gm = group_mask();
+    const int groups = gridDim.x * blockDim.x / TS_G;
+    for (int idx = 8 * nSplit + (blockIdx.x * blockDim.x + threadIdx.x) / TS_G; idx < nSub; idx += groups) {
         const int slot = T.subIds[idx];
         const float4 x = T.subPos[slot];
         const Stencil st = stencil(x, hs, g);
@@ -285,7 +307,7 @@ __global__ void k_ts_project(const float4* __restrict__ coarsePos, const int* __
             for (int y = st.y0; y <= st.y1; y++) {
                 const int row = g.dim[0] * (g.dim[1] * z + y);
                 const int s = __ldg(cellOffset + row + st.x0), e = __ldg(cellOffset + row + st.x1 + 1);
-                for (int t = s; t < e; t++) {
+                for (int t = s + lane; t < e; t += TS_G) {
                     const float4 xj = byId ? coarsePos[workIds[t]] : coarsePos[t];
                     if (ref_r2(x, xj) <= hs2) {
                         const float4 rj = rho4S[t];
@@ -295,7 +317,10 @@ __global__ void k_ts_project(const float4* __restrict__ coarsePos, const int* __
                     }
                 }
             }
-        T.subRho[slot] = cnt > 0.f ? make_float2(d / cnt, p / cnt) : make_float2(0.f, 0.f);
+        d = group_sum(d, gm);
+        p = group_sum(p, gm);
+        cnt = group_sum(cnt, gm);
+        if (lane == 0) T.subRho[slot] = cnt > 0.f ? make_float2(d / cnt, p / cnt) : make_float2(0.f, 0.f);
     }
 }
 
@@ -345,7 +370,10 @@ __global__ void k_ts_subrank(TwoScaleDev T) {
 // ---------------------------------------------------------------------------
 __global__ void k_ts_subdensity(GridDev g, PhysDev ph, TwoScaleDev T) {
     const int nReg = 8 * T.counts[0];
-    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < nReg; idx += gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & (TS_G - 1);
+    const unsigned int gm = group_mask();
+    const int groups = gridDim.x * blockDim.x / TS_G;
+    for (int idx = (blockIdx.x * blockDim.x + threadIdx.x) / TS_G; idx < nReg; idx += groups) {
         const int slot = T.subIds[idx];
         const float4 x = T.subPos[slot];
         const Stencil st = stencil(x, ph.h, g);
@@ -355,15 +383,16 @@ __global__ void k_ts_subdensity(GridDev g, PhysDev ph, TwoScaleDev T) {
                 const int row = g.dim[0] * (g.dim[1] * z + y);
                 const int s = __ldg(T.subOffset + row + st.x0), e = __ldg(T.subOffset + row + st.x1 + 1);
                 float rs = 0.f;
-                for (int t = s; t < e; t++) {
+                for (int t = s + lane; t < e; t += TS_G) {
                     const float r2 = dist2(x, T.subPos[T.subSortedIds[t]]);
                     const float w = fmaxf(ph.h2 - r2, 0.f);
                     rs = fmaf(w * w, w, rs);
                 }
+                rs = group_sum(rs, gm);  // every lane of the group holds the row sum
                 if (rs > 0.f) kahan_add(sum, comp, rs);
             }
         const float rho = __fsub_rn(sum, comp) * ph.poly6m;
-        T.subRho[slot] = make_float2(rho, ph.stiffness * (rho - ph.restDensity));
+        if (lane == 0) T.subRho[slot] = make_float2(rho, ph.stiffness * (rho - ph.restDensity));
     }
 }
 
@@ -374,7 +403,10 @@ __global__ void k_ts_subdensity(GridDev g, PhysDev ph, TwoScaleDev T) {
 // ---------------------------------------------------------------------------
 __global__ void k_ts_subforce(GridDev g, PhysDev ph, TwoScaleDev T) {
     const int nReg = 8 * T.counts[0];
-    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < nReg; idx += gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & (TS_G - 1);
+    const unsigned int gm = group_mask();
+    const int groups = gridDim.x * blockDim.x / TS_G;
+    for (int idx = (blockIdx.x * blockDim.x + threadIdx.x) / TS_G; idx < nReg; idx += groups) {
         const int slot = T.subIds[idx];
         const float4 xi = T.subPos[slot], vi = T.subVel[slot];
         const float2 ri = T.subRho[slot];
@@ -386,7 +418,7 @@ __global__ void k_ts_subforce(GridDev g, PhysDev ph, TwoScaleDev T) {
             for (int y = st.y0; y <= st.y1; y++) {
                 const int row = g.dim[0] * (g.dim[1] * z + y);
                 const int s = __ldg(T.subOffset + row + st.x0), e = __ldg(T.subOffset + row + st.x1 + 1);
-                for (int t = s; t < e; t++) {
+                for (int t = s + lane; t < e; t += TS_G) {
                     const int j = T.subSortedIds[t];
                     const float4 xj = T.subPos[j];
                     const float r2 = dist2(xi, xj);
@@ -413,6 +445,13 @@ __global__ void k_ts_subforce(GridDev g, PhysDev ph, TwoScaleDev T) {
                     cl = fmaf(invj * d2, 3.f * ph.h2 - 7.f * r2, cl);
                 }
             }
+        for (int a = 0; a < 3; a++) {
+            fp[a] = group_sum(fp[a], gm);
+            fv[a] = group_sum(fv[a], gm);
+            cg[a] = group_sum(cg[a], gm);
+        }
+        cl = group_sum(cl, gm);
+        if (lane != 0) continue;
         const float pc = ph.pressCoef * rhoi;
         float force[3];
         for (int a = 0; a < 3; a++) force[a] = ph.viscCoef * fv[a] + pc * fp[a];
@@ -481,7 +520,8 @@ void launch_ts_states(int n, const float4* posS, const int* workIds, const int* 
                       const TwoScaleDev& T, cudaStream_t s) {
     if (n <= 0) return;
     k_ts_state<<<(n + 255) / 256, 256, 0, s>>>(n, posS, workIds, T);
-    k_ts_mark<<<(n + 127) / 128, 128, 0, s>>>(n, posS, workIds, cellOffset, g, h, T);
+    k_ts_mark<<<(unsigned int)(((long long)n * TS_G + 255) / 256), 256, 0, s>>>(n, posS, workIds, cellOffset, g, h,
+                                                                              T);
     const int nb = (n + TS_BLOCK - 1) / TS_BLOCK;
     k_ts_count<<<nb, TS_BLOCK, 0, s>>>(n, T);
     k_ts_scan_blocks<<<1, TS_BLOCK, 0, s>>>(nb, T);
@@ -502,7 +542,8 @@ void launch_ts_merge(int n, float4* posS, float4* velS, const float4* accS, cons
 void launch_ts_project(const float4* coarsePos, const int* workIds, int byId, const float4* rho4S,
                        const int* cellOffset, GridDev g, float hs, const TwoScaleDev& T, int capacity,
                        cudaStream_t s) {
-    k_ts_project<<<stride_grid(capacity, 128), 128, 0, s>>>(coarsePos, workIds, byId, rho4S, cellOffset, g, hs, T);
+    k_ts_project<<<stride_grid((long long)capacity * TS_G, 128), 128, 0, s>>>(coarsePos, workIds, byId, rho4S,
+                                                                              cellOffset, g, hs, T);
 }
 
 void launch_ts_sub_sort(GridDev sg, const TwoScaleDev& T, SortBuffers subSb, int capacity, unsigned int* status,
@@ -514,11 +555,11 @@ void launch_ts_sub_sort(GridDev sg, const TwoScaleDev& T, SortBuffers subSb, int
 }
 
 void launch_ts_sub_density(GridDev sg, PhysDev sph, const TwoScaleDev& T, int capacity, cudaStream_t s) {
-    k_ts_subdensity<<<stride_grid(capacity, 128), 128, 0, s>>>(sg, sph, T);
+    k_ts_subdensity<<<stride_grid((long long)capacity * TS_G, 128), 128, 0, s>>>(sg, sph, T);
 }
 
 void launch_ts_sub_force(GridDev sg, PhysDev sph, const TwoScaleDev& T, int capacity, cudaStream_t s) {
-    k_ts_subforce<<<stride_grid(capacity, 128), 128, 0, s>>>(sg, sph, T);
+    k_ts_subforce<<<stride_grid((long long)capacity * TS_G, 128), 128, 0, s>>>(sg, sph, T);
 }
 
 void launch_ts_sub_integrate(PhysDev sph, const TwoScaleDev& T, int capacity, cudaStream_t s) {
