@@ -229,11 +229,12 @@ sph_status ensure_two_scale(sph_sim* s) {
 
 // Enqueues one step of `mode` (no host synchronisation).
 void enqueue_coarse(sph_sim* s, const GridDev& g, const PhysDev& ph, int collide, cudaEvent_t* ev,
-                    const FeatureOut* feat) {
+                    const FeatureOut* feat, bool force) {
     cudaStream_t st = s->stream;
     const int n = s->n;
     StepConfig cfg = s->cfg;
-    if (feat) cfg.forceVariant = FORCE_PRETESTED;  // the feature form reads the density stage's masks
+    // the feature form and the fused learned form read the density stage's masks
+    if (feat || !force) cfg.forceVariant = FORCE_PRETESTED;
     auto mark = [&](int k) {
         if (ev) cudaEventRecord(ev[k], st);
     };
@@ -249,6 +250,7 @@ void enqueue_coarse(sph_sim* s, const GridDev& g, const PhysDev& ph, int collide
     // density and forces read the sorted copies only
     launch_density(n, s->posS, rows_of(s), g, ph, s->map, s->rho4S, s->rowStart, s->rowMask, cfg, st);
     mark(ST_FORCE);
+    if (!force) return;
     launch_force(n, s->posS, s->velS, s->rho4S, s->sb.workIds, rows_of(s), g, ph, s->map, collide, s->rowStart,
                  s->rowMask, s->pos, s->vel, s->accS, cfg, st, feat);
     mark(ST_COUNT);

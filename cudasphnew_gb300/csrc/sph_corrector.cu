@@ -41,7 +41,9 @@ struct Corrector {
     float* norm = nullptr;
     float stats[NSTATS] = {};  // feature means, deviations; target means, deviations, scales
     // learned step and audit scratch
-    float* feat = nullptr;  // n x 24, particle order: the last learned step's features
+    float* feat = nullptr;  // n x 24, particle order: the last recorded learned step's features
+    bool record = false;    // learned steps write their features to `feat`
+    bool recorded = false;  // `feat` holds a learned step's features
     float4 *savePos = nullptr, *saveVel = nullptr, *lPos = nullptr, *lVel = nullptr;
     float *rhoA = nullptr, *rhoB = nullptr;
     unsigned int* errBits = nullptr;
@@ -161,10 +163,13 @@ void enqueue_learned(sph_sim* s, Corrector* C) {
     const int K = C->cfg.stride;
     GridDev g = grid_of(s);
     PhysDev ph = learned_phys(s, K);
-    const FeatureOut fo{C->feat, 1, s->O.boxCollision, ph.dt};
-    enqueue_coarse(s, g, ph, s->O.boxCollision, nullptr, &fo);
-    launch_mlp_apply(s->n, C->feat, mdev(C), 0, s->sb.workIds, s->pos, s->vel, ph, s->O.boxCollision, nullptr,
-                     s->status, s->stream);
+    enqueue_coarse(s, g, ph, s->O.boxCollision, nullptr, nullptr, false);
+    StepConfig cfg = s->cfg;
+    cfg.forceVariant = FORCE_PRETESTED;
+    const FeatureOut fo{C->record ? C->feat : nullptr, 1, s->O.boxCollision, ph.dt};
+    launch_force_learned(s->n, s->posS, s->velS, s->rho4S, s->sb.workIds, rows_of(s), g, ph, s->map,
+                         s->O.boxCollision, s->rowStart, s->rowMask, s->pos, s->vel, s->accS, cfg, fo, mdev(C),
+                         s->status, s->stream);
 }
 
 void enqueue_audit(sph_sim* s, Corrector* C) {
@@ -250,6 +255,7 @@ sph_status corrector_step(sph_sim* s, int count, bool useGraph) {
         }
         C->sinceAudit = audit ? 0 : C->sinceAudit + 1;
         C->rep.learnedSteps++;
+        C->recorded = C->recorded || C->record;
     }
     s->numTimeSteps += (unsigned int)count;
     s->stepped = true;
@@ -592,9 +598,21 @@ sph_status sph_corrector_gradient(sph_handle s, const float* features, const flo
     return latched_status(s);
 }
 
+sph_status sph_corrector_record_features(sph_handle s, int enable) {
+    if (!s) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "handle is NULL");
+    if (!s->corr || !s->corr->ready) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "no corrector is loaded");
+    Corrector* C = s->corr;
+    if (C->record != (enable != 0)) {
+        C->record = enable != 0;
+        C->valid[0] = C->valid[1] = false;  // the captured steps change
+    }
+    return SPH_OK;
+}
+
 sph_status sph_read_features(sph_handle s, float* dst, size_t bytes) {
     if (!s || !dst) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "NULL argument");
-    if (!s->corr || s->corr->rep.learnedSteps == 0) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "no learned step has run");
+    if (!s->corr || !s->corr->recorded)
+        SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "no learned step has run with feature recording on");
     const size_t need = sizeof(float) * (size_t)s->n * IN;
     if (bytes < need) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "destination too small");
     SPH_CUDA(cudaMemcpyAsync(dst, s->corr->feat, need, cudaMemcpyDeviceToHost, s->stream));

@@ -1,7 +1,7 @@
 // Internal declarations of the learned step corrector: the per-particle MLP
 // 24 -> 64 -> 64 -> 6 (SiLU) with BF16 weights and activations on tcgen05
 // tensor cores (FP32 accumulation in TMEM) and its Adam trainer.  The
-// features it reads are recorded by the force stage (write_features,
+// features it reads are computed by the force stage (feature_values,
 // sph_step.cu).  Not part of the public ABI.
 #pragma once
 
@@ -102,5 +102,14 @@ void launch_audit(int n, const float* rhoA, const float* rhoB, unsigned int* err
 void launch_audit_select(int n, const unsigned int* errBits, float tol, const float4* srcPos,
                          const float4* srcVel, float4* pos, float4* vel, unsigned int* counters,
                          cudaStream_t s);
+
+// The learned step's force stage with the MLP fused in (sph_step.cu): the
+// pretested pair loop (the density stage must have recorded the masks),
+// wall terms, integration and collision, the features, the correction and
+// one write-back; the raw features also go to feat.feat when it is set.
+void launch_force_learned(int n, const float4* posS, const float4* velS, const float4* rho4S, const int* workIds,
+                          RowTables T, GridDev g, PhysDev ph, MapDev map, int collide, const int* rowStart,
+                          const unsigned int* rowMask, float4* pos, float4* vel, float4* accS, const StepConfig& cfg,
+                          const FeatureOut& feat, MlpDev m, unsigned int* status, cudaStream_t s);
 
 }  // namespace sph

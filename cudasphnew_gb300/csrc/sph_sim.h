@@ -117,9 +117,11 @@ sph_status ensure_two_scale(sph_sim* s);
 void enqueue_step(sph_sim* s, int mode, bool timing);
 // Hash, sort, density and force + integration (+ box collision) of the
 // coarse particles with the given constants; stage events when `ev`; the
-// force stage also records the corrector's features when `feat`.
+// force stage also records the corrector's features when `feat`.  With
+// `force` false it stops after the density stage (which then records the
+// pretested neighbour masks), for a caller that runs its own force stage.
 void enqueue_coarse(sph_sim* s, const GridDev& g, const PhysDev& ph, int collide, cudaEvent_t* ev,
-                    const FeatureOut* feat = nullptr);
+                    const FeatureOut* feat = nullptr, bool force = true);
 // Hash, sort and density of the state (pos, vel) into the handle's sorted
 // copies (posS, velS, rho4S) and tables; nothing is integrated.
 void enqueue_density_only(sph_sim* s, const float4* pos, const float4* vel);

@@ -19,6 +19,7 @@
 //                the force stage runs the interactions of the set bits only
 //                (rows longer than 32 candidates fall back to testing).
 #include "sph_device.cuh"
+#include "sph_mlp_tile.cuh"
 
 namespace sph {
 
@@ -89,6 +90,23 @@ k_density(int n, const float4* __restrict__ posS, RowTables T, GridDev g_, PhysD
 // Pair interaction (compute_viscosity_pressure_forces_and_ifsurf_cell,
 // :1459-1556), per-row partial sums, compensated totals.
 // ---------------------------------------------------------------------------
+// The quantities of one pair (i, j) both the force sums and the feature
+// sums use: offset, r^2, 1/r, h - r and the velocity difference v_j - v_i.
+struct Pair {
+    float dx, dy, dz, r2, rinv, hr, ux, uy, uz;
+    __device__ __forceinline__ Pair(const PhysDev& ph, float4 xi, float4 vi, float4 xj, float4 vj) {
+        dx = __fsub_rn(xi.x, xj.x);
+        dy = __fsub_rn(xi.y, xj.y);
+        dz = __fsub_rn(xi.z, xj.z);
+        r2 = dist2(xi, xj);
+        rinv = rsqrtf(r2);
+        hr = ph.h - r2 * rinv;
+        ux = vj.x - vi.x;
+        uy = vj.y - vi.y;
+        uz = vj.z - vi.z;
+    }
+};
+
 template <bool TENSION>
 struct RowSums {
     float fp[3], fv[3], cg[3], cl;
@@ -99,59 +117,53 @@ struct RowSums {
         cl = 0.f;
         hits = 0;
     }
-    __device__ __forceinline__ void add(const PhysDev& ph, float4 xi, float4 vi, float qi, float4 xj, float4 vj,
-                                        float4 rj) {
-        const float dx = __fsub_rn(xi.x, xj.x), dy = __fsub_rn(xi.y, xj.y), dz = __fsub_rn(xi.z, xj.z);
-        const float r2 = dist2(xi, xj);
-        const float rinv = rsqrtf(r2);
-        const float hr = ph.h - r2 * rinv;
-        const float sp = (qi + rj.z) * hr * hr * rinv;  // (p_i/rho_i^2 + p_j/rho_j^2)(h-r)^2/r
-        const float sv = rj.w * hr;                     // (h-r)/rho_j
-        fp[0] = fmaf(sp, dx, fp[0]);
-        fp[1] = fmaf(sp, dy, fp[1]);
-        fp[2] = fmaf(sp, dz, fp[2]);
-        fv[0] = fmaf(sv, vj.x - vi.x, fv[0]);
-        fv[1] = fmaf(sv, vj.y - vi.y, fv[1]);
-        fv[2] = fmaf(sv, vj.z - vi.z, fv[2]);
+    __device__ __forceinline__ void add(const PhysDev& ph, const Pair& p, float qi, float4 rj) {
+        const float sp = (qi + rj.z) * p.hr * p.hr * p.rinv;  // (p_i/rho_i^2 + p_j/rho_j^2)(h-r)^2/r
+        const float sv = rj.w * p.hr;                         // (h-r)/rho_j
+        fp[0] = fmaf(sp, p.dx, fp[0]);
+        fp[1] = fmaf(sp, p.dy, fp[1]);
+        fp[2] = fmaf(sp, p.dz, fp[2]);
+        fv[0] = fmaf(sv, p.ux, fv[0]);
+        fv[1] = fmaf(sv, p.uy, fv[1]);
+        fv[2] = fmaf(sv, p.uz, fv[2]);
         if (TENSION) {
-            const float d2 = ph.h2 - r2;
+            const float d2 = ph.h2 - p.r2;
             const float sc = rj.w * d2 * d2;
-            cg[0] = fmaf(sc, dx, cg[0]);
-            cg[1] = fmaf(sc, dy, cg[1]);
-            cg[2] = fmaf(sc, dz, cg[2]);
-            cl = fmaf(rj.w * d2, 3.f * ph.h2 - 7.f * r2, cl);
+            cg[0] = fmaf(sc, p.dx, cg[0]);
+            cg[1] = fmaf(sc, p.dy, cg[1]);
+            cg[2] = fmaf(sc, p.dz, cg[2]);
+            cl = fmaf(rj.w * d2, 3.f * ph.h2 - 7.f * p.r2, cl);
         }
         hits++;
+    }
+    __device__ __forceinline__ void add(const PhysDev& ph, float4 xi, float4 vi, float qi, float4 xj, float4 vj,
+                                        float4 rj) {
+        add(ph, Pair(ph, xi, vi, xj, vj), qi, rj);
     }
 };
 
 // Neighbour sums of the learned corrector's input features (FEAT forms
-// only; the scale factors poly6*m and m*gradSpiky are applied once at the end).
+// only; the scale factors poly6*m and m*gradSpiky are applied once at the
+// end).  The neighbour count is the force sums' hit count.
 struct FeatSums {
     float shep = 0.f, m1[3] = {0.f, 0.f, 0.f}, div = 0.f, curl[3] = {0.f, 0.f, 0.f}, cg[3] = {0.f, 0.f, 0.f};
-    float cnt = 0.f;
-    __device__ __forceinline__ void add(const PhysDev& ph, float4 xi, float4 vi, float4 xj, float4 vj, float4 rj) {
-        const float dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
-        const float r2 = dist2(xi, xj);
-        const float rinv = rsqrtf(r2);
-        const float hr = ph.h - r2 * rinv;
-        const float q = ph.h2 - r2;
-        const float w = q * q * q * rj.w;          // W_ij / (poly6 m) * m/rho_j
-        const float gs = hr * hr * rinv * rj.w;    // |gradW_ij| / (m gradSpiky) * m/rho_j / r
-        const float ux = vj.x - vi.x, uy = vj.y - vi.y, uz = vj.z - vi.z;
-        const float ex = gs * dx, ey = gs * dy, ez = gs * dz;
+    int cnt = 0;
+    __device__ __forceinline__ void add(const PhysDev& ph, const Pair& p, float4 rj) {
+        const float q = ph.h2 - p.r2;
+        const float w = q * q * q * rj.w;              // W_ij / (poly6 m) * m/rho_j
+        const float gs = p.hr * p.hr * p.rinv * rj.w;  // |gradW_ij| / (m gradSpiky) * m/rho_j / r
+        const float ex = gs * p.dx, ey = gs * p.dy, ez = gs * p.dz;
         shep += w;
-        m1[0] = fmaf(w, ux, m1[0]);
-        m1[1] = fmaf(w, uy, m1[1]);
-        m1[2] = fmaf(w, uz, m1[2]);
-        div += ux * ex + uy * ey + uz * ez;
-        curl[0] += uy * ez - uz * ey;
-        curl[1] += uz * ex - ux * ez;
-        curl[2] += ux * ey - uy * ex;
+        m1[0] = fmaf(w, p.ux, m1[0]);
+        m1[1] = fmaf(w, p.uy, m1[1]);
+        m1[2] = fmaf(w, p.uz, m1[2]);
+        div += p.ux * ex + p.uy * ey + p.uz * ez;
+        curl[0] += p.uy * ez - p.uz * ey;
+        curl[1] += p.uz * ex - p.ux * ez;
+        curl[2] += p.ux * ey - p.uy * ex;
         cg[0] += ex;
         cg[1] += ey;
         cg[2] += ez;
-        cnt += 1.f;
     }
 };
 
@@ -193,12 +205,12 @@ struct ForceTotals {
 //   20-22 unit wall normal into the fluid;  23 |v| dtL/h.
 // W is poly6, gradW the spiky gradient, sums over neighbours within h of
 // the pre-step state.  No reference counterpart.
-__device__ __forceinline__ void write_features(const FeatSums& fs, const FeatOut& fo, int i, int id, float4 xi,
-                                               float4 vi, float4 ri, const float* acc, float mapDist,
-                                               const float* mapN, const PhysDev& ph) {
+__device__ __forceinline__ void feature_values(const FeatSums& fs, int boxWalls, float dtL, float4 xi, float4 vi,
+                                               float4 ri, const float* acc, float mapDist, const float* mapN,
+                                               const PhysDev& ph, float* f) {
     const float h = ph.h;
     float dw = 4.f * h, nx = 0.f, ny = 0.f, nz = 0.f;
-    if (fo.boxWalls) {
+    if (boxWalls) {
         const float c[3] = {xi.x - ph.boxCen[0], xi.y - ph.boxCen[1], xi.z - ph.boxCen[2]};
 #pragma unroll
         for (int a = 0; a < 3; a++) {
@@ -221,29 +233,52 @@ __device__ __forceinline__ void write_features(const FeatSums& fs, const FeatOut
     dw = fminf(fmaxf(dw, 0.f), 4.f * h);
     const float gInv = ph.gravity != 0.f ? 1.f / ph.gravity : 1.f;
     const float gw = -ph.pressCoef;  // m gradSpiky
-    const float kd = gw * fo.dtL;
+    const float kd = gw * dtL;
     const float vn = sqrtf(vi.x * vi.x + vi.y * vi.y + vi.z * vi.z);
-    float4* dst = reinterpret_cast<float4*>(fo.feat + (size_t)(fo.byId ? id : i) * 24);
-    dst[0] = make_float4(ri.x / ph.restDensity - 1.f, ph.poly6m * fs.shep, vi.x, vi.y);
-    dst[1] = make_float4(vi.z, acc[0] * gInv, acc[1] * gInv, acc[2] * gInv);
-    dst[2] = make_float4(ph.poly6m * fs.m1[0], ph.poly6m * fs.m1[1], ph.poly6m * fs.m1[2], kd * fs.div);
-    dst[3] = make_float4(kd * fs.curl[0], kd * fs.curl[1], kd * fs.curl[2], gw * h * fs.cg[0]);
-    dst[4] = make_float4(gw * h * fs.cg[1], gw * h * fs.cg[2], fs.cnt * (1.f / 32.f), dw / h);
-    dst[5] = make_float4(nx, ny, nz, vn * fo.dtL / h);
+    f[0] = ri.x / ph.restDensity - 1.f;
+    f[1] = ph.poly6m * fs.shep;
+    f[2] = vi.x;
+    f[3] = vi.y;
+    f[4] = vi.z;
+    f[5] = acc[0] * gInv;
+    f[6] = acc[1] * gInv;
+    f[7] = acc[2] * gInv;
+    f[8] = ph.poly6m * fs.m1[0];
+    f[9] = ph.poly6m * fs.m1[1];
+    f[10] = ph.poly6m * fs.m1[2];
+    f[11] = kd * fs.div;
+    f[12] = kd * fs.curl[0];
+    f[13] = kd * fs.curl[1];
+    f[14] = kd * fs.curl[2];
+    f[15] = gw * h * fs.cg[0];
+    f[16] = gw * h * fs.cg[1];
+    f[17] = gw * h * fs.cg[2];
+    f[18] = (float)fs.cnt * (1.f / 32.f);
+    f[19] = dw / h;
+    f[20] = nx;
+    f[21] = ny;
+    f[22] = nz;
+    f[23] = vn * dtL / h;
+}
+
+__device__ __forceinline__ void store_features(float* feat, size_t row, const float* f) {
+    float4* dst = reinterpret_cast<float4*>(feat + row * 24);
+#pragma unroll
+    for (int c = 0; c < 6; c++) dst[c] = make_float4(f[4 * c], f[4 * c + 1], f[4 * c + 2], f[4 * c + 3]);
 }
 
 // Wall terms, surface tension, a = F/rho - g, symplectic Euler, box
 // collision, and the write-back (compute_particle_acceleration_ifsurf
 // :407-473, integrate_euler :632-665, collision_handling :742-834).  The wall
 // terms follow the reference's operation order exactly.
+// Returns the new state (x, v) and the acceleration; the FEAT forms also
+// return the boundary map's wall distance and unit normal (mapDist stays as
+// given where the map is absent, mapN where the particle is beyond the
+// map's rest distance).
 template <bool KAHAN, bool TENSION, bool FEAT>
-__device__ __forceinline__ void force_epilogue(const ForceTotals<KAHAN, TENSION>& A, int i, float4 xi,
-                                               float4 vi, float4 ri, const PhysDev& ph, const MapDev& map,
-                                               int collideFlag, const int* __restrict__ workIds,
-                                               float4* __restrict__ pos, float4* __restrict__ vel,
-                                               float4* __restrict__ accS, const FeatSums& fs,
-                                               const FeatOut& fo) {
-    float mapDist = 1e30f, mapN[3] = {0.f, 0.f, 0.f};  // learned features only
+__device__ __forceinline__ void force_finish(const ForceTotals<KAHAN, TENSION>& A, float4 xi, float4 vi, float4 ri,
+                                             const PhysDev& ph, const MapDev& map, int collideFlag, float3& x,
+                                             float3& v, float* acc, float& mapDist, float* mapN) {
     const float rho = ri.x;
     const float pc = ph.pressCoef * rho;
     float force[3];
@@ -299,18 +334,37 @@ __device__ __forceinline__ void force_epilogue(const ForceTotals<KAHAN, TENSION>
             force[2] -= fc * cgz;
         }
     }
-    float acc[3] = {force[0] / rho, force[1] / rho, force[2] / rho};
+    acc[0] = force[0] / rho;
+    acc[1] = force[1] / rho;
+    acc[2] = force[2] / rho;
     acc[0] -= ph.gravityAxis == 0 ? ph.gravity : 0.f;
     acc[1] -= ph.gravityAxis == 1 ? ph.gravity : 0.f;
     acc[2] -= ph.gravityAxis == 2 ? ph.gravity : 0.f;
-    float3 v = make_float3(vi.x + ph.dt * acc[0], vi.y + ph.dt * acc[1], vi.z + ph.dt * acc[2]);
-    float3 x = make_float3(xi.x + ph.dt * v.x, xi.y + ph.dt * v.y, xi.z + ph.dt * v.z);
+    v = make_float3(vi.x + ph.dt * acc[0], vi.y + ph.dt * acc[1], vi.z + ph.dt * acc[2]);
+    x = make_float3(xi.x + ph.dt * v.x, xi.y + ph.dt * v.y, xi.z + ph.dt * v.z);
     if (collideFlag) collide(ph, x, v);
+}
+
+template <bool KAHAN, bool TENSION, bool FEAT>
+__device__ __forceinline__ void force_epilogue(const ForceTotals<KAHAN, TENSION>& A, int i, float4 xi,
+                                               float4 vi, float4 ri, const PhysDev& ph, const MapDev& map,
+                                               int collideFlag, const int* __restrict__ workIds,
+                                               float4* __restrict__ pos, float4* __restrict__ vel,
+                                               float4* __restrict__ accS, const FeatSums& fs,
+                                               const FeatOut& fo) {
+    float mapDist = 1e30f, mapN[3] = {0.f, 0.f, 0.f};  // learned features only
+    float3 x, v;
+    float acc[3];
+    force_finish<KAHAN, TENSION, FEAT>(A, xi, vi, ri, ph, map, collideFlag, x, v, acc, mapDist, mapN);
     const int id = workIds[i];
     pos[id] = make_float4(x.x, x.y, x.z, xi.w);  // .w: the scene index of batched handles
     vel[id] = make_float4(v.x, v.y, v.z, 0.f);
     accS[i] = make_float4(acc[0], acc[1], acc[2], 0.f);
-    if (FEAT) write_features(fs, fo, i, id, xi, vi, ri, acc, mapDist, mapN, ph);
+    if (FEAT) {
+        float f[24];
+        feature_values(fs, fo.boxWalls, fo.dtL, xi, vi, ri, acc, mapDist, mapN, ph, f);
+        store_features(fo.feat, (size_t)(fo.byId ? id : i), f);
+    }
 }
 
 struct ForceArgs {
@@ -335,9 +389,9 @@ struct ForceArgs {
 // Occupancy: the plain forms fit 64 registers without spilling, so four
 // 256-thread blocks share an SM (the force stage is latency bound: 210 ->
 // 150 us per million particles against two blocks); the feature and batched
-// forms need more registers.
+// forms take up to 80 registers, three blocks.
 template <bool KAHAN, bool TENSION, int FORM, bool FEAT, bool BATCH>
-__global__ void __launch_bounds__(256, FEAT ? 2 : (BATCH ? 3 : 4)) k_force(ForceArgs F) {
+__global__ void __launch_bounds__(256, FEAT ? 3 : (BATCH ? 3 : 4)) k_force(ForceArgs F) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= F.n) return;
     const float4 xi = F.posS[i];
@@ -358,8 +412,9 @@ __global__ void __launch_bounds__(256, FEAT ? 2 : (BATCH ? 3 : 4)) k_force(Force
             const float r2 = dist2(xi, xj);
             if (r2 <= h2 && r2 > 0.f) {
                 const float4 vj = __ldg(F.velS + t), rj = __ldg(F.rho4S + t);
-                R.add(ph, xi, vi, ri.z, xj, vj, rj);
-                if (FEAT) fs.add(ph, xi, vi, xj, vj, rj);
+                const Pair p(ph, xi, vi, xj, vj);
+                R.add(ph, p, ri.z, rj);
+                if (FEAT) fs.add(ph, p, rj);
             }
         }
     };
@@ -368,8 +423,9 @@ __global__ void __launch_bounds__(256, FEAT ? 2 : (BATCH ? 3 : 4)) k_force(Force
             const int t = base + __ffs(m) - 1;
             m &= m - 1u;
             const float4 xj = __ldg(F.posS + t), vj = __ldg(F.velS + t), rj = __ldg(F.rho4S + t);
-            R.add(ph, xi, vi, ri.z, xj, vj, rj);
-            if (FEAT) fs.add(ph, xi, vi, xj, vj, rj);
+            const Pair p(ph, xi, vi, xj, vj);
+            R.add(ph, p, ri.z, rj);
+            if (FEAT) fs.add(ph, p, rj);
         }
     };
 #pragma unroll
@@ -399,9 +455,154 @@ __global__ void __launch_bounds__(256, FEAT ? 2 : (BATCH ? 3 : 4)) k_force(Force
             }
         }
         A.add(R);
+        if (FEAT) fs.cnt += R.hits;
     }
     force_epilogue<KAHAN, TENSION, FEAT>(A, i, xi, vi, ri, ph, map, F.collide, F.workIds, F.pos, F.vel,
                                          F.accS, fs, F.fo);
+}
+
+// ---------------------------------------------------------------------------
+// The learned step's force stage with the corrector fused in.  The pretested
+// pair loop, wall terms, integration and collision of k_force, then the
+// 24 features of each particle go straight to shared memory as a BF16 MMA
+// operand.  The block's two 128-particle tiles run the MLP together: each
+// layer is two tcgen05.mma groups (one per tile, accumulators in TMEM
+// columns 64 * tile) behind one commit, and every warp then reads its own
+// tile's accumulator lanes.  Each particle's correction is added before its
+// single write-back.  Three blocks share an SM, so one block's MMA round
+// trips overlap the others' pair loops.  The raw features also go to
+// `fo.feat` when it is set.
+// ---------------------------------------------------------------------------
+constexpr int L_W = 0;                        // W1, W2, W3 (mlp::IMG_FWD_BYTES)
+constexpr int L_X = 16384;                    // two 128 x 32 feature tiles
+constexpr int L_H = L_X + 2 * 8192;           // two 128 x 64 hidden tiles (layer 1, then layer 2)
+constexpr int L_BIAS = L_H + 2 * 16384;
+constexpr int L_NORM = L_BIAS + 4 * mlp::NBIAS;
+constexpr int L_BAR = L_NORM + 4 * mlp::NNORM;
+constexpr int L_SMEM = L_BAR + 16;
+constexpr int L_TMEM = 128;                   // 3 blocks x 128 <= 512 columns
+constexpr int L_THREADS = 256;
+static_assert(mlp::IMG_FWD_BYTES <= L_X && L_BIAS % 16 == 0 && L_NORM % 16 == 0 && L_BAR % 8 == 0, "layout");
+static_assert(3 * (L_SMEM + 1024) <= 227 * 1024 && 3 * L_TMEM <= 512, "three blocks per SM");
+
+template <bool KAHAN, bool TENSION>
+__global__ void __launch_bounds__(L_THREADS, 3) k_force_learned(ForceArgs F, MlpDev m, unsigned int* status) {
+    using namespace mlp;
+    extern __shared__ __align__(1024) unsigned char sm[];
+    __shared__ int sOk;
+    const int t = threadIdx.x, warp = t >> 5, half = t >> 7, r = t & 127;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(sm + L_BAR);
+    uint32_t* slot = reinterpret_cast<uint32_t*>(sm + L_BAR + 8);
+    float* sBias = reinterpret_cast<float*>(sm + L_BIAS);
+    float* sNorm = reinterpret_cast<float*>(sm + L_NORM);
+    for (int k = t; k < IMG_FWD_BYTES / 16; k += L_THREADS)
+        reinterpret_cast<uint4*>(sm + L_W)[k] = reinterpret_cast<const uint4*>(m.image)[k];
+    for (int k = t; k < NBIAS; k += L_THREADS) sBias[k] = m.bias[k];
+    for (int k = t; k < NNORM; k += L_THREADS) sNorm[k] = m.norm[k];
+    if (t == 0) {
+        tc::mbar_init(bar, 1);
+        sOk = 1;
+    }
+    if (warp == 0) tc::tmem_alloc(slot, L_TMEM);
+    tc::cta_sync();
+    const uint32_t tb = *slot;
+    const int i = blockIdx.x * L_THREADS + t;
+    const bool valid = i < F.n;
+    float3 x = make_float3(0.f, 0.f, 0.f), v = x;
+    float4 xi = make_float4(0.f, 0.f, 0.f, 0.f);
+    int id = 0;
+    {
+        float f[IN];
+        if (valid) {
+            xi = F.posS[i];
+            const float4 vi = F.velS[i];
+            const float4 ri = F.rho4S[i];
+            const PhysDev& ph = F.ph;
+            ForceTotals<KAHAN, TENSION> A;
+            FeatSums fs;
+#pragma unroll
+            for (int row = 0; row < 9; row++) {
+                RowSums<TENSION> R;
+                R.clear();
+                const int sv = __ldg(F.M.start + (size_t)row * F.n + i);
+                unsigned int mk = __ldg(F.M.mask + (size_t)row * F.n + i);
+                if (sv < 0) {
+                    for (int tt = sv & 0x7fffffff; tt < (int)mk; tt++) {
+                        const float4 xj = __ldg(F.posS + tt);
+                        const float r2 = dist2(xi, xj);
+                        if (r2 <= ph.h2 && r2 > 0.f) {
+                            const float4 vj = __ldg(F.velS + tt), rj = __ldg(F.rho4S + tt);
+                            const Pair p(ph, xi, vi, xj, vj);
+                            R.add(ph, p, ri.z, rj);
+                            fs.add(ph, p, rj);
+                        }
+                    }
+                } else {
+                    while (mk) {
+                        const int tt = sv + __ffs(mk) - 1;
+                        mk &= mk - 1u;
+                        const float4 xj = __ldg(F.posS + tt), vj = __ldg(F.velS + tt), rj = __ldg(F.rho4S + tt);
+                        const Pair p(ph, xi, vi, xj, vj);
+                        R.add(ph, p, ri.z, rj);
+                        fs.add(ph, p, rj);
+                    }
+                }
+                A.add(R);
+                fs.cnt += R.hits;
+            }
+            float acc[3], mapDist = 1e30f, mapN[3] = {0.f, 0.f, 0.f};
+            force_finish<KAHAN, TENSION, true>(A, xi, vi, ri, ph, F.map, F.collide, x, v, acc, mapDist, mapN);
+            id = F.workIds[i];
+            F.accS[i] = make_float4(acc[0], acc[1], acc[2], 0.f);
+            feature_values(fs, F.fo.boxWalls, F.fo.dtL, xi, vi, ri, acc, mapDist, mapN, ph, f);
+            if (F.fo.feat) store_features(F.fo.feat, (size_t)(F.fo.byId ? id : i), f);
+        }
+        store_feature_row(sm + L_X + half * 8192, r, f, valid, sNorm);
+    }
+    const uint32_t sW = tc::smem_u32(sm + L_W);
+    const uint32_t sX = tc::smem_u32(sm + L_X), sH = tc::smem_u32(sm + L_H);
+    unsigned char* myH = sm + L_H + half * 16384;
+    const uint32_t tl = tc::tmem_at(tb, 32 * (warp & 3), 64 * half);  // this warp's lanes of its tile
+    uint32_t phase = 0;
+    do {
+        tc::cta_sync();
+        if (t == 0) {
+            tc::mma_chain(tb, sX, sW + IMG_W1, INP, HID, false);
+            tc::mma_chain(tb + 64, sX + 8192, sW + IMG_W1, INP, HID, false);
+        }
+        if (!commit_and_wait(bar, phase, &sOk, t)) break;
+        hidden_layer_out(tl, sBias, myH, r);
+        tc::cta_sync();
+        if (t == 0) {
+            tc::mma_chain(tb, sH, sW + IMG_W2, HID, HID, false);
+            tc::mma_chain(tb + 64, sH + 16384, sW + IMG_W2, HID, HID, false);
+        }
+        // once the wait returns the MMAs have read layer 1's tiles: layer 2
+        // overwrites them
+        if (!commit_and_wait(bar, phase, &sOk, t)) break;
+        hidden_layer_out(tl, sBias + HID, myH, r);
+        tc::cta_sync();
+        if (t == 0) {
+            tc::mma_chain(tb, sH, sW + IMG_W3, HID, OUTP, false);
+            tc::mma_chain(tb + 64, sH + 16384, sW + IMG_W3, HID, OUTP, false);
+        }
+        if (!commit_and_wait(bar, phase, &sOk, t)) break;
+        float y[16];
+        tc::tmem_ld16(tl, y);
+        if (valid) {
+            float c[OUT];
+            decode_correction(sNorm, sBias + 2 * HID, y, c);
+            x = make_float3(x.x + c[0], x.y + c[1], x.z + c[2]);
+            v = make_float3(v.x + c[3], v.y + c[4], v.z + c[5]);
+            if (F.collide) collide(F.ph, x, v);
+            F.pos[id] = make_float4(x.x, x.y, x.z, xi.w);
+            F.vel[id] = make_float4(v.x, v.y, v.z, 0.f);
+        }
+    } while (false);
+    tc::cta_sync();
+    if (!sOk) drain(bar, phase, t, status);
+    tc::cta_sync();
+    if (warp == 0) tc::tmem_dealloc(tb, L_TMEM);
 }
 
 // ---------------------------------------------------------------------------
@@ -476,6 +677,34 @@ void launch_force(int n, const float4* posS, const float4* velS, const float4* r
     } else {
         if (tension) force_dispatch<false, true>(F, cfg, s);
         else force_dispatch<false, false>(F, cfg, s);
+    }
+}
+
+template <bool KAHAN, bool TENSION>
+static void force_learned_dispatch(const ForceArgs& F, MlpDev m, unsigned int* status, cudaStream_t s) {
+    static bool configured = false;
+    if (!configured) {
+        cudaFuncSetAttribute(k_force_learned<KAHAN, TENSION>, cudaFuncAttributeMaxDynamicSharedMemorySize, L_SMEM);
+        configured = true;
+    }
+    k_force_learned<KAHAN, TENSION><<<(F.n + L_THREADS - 1) / L_THREADS, L_THREADS, L_SMEM, s>>>(F, m, status);
+}
+
+void launch_force_learned(int n, const float4* posS, const float4* velS, const float4* rho4S, const int* workIds,
+                          RowTables T, GridDev g, PhysDev ph, MapDev map, int collide, const int* rowStart,
+                          const unsigned int* rowMask, float4* pos, float4* vel, float4* accS, const StepConfig& cfg,
+                          const FeatureOut& feat, MlpDev m, unsigned int* status, cudaStream_t s) {
+    if (n <= 0) return;
+    const FeatOut fo{feat.feat, feat.byId, feat.boxWalls, feat.dtL};
+    ForceArgs F{n,  posS, velS, rho4S, workIds, T, g, ph, map, collide, cfg.prune,
+                RowMasks{const_cast<int*>(rowStart), const_cast<unsigned int*>(rowMask)}, pos, vel, accS, fo};
+    const bool tension = ph.tension != 0.0f;
+    if (cfg.kahan) {
+        if (tension) force_learned_dispatch<true, true>(F, m, status, s);
+        else force_learned_dispatch<true, false>(F, m, status, s);
+    } else {
+        if (tension) force_learned_dispatch<false, true>(F, m, status, s);
+        else force_learned_dispatch<false, false>(F, m, status, s);
     }
 }
 

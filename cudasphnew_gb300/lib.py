@@ -64,6 +64,7 @@ SIGNATURES = {
     "sph_corrector_predict": (_i, [_vp, _vp, _i, _vp]),
     "sph_corrector_gradient": (_i, [_vp, _vp, _vp, _i, _vp, _vp]),
     "sph_read_features": (_i, [_vp, _vp, ctypes.c_size_t]),
+    "sph_corrector_record_features": (_i, [_vp, ctypes.c_int]),
     "sph_obj_load": (_i, [ctypes.c_char_p, _vp]),
     "sph_mesh_free": (None, [_vp]),
     "sph_sdf_from_mesh": (_i, [_vp, ctypes.c_float, ctypes.c_float, ctypes.c_float, _vp]),
@@ -439,8 +440,12 @@ class ParticleSimulation:
                                             loss.ctypes.data))
         return g, float(loss[0])
 
+    def record_features(self, enable: bool = True) -> None:
+        """Learned steps also write their input features (96 bytes per particle)."""
+        check(load().sph_corrector_record_features(self._h, 1 if enable else 0))
+
     def features(self) -> np.ndarray:
-        """Features the last learned step computed (particle order)."""
+        """Features the last learned step with recording on computed (particle order)."""
         out = np.zeros((self.n, CORRECTOR_FEATURES), np.float32)
         check(load().sph_read_features(self._h, out.ctypes.data, out.nbytes))
         return out

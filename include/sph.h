@@ -397,8 +397,15 @@ sph_status sph_corrector_predict(sph_handle h, const float* features, int count,
 sph_status sph_corrector_gradient(sph_handle h, const float* features, const float* targets, int count,
                                   float* grad, float* loss);
 
+/* Feature recording (off by default): while enabled, each SPH_STEP_LEARNED
+ * step also writes its particles' input features (24 floats each) to the
+ * handle, 96 bytes per particle and step of extra device-memory writes.
+ * Needs a trained or loaded corrector.  No reference counterpart. */
+sph_status sph_corrector_record_features(sph_handle h, int enable);
+
 /* The corrector's input features (n x 24, particle order) that the last
- * SPH_STEP_LEARNED step computed from the state it started from. */
+ * SPH_STEP_LEARNED step taken with recording enabled computed from the state
+ * it started from. */
 sph_status sph_read_features(sph_handle h, float* dst, size_t bytes);
 
 /* CreateIsParticleSurfaceList (particle_simulation.cu:1818-1839): flags[i] =

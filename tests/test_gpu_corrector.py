@@ -2,10 +2,13 @@
 
 * The tensor-core MLP (predict and loss gradient) against a numpy
   restatement that rounds the same operands to BF16; the remaining differences
-  come from FP32 accumulation order and the device exponential, so the bars
-  are relative (1e-3 of the output scale, 2e-2 of each gradient block's norm).
+  come from FP32 accumulation order and the hardware tanh the SiLU is
+  evaluated with (relative error about 2^-11, which now and then moves an
+  activation across a BF16 rounding boundary), so the bars are relative
+  (4e-3 of the output scale, 2e-2 of each gradient block's norm).
 * The neighbour features (recorded by the learned step's force stage)
-  against a brute-force float64 restatement.
+  against a brute-force float64 restatement; the fused force + MLP kernel
+  against a plain long step plus the separate MLP kernel's prediction.
 * Training lowers the loss; the learned step beats the uncorrected plain step
   of the same size against the plain trajectory.
 * The audit: with tolerance 0 every audited step is rolled back to exactly the
@@ -166,7 +169,7 @@ def test_mlp_predict_matches_numpy(sphlib, count, scaled):
     mut, st = blob[NPARAM + 48:NPARAM + 54], blob[NPARAM + 54:NPARAM + 60]
     y = (encode(blob, got.astype(np.float64)) - mut) / st  # back to the network's output space
     assert np.isfinite(got).all()
-    assert np.abs(y - ref).max() <= 2e-3 * max(1.0, np.abs(ref).max())
+    assert np.abs(y - ref).max() <= 4e-3 * max(1.0, np.abs(ref).max())
     if scaled:  # and through the decoding itself
         np.testing.assert_allclose(got, decode(blob, ref), rtol=2e-2, atol=1e-9)
 
@@ -242,6 +245,9 @@ def test_features_match_numpy(sphlib):
         sim.step(count=30)
         x0, v0 = sim.positions(), sim.velocities()
         sim.load_corrector(random_blob(4), stride=4, auditInterval=0)
+        with pytest.raises(sphlib.SphError):
+            sim.features()  # nothing recorded yet
+        sim.record_features()
         sim.step(mode=sphlib.SPH_STEP_LEARNED)
         rho, acc = sim.read(sphlib.FIELD_DENSITY), sim.read(sphlib.FIELD_ACCELERATION)
         got = sim.features()
@@ -250,6 +256,36 @@ def test_features_match_numpy(sphlib):
     err = np.abs(got - ref) / scale
     assert err.max() < 1e-4, (err.max(0))
     assert np.abs(ref[:, 11:18]).max() > 0 and ref[:, 20:23].any()
+
+
+@pytest.mark.parametrize("scaled", [False, True])
+def test_learned_step_is_the_long_step_plus_the_prediction(sphlib, scaled):
+    """The fused force + MLP kernel against its definition: a plain step of
+    stride*dt from the same state, plus the corrector's prediction from the
+    recorded features (evaluated by the separate MLP kernel).  Particles the
+    correction pushes through a wall are collided a second time and left out."""
+    sc = tiny()
+    stride = 4
+    blob = scaled_blob(8) if scaled else random_blob(8)
+    with make(sphlib, sc) as sim:
+        sim.step(count=20)
+        x0, v0 = sim.positions(), sim.velocities()
+        sim.load_corrector(blob, stride=stride, auditInterval=0)
+        sim.record_features()
+        sim.step(mode=sphlib.SPH_STEP_LEARNED)
+        xl, vl = sim.positions(), sim.velocities()
+        c = sim.corrector_predict(sim.features())
+    with make(sphlib, sc, x0, v0, dt_scale=stride) as plain:
+        plain.step()
+        xp, vp = plain.positions(), plain.velocities()
+    ex, ev = xp + c[:, :3], vp + c[:, 3:]
+    p = sc.params
+    inside = (np.abs(ex - np.asarray(p.boxCen, np.float32)) < np.asarray(p.boxDim, np.float32)).all(1)
+    assert inside.mean() > 0.5 and np.abs(c).max() > 0
+    tol_x = 4 * np.spacing(np.abs(ex[inside]))
+    tol_v = 4 * np.spacing(np.abs(ev[inside]))
+    assert (np.abs(xl[inside] - ex[inside]) <= tol_x).all()
+    assert (np.abs(vl[inside] - ev[inside]) <= tol_v).all()
 
 
 def test_training_lowers_loss_and_corrects_the_long_step(sphlib):
