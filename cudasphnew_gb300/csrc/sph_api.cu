@@ -265,7 +265,9 @@ void enqueue_density_only(sph_sim* s, const float4* pos, const float4* vel) {
     launch_cell_scan(g.numCells, s->sb, s->status, st);
     launch_scatter(n, s->sb, st);
     launch_rank_gather(n, s->sb, pos, vel, g, s->posS, s->velS, st);
-    launch_density(n, s->posS, rows_of(s), g, ph, s->map, s->rho4S, s->rowStart, s->rowMask, s->cfg, st);
+    StepConfig cfg = s->cfg;
+    cfg.forceVariant = FORCE_MASK;  // no force stage follows: record no neighbour masks
+    launch_density(n, s->posS, rows_of(s), g, ph, s->map, s->rho4S, s->rowStart, s->rowMask, cfg, st);
 }
 
 void invalidate_graphs(sph_sim* s) {

@@ -44,7 +44,7 @@ struct Corrector {
     float* feat = nullptr;  // n x 24, particle order: the last recorded learned step's features
     bool record = false;    // learned steps write their features to `feat`
     bool recorded = false;  // `feat` holds a learned step's features
-    float4 *savePos = nullptr, *saveVel = nullptr, *lPos = nullptr, *lVel = nullptr;
+    float4 *lPos = nullptr, *lVel = nullptr;
     float *rhoA = nullptr, *rhoB = nullptr;
     unsigned int* errBits = nullptr;
     unsigned int* counters = nullptr;  // audits, rollbacks, last error bits, max error bits
@@ -118,8 +118,6 @@ sph_status ensure_corrector(sph_sim* s) {
     SPH_CUDA(dalloc(&C->bias, NBIAS));
     SPH_CUDA(dalloc(&C->norm, NNORM));
     SPH_CUDA(dalloc(&C->feat, n * IN));
-    SPH_CUDA(dalloc(&C->savePos, n));
-    SPH_CUDA(dalloc(&C->saveVel, n));
     SPH_CUDA(dalloc(&C->lPos, n));
     SPH_CUDA(dalloc(&C->lVel, n));
     SPH_CUDA(dalloc(&C->rhoA, n));
@@ -175,14 +173,16 @@ void enqueue_learned(sph_sim* s, Corrector* C) {
 void enqueue_audit(sph_sim* s, Corrector* C) {
     const size_t bytes = sizeof(float4) * (size_t)s->n;
     cudaStream_t q = s->stream;
-    cudaMemcpyAsync(C->savePos, s->pos, bytes, cudaMemcpyDeviceToDevice, q);
-    cudaMemcpyAsync(C->saveVel, s->vel, bytes, cudaMemcpyDeviceToDevice, q);
     enqueue_learned(s, C);
     cudaMemcpyAsync(C->lPos, s->pos, bytes, cudaMemcpyDeviceToDevice, q);
     cudaMemcpyAsync(C->lVel, s->vel, bytes, cudaMemcpyDeviceToDevice, q);
-    cudaMemcpyAsync(s->pos, C->savePos, bytes, cudaMemcpyDeviceToDevice, q);
-    cudaMemcpyAsync(s->vel, C->saveVel, bytes, cudaMemcpyDeviceToDevice, q);
-    for (int k = 0; k < C->cfg.stride; k++) enqueue_step(s, SPH_STEP_PLAIN, false);
+    // The plain solver from the same start: its first step's sort and density
+    // are the learned step's (neither depends on dt, and the sorted copies
+    // still hold the start state), so only its force stage runs; it writes
+    // every particle's new state.
+    launch_force(s->n, s->posS, s->velS, s->rho4S, s->sb.workIds, rows_of(s), grid_of(s), make_phys(s->P, s->O),
+                 s->map, s->O.boxCollision, s->rowStart, s->rowMask, s->pos, s->vel, s->accS, s->cfg, q);
+    for (int k = 1; k < C->cfg.stride; k++) enqueue_step(s, SPH_STEP_PLAIN, false);
     enqueue_density_only(s, s->pos, s->vel);
     launch_unpermute(s->n, s->sb.workIds, s->rho4S, 0, C->rhoB, 1, 0, q);
     enqueue_density_only(s, C->lPos, C->lVel);
@@ -231,7 +231,7 @@ void corrector_free(sph_sim* s) {
     if (!C) return;
     free_graphs(C);
     void* ptrs[] = {C->master, C->m1,   C->m2,   C->image,  C->bias,     C->norm,    C->feat,
-                    C->savePos, C->saveVel, C->lPos, C->lVel, C->rhoA, C->rhoB, C->errBits,
+                    C->lPos, C->lVel, C->rhoA, C->rhoB, C->errBits,
                     C->counters, C->partial};
     for (void* p : ptrs)
         if (p) cudaFree(p);

@@ -123,7 +123,8 @@ void enqueue_step(sph_sim* s, int mode, bool timing);
 void enqueue_coarse(sph_sim* s, const GridDev& g, const PhysDev& ph, int collide, cudaEvent_t* ev,
                     const FeatureOut* feat = nullptr, bool force = true);
 // Hash, sort and density of the state (pos, vel) into the handle's sorted
-// copies (posS, velS, rho4S) and tables; nothing is integrated.
+// copies (posS, velS, rho4S) and cell tables (no neighbour masks); nothing
+// is integrated.
 void enqueue_density_only(sph_sim* s, const float4* pos, const float4* vel);
 // Marks every captured step graph of the handle stale.
 void invalidate_graphs(sph_sim* s);
