@@ -77,7 +77,7 @@ __global__ void __launch_bounds__(TILE, 1)
     float* sNorm = reinterpret_cast<float*>(sm + A_NORM);
     for (int i = t; i < IMG_FWD_BYTES / 16; i += TILE)
         reinterpret_cast<uint4*>(sm + A_W)[i] = reinterpret_cast<const uint4*>(m.image)[i];
-    for (int i = t; i < NBIAS; i += TILE) sBias[i] = m.bias[i];
+    for (int i = t; i < NBIAS; i += TILE) sBias[i] = epilogue_bias(m.bias, i);
     for (int i = t; i < NNORM; i += TILE) sNorm[i] = m.norm[i];
     if (t == 0) {
         mbar_init(bar, 1);

@@ -114,26 +114,34 @@ __device__ __forceinline__ void drain(uint64_t* bar, uint32_t phase, int t, unsi
     }
 }
 
+// Layer-1 and layer-2 biases as the epilogue below takes them: halved
+// (the SiLU works on h = z/2, and 0.5 v + 0.5 b rounds to exactly half of
+// v + b), the output bias as it is.
+__device__ __forceinline__ float epilogue_bias(const float* bias, int k) {
+    return k < 2 * HID ? 0.5f * bias[k] : bias[k];
+}
+
 // bias + SiLU of the 64 accumulator columns at TMEM address `acc` (this
 // warp's 32 lanes, from its first column), stored as BF16 row r of `dst`
-// (K = 64); `bias` is 16-byte aligned.
-__device__ __forceinline__ void hidden_layer_out(uint32_t acc, const float* bias, unsigned char* dst, int r) {
+// (K = 64); `hbias` holds the halved biases (epilogue_bias), 16-byte aligned.
+// Equal, bit for bit, to silu(acc + bias).
+__device__ __forceinline__ void hidden_layer_out(uint32_t acc, const float* hbias, unsigned char* dst, int r) {
 #pragma unroll 1
-    for (int q = 0; q < 4; q++) {
-        float v[16];
-        tc::tmem_ld16(acc + 16 * q, v);
+    for (int q = 0; q < 2; q++) {
+        float v[32];
+        tc::tmem_ld32(acc + 32 * q, v);
 #pragma unroll
-        for (int c = 0; c < 4; c++) {
-            const float4 b = reinterpret_cast<const float4*>(bias + 16 * q)[c];
-            const float z0 = v[4 * c] + b.x, z1 = v[4 * c + 1] + b.y;
-            const float z2 = v[4 * c + 2] + b.z, z3 = v[4 * c + 3] + b.w;
-            v[4 * c] = silu(z0);
-            v[4 * c + 1] = silu(z1);
-            v[4 * c + 2] = silu(z2);
-            v[4 * c + 3] = silu(z3);
+        for (int c = 0; c < 8; c++) {
+            const float4 b = reinterpret_cast<const float4*>(hbias + 32 * q)[c];
+            const float h0 = fmaf(0.5f, v[4 * c], b.x), h1 = fmaf(0.5f, v[4 * c + 1], b.y);
+            const float h2 = fmaf(0.5f, v[4 * c + 2], b.z), h3 = fmaf(0.5f, v[4 * c + 3], b.w);
+            v[4 * c] = fmaf(h0, tanh_fast(h0), h0);
+            v[4 * c + 1] = fmaf(h1, tanh_fast(h1), h1);
+            v[4 * c + 2] = fmaf(h2, tanh_fast(h2), h2);
+            v[4 * c + 3] = fmaf(h3, tanh_fast(h3), h3);
         }
-        store_row8(dst, r, 16 * q, HID, v);
-        store_row8(dst, r, 16 * q + 8, HID, v + 8);
+#pragma unroll
+        for (int c = 0; c < 4; c++) store_row8(dst, r, 32 * q + 8 * c, HID, v + 8 * c);
     }
 }
 

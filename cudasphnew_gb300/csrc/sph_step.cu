@@ -473,16 +473,20 @@ __global__ void __launch_bounds__(256, FEAT ? 3 : (BATCH ? 3 : 4)) k_force(Force
 // trips overlap the others' pair loops.  The raw features also go to
 // `fo.feat` when it is set.
 // ---------------------------------------------------------------------------
+// Shared memory is kept small: the pair loop's neighbour gathers live on
+// the L1 cache, which shares the SM's 256 KB with it.  The operand region
+// holds the two feature tiles until layer 1's MMAs have read them, then the
+// two hidden tiles of layer 1, then those of layer 2.
 constexpr int L_W = 0;                        // W1, W2, W3 (mlp::IMG_FWD_BYTES)
-constexpr int L_X = 16384;                    // two 128 x 32 feature tiles
-constexpr int L_H = L_X + 2 * 8192;           // two 128 x 64 hidden tiles (layer 1, then layer 2)
+constexpr int L_X = mlp::IMG_FWD_BYTES;       // operand region: two 128 x 32 feature tiles, ...
+constexpr int L_H = L_X;                      // ... later two 128 x 64 hidden tiles
 constexpr int L_BIAS = L_H + 2 * 16384;
 constexpr int L_NORM = L_BIAS + 4 * mlp::NBIAS;
 constexpr int L_BAR = L_NORM + 4 * mlp::NNORM;
 constexpr int L_SMEM = L_BAR + 16;
 constexpr int L_TMEM = 128;                   // 3 blocks x 128 <= 512 columns
 constexpr int L_THREADS = 256;
-static_assert(mlp::IMG_FWD_BYTES <= L_X && L_BIAS % 16 == 0 && L_NORM % 16 == 0 && L_BAR % 8 == 0, "layout");
+static_assert(L_X % 1024 == 0 && L_BIAS % 16 == 0 && L_NORM % 16 == 0 && L_BAR % 8 == 0, "layout");
 static_assert(3 * (L_SMEM + 1024) <= 227 * 1024 && 3 * L_TMEM <= 512, "three blocks per SM");
 
 template <bool KAHAN, bool TENSION>
@@ -497,7 +501,7 @@ __global__ void __launch_bounds__(L_THREADS, 3) k_force_learned(ForceArgs F, Mlp
     float* sNorm = reinterpret_cast<float*>(sm + L_NORM);
     for (int k = t; k < IMG_FWD_BYTES / 16; k += L_THREADS)
         reinterpret_cast<uint4*>(sm + L_W)[k] = reinterpret_cast<const uint4*>(m.image)[k];
-    for (int k = t; k < NBIAS; k += L_THREADS) sBias[k] = m.bias[k];
+    for (int k = t; k < NBIAS; k += L_THREADS) sBias[k] = epilogue_bias(m.bias, k);
     for (int k = t; k < NNORM; k += L_THREADS) sNorm[k] = m.norm[k];
     if (t == 0) {
         tc::mbar_init(bar, 1);
