@@ -152,18 +152,17 @@ struct FeatSums {
         const float q = ph.h2 - p.r2;
         const float w = q * q * q * rj.w;              // W_ij / (poly6 m) * m/rho_j
         const float gs = p.hr * p.hr * p.rinv * rj.w;  // |gradW_ij| / (m gradSpiky) * m/rho_j / r
-        const float ex = gs * p.dx, ey = gs * p.dy, ez = gs * p.dz;
         shep += w;
         m1[0] = fmaf(w, p.ux, m1[0]);
         m1[1] = fmaf(w, p.uy, m1[1]);
         m1[2] = fmaf(w, p.uz, m1[2]);
-        div += p.ux * ex + p.uy * ey + p.uz * ez;
-        curl[0] += p.uy * ez - p.uz * ey;
-        curl[1] += p.uz * ex - p.ux * ez;
-        curl[2] += p.ux * ey - p.uy * ex;
-        cg[0] += ex;
-        cg[1] += ey;
-        cg[2] += ez;
+        cg[0] = fmaf(gs, p.dx, cg[0]);
+        cg[1] = fmaf(gs, p.dy, cg[1]);
+        cg[2] = fmaf(gs, p.dz, cg[2]);
+        div = fmaf(gs, p.ux * p.dx + p.uy * p.dy + p.uz * p.dz, div);   // u . d
+        curl[0] = fmaf(gs, p.uy * p.dz - p.uz * p.dy, curl[0]);        // u x d
+        curl[1] = fmaf(gs, p.uz * p.dx - p.ux * p.dz, curl[1]);
+        curl[2] = fmaf(gs, p.ux * p.dy - p.uy * p.dx, curl[2]);
     }
 };
 
@@ -469,7 +468,7 @@ __global__ void __launch_bounds__(256, FEAT ? 3 : (BATCH ? 3 : 4)) k_force(Force
 // layer is two tcgen05.mma groups (one per tile, accumulators in TMEM
 // columns 64 * tile) behind one commit, and every warp then reads its own
 // tile's accumulator lanes.  Each particle's correction is added before its
-// single write-back.  Three blocks share an SM, so one block's MMA round
+// single write-back.  Four blocks share an SM, so one block's MMA round
 // trips overlap the others' pair loops.  The raw features also go to
 // `fo.feat` when it is set.
 // ---------------------------------------------------------------------------
@@ -484,13 +483,16 @@ constexpr int L_BIAS = L_H + 2 * 16384;
 constexpr int L_NORM = L_BIAS + 4 * mlp::NBIAS;
 constexpr int L_BAR = L_NORM + 4 * mlp::NNORM;
 constexpr int L_SMEM = L_BAR + 16;
-constexpr int L_TMEM = 128;                   // 3 blocks x 128 <= 512 columns
+constexpr int L_TMEM = 128;                   // 4 blocks x 128 = 512 columns
 constexpr int L_THREADS = 256;
+// Four resident blocks (64 registers, a few spilled in the epilogue) beat
+// three at 80 registers: the pair loop is latency bound.
+constexpr int L_BLOCKS = 4;
 static_assert(L_X % 1024 == 0 && L_BIAS % 16 == 0 && L_NORM % 16 == 0 && L_BAR % 8 == 0, "layout");
-static_assert(3 * (L_SMEM + 1024) <= 227 * 1024 && 3 * L_TMEM <= 512, "three blocks per SM");
+static_assert(L_BLOCKS * (L_SMEM + 1024) <= 227 * 1024 && L_BLOCKS * L_TMEM <= 512, "resident blocks per SM");
 
 template <bool KAHAN, bool TENSION>
-__global__ void __launch_bounds__(L_THREADS, 3) k_force_learned(ForceArgs F, MlpDev m, unsigned int* status) {
+__global__ void __launch_bounds__(L_THREADS, L_BLOCKS) k_force_learned(ForceArgs F, MlpDev m, unsigned int* status) {
     using namespace mlp;
     extern __shared__ __align__(1024) unsigned char sm[];
     __shared__ int sOk;
