@@ -468,8 +468,8 @@ __global__ void __launch_bounds__(256, FEAT ? 3 : (BATCH ? 3 : 4)) k_force(Force
 // layer is two tcgen05.mma groups (one per tile, accumulators in TMEM
 // columns 64 * tile) behind one commit, and every warp then reads its own
 // tile's accumulator lanes.  Each particle's correction is added before its
-// single write-back.  Four blocks share an SM, so one block's MMA round
-// trips overlap the others' pair loops.  The raw features also go to
+// single write-back.  Three or four blocks share an SM, so one block's MMA
+// round trips overlap the others' pair loops.  The raw features also go to
 // `fo.feat` when it is set.
 // ---------------------------------------------------------------------------
 // Shared memory is kept small: the pair loop's neighbour gathers live on
@@ -485,14 +485,16 @@ constexpr int L_BAR = L_NORM + 4 * mlp::NNORM;
 constexpr int L_SMEM = L_BAR + 16;
 constexpr int L_TMEM = 128;                   // 4 blocks x 128 = 512 columns
 constexpr int L_THREADS = 256;
-// Four resident blocks (64 registers, a few spilled in the epilogue) beat
-// three at 80 registers: the pair loop is latency bound.
-constexpr int L_BLOCKS = 4;
+// Resident blocks per SM: four (64 registers, a few spilled) when the grid
+// fills the GPU several times over, the pair loop being latency bound; three
+// (80 registers, no spills) for small grids, where per-thread latency counts.
+constexpr int L_BLOCKS_MAX = 4;
 static_assert(L_X % 1024 == 0 && L_BIAS % 16 == 0 && L_NORM % 16 == 0 && L_BAR % 8 == 0, "layout");
-static_assert(L_BLOCKS * (L_SMEM + 1024) <= 227 * 1024 && L_BLOCKS * L_TMEM <= 512, "resident blocks per SM");
+static_assert(L_BLOCKS_MAX * (L_SMEM + 1024) <= 227 * 1024 && L_BLOCKS_MAX * L_TMEM <= 512,
+              "resident blocks per SM");
 
-template <bool KAHAN, bool TENSION>
-__global__ void __launch_bounds__(L_THREADS, L_BLOCKS) k_force_learned(ForceArgs F, MlpDev m, unsigned int* status) {
+template <bool KAHAN, bool TENSION, int BLOCKS>
+__global__ void __launch_bounds__(L_THREADS, BLOCKS) k_force_learned(ForceArgs F, MlpDev m, unsigned int* status) {
     using namespace mlp;
     extern __shared__ __align__(1024) unsigned char sm[];
     __shared__ int sOk;
@@ -686,14 +688,30 @@ void launch_force(int n, const float4* posS, const float4* velS, const float4* r
     }
 }
 
-template <bool KAHAN, bool TENSION>
-static void force_learned_dispatch(const ForceArgs& F, MlpDev m, unsigned int* status, cudaStream_t s) {
+template <bool KAHAN, bool TENSION, int BLOCKS>
+static void force_learned_launch(const ForceArgs& F, MlpDev m, unsigned int* status, cudaStream_t s) {
     static bool configured = false;
     if (!configured) {
-        cudaFuncSetAttribute(k_force_learned<KAHAN, TENSION>, cudaFuncAttributeMaxDynamicSharedMemorySize, L_SMEM);
+        cudaFuncSetAttribute(k_force_learned<KAHAN, TENSION, BLOCKS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             L_SMEM);
         configured = true;
     }
-    k_force_learned<KAHAN, TENSION><<<(F.n + L_THREADS - 1) / L_THREADS, L_THREADS, L_SMEM, s>>>(F, m, status);
+    k_force_learned<KAHAN, TENSION, BLOCKS><<<(F.n + L_THREADS - 1) / L_THREADS, L_THREADS, L_SMEM, s>>>(F, m,
+                                                                                                       status);
+}
+
+template <bool KAHAN, bool TENSION>
+static void force_learned_dispatch(const ForceArgs& F, MlpDev m, unsigned int* status, cudaStream_t s) {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
+    }
+    const long long blocks = (F.n + L_THREADS - 1) / L_THREADS;
+    if (blocks >= 2LL * L_BLOCKS_MAX * sms) force_learned_launch<KAHAN, TENSION, L_BLOCKS_MAX>(F, m, status, s);
+    else force_learned_launch<KAHAN, TENSION, 3>(F, m, status, s);
 }
 
 void launch_force_learned(int n, const float4* posS, const float4* velS, const float4* rho4S, const int* workIds,
