@@ -6,6 +6,7 @@ boundary map.  A "step" is one plain SPH step of that scene (hash, sort, cell
 table, density, forces + wall terms + integration + box collision).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+  python bench.py --leg batched|learned_1m --steps K     (one leg alone, for profiling)
 
 --impl reference times the reference algorithm on the host cores (the oracle's
 FP32 restatement: the reference itself does not build here) on the same scene.
@@ -52,6 +53,10 @@ def parse():
                     help="skip the 64-scene batched leg and the two-scale leg")
     ap.add_argument("--no-learned", action="store_true",
                     help="skip the learned-corrector legs (16,384-particle scene and the 1M scene)")
+    ap.add_argument("--leg", choices=["batched", "learned_1m"], default=None,
+                    help="run only this leg (batched: the 64-scene batch; learned_1m: train the corrector on the "
+                         "16,384-particle scene, then the learned leg of the 1M scene) and print its JSON object; "
+                         "for profiling")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the library's default launch shapes (for profiling runs)")
     return ap.parse_args()
@@ -352,6 +357,18 @@ def learned_leg(lib, torch, stream):
             "l2": "not flushed: the 16,384-particle state (~3 MB) stays L2-resident in use"}, cfg, model
 
 
+def train_corrector_16k(lib, stream):
+    """The learned leg's corrector alone: trained on 2,000 plain steps of the
+    16,384-particle scene (the same configuration as learned_leg)."""
+    from cudasphnew_gb300 import scenes
+    sc = scenes.config1()
+    cfg = lib.CorrectorConfig.default(trainSteps=2000, stride=4, auditInterval=16, densityTolerance=0.01)
+    with lib.ParticleSimulation(sc.params, sc.positions, sc.velocities, sc.options, sc.boundary) as sim:
+        sim.set_stream(stream.cuda_stream)
+        sim.train_corrector(cfg)
+        return sim.save_corrector(), cfg
+
+
 def learned_leg_1m(lib, torch, stream, model, cfg, sc, steps):
     """The corrector trained on the 16,384-particle scene, run on the 1M obstacle
     scene: `steps` plain steps against steps/4 learned steps from the same start;
@@ -472,6 +489,15 @@ def run_ours(args):
     sc = make_scene(args.config)
     n = sc.n
     stream = torch.cuda.Stream()
+    if args.leg is not None:
+        if rank == 0:
+            if args.leg == "batched":
+                res = batched_leg(lib, torch, stream, steps=args.steps)
+            else:
+                model, lcfg = train_corrector_16k(lib, stream)
+                res = learned_leg_1m(lib, torch, stream, model, lcfg, sc, args.steps)
+            print(json.dumps({"leg": args.leg, **res}), flush=True)
+        return
     sim = lib.ParticleSimulation(sc.params, sc.positions, sc.velocities, sc.options, sc.boundary)
     sim.set_stream(stream.cuda_stream)
 
