@@ -148,7 +148,7 @@ void launch_density(int n, const float4* posS, RowTables T, GridDev g, PhysDev p
                     float4* rho4S, int* rowStart, unsigned int* rowMask, const StepConfig& cfg,
                     cudaStream_t s);
 // Learned-step features recorded by the force stage (24 floats per particle
-// at index workIds[i] when byId, else i; see write_features in sph_step.cu).
+// at index workIds[i] when byId, else i; see feature_values in sph_step.cu).
 struct FeatureOut {
     float* feat;
     int byId;
