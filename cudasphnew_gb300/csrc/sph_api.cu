@@ -55,6 +55,7 @@ GridDev make_grid(const SimulationParameters& P, bool sub) {
     g.spacing = sub ? P.gridSpacingSubParticles : P.gridSpacing;
     g.numCells = g.dim[0] * g.dim[1] * g.dim[2];
     g.cellBase = 0;
+    g.rel = 0;
     return g;
 }
 
@@ -102,6 +103,11 @@ sph_status validate_params(const SimulationParameters* P, const sph_options* O) 
     if (O && (O->gravityAxis < 0 || O->gravityAxis > 2))
         SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "gravityAxis must be 0, 1 or 2");
     if (O && (O->childMode < 0 || O->childMode > 1)) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "childMode must be 0 or 1");
+    if (O && (O->cellRelative < 0 || O->cellRelative > 1))
+        SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "cellRelative must be 0 or 1");
+    if (O && O->cellRelative &&
+        (P->gridDim[0] > REL_MAX_X || P->gridDim[1] > REL_MAX_Y || P->gridDim[2] > REL_MAX_Z))
+        SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "cellRelative needs gridDim of at most 2048 x 2048 x 1024");
     return SPH_OK;
 }
 
@@ -388,6 +394,7 @@ MapDev map_of(const sph_boundary_desc& d, const unsigned int dims[3], const floa
 GridDev grid_of(const sph_sim* s) {
     GridDev g = make_grid(s->P, false);
     g.numCells = (int)s->numCellsTotal;
+    g.rel = s->O.cellRelative;
     return g;
 }
 
@@ -513,6 +520,7 @@ sph_status sph_create(const SimulationParameters* params, const sph_options* opt
     CREATE_CUDA(cudaMemcpyAsync(s->staging, vertexData, sizeof(float) * 3 * (size_t)n,
                                 cudaMemcpyHostToDevice, s->stream));
     launch_unpack_aos(s->staging, 3, 0, n, s->pos, s->stream);
+    if (s->O.cellRelative) launch_abs_to_rel(n, s->pos, grid_of(s), s->stream);
     if (simulationData) {
         CREATE_CUDA(cudaStreamSynchronize(s->stream));
         CREATE_CUDA(cudaMemcpyAsync(s->staging, simulationData, sizeof(float) * 10 * (size_t)n,
@@ -556,6 +564,24 @@ sph_status sph_bind(sph_handle s, const SimulationParameters* params) {
         if (params->gridDim[a] != s->P.gridDim[a] ||
             params->gridDimSubParticles[a] != s->P.gridDimSubParticles[a])
             SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "grid dimensions cannot change after Init");
+    if (s->O.cellRelative) {
+        // positions are relative to the grid: carry them over to the new one
+        SPH_CUDA(cudaStreamSynchronize(s->stream));
+        float4* tmp = nullptr;
+        SPH_CUDA(dalloc(&tmp, (size_t)s->n));
+        GridDev g0 = grid_of(s);
+        SimulationParameters keep = s->P;
+        s->P = *params;
+        GridDev g1 = grid_of(s);
+        s->P = keep;
+        launch_rel_to_abs(s->n, s->pos, g0, nullptr, 0, tmp, s->stream);
+        launch_abs_to_rel(s->n, tmp, g1, s->stream);
+        cudaError_t e = cudaMemcpyAsync(s->pos, tmp, sizeof(float4) * (size_t)s->n, cudaMemcpyDeviceToDevice,
+                                        s->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+        cudaFree(tmp);
+        SPH_CUDA(e);
+    }
     s->P = *params;
     invalidate_graphs(s);
     return SPH_OK;
@@ -574,6 +600,8 @@ sph_status sph_step(sph_handle s, int mode) {
     if (mode < SPH_STEP_PLAIN || mode > SPH_STEP_LEARNED) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "unknown step mode");
     if (s->numScenes > 1 && mode != SPH_STEP_PLAIN)
         SPH_FAIL(SPH_ERR_NOT_SUPPORTED, "batched handles take plain steps only");
+    if (s->O.cellRelative && mode != SPH_STEP_PLAIN)
+        SPH_FAIL(SPH_ERR_NOT_SUPPORTED, "cell-relative positions take plain steps only");
     if (mode == SPH_STEP_LEARNED) return corrector_step(s, 1, false);
     if (mode != SPH_STEP_PLAIN) {
         sph_status st = ensure_two_scale(s);
@@ -594,6 +622,8 @@ sph_status sph_step_many(sph_handle s, int mode, int count) {
     if (count <= 0) return SPH_OK;
     if (s->numScenes > 1 && mode != SPH_STEP_PLAIN)
         SPH_FAIL(SPH_ERR_NOT_SUPPORTED, "batched handles take plain steps only");
+    if (s->O.cellRelative && mode != SPH_STEP_PLAIN)
+        SPH_FAIL(SPH_ERR_NOT_SUPPORTED, "cell-relative positions take plain steps only");
     if (mode == SPH_STEP_LEARNED) return corrector_step(s, count, true);
     if (mode != SPH_STEP_PLAIN) {
         sph_status st = ensure_two_scale(s);
@@ -720,7 +750,10 @@ sph_status sph_read(sph_handle s, int field, void* dst, size_t bytes) {
     if (st) return st;
     cudaStream_t q = s->stream;
     switch (field) {
-        case SPH_FIELD_VERTEX_DATA: launch_pack_aos(s->pos, n, s->staging, 3, 0, q); break;
+        case SPH_FIELD_VERTEX_DATA:
+            if (s->O.cellRelative) launch_rel_to_abs(n, s->pos, grid_of(s), s->staging, 3, nullptr, q);
+            else launch_pack_aos(s->pos, n, s->staging, 3, 0, q);
+            break;
         case SPH_FIELD_VELOCITY: launch_pack_aos(s->vel, n, s->staging, 3, 0, q); break;
         case SPH_FIELD_ACCELERATION:
             if (s->stepped) launch_unpermute(n, s->sb.workIds, s->accS, -1, s->staging, 3, 0, q);
@@ -766,6 +799,7 @@ sph_status sph_write(sph_handle s, int field, const void* src, size_t bytes) {
             if (bytes < sizeof(float) * 3 * (size_t)n) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "source too small");
             SPH_CUDA(cudaMemcpyAsync(s->staging, src, sizeof(float) * 3 * (size_t)n, cudaMemcpyHostToDevice, q));
             launch_unpack_aos(s->staging, 3, 0, n, field == SPH_FIELD_VERTEX_DATA ? s->pos : s->vel, q);
+            if (field == SPH_FIELD_VERTEX_DATA && s->O.cellRelative) launch_abs_to_rel(n, s->pos, grid_of(s), q);
             if (field == SPH_FIELD_VERTEX_DATA && s->numScenes > 1)  // restore the scene index lanes
                 for (int k = 0; k < s->numScenes; k++)
                     launch_set_scene(s->pos + s->sceneStart[k], (int)(s->sceneStart[k + 1] - s->sceneStart[k]), k, q);
@@ -872,7 +906,12 @@ sph_status sph_get_diagnostics(sph_handle s, sph_diagnostics* out) {
     const int rows = diag_partial_rows();
     if (!s->diagBuf) SPH_CUDA(dalloc(&s->diagBuf, (size_t)(rows + 1) * DIAG_TERMS));
     double* res = s->diagBuf + (size_t)rows * DIAG_TERMS;
-    launch_diagnostics(s->n, s->pos, s->vel, s->rho4S, s->stepped ? 1 : 0, (double)s->P.particleMass,
+    const float4* posAbs = s->pos;
+    if (s->O.cellRelative) {  // the potential energy needs absolute heights: staging holds 10n floats
+        launch_rel_to_abs(s->n, s->pos, grid_of(s), nullptr, 0, reinterpret_cast<float4*>(s->staging), s->stream);
+        posAbs = reinterpret_cast<const float4*>(s->staging);
+    }
+    launch_diagnostics(s->n, posAbs, s->vel, s->rho4S, s->stepped ? 1 : 0, (double)s->P.particleMass,
                        (double)s->P.gravity, (double)s->P.restDensity, s->O.gravityAxis, s->diagBuf, res,
                        s->stream);
     SPH_CUDA(cudaGetLastError());
@@ -893,6 +932,8 @@ sph_status sph_get_diagnostics(sph_handle s, sph_diagnostics* out) {
 
 sph_status sph_device_pointer(sph_handle s, int which, void** devicePtr) {
     if (!s || !devicePtr) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (which == 0 && s->O.cellRelative)
+        SPH_FAIL(SPH_ERR_NOT_SUPPORTED, "cell-relative positions are not absolute float4s: use sph_read");
     if (which == 0) *devicePtr = s->pos;
     else if (which == 1) *devicePtr = s->vel;
     else SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "unknown device field");

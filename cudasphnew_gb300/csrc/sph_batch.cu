@@ -31,6 +31,7 @@ sph_status sph_create_batch(const sph_scene* scenes, int numScenes, const sph_op
     sph_options O;
     if (opts) O = *opts;
     else sph_default_options(&O);
+    if (O.cellRelative) SPH_FAIL(SPH_ERR_NOT_SUPPORTED, "batched handles keep absolute positions");
     long long n = 0, C = 0;
     size_t mapNodes = 0;
     float tension = 0.0f;

@@ -284,6 +284,7 @@ sph_status sph_corrector_train(sph_handle s, const sph_corrector_config* cfg) {
     sph_status st = check_config(cfg);
     if (st) return st;
     if (cfg->trainSteps < cfg->stride) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "trainSteps must be >= stride");
+    if (s->O.cellRelative) SPH_FAIL(SPH_ERR_NOT_SUPPORTED, "the corrector takes absolute positions");
     if (cfg->epochs < 1 || cfg->batchTiles < 1) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "epochs and batchTiles >= 1");
     if (!(cfg->learningRate > 0.0f)) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "learningRate must be positive");
     st = ensure_corrector(s);
@@ -489,6 +490,7 @@ sph_status sph_corrector_load(sph_handle s, const sph_corrector_config* cfg, con
     sph_status st = check_config(cfg);
     if (st) return st;
     if (count < (size_t)SPH_CORRECTOR_FLOATS) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "model blob too small");
+    if (s->O.cellRelative) SPH_FAIL(SPH_ERR_NOT_SUPPORTED, "the corrector takes absolute positions");
     st = ensure_corrector(s);
     if (st) return st;
     Corrector* C = s->corr;

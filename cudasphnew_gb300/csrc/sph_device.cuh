@@ -193,6 +193,115 @@ __device__ __forceinline__ void row_range(float4 xi, const Stencil& st, float h,
     if (e < s) e = s;
 }
 
+// ---------------------------------------------------------------------------
+// Cell-relative positions (sph_options.cellRelative): .xyz is the offset from
+// the low corner of the particle's cell, .w carries the cell's integer
+// coordinates packed 11:11:10 bits (x lowest).  A neighbour in a cell dc
+// cells away sits at rel_j + dc * spacing in i's frame; every pair offset is
+// then a difference of numbers no larger than two cells, whatever the
+// distance from the grid origin.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int3 rel_cell(float4 p) {
+    const unsigned int u = __float_as_uint(p.w);
+    return make_int3((int)(u & 0x7ffu), (int)((u >> 11) & 0x7ffu), (int)(u >> 22));
+}
+
+__device__ __forceinline__ float rel_pack(int cx, int cy, int cz) {
+    return __uint_as_float((unsigned int)cx | ((unsigned int)cy << 11) | ((unsigned int)cz << 22));
+}
+
+__device__ __forceinline__ int rel_cx(float w) { return (int)(__float_as_uint(w) & 0x7ffu); }
+
+// The absolute FP32 position origin + c * spacing + rel, summed in FP64 and
+// rounded once (for the boundary maps, the wall box and read-back): a
+// position converted in with rel_from_abs comes back bit for bit.
+__device__ __forceinline__ float4 rel_abs(float4 p, int3 c, const GridDev& g) {
+    const double s = (double)g.spacing;
+    return make_float4((float)((double)g.origin[0] + (double)c.x * s + (double)p.x),
+                       (float)((double)g.origin[1] + (double)c.y * s + (double)p.y),
+                       (float)((double)g.origin[2] + (double)c.z * s + (double)p.z), 0.f);
+}
+
+// Neighbour j (cell-relative, in its own cell) in i's frame: y and z cell
+// offsets are those of the stencil row (dyo, dzo already times spacing), the
+// x offset is read from j's packed cell.
+__device__ __forceinline__ float4 rel_in_frame(float4 pj, int cxi, float dyo, float dzo, float spacing) {
+    return make_float4(fmaf((float)(rel_cx(pj.w) - cxi), spacing, pj.x), pj.y + dyo, pj.z + dzo, 0.f);
+}
+
+// An absolute position's cell (the reference hash's coordinates, clamped to
+// the grid) and its offset from that cell's low corner, formed in FP64 so the
+// offset is the FP32 position's own, correctly rounded.
+__device__ __forceinline__ void rel_from_abs(float3 xa, const GridDev& g, float3& rel, int3& c) {
+    const float v[3] = {xa.x, xa.y, xa.z};
+    float o[3];
+    int cc[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const float f = __fdiv_rn(__fsub_rn(v[a], g.origin[a]), g.spacing);
+        int k = isfinite(f) ? (int)f : 0;
+        k = k % g.dim[a];
+        k = min(max(k, 0), g.dim[a] - 1);
+        cc[a] = k;
+        o[a] = (float)((double)v[a] - ((double)g.origin[a] + (double)k * (double)g.spacing));
+    }
+    rel = make_float3(o[0], o[1], o[2]);
+    c = make_int3(cc[0], cc[1], cc[2]);
+}
+
+// The stencil of a cell-relative particle: the neighbour cells its sphere of
+// radius h <= spacing can reach, clamped to the grid.
+__device__ __forceinline__ Stencil stencil_rel(float4 x, int3 c, float h, const GridDev& g) {
+    Stencil s;
+    s.x0 = x.x - h < 0.f ? max(c.x - 1, 0) : c.x;
+    s.x1 = x.x + h >= g.spacing ? min(c.x + 1, g.dim[0] - 1) : c.x;
+    s.y0 = x.y - h < 0.f ? max(c.y - 1, 0) : c.y;
+    s.y1 = x.y + h >= g.spacing ? min(c.y + 1, g.dim[1] - 1) : c.y;
+    s.z0 = x.z - h < 0.f ? max(c.z - 1, 0) : c.z;
+    s.z1 = x.z + h >= g.spacing ? min(c.z + 1, g.dim[2] - 1) : c.z;
+    return s;
+}
+
+// row_range for a cell-relative particle: the same rows and half-cell cut,
+// with every boundary taken in the particle's own cell frame.  Also returns
+// the row's y and z offsets (times spacing) for rel_in_frame.
+__device__ __forceinline__ void row_range_rel(float4 xi, int3 c, const Stencil& st, float h, const GridDev& g,
+                                              RowTables T, bool window, int r, int& s, int& e, float& dyo,
+                                              float& dzo) {
+    s = e = 0;
+    const int z = st.z0 + r / 3, y = st.y0 + r % 3;
+    dyo = (float)(y - c.y) * g.spacing;
+    dzo = (float)(z - c.z) * g.spacing;
+    if (z > st.z1 || y > st.y1) return;
+    const int row = g.cellBase + g.dim[0] * (g.dim[1] * z + y);
+    if (!window) {
+        s = __ldg(T.cellOffset + row + st.x0);
+        e = __ldg(T.cellOffset + row + st.x1 + 1);
+        return;
+    }
+    const float eps = 1e-3f * h;
+    const float h2 = h * h;
+    const float gz = cell_gap(xi.z, 0, dzo, g.spacing, eps);
+    const float gy = cell_gap(xi.y, 0, dyo, g.spacing, eps);
+    const float g2 = gy * gy + gz * gz;
+    if (g2 > h2) return;
+    const float inv = 1.0f / g.spacing;
+    const float rx = sqrtf(h2 - g2) + eps;
+    const float xl = xi.x - rx, xr = xi.x + rx;
+    const int cl = max(st.x0, c.x + (int)floorf(xl * inv));
+    const int cr = min(st.x1, c.x + (int)floorf(xr * inv));
+    if (cl > cr) return;
+    const int a0 = __ldg(T.cellOffset + row + cl), a1 = __ldg(T.cellOffset + row + cl + 1);
+    const int b0 = __ldg(T.cellOffset + row + cr), b1 = __ldg(T.cellOffset + row + cr + 1);
+    const float midL = ((float)(cl - c.x) + 0.5f) * g.spacing;
+    const float midR = ((float)(cr - c.x) + 0.5f) * g.spacing;
+    s = a0;
+    e = b1;
+    if (xl >= midL) s = min(max(__ldg(T.halfOffset + row + cl), a0), a1);
+    if (xr < midR) e = min(max(__ldg(T.halfOffset + row + cr), b0), b1);
+    if (e < s) e = s;
+}
+
 __device__ __forceinline__ void kahan_add(float& sum, float& comp, float term) {
     float y = __fsub_rn(term, comp);
     float t = __fadd_rn(sum, y);
@@ -204,14 +313,17 @@ __device__ __forceinline__ void kahan_add(float& sum, float& comp, float term) {
 // two guards the reference lacks (it yields NaN there): |v| == 0 drops the
 // restitution term, and a contact point that rounds onto the particle leaves
 // it untouched.
-__device__ __forceinline__ void collide(const PhysDev& ph, float3& x, float3& v) {
-    float lx = x.x - ph.boxCen[0], ly = x.y - ph.boxCen[1], lz = x.z - ph.boxCen[2];
+// `cen` is the box centre in the frame x is given in (the absolute
+// ph.boxCen, or the centre relative to a cell corner for cell-relative
+// positions).
+__device__ __forceinline__ void collide_box(const float* cen, const PhysDev& ph, float3& x, float3& v) {
+    float lx = x.x - cen[0], ly = x.y - cen[1], lz = x.z - cen[2];
     float dist = fmaxf(fmaxf(fabsf(lx) - ph.boxDim[0], fabsf(ly) - ph.boxDim[1]),
                        fabsf(lz) - ph.boxDim[2]);
     if (!(dist > 0.f)) return;
-    float cx = fminf(ph.boxDim[0], fmaxf(-ph.boxDim[0], lx)) + ph.boxCen[0];
-    float cy = fminf(ph.boxDim[1], fmaxf(-ph.boxDim[1], ly)) + ph.boxCen[1];
-    float cz = fminf(ph.boxDim[2], fmaxf(-ph.boxDim[2], lz)) + ph.boxCen[2];
+    float cx = fminf(ph.boxDim[0], fmaxf(-ph.boxDim[0], lx)) + cen[0];
+    float cy = fminf(ph.boxDim[1], fmaxf(-ph.boxDim[1], ly)) + cen[1];
+    float cz = fminf(ph.boxDim[2], fmaxf(-ph.boxDim[2], lz)) + cen[2];
     float nx = x.x - cx, ny = x.y - cy, nz = x.z - cz;
     float depth = sqrtf(nx * nx + ny * ny + nz * nz);
     if (!(depth > 0.f)) return;
@@ -226,5 +338,7 @@ __device__ __forceinline__ void collide(const PhysDev& ph, float3& x, float3& v)
     v.z -= coeff * nz;
     x = make_float3(cx, cy, cz);
 }
+
+__device__ __forceinline__ void collide(const PhysDev& ph, float3& x, float3& v) { collide_box(ph.boxCen, ph, x, v); }
 
 }  // namespace sph

@@ -23,7 +23,11 @@ struct GridDev {
     int dim[3];
     int numCells;
     int cellBase;  // first global cell index of this grid (batched scenes; else 0)
+    int rel;       // positions are cell-relative (sph_options.cellRelative)
 };
+
+// Largest grid of a cell-relative handle: cell coordinates pack 11:11:10 bits.
+constexpr int REL_MAX_X = 2048, REL_MAX_Y = 2048, REL_MAX_Z = 1024;
 
 // Trilinear boundary maps: map4 = (signed distance, wall density, wall
 // viscosity, 0) per node, dist = signed distance alone (gradient samples).
@@ -138,6 +142,10 @@ void launch_unpack_aos(const float* aos, int stride, int offset, int n, float4* 
 // pos[i].w = scene index `sid` (as integer bits) for i < count.
 void launch_set_scene(float4* pos, int count, int sid, cudaStream_t s);
 void launch_pack_aos(const float4* in, int n, float* aos, int stride, int offset, cudaStream_t s);
+// Cell-relative positions: absolute -> (offset, packed cell) in place, and
+// back to absolute (AoS with `stride` floats per particle and/or float4s).
+void launch_abs_to_rel(int n, float4* pos, GridDev g, cudaStream_t s);
+void launch_rel_to_abs(int n, const float4* pos, GridDev g, float* aos, int stride, float4* out4, cudaStream_t s);
 void launch_hash_count(int n, const float4* pos, GridDev g, SortBuffers sb, unsigned int* status,
                        cudaStream_t s);
 void launch_cell_scan(int numCells, SortBuffers sb, unsigned int* status, cudaStream_t s);

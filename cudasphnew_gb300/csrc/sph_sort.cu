@@ -1,7 +1,9 @@
 // Sorting stages of the GB300 SPH step and read-back helpers.
 //
 // Data layout in HBM (one handle, n particles, C cells):
-//   pos, vel           float4[n]  particle-index order (the state; .w unused)
+//   pos, vel           float4[n]  particle-index order (the state; pos.w: the
+//                                 scene of a batched handle, or the packed cell of
+//                                 a cell-relative one)
 //   posS, velS         float4[n]  copies in sorted (cell, id) order, per step
 //   rho4S              float4[n]  (rho, p, p/rho^2, 1/rho) in sorted order
 //   accS               float4[n]  acceleration in sorted order
@@ -48,6 +50,40 @@ __global__ void k_pack_aos(const float4* __restrict__ in, int n, float* __restri
     p[2] = v.z;
 }
 
+// Cell-relative state <-> absolute positions (sph_options.cellRelative).
+__global__ void k_abs_to_rel(int n, float4* __restrict__ pos, GridDev g) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 p = pos[i];
+    float3 rel;
+    int3 c;
+    rel_from_abs(make_float3(p.x, p.y, p.z), g, rel, c);
+    pos[i] = make_float4(rel.x, rel.y, rel.z, rel_pack(c.x, c.y, c.z));
+}
+
+__global__ void k_rel_to_abs(int n, const float4* __restrict__ in, GridDev g, float* __restrict__ aos, int stride,
+                             float4* __restrict__ out4) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 p = in[i];
+    const float4 a = rel_abs(p, rel_cell(p), g);
+    if (aos) {
+        float* p = aos + (size_t)i * stride;
+        p[0] = a.x;
+        p[1] = a.y;
+        p[2] = a.z;
+    }
+    if (out4) out4[i] = make_float4(a.x, a.y, a.z, 0.f);
+}
+
+void launch_abs_to_rel(int n, float4* pos, GridDev g, cudaStream_t s) {
+    if (n > 0) k_abs_to_rel<<<(n + 255) / 256, 256, 0, s>>>(n, pos, g);
+}
+
+void launch_rel_to_abs(int n, const float4* pos, GridDev g, float* aos, int stride, float4* out4, cudaStream_t s) {
+    if (n > 0) k_rel_to_abs<<<(n + 255) / 256, 256, 0, s>>>(n, pos, g, aos, stride, out4);
+}
+
 void launch_unpack_aos(const float* aos, int stride, int offset, int n, float4* out, cudaStream_t s) {
     if (n <= 0) return;
     k_unpack_aos<<<(n + 255) / 256, 256, 0, s>>>(aos, stride, offset, n, out);
@@ -63,7 +99,9 @@ void launch_pack_aos(const float4* in, int n, float* aos, int stride, int offset
 // ---------------------------------------------------------------------------
 // With BATCH the particle's scene (pos.w) supplies its grid, whose cells
 // start at that scene's cellBase in the concatenated cell space.
-template <bool BATCH>
+// With REL the position is cell-relative and the hash comes from its packed
+// cell coordinates.
+template <bool BATCH, bool REL>
 __global__ void k_hash_count(int n, const float4* __restrict__ pos, GridDev g_, const SceneDev* __restrict__ scenes,
                              int* __restrict__ cnt, int2* __restrict__ keySlot, unsigned int* status) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -71,11 +109,18 @@ __global__ void k_hash_count(int n, const float4* __restrict__ pos, GridDev g_, 
     float4 p = pos[i];
     const GridDev& g = BATCH ? scenes[__float_as_int(p.w)].g : g_;
     bool outside = false;
-    if (!(isfinite(p.x) && isfinite(p.y) && isfinite(p.z))) {
+    const bool finite = isfinite(p.x) && isfinite(p.y) && isfinite(p.z);
+    if (!finite) {
         atomicOr(status, STATUS_NON_FINITE);
         p = make_float4(g.origin[0], g.origin[1], g.origin[2], 0.f);
     }
-    int h = particle_hash(p, g, &outside);
+    int h;
+    if (REL) {
+        const int3 c = finite ? rel_cell(p) : make_int3(0, 0, 0);
+        h = g.cellBase + g.dim[0] * (g.dim[1] * c.z + c.y) + c.x;
+    } else {
+        h = particle_hash(p, g, &outside);
+    }
     if (outside) atomicOr(status, STATUS_OUT_OF_DOMAIN);
     int slot = atomicAdd(cnt + h, 1);
     keySlot[i] = make_int2(h, slot);
@@ -85,9 +130,11 @@ void launch_hash_count(int n, const float4* pos, GridDev g, SortBuffers sb, unsi
                        cudaStream_t s) {
     if (n <= 0) return;
     if (sb.scenes)
-        k_hash_count<true><<<(n + 255) / 256, 256, 0, s>>>(n, pos, g, sb.scenes, sb.cnt, sb.keySlot, status);
+        k_hash_count<true, false><<<(n + 255) / 256, 256, 0, s>>>(n, pos, g, sb.scenes, sb.cnt, sb.keySlot, status);
+    else if (g.rel)
+        k_hash_count<false, true><<<(n + 255) / 256, 256, 0, s>>>(n, pos, g, nullptr, sb.cnt, sb.keySlot, status);
     else
-        k_hash_count<false><<<(n + 255) / 256, 256, 0, s>>>(n, pos, g, nullptr, sb.cnt, sb.keySlot, status);
+        k_hash_count<false, false><<<(n + 255) / 256, 256, 0, s>>>(n, pos, g, nullptr, sb.cnt, sb.keySlot, status);
 }
 
 // ---------------------------------------------------------------------------
@@ -265,7 +312,7 @@ __device__ __forceinline__ unsigned int ordered_bits(float x) {
 // The same pass records, per cell, where its upper x-half starts in the
 // working order (halfOffset[c] = first index with x >= the cell's mid-plane),
 // so a neighbour search can cut a row at half-cell granularity from a table.
-template <bool BATCH>
+template <bool BATCH, bool REL>
 __global__ void k_rank_gather(int n, const int* __restrict__ sortedHash, const int* __restrict__ cellOffset,
                               const int* __restrict__ tmpIds, const float4* __restrict__ pos,
                               const float4* __restrict__ vel, GridDev g_, const SceneDev* __restrict__ scenes,
@@ -279,7 +326,9 @@ __global__ void k_rank_gather(int n, const int* __restrict__ sortedHash, const i
     float4 p = __ldg(pos + my);
     const GridDev& g = BATCH ? scenes[__float_as_int(p.w)].g : g_;
     unsigned int key = ordered_bits(p.x);
-    const float mid = g.origin[0] + ((float)((c - g.cellBase) % g.dim[0]) + 0.5f) * g.spacing;
+    // the cell's mid-plane, in the frame its members' x is stored in
+    const float mid = REL ? 0.5f * g.spacing
+                          : g.origin[0] + ((float)((c - g.cellBase) % g.dim[0]) + 0.5f) * g.spacing;
     int rId = 0, rX = 0, below = 0;
     for (int t = s; t < e; t++) {
         int o = __ldg(tmpIds + t);
@@ -300,14 +349,19 @@ __global__ void k_rank_gather(int n, const int* __restrict__ sortedHash, const i
 void launch_rank_gather(int n, SortBuffers sb, const float4* pos, const float4* vel, GridDev g, float4* posS,
                         float4* velS, cudaStream_t s) {
     if (n <= 0) return;
+    const int grid = (n + 255) / 256;
     if (sb.scenes)
-        k_rank_gather<true><<<(n + 255) / 256, 256, 0, s>>>(n, sb.sortedHash, sb.cellOffset, sb.tmpIds, pos, vel, g,
-                                                            sb.scenes, sb.sortedIds, sb.workIds, sb.halfOffset, posS,
-                                                            velS, sb.xS);
+        k_rank_gather<true, false><<<grid, 256, 0, s>>>(n, sb.sortedHash, sb.cellOffset, sb.tmpIds, pos, vel, g,
+                                                        sb.scenes, sb.sortedIds, sb.workIds, sb.halfOffset, posS,
+                                                        velS, sb.xS);
+    else if (g.rel)
+        k_rank_gather<false, true><<<grid, 256, 0, s>>>(n, sb.sortedHash, sb.cellOffset, sb.tmpIds, pos, vel, g,
+                                                        nullptr, sb.sortedIds, sb.workIds, sb.halfOffset, posS, velS,
+                                                        sb.xS);
     else
-        k_rank_gather<false><<<(n + 255) / 256, 256, 0, s>>>(n, sb.sortedHash, sb.cellOffset, sb.tmpIds, pos, vel,
-                                                             g, nullptr, sb.sortedIds, sb.workIds, sb.halfOffset,
-                                                             posS, velS, sb.xS);
+        k_rank_gather<false, false><<<grid, 256, 0, s>>>(n, sb.sortedHash, sb.cellOffset, sb.tmpIds, pos, vel, g,
+                                                         nullptr, sb.sortedIds, sb.workIds, sb.halfOffset, posS,
+                                                         velS, sb.xS);
 }
 
 // ---------------------------------------------------------------------------

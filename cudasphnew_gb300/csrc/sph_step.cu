@@ -34,7 +34,9 @@ struct RowMasks {
     unsigned int* mask;  // [9][n] neighbour bits relative to start, or the window end
 };
 
-template <bool KAHAN, bool EMIT, bool BATCH>
+// With REL the positions are cell-relative: every neighbour is moved into
+// particle i's cell frame before its distance is taken.
+template <bool KAHAN, bool EMIT, bool BATCH, bool REL>
 __global__ void __launch_bounds__(256)
 k_density(int n, const float4* __restrict__ posS, RowTables T, GridDev g_, PhysDev ph_, MapDev map_, int window,
           float4* __restrict__ rho4S, RowMasks M) {
@@ -46,17 +48,22 @@ k_density(int n, const float4* __restrict__ posS, RowTables T, GridDev g_, PhysD
     const GridDev& g = BATCH ? S->g : g_;
     const PhysDev& ph = BATCH ? S->ph : ph_;
     const MapDev& map = BATCH ? S->map : map_;
-    const Stencil st = stencil(xi, ph.h, g);
+    const int3 ci = REL ? rel_cell(xi) : make_int3(0, 0, 0);
+    const Stencil st = REL ? stencil_rel(xi, ci, ph.h, g) : stencil(xi, ph.h, g);
     const float h2 = ph.h2;
     float sum = 0.f, comp = 0.f;
 #pragma unroll
     for (int r = 0; r < 9; r++) {
         int s, e;
-        row_range(xi, st, ph.h, g, T, window != 0, r, s, e);
+        float dyo = 0.f, dzo = 0.f;
+        if (REL) row_range_rel(xi, ci, st, ph.h, g, T, window != 0, r, s, e, dyo, dzo);
+        else row_range(xi, st, ph.h, g, T, window != 0, r, s, e);
         float rs = 0.f;
         unsigned int m = 0u, bit = 1u;
         for (int t = s; t < e; t++) {
-            const float r2 = dist2(xi, __ldg(posS + t));
+            float4 xj = __ldg(posS + t);
+            if (REL) xj = rel_in_frame(xj, ci.x, dyo, dzo, g.spacing);
+            const float r2 = dist2(xi, xj);
             const float w = fmaxf(h2 - r2, 0.f);
             rs = fmaf(w * w, w, rs);
             if (EMIT) {
@@ -78,7 +85,7 @@ k_density(int n, const float4* __restrict__ posS, RowTables T, GridDev g_, PhysD
     float rho = (KAHAN ? __fsub_rn(sum, comp) : sum) * ph.poly6m;
     if (map.present) {
         float uvw[3];
-        map_uvw(map, xi, uvw);
+        map_uvw(map, REL ? rel_abs(xi, ci, g) : xi, uvw);
         rho += tri_vec(map, uvw[0], uvw[1], uvw[2]).y;  // wall density, :242-248
     }
     const float p = ph.stiffness * (rho - ph.restDensity);
@@ -273,11 +280,12 @@ __device__ __forceinline__ void store_features(float* feat, size_t row, const fl
 // Returns the new state (x, v) and the acceleration; the FEAT forms also
 // return the boundary map's wall distance and unit normal (mapDist stays as
 // given where the map is absent, mapN where the particle is beyond the
-// map's rest distance).
+// map's rest distance).  xm is the absolute position the boundary map is
+// read at (xi itself unless positions are cell-relative).
 template <bool KAHAN, bool TENSION, bool FEAT>
 __device__ __forceinline__ void force_finish(const ForceTotals<KAHAN, TENSION>& A, float4 xi, float4 vi, float4 ri,
                                              const PhysDev& ph, const MapDev& map, int collideFlag, float3& x,
-                                             float3& v, float* acc, float& mapDist, float* mapN) {
+                                             float3& v, float* acc, float& mapDist, float* mapN, float4 xm) {
     const float rho = ri.x;
     const float pc = ph.pressCoef * rho;
     float force[3];
@@ -290,7 +298,7 @@ __device__ __forceinline__ void force_finish(const ForceTotals<KAHAN, TENSION>& 
     bool tension = TENSION;
     if (map.present) {
         float uvw[3];
-        map_uvw(map, xi, uvw);
+        map_uvw(map, xm, uvw);
         const float4 s = tri_vec(map, uvw[0], uvw[1], uvw[2]);
         const float distWall = -s.x;
         if (FEAT) mapDist = distWall;
@@ -354,7 +362,7 @@ __device__ __forceinline__ void force_epilogue(const ForceTotals<KAHAN, TENSION>
     float mapDist = 1e30f, mapN[3] = {0.f, 0.f, 0.f};  // learned features only
     float3 x, v;
     float acc[3];
-    force_finish<KAHAN, TENSION, FEAT>(A, xi, vi, ri, ph, map, collideFlag, x, v, acc, mapDist, mapN);
+    force_finish<KAHAN, TENSION, FEAT>(A, xi, vi, ri, ph, map, collideFlag, x, v, acc, mapDist, mapN, xi);
     const int id = workIds[i];
     pos[id] = make_float4(x.x, x.y, x.z, xi.w);  // .w: the scene index of batched handles
     vel[id] = make_float4(v.x, v.y, v.z, 0.f);
@@ -364,6 +372,54 @@ __device__ __forceinline__ void force_epilogue(const ForceTotals<KAHAN, TENSION>
         feature_values(fs, fo.boxWalls, fo.dtL, xi, vi, ri, acc, mapDist, mapN, ph, f);
         store_features(fo.feat, (size_t)(fo.byId ? id : i), f);
     }
+}
+
+// The cell-relative form's epilogue: the step is integrated in the
+// particle's cell frame, then the position moves to the cell it now lies in
+// (whole-cell steps, clamped to the grid).  The wall box collision works in
+// that cell's frame too, and a particle it moves is re-binned again.
+__device__ __forceinline__ void rel_rebin(float3& x, int3& c, const GridDev& g) {
+    const float inv = 1.0f / g.spacing;
+    float* xs[3] = {&x.x, &x.y, &x.z};
+    int* cs[3] = {&c.x, &c.y, &c.z};
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const float k = floorf(*xs[a] * inv);
+        if (k != 0.f) {
+            const int cn = min(max(*cs[a] + (int)k, 0), g.dim[a] - 1);
+            *xs[a] = fmaf(-(float)(cn - *cs[a]), g.spacing, *xs[a]);
+            *cs[a] = cn;
+        }
+    }
+}
+
+template <bool KAHAN, bool TENSION>
+__device__ __forceinline__ void force_epilogue_rel(const ForceTotals<KAHAN, TENSION>& A, int i, float4 xi, int3 ci,
+                                                   float4 vi, float4 ri, const PhysDev& ph, const GridDev& g,
+                                                   const MapDev& map, int collideFlag, const int* __restrict__ workIds,
+                                                   float4* __restrict__ pos, float4* __restrict__ vel,
+                                                   float4* __restrict__ accS) {
+    float mapDist = 1e30f, mapN[3] = {0.f, 0.f, 0.f};
+    float3 x, v;
+    float acc[3];
+    force_finish<KAHAN, TENSION, false>(A, xi, vi, ri, ph, map, 0, x, v, acc, mapDist, mapN, rel_abs(xi, ci, g));
+    int3 c = ci;
+    rel_rebin(x, c, g);
+    if (collideFlag) {
+        // the wall box in this cell's frame: the collision keeps the offset's resolution
+        const int cc[3] = {c.x, c.y, c.z};
+        float cen[3];
+#pragma unroll
+        for (int a = 0; a < 3; a++)
+            cen[a] = (float)((double)ph.boxCen[a] - ((double)g.origin[a] + (double)cc[a] * (double)g.spacing));
+        const float3 before = x;
+        collide_box(cen, ph, x, v);
+        if (x.x != before.x || x.y != before.y || x.z != before.z) rel_rebin(x, c, g);
+    }
+    const int id = workIds[i];
+    pos[id] = make_float4(x.x, x.y, x.z, rel_pack(c.x, c.y, c.z));
+    vel[id] = make_float4(v.x, v.y, v.z, 0.f);
+    accS[i] = make_float4(acc[0], acc[1], acc[2], 0.f);
 }
 
 struct ForceArgs {
@@ -389,7 +445,9 @@ struct ForceArgs {
 // 256-thread blocks share an SM (the force stage is latency bound: 210 ->
 // 150 us per million particles against two blocks); the feature and batched
 // forms take up to 80 registers, three blocks.
-template <bool KAHAN, bool TENSION, int FORM, bool FEAT, bool BATCH>
+// REL: cell-relative positions (plain forms only): neighbours are moved into
+// particle i's cell frame, the step is integrated there and re-binned.
+template <bool KAHAN, bool TENSION, int FORM, bool FEAT, bool BATCH, bool REL = false>
 __global__ void __launch_bounds__(256, FEAT ? 3 : (BATCH ? 3 : 4)) k_force(ForceArgs F) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= F.n) return;
@@ -401,13 +459,21 @@ __global__ void __launch_bounds__(256, FEAT ? 3 : (BATCH ? 3 : 4)) k_force(Force
     const PhysDev& ph = BATCH ? S->ph : F.ph;
     const MapDev& map = BATCH ? S->map : F.map;
     const float h2 = ph.h2;
+    const int3 ci = REL ? rel_cell(xi) : make_int3(0, 0, 0);
     Stencil st;
-    if (FORM != FORCE_PRETESTED) st = stencil(xi, ph.h, g);
+    if (REL) st = stencil_rel(xi, ci, ph.h, g);
+    else if (FORM != FORCE_PRETESTED) st = stencil(xi, ph.h, g);
+    float dyo = 0.f, dzo = 0.f;  // REL: the current row's y and z cell offsets (times spacing)
+    auto neighbour = [&](int t) {
+        float4 xj = __ldg(F.posS + t);
+        if (REL) xj = rel_in_frame(xj, ci.x, dyo, dzo, g.spacing);
+        return xj;
+    };
     ForceTotals<KAHAN, TENSION> A;
     FeatSums fs;
     auto direct = [&](RowSums<TENSION>& R, int s, int e) {
         for (int t = s; t < e; t++) {
-            const float4 xj = __ldg(F.posS + t);
+            const float4 xj = neighbour(t);
             const float r2 = dist2(xi, xj);
             if (r2 <= h2 && r2 > 0.f) {
                 const float4 vj = __ldg(F.velS + t), rj = __ldg(F.rho4S + t);
@@ -421,7 +487,7 @@ __global__ void __launch_bounds__(256, FEAT ? 3 : (BATCH ? 3 : 4)) k_force(Force
         while (m) {
             const int t = base + __ffs(m) - 1;
             m &= m - 1u;
-            const float4 xj = __ldg(F.posS + t), vj = __ldg(F.velS + t), rj = __ldg(F.rho4S + t);
+            const float4 xj = neighbour(t), vj = __ldg(F.velS + t), rj = __ldg(F.rho4S + t);
             const Pair p(ph, xi, vi, xj, vj);
             R.add(ph, p, ri.z, rj);
             if (FEAT) fs.add(ph, p, rj);
@@ -432,13 +498,18 @@ __global__ void __launch_bounds__(256, FEAT ? 3 : (BATCH ? 3 : 4)) k_force(Force
         RowSums<TENSION> R;
         R.clear();
         if (FORM == FORCE_PRETESTED) {
+            if (REL) {
+                dyo = (float)(st.y0 + r % 3 - ci.y) * g.spacing;
+                dzo = (float)(st.z0 + r / 3 - ci.z) * g.spacing;
+            }
             const int sv = __ldg(F.M.start + (size_t)r * F.n + i);
             const unsigned int m = __ldg(F.M.mask + (size_t)r * F.n + i);
             if (sv < 0) direct(R, sv & 0x7fffffff, (int)m);
             else bits(R, sv, m);
         } else {
             int s, e;
-            row_range(xi, st, ph.h, g, F.T, F.window != 0, r, s, e);
+            if (REL) row_range_rel(xi, ci, st, ph.h, g, F.T, F.window != 0, r, s, e, dyo, dzo);
+            else row_range(xi, st, ph.h, g, F.T, F.window != 0, r, s, e);
             if (FORM == FORCE_DIRECT) {
                 direct(R, s, e);
             } else {
@@ -446,7 +517,7 @@ __global__ void __launch_bounds__(256, FEAT ? 3 : (BATCH ? 3 : 4)) k_force(Force
                     const int cnt = min(32, e - base);
                     unsigned int m = 0u;
                     for (int k = 0; k < cnt; k++) {
-                        const float r2 = dist2(xi, __ldg(F.posS + base + k));
+                        const float r2 = dist2(xi, neighbour(base + k));
                         m |= (r2 <= h2 && r2 > 0.f) ? (1u << k) : 0u;
                     }
                     bits(R, base, m);
@@ -456,8 +527,12 @@ __global__ void __launch_bounds__(256, FEAT ? 3 : (BATCH ? 3 : 4)) k_force(Force
         A.add(R);
         if (FEAT) fs.cnt += R.hits;
     }
-    force_epilogue<KAHAN, TENSION, FEAT>(A, i, xi, vi, ri, ph, map, F.collide, F.workIds, F.pos, F.vel,
-                                         F.accS, fs, F.fo);
+    if (REL)
+        force_epilogue_rel<KAHAN, TENSION>(A, i, xi, ci, vi, ri, ph, g, map, F.collide, F.workIds, F.pos, F.vel,
+                                           F.accS);
+    else
+        force_epilogue<KAHAN, TENSION, FEAT>(A, i, xi, vi, ri, ph, map, F.collide, F.workIds, F.pos, F.vel,
+                                             F.accS, fs, F.fo);
 }
 
 // ---------------------------------------------------------------------------
@@ -559,7 +634,7 @@ __global__ void __launch_bounds__(L_THREADS, BLOCKS) k_force_learned(ForceArgs F
                 fs.cnt += R.hits;
             }
             float acc[3], mapDist = 1e30f, mapN[3] = {0.f, 0.f, 0.f};
-            force_finish<KAHAN, TENSION, true>(A, xi, vi, ri, ph, F.map, F.collide, x, v, acc, mapDist, mapN);
+            force_finish<KAHAN, TENSION, true>(A, xi, vi, ri, ph, F.map, F.collide, x, v, acc, mapDist, mapN, xi);
             id = F.workIds[i];
             F.accS[i] = make_float4(acc[0], acc[1], acc[2], 0.f);
             feature_values(fs, F.fo.boxWalls, F.fo.dtL, xi, vi, ri, acc, mapDist, mapN, ph, f);
@@ -623,8 +698,17 @@ void launch_density(int n, const float4* posS, RowTables T, GridDev g, PhysDev p
     const int grid = (n + bs - 1) / bs;
     const RowMasks M{rowStart, rowMask};
     const bool emit = cfg.forceVariant == FORCE_PRETESTED;
-#define SPH_DENSITY(K, E, B) k_density<K, E, B><<<grid, bs, 0, s>>>(n, posS, T, g, ph, map, cfg.prune, rho4S, M)
-    if (T.scenes) {
+#define SPH_DENSITY(K, E, B) k_density<K, E, B, false><<<grid, bs, 0, s>>>(n, posS, T, g, ph, map, cfg.prune, rho4S, M)
+#define SPH_DENSITY_REL(K, E) k_density<K, E, false, true><<<grid, bs, 0, s>>>(n, posS, T, g, ph, map, cfg.prune, rho4S, M)
+    if (g.rel) {
+        if (cfg.kahan) {
+            if (emit) SPH_DENSITY_REL(true, true);
+            else SPH_DENSITY_REL(true, false);
+        } else {
+            if (emit) SPH_DENSITY_REL(false, true);
+            else SPH_DENSITY_REL(false, false);
+        }
+    } else if (T.scenes) {
         if (cfg.kahan) {
             if (emit) SPH_DENSITY(true, true, true);
             else SPH_DENSITY(true, false, true);
@@ -642,6 +726,7 @@ void launch_density(int n, const float4* posS, RowTables T, GridDev g, PhysDev p
         }
     }
 #undef SPH_DENSITY
+#undef SPH_DENSITY_REL
 }
 
 template <bool KAHAN, bool TENSION>
@@ -656,6 +741,14 @@ static void force_dispatch(const ForceArgs& F, const StepConfig& cfg, cudaStream
             k_force<KAHAN, TENSION, FORCE_MASK, false, true><<<grid, bs, 0, s>>>(F);
         else
             k_force<KAHAN, TENSION, FORCE_DIRECT, false, true><<<grid, bs, 0, s>>>(F);
+    } else if (F.g.rel) {
+        // cell-relative positions (plain steps only)
+        if (cfg.forceVariant == FORCE_PRETESTED)
+            k_force<KAHAN, TENSION, FORCE_PRETESTED, false, false, true><<<grid, bs, 0, s>>>(F);
+        else if (cfg.forceVariant == FORCE_MASK)
+            k_force<KAHAN, TENSION, FORCE_MASK, false, false, true><<<grid, bs, 0, s>>>(F);
+        else
+            k_force<KAHAN, TENSION, FORCE_DIRECT, false, false, true><<<grid, bs, 0, s>>>(F);
     } else if (F.fo.feat) {
         // the learned step's force stage records the corrector's features; the
         // density stage has recorded the neighbour masks (pretested form)

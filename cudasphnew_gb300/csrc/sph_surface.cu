@@ -57,13 +57,26 @@ extern "C" sph_status sph_surface_particles(sph_handle s, int* flags) {
     int* d = nullptr;
     SPH_CUDA(dalloc(&d, (size_t)s->n));
     GridDev g = grid_of(s);
-    k_surface<<<(s->n + 127) / 128, 128, 0, s->stream>>>(s->n, s->posS, s->sb.workIds, rows_of(s), g,
+    const float4* posS = s->posS;
+    float4* absS = nullptr;
+    if (g.rel) {  // cell-relative positions: search an absolute copy
+        cudaError_t ea = dalloc(&absS, (size_t)s->n);
+        if (ea != cudaSuccess) {
+            cudaFree(d);
+            SPH_CUDA(ea);
+        }
+        launch_rel_to_abs(s->n, s->posS, g, nullptr, 0, absS, s->stream);
+        posS = absS;
+        g.rel = 0;
+    }
+    k_surface<<<(s->n + 127) / 128, 128, 0, s->stream>>>(s->n, posS, s->sb.workIds, rows_of(s), g,
                                                          s->P.compactSupport, s->P.cmDistanceThresh,
                                                          s->P.nPartTresh, d);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemcpyAsync(flags, d, sizeof(int) * (size_t)s->n, cudaMemcpyDeviceToHost, s->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
     cudaFree(d);
+    if (absS) cudaFree(absS);
     SPH_CUDA(e);
     return latched_status(s);
 }

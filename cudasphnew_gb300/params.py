@@ -74,7 +74,7 @@ class Options(ctypes.Structure):
         ("gravityAxis", ctypes.c_int),
         ("boxCollision", ctypes.c_int),
         ("childMode", ctypes.c_int),
-        ("reserved1", ctypes.c_int),
+        ("cellRelative", ctypes.c_int),
         ("splitMin", F3),
         ("splitMax", F3),
     ]

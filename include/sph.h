@@ -87,7 +87,15 @@ typedef struct sph_options {
                            :1052-1055); a parent leaving the split class
                            first takes its children's mean position and
                            velocity (merge-back, no reference counterpart) */
-    int reserved1;
+    int cellRelative;   /* 1: positions are stored relative to the low corner
+                           of their grid cell (the cell's integer coordinates
+                           beside them), so pair offsets and the integration
+                           step keep FP32 precision however far the scene lies
+                           from the origin (every position resolves half a
+                           unit in the last place of gridSpacing); the
+                           reference stores absolute FP32 positions (0).
+                           Plain steps only; gridDim at most 2048 x 2048 x
+                           1024.  No reference counterpart. */
     float splitMin[3];  /* two-scale split region; reference: 0.2 <= x <= 0.5 */
     float splitMax[3];  /* (find_split_particles, :948) */
 } sph_options;
