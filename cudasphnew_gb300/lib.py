@@ -73,6 +73,10 @@ SIGNATURES = {
     "sph_sdf_load": (_i, [ctypes.c_char_p, _vp]),
     "sph_sdf_free": (None, [_vp]),
     "sph_surface_particles": (_i, [_vp, _vp]),
+    "sph_camera_look_at": (_i, [_vp, _vp, _vp, _vp]),
+    "sph_camera_perspective": (_i, [_vp, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float]),
+    "sph_render": (_i, [_vp, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, _vp]),
+    "sph_image_save_ppm": (_i, [ctypes.c_char_p, _vp, ctypes.c_int, ctypes.c_int]),
     "sph_last_error": (ctypes.c_char_p, []),
     "sph_status_string": (ctypes.c_char_p, [_i]),
 }
@@ -82,6 +86,31 @@ class Counts(ctypes.Structure):
     _fields_ = [(name, ctypes.c_uint) for name in (
         "numParticles", "numParticlesDefault", "numParticlesSplit", "numParticlesBoundary",
         "numSubParticles", "numTimeSteps", "numCells", "numSubCells")]
+
+
+SPH_RENDER_PARTICLES, SPH_RENDER_TWO_SCALE, SPH_RENDER_SUB_PARTICLES = 0, 1, 2
+
+
+class Camera(ctypes.Structure):
+    """sph_camera: column-major view and projection matrices."""
+
+    _fields_ = [("view", ctypes.c_float * 16), ("proj", ctypes.c_float * 16)]
+
+    @classmethod
+    def look(cls, eye, centre, up, fovy, aspect, znear, zfar):
+        """cgtkGLLookAt + cgtkGLPerspective, as the reference's renderers set them."""
+        c = cls()
+        f3 = ctypes.c_float * 3
+        check(load().sph_camera_look_at(ctypes.byref(c), f3(*eye), f3(*centre), f3(*up)))
+        check(load().sph_camera_perspective(ctypes.byref(c), fovy, aspect, znear, zfar))
+        return c
+
+
+def save_ppm(path: str, rgba: np.ndarray) -> None:
+    """PortablePixmap's ASCII P3 layout of an (H, W, 4) uint8 image."""
+    img = np.ascontiguousarray(rgba, np.uint8)
+    h, w = img.shape[:2]
+    check(load().sph_image_save_ppm(path.encode(), img.ctypes.data, w, h))
 
 
 class Diagnostics(ctypes.Structure):
@@ -449,6 +478,15 @@ class ParticleSimulation:
         out = np.zeros((self.n, CORRECTOR_FEATURES), np.float32)
         check(load().sph_read_features(self._h, out.ctypes.data, out.nbytes))
         return out
+
+    def render(self, camera: "Camera", width: int, height: int, what: int = 0, depth: bool = False):
+        """sph_render: (height, width, 4) uint8 RGBA, rows top to bottom (and
+        the (height, width) float depth when asked)."""
+        img = np.zeros((height, width, 4), np.uint8)
+        dep = np.zeros((height, width), np.float32) if depth else None
+        check(load().sph_render(self._h, ctypes.byref(camera), width, height, what, img.ctypes.data,
+                                dep.ctypes.data if dep is not None else None))
+        return (img, dep) if depth else img
 
     def surface_particles(self) -> np.ndarray:
         """CreateIsParticleSurfaceList: 1 for surface particles (particle order)."""

@@ -424,6 +424,45 @@ sph_status sph_read_features(sph_handle h, float* dst, size_t bytes);
  * list).  int[n], particle order. */
 sph_status sph_surface_particles(sph_handle h, int* flags);
 
+/* Headless renderer: the sphere imposters of the reference's
+ * TwoScaleStateSub renderer (twoscalestatesub.cpp:84-161,
+ * twoscalestatesub_{v,g,f}.glsl) splatted by CUDA kernels into an image, no
+ * graphics API.  Matrices are column-major, as OpenGL takes them. */
+typedef struct sph_camera {
+    float view[16];
+    float proj[16];
+} sph_camera;
+
+/* cgtkGLLookAt (cgtk/src/opengl.c:10-46): the view matrix of an eye looking
+ * at centre with the given up vector. */
+sph_status sph_camera_look_at(sph_camera* cam, const float eye[3], const float centre[3], const float up[3]);
+/* cgtkGLPerspective + cgtkGLFrustum (cgtk/src/opengl.c:48-78). */
+sph_status sph_camera_perspective(sph_camera* cam, float fovy, float aspect, float znear, float zfar);
+
+enum {
+    SPH_RENDER_PARTICLES = 0,     /* renderLow: every coarse particle, blue */
+    SPH_RENDER_TWO_SCALE = 1,     /* render: default particles (blue), regular
+                                     (yellow) and boundary (red) sub-particles
+                                     at half the radius, in that draw order */
+    SPH_RENDER_SUB_PARTICLES = 2  /* renderRegularSubParticles: the
+                                     sub-particles alone */
+};
+
+/* Renders the current state: particle radius GetParticleRadius()
+ * ((3 fluidVolume / (4 pi n))^(1/3), particle_simulation.cu:2227-2236),
+ * white background, shading 0.9 + 0.1 max(0, n.z), GL_LESS depth test on a
+ * 24-bit depth buffer (the first drawn fragment keeps a tie).  rgba: host
+ * uint8[height][width][4], rows top to bottom; depth (optional): host
+ * float[height][width], the stored depth in [0, 1] (1 where nothing was
+ * drawn).  The two-scale modes need a two-scale step to have run.  At most
+ * 2^26 pixels. */
+sph_status sph_render(sph_handle h, const sph_camera* cam, int width, int height, int what, unsigned char* rgba,
+                      float* depth);
+
+/* PortablePixmap::save's format (portable_pixmap.cpp:23-40): ASCII P3,
+ * maximum 255, one value per line, the RGB of `rgba` rows top to bottom. */
+sph_status sph_image_save_ppm(const char* path, const unsigned char* rgba, int width, int height);
+
 /* Device pointer of a field in the handle's layout, for zero-copy consumers
  * (replaces the OpenGL VBO getters, :2278-2301): 0 = positions (float4[n],
  * particle order), 1 = velocities (float4[n]). */

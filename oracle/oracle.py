@@ -293,3 +293,88 @@ def mesh_sdf(vertices, faces, origin, dx, dims, max_dist):
     nrm = np.zeros(dist.shape + (3,), np.float32)
     fn(_ptr(v), len(v), _ptr(f), len(f), _ptr(o), float(dx), _ptr(d), float(max_dist), _ptr(dist), _ptr(nrm))
     return dist, nrm
+
+
+def look_at(eye, centre, up):
+    """cgtkGLLookAt (cgtk/src/opengl.c:10-46): column-major view matrix, float64."""
+    e, c, u0 = (np.asarray(a, np.float64) for a in (eye, centre, up))
+    n = c - e
+    n /= np.linalg.norm(n)
+    u = np.cross(n, u0)
+    u /= np.linalg.norm(u)
+    v = np.cross(u, n)
+    m = np.zeros(16)
+    for a in range(3):
+        m[4 * a:4 * a + 3] = (u[a], v[a], -n[a])
+    m[12], m[13], m[14], m[15] = -u @ e, -v @ e, n @ e, 1.0
+    return m
+
+
+def perspective(fovy, aspect, znear, zfar):
+    """cgtkGLPerspective + cgtkGLFrustum (cgtk/src/opengl.c:48-78), float64."""
+    t = np.tan((fovy / 2.0) * (3.141593 / 180.0))
+    h = znear * t
+    w = h * aspect
+    m = np.zeros(16)
+    m[0] = 2 * znear / (2 * w)
+    m[5] = 2 * znear / (2 * h)
+    m[10] = (zfar + znear) / (znear - zfar)
+    m[11] = -1.0
+    m[14] = -2 * zfar * znear / (zfar - znear)
+    return m
+
+
+def render_splats(view, proj, passes, width, height):
+    """The TwoScaleStateSub shaders (twoscalestatesub_{v,g,f}.glsl) restated in
+    float64 with GL's rasterisation: a pixel is covered when its centre lies
+    inside a particle's quad, the fragment is kept when inside the unit disk,
+    depth -proj[2][2] - proj[2][3]/zEye clamped to [0, 1] and stored as 24-bit
+    fixed point, GL_LESS (the first drawn fragment keeps a tie), white clear.
+    passes: [(positions (k, 3), radius, (r, g, b)), ...] in draw order.
+    Returns (rgba uint8 (H, W, 4) rows top to bottom, winner draw index or -1)."""
+    V = np.asarray(view, np.float64).reshape(4, 4).T  # column-major -> math
+    Pm = np.asarray(proj, np.float64).reshape(4, 4).T
+    key = np.full((height, width), np.iinfo(np.int64).max, np.int64)
+    shade = np.zeros((height, width, 4))
+    base = 0
+    info = []
+    for pos, R, rgb in passes:
+        pos = np.asarray(pos, np.float64).reshape(-1, 3)
+        for k in range(len(pos)):
+            eye = V @ np.append(pos[k], 1.0)
+            w = -eye[2]
+            clip = Pm @ eye
+            if not (w > 0 and abs(clip[2] / w) <= 1):
+                continue
+            cx, cy = clip[0] / w, clip[1] / w
+            dx, dy = Pm[0, 0] * R / w, Pm[1, 1] * R / w
+            i0 = max(int(np.ceil((cx - dx + 1) * 0.5 * width - 0.5)), 0)
+            i1 = min(int(np.ceil((cx + dx + 1) * 0.5 * width - 0.5)) - 1, width - 1)
+            j0 = max(int(np.ceil((cy - dy + 1) * 0.5 * height - 0.5)), 0)
+            j1 = min(int(np.ceil((cy + dy + 1) * 0.5 * height - 0.5)) - 1, height - 1)
+            if i1 < i0 or j1 < j0:
+                continue
+            ii, jj = np.meshgrid(np.arange(i0, i1 + 1), np.arange(j0, j1 + 1))
+            u = ((ii + 0.5) * 2 / width - 1 - cx) / dx
+            v = ((jj + 0.5) * 2 / height - 1 - cy) / dy
+            norm = u * u + v * v
+            inside = norm <= 1
+            nz = np.sqrt(np.maximum(1 - norm, 0))
+            zeye = eye[2] + R * nz
+            z = np.clip(-Pm[2, 2] - Pm[3, 2] / zeye, 0, 1)
+            d24 = np.rint(z * 16777215).astype(np.int64)
+            kk = (d24 << 32) | (base + k)
+            rows = height - 1 - jj
+            cur = key[rows, ii]
+            win = inside & (kk < cur)
+            key[rows[win], ii[win]] = kk[win]
+            atten = 0.9 + 0.1 * np.maximum(0, nz)
+            col = np.stack([atten * rgb[0], atten * rgb[1], atten * rgb[2], atten], -1)
+            shade[rows[win], ii[win]] = col[win]
+        info.append(base)
+        base += len(pos)
+    empty = key == np.iinfo(np.int64).max
+    rgba = np.rint(np.clip(shade, 0, 1) * 255).astype(np.uint8)
+    rgba[empty] = 255
+    winner = np.where(empty, -1, key & 0xFFFFFFFF)
+    return rgba, winner
