@@ -17,11 +17,20 @@ import oracle
 pytestmark = pytest.mark.gpu
 
 W, H = 160, 100
-EYE, CENTRE, UP = (0.25, 0.6, 1.4), (0.25, 0.15, 0.25), (0.0, 1.0, 0.0)
+UP = (0.0, 1.0, 0.0)
+TINY_VIEW = ((0.05, 0.1, 0.18), (0.05, 0.05, 0.05), 0.01, 10.0)   # eye, centre, near, far
+PAIR_VIEW = ((0.25, 0.151, 0.13), (0.25, 0.15, 0.0), 0.01, 10.0)
+TS_VIEW = ((0.15, 0.3, 0.55), (0.15, 0.12, 0.15), 0.1, 100.0)
 
 
-def camera(sphlib):
-    return sphlib.Camera.look(EYE, CENTRE, UP, 60.0, W / H, 0.1, 100.0)
+def camera(sphlib, view):
+    eye, centre, zn, zf = view
+    return sphlib.Camera.look(eye, centre, UP, 60.0, W / H, zn, zf)
+
+
+def reference(view, passes):
+    eye, centre, zn, zf = view
+    return oracle.render_splats(oracle.look_at(eye, centre, UP), oracle.perspective(60.0, W / H, zn, zf), passes, W, H)
 
 
 def radius(sc):
@@ -41,10 +50,9 @@ def test_particles_match_oracle(sphlib):
     sc = scenes.dam_break(8, 8, 8, (0, 0, 0), (0.5, 0.5, 0.5), 3, "tiny", 1)
     with sphlib.ParticleSimulation(sc.params, sc.positions, sc.velocities, sc.options) as sim:
         sim.step(count=5)
-        img, depth = sim.render(camera(sphlib), W, H, sphlib.SPH_RENDER_PARTICLES, depth=True)
+        img, depth = sim.render(camera(sphlib, TINY_VIEW), W, H, sphlib.SPH_RENDER_PARTICLES, depth=True)
         pos = sim.positions()
-    ref, win = oracle.render_splats(oracle.look_at(EYE, CENTRE, UP), oracle.perspective(60, W / H, 0.1, 100),
-                                    [(pos, radius(sc), (0.0, 0.0, 0.9))], W, H)
+    ref, win = reference(TINY_VIEW, [(pos, radius(sc), (0.0, 0.0, 0.9))])
     compare(img, ref)
     assert (depth[win < 0] == 1.0).all() and (depth[win >= 0] < 1.0).mean() > 0.99
     # colours are the shader's: blue, shaded 0.9 + 0.1 n.z
@@ -59,16 +67,15 @@ def test_depth_order_and_ties(sphlib):
     sc = scenes.dam_break(1, 1, 1, (0.2, 0.2, 0.2), (0.5, 0.5, 0.5), 1, "one", 1)
     p = P.SimulationParameters.from_buffer_copy(bytes(sc.params))
     p.numParticles = 3
-    pos = np.array([[0.25, 0.15, 0.10],   # behind
-                    [0.25, 0.15, 0.30],   # in front (nearer the eye at z = 1.4), drawn after
-                    [0.25, 0.15, 0.30]],  # the same place as particle 1, drawn last
+    R = radius(scenes.Scene("t", p, sc.options, None, None))
+    pos = np.array([[0.25 + 0.8 * R, 0.15, 0.10],   # behind, drawn first
+                    [0.25, 0.15, 0.11],             # in front (the eye is at z = 0.13), drawn after
+                    [0.25, 0.15, 0.11]],            # the same place as particle 1, drawn last
                    np.float32)
     with sphlib.ParticleSimulation(p, pos, np.zeros_like(pos), sc.options) as sim:
-        img, depth = sim.render(camera(sphlib), W, H, sphlib.SPH_RENDER_PARTICLES, depth=True)
-    R = radius(scenes.Scene("t", p, sc.options, pos, pos))
-    ref, win = oracle.render_splats(oracle.look_at(EYE, CENTRE, UP), oracle.perspective(60, W / H, 0.1, 100),
-                                    [(pos, R, (0.0, 0.0, 0.9))], W, H)
-    assert (win == 0).sum() > 0 and (win == 1).sum() > 0 and (win == 2).sum() == 0
+        img = sim.render(camera(sphlib, PAIR_VIEW), W, H, sphlib.SPH_RENDER_PARTICLES)
+    ref, win = reference(PAIR_VIEW, [(pos, R, (0.0, 0.0, 0.9))])
+    assert (win == 0).sum() > 100 and (win == 1).sum() > 100 and (win == 2).sum() == 0
     compare(img, ref, min_equal=0.995)
 
 
@@ -77,7 +84,7 @@ def test_two_scale_render_matches_oracle(sphlib):
     with sphlib.ParticleSimulation(sc.params, sc.positions, sc.velocities, sc.options) as sim:
         for _ in range(3):
             sim.step(mode=sphlib.SPH_STEP_TWO_SCALE)
-        cam = camera(sphlib)
+        cam = camera(sphlib, TS_VIEW)
         img = sim.render(cam, W, H, sphlib.SPH_RENDER_TWO_SCALE)
         sub = sim.render(cam, W, H, sphlib.SPH_RENDER_SUB_PARTICLES)
         c = sim.counts()
@@ -90,10 +97,9 @@ def test_two_scale_render_matches_oracle(sphlib):
     R = radius(sc)
     passes = [(pos[dflt], R, (0.0, 0.0, 0.9)), (spos[slots[:reg]], R / 2, (0.9, 0.9, 0.0)),
               (spos[slots[reg:]], R / 2, (0.9, 0.0, 0.0))]
-    V, Pm = oracle.look_at(EYE, CENTRE, UP), oracle.perspective(60, W / H, 0.1, 100)
-    ref, _ = oracle.render_splats(V, Pm, passes, W, H)
+    ref, _ = reference(TS_VIEW, passes)
     compare(img, ref)
-    ref_sub, _ = oracle.render_splats(V, Pm, passes[1:], W, H)
+    ref_sub, _ = reference(TS_VIEW, passes[1:])
     compare(sub, ref_sub)
     # red and yellow sub-particles are both in view
     assert ((img[..., 0] > 200) & (img[..., 1] < 30)).any() and ((img[..., 0] > 200) & (img[..., 1] > 200)).any()
@@ -103,7 +109,7 @@ def test_render_refuses_before_a_two_scale_step(sphlib):
     sc = scenes.dam_break(8, 8, 8, (0, 0, 0), (0.5, 0.5, 0.5), 3, "tiny", 1)
     with sphlib.ParticleSimulation(sc.params, sc.positions, sc.velocities, sc.options) as sim:
         with pytest.raises(sphlib.SphError):
-            sim.render(camera(sphlib), W, H, sphlib.SPH_RENDER_TWO_SCALE)
+            sim.render(camera(sphlib, TINY_VIEW), W, H, sphlib.SPH_RENDER_TWO_SCALE)
 
 
 def test_cell_relative_renders_the_same_image(sphlib):
@@ -113,5 +119,5 @@ def test_cell_relative_renders_the_same_image(sphlib):
     imgs = []
     for opts in (sc.options, o):
         with sphlib.ParticleSimulation(sc.params, sc.positions, sc.velocities, opts) as sim:
-            imgs.append(sim.render(camera(sphlib), W, H, sphlib.SPH_RENDER_PARTICLES))
+            imgs.append(sim.render(camera(sphlib, TINY_VIEW), W, H, sphlib.SPH_RENDER_PARTICLES))
     np.testing.assert_array_equal(imgs[0], imgs[1])
