@@ -101,8 +101,10 @@ def test_two_scale_render_matches_oracle(sphlib):
     compare(img, ref)
     ref_sub, _ = reference(TS_VIEW, passes[1:])
     compare(sub, ref_sub)
-    # red and yellow sub-particles are both in view
-    assert ((img[..., 0] > 200) & (img[..., 1] < 30)).any() and ((img[..., 0] > 200) & (img[..., 1] > 200)).any()
+    # the default particles are blue; without them the boundary children (red)
+    # that wrap the split region are in view
+    assert ((img[..., 2] > 200) & (img[..., 0] < 30)).any()
+    assert ((sub[..., 0] > 200) & (sub[..., 1] < 30)).any()
 
 
 def test_render_refuses_before_a_two_scale_step(sphlib):
