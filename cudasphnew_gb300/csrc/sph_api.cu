@@ -44,7 +44,9 @@ sph_status record_error(sph_status st, const char* file, int line, const std::st
 
 namespace sph {
 
-RowTables rows_of(const sph_sim* s) { return RowTables{s->sb.cellOffset, s->sb.halfOffset, s->sb.scenes}; }
+RowTables rows_of(const sph_sim* s) {
+    return RowTables{s->sb.cellOffset, s->sb.halfOffset, s->sb.scenes, s->sb.skip};
+}
 
 GridDev make_grid(const SimulationParameters& P, bool sub) {
     GridDev g;
@@ -151,7 +153,7 @@ void free_all(sph_sim* s) {
                     s->sb.keySlot, s->sb.tmpIds, s->sb.sortedHash, s->sb.sortedIds, s->sb.workIds,
                     s->sb.xS, s->sb.halfOffset, s->scanBlock,
                     s->status, s->staging, s->map4, s->mapDist, s->rowStart, s->rowMask, s->diagBuf,
-                    s->scenesDev};
+                    s->scenesDev, s->reuse};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     void* tsPtrs[] = {s->ts.state,     s->ts.blockCounts, s->ts.blockOffsets, s->ts.counts,
@@ -255,6 +257,8 @@ void enqueue_coarse(sph_sim* s, const GridDev& g, const PhysDev& ph, int collide
     mark(ST_DENSITY);
     // density and forces read the sorted copies only
     launch_density(n, s->posS, rows_of(s), g, ph, s->map, s->rho4S, s->rowStart, s->rowMask, cfg, st);
+    // the sorted copies are now this step's own: a reuse the audit granted is used up
+    cudaMemsetAsync(s->reuse, 0, sizeof(int), st);
     mark(ST_FORCE);
     if (!force) return;
     launch_force(n, s->posS, s->velS, s->rho4S, s->sb.workIds, rows_of(s), g, ph, s->map, collide, s->rowStart,
@@ -262,7 +266,7 @@ void enqueue_coarse(sph_sim* s, const GridDev& g, const PhysDev& ph, int collide
     mark(ST_COUNT);
 }
 
-void enqueue_density_only(sph_sim* s, const float4* pos, const float4* vel) {
+void enqueue_density_only(sph_sim* s, const float4* pos, const float4* vel, bool masks) {
     cudaStream_t st = s->stream;
     const int n = s->n;
     GridDev g = grid_of(s);
@@ -272,7 +276,7 @@ void enqueue_density_only(sph_sim* s, const float4* pos, const float4* vel) {
     launch_scatter(n, s->sb, st);
     launch_rank_gather(n, s->sb, pos, vel, g, s->posS, s->velS, st);
     StepConfig cfg = s->cfg;
-    cfg.forceVariant = FORCE_MASK;  // no force stage follows: record no neighbour masks
+    cfg.forceVariant = masks ? FORCE_PRETESTED : FORCE_MASK;  // whether to record the neighbour masks
     launch_density(n, s->posS, rows_of(s), g, ph, s->map, s->rho4S, s->rowStart, s->rowMask, cfg, st);
 }
 
@@ -363,10 +367,13 @@ sph_status alloc_handle(sph_sim* s, int n, long long C) {
     s->sb.scanFlags = s->scanBlock + 2;
     s->sb.maxTiles = (int)tiles;
     SPH_CUDA(dalloc(&s->status, 1));
+    SPH_CUDA(dalloc(&s->reuse, 1));
+    s->sb.skip = s->reuse;
     SPH_CUDA(cudaMallocHost((void**)&s->statusHost, sizeof(unsigned int)));
     SPH_CUDA(dalloc(&s->staging, (size_t)n * 10));
     SPH_CUDA(cudaMemsetAsync(s->sb.cnt, 0, sizeof(int) * ((size_t)C + 1 + SCAN_TILE), s->stream));
     SPH_CUDA(cudaMemsetAsync(s->status, 0, sizeof(unsigned int), s->stream));
+    SPH_CUDA(cudaMemsetAsync(s->reuse, 0, sizeof(int), s->stream));
     SPH_CUDA(cudaMemsetAsync(s->vel, 0, sizeof(float4) * n, s->stream));
     SPH_CUDA(cudaMemsetAsync(s->rho4S, 0, sizeof(float4) * n, s->stream));
     SPH_CUDA(cudaMemsetAsync(s->accS, 0, sizeof(float4) * n, s->stream));
@@ -582,6 +589,7 @@ sph_status sph_bind(sph_handle s, const SimulationParameters* params) {
         cudaFree(tmp);
         SPH_CUDA(e);
     }
+    SPH_CUDA(cudaMemsetAsync(s->reuse, 0, sizeof(int), s->stream));
     s->P = *params;
     invalidate_graphs(s);
     return SPH_OK;
@@ -793,6 +801,7 @@ sph_status sph_write(sph_handle s, int field, const void* src, size_t bytes) {
     if (!s || !src) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "NULL argument");
     const int n = s->n;
     cudaStream_t q = s->stream;
+    SPH_CUDA(cudaMemsetAsync(s->reuse, 0, sizeof(int), q));  // the state changes under the sorted copies
     switch (field) {
         case SPH_FIELD_VERTEX_DATA:
         case SPH_FIELD_VELOCITY:

@@ -185,12 +185,14 @@ void enqueue_audit(sph_sim* s, Corrector* C) {
     for (int k = 1; k < C->cfg.stride; k++) enqueue_step(s, SPH_STEP_PLAIN, false);
     enqueue_density_only(s, s->pos, s->vel);
     launch_unpermute(s->n, s->sb.workIds, s->rho4S, 0, C->rhoB, 1, 0, q);
-    enqueue_density_only(s, C->lPos, C->lVel);
+    // last: the learned result, with the neighbour masks, so that when the
+    // audit keeps it the next step finds its sort and density done
+    enqueue_density_only(s, C->lPos, C->lVel, true);
     launch_unpermute(s->n, s->sb.workIds, s->rho4S, 0, C->rhoA, 1, 0, q);
     cudaMemsetAsync(C->errBits, 0, sizeof(unsigned int), q);
     launch_audit(s->n, C->rhoA, C->rhoB, C->errBits, q);
     launch_audit_select(s->n, C->errBits, C->cfg.densityTolerance, C->lPos, C->lVel, s->pos, s->vel, C->counters,
-                        q);
+                        s->reuse, q);
 }
 
 void enqueue_kind(sph_sim* s, Corrector* C, int kind) {

@@ -99,8 +99,11 @@ void launch_targets(int n, const float4* refPos, const float4* refVel, const flo
 // in *errBits, which must start at 0); then, when err <= tol, copies
 // (srcPos, srcVel) over (pos, vel) and counts an acceptance, else a rollback.
 void launch_audit(int n, const float* rhoA, const float* rhoB, unsigned int* errBits, cudaStream_t s);
+// Keeps the learned result (srcPos, srcVel) when the audit error is within
+// tol, else the plain one already in (pos, vel); *reuse = kept learned (the
+// sorted copies, last made from the learned result, then hold the state).
 void launch_audit_select(int n, const unsigned int* errBits, float tol, const float4* srcPos,
-                         const float4* srcVel, float4* pos, float4* vel, unsigned int* counters,
+                         const float4* srcVel, float4* pos, float4* vel, unsigned int* counters, int* reuse,
                          cudaStream_t s);
 
 // The learned step's force stage with the MLP fused in (sph_step.cu): the

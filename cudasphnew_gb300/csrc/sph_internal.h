@@ -86,6 +86,8 @@ struct SortBuffers {
     unsigned int* tileCounter;
     int maxTiles;
     const SceneDev* scenes;   // batched handles: per-scene grids (else NULL)
+    const int* skip;          // when non-NULL and set on the device, the sorted copies and
+                              // tables already hold the current state: the sort stages return
 };
 
 // Two-scale state (AdvanceTwoScale): particle states, the three-way lists,
@@ -118,6 +120,7 @@ struct RowTables {
     const int* cellOffset;  // [C+1]
     const int* halfOffset;  // [C+1], valid for occupied cells
     const SceneDev* scenes; // batched handles: per-scene grids, constants, maps (else NULL)
+    const int* skip;        // as SortBuffers::skip, read by the density stage only
 };
 
 // Launch configuration of the step (chosen per handle; see the autotuner).

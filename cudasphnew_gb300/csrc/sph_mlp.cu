@@ -485,7 +485,8 @@ __global__ void k_audit(int n, const float* __restrict__ rhoA, const float* __re
 
 __global__ void k_audit_select(int n, const unsigned int* __restrict__ errBits, float tol,
                                const float4* __restrict__ srcPos, const float4* __restrict__ srcVel,
-                               float4* __restrict__ pos, float4* __restrict__ vel, unsigned int* counters) {
+                               float4* __restrict__ pos, float4* __restrict__ vel, unsigned int* counters,
+                               int* reuse) {
     const unsigned int bits = *errBits;
     const bool accept = __uint_as_float(bits) <= tol;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -494,6 +495,7 @@ __global__ void k_audit_select(int n, const unsigned int* __restrict__ errBits, 
         if (!accept) counters[1] += 1;  // rollbacks
         counters[2] = bits;             // last error
         counters[3] = max(counters[3], bits);
+        if (reuse) *reuse = accept ? 1 : 0;
     }
     if (accept && i < n) {
         pos[i] = srcPos[i];
@@ -562,10 +564,9 @@ void launch_audit(int n, const float* rhoA, const float* rhoB, unsigned int* err
     k_audit<<<(n + 255) / 256, 256, 0, s>>>(n, rhoA, rhoB, errBits);
 }
 
-void launch_audit_select(int n, const unsigned int* errBits, float tol, const float4* srcPos,
-                         const float4* srcVel, float4* pos, float4* vel, unsigned int* counters,
-                         cudaStream_t s) {
-    k_audit_select<<<(n + 255) / 256, 256, 0, s>>>(n, errBits, tol, srcPos, srcVel, pos, vel, counters);
+void launch_audit_select(int n, const unsigned int* errBits, float tol, const float4* srcPos, const float4* srcVel,
+                         float4* pos, float4* vel, unsigned int* counters, int* reuse, cudaStream_t s) {
+    k_audit_select<<<(n + 255) / 256, 256, 0, s>>>(n, errBits, tol, srcPos, srcVel, pos, vel, counters, reuse);
 }
 
 }  // namespace sph

@@ -54,6 +54,8 @@ struct sph_sim {
     sph::SortBuffers sb{};
     unsigned long long* scanBlock = nullptr;
     unsigned int* status = nullptr;     // device status word
+    int* reuse = nullptr;               // device flag: the sorted copies hold the current state
+                                        // (set by an accepting audit, used up by the next step)
     unsigned int* statusHost = nullptr; // pinned copy
     float* staging = nullptr;           // device AoS staging, n*10 floats
     std::vector<float> sdMass, sdEnergy;  // SD_MASS / SD_ENERGY columns (never touched by the step)
@@ -123,9 +125,9 @@ void enqueue_step(sph_sim* s, int mode, bool timing);
 void enqueue_coarse(sph_sim* s, const GridDev& g, const PhysDev& ph, int collide, cudaEvent_t* ev,
                     const FeatureOut* feat = nullptr, bool force = true);
 // Hash, sort and density of the state (pos, vel) into the handle's sorted
-// copies (posS, velS, rho4S) and cell tables (no neighbour masks); nothing
-// is integrated.
-void enqueue_density_only(sph_sim* s, const float4* pos, const float4* vel);
+// copies (posS, velS, rho4S) and cell tables, with the neighbour masks when
+// `masks`; nothing is integrated.
+void enqueue_density_only(sph_sim* s, const float4* pos, const float4* vel, bool masks = false);
 // Marks every captured step graph of the handle stale.
 void invalidate_graphs(sph_sim* s);
 

@@ -103,9 +103,10 @@ void launch_pack_aos(const float4* in, int n, float* aos, int stride, int offset
 // cell coordinates.
 template <bool BATCH, bool REL>
 __global__ void k_hash_count(int n, const float4* __restrict__ pos, GridDev g_, const SceneDev* __restrict__ scenes,
-                             int* __restrict__ cnt, int2* __restrict__ keySlot, unsigned int* status) {
+                             int* __restrict__ cnt, int2* __restrict__ keySlot, unsigned int* status,
+                             const int* __restrict__ skip) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    if (i >= n || (skip && *skip)) return;
     float4 p = pos[i];
     const GridDev& g = BATCH ? scenes[__float_as_int(p.w)].g : g_;
     bool outside = false;
@@ -130,11 +131,14 @@ void launch_hash_count(int n, const float4* pos, GridDev g, SortBuffers sb, unsi
                        cudaStream_t s) {
     if (n <= 0) return;
     if (sb.scenes)
-        k_hash_count<true, false><<<(n + 255) / 256, 256, 0, s>>>(n, pos, g, sb.scenes, sb.cnt, sb.keySlot, status);
+        k_hash_count<true, false><<<(n + 255) / 256, 256, 0, s>>>(n, pos, g, sb.scenes, sb.cnt, sb.keySlot, status,
+                                                                  sb.skip);
     else if (g.rel)
-        k_hash_count<false, true><<<(n + 255) / 256, 256, 0, s>>>(n, pos, g, nullptr, sb.cnt, sb.keySlot, status);
+        k_hash_count<false, true><<<(n + 255) / 256, 256, 0, s>>>(n, pos, g, nullptr, sb.cnt, sb.keySlot, status,
+                                                                  sb.skip);
     else
-        k_hash_count<false, false><<<(n + 255) / 256, 256, 0, s>>>(n, pos, g, nullptr, sb.cnt, sb.keySlot, status);
+        k_hash_count<false, false><<<(n + 255) / 256, 256, 0, s>>>(n, pos, g, nullptr, sb.cnt, sb.keySlot, status,
+                                                                  sb.skip);
 }
 
 // ---------------------------------------------------------------------------
@@ -150,7 +154,8 @@ constexpr int SPIN_LIMIT = 1 << 22;
 
 __global__ void __launch_bounds__(SCAN_THREADS)
 k_cell_scan(int total, int* __restrict__ cnt, int* __restrict__ out, unsigned long long* flags,
-            unsigned int* tileCounter, unsigned int* status) {
+            unsigned int* tileCounter, unsigned int* status, const int* __restrict__ skip) {
+    if (skip && *skip) return;  // every block: no tile is taken, none waited on
     __shared__ int s_tile;
     __shared__ int s_warp[SCAN_THREADS / 32];
     __shared__ int s_prefix;
@@ -271,16 +276,16 @@ void launch_cell_scan(int numCells, SortBuffers sb, unsigned int* status, cudaSt
     // tile counter (first 16 bytes) and the tile states that follow it
     cudaMemsetAsync(sb.tileCounter, 0, 16 + sizeof(unsigned long long) * (size_t)tiles, s);
     k_cell_scan<<<tiles, SCAN_THREADS, 0, s>>>(total, sb.cnt, sb.cellOffset, sb.scanFlags,
-                                               sb.tileCounter, status);
+                                               sb.tileCounter, status, sb.skip);
 }
 
 // ---------------------------------------------------------------------------
 // Stage 3: scatter ids into their cell segments (arrival order)
 // ---------------------------------------------------------------------------
 __global__ void k_scatter(int n, const int2* __restrict__ keySlot, const int* __restrict__ cellOffset,
-                          int* __restrict__ tmpIds, int* __restrict__ sortedHash) {
+                          int* __restrict__ tmpIds, int* __restrict__ sortedHash, const int* __restrict__ skip) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    if (i >= n || (skip && *skip)) return;
     int2 ks = keySlot[i];
     int dst = __ldg(cellOffset + ks.x) + ks.y;
     tmpIds[dst] = i;
@@ -289,7 +294,7 @@ __global__ void k_scatter(int n, const int2* __restrict__ keySlot, const int* __
 
 void launch_scatter(int n, SortBuffers sb, cudaStream_t s) {
     if (n <= 0) return;
-    k_scatter<<<(n + 255) / 256, 256, 0, s>>>(n, sb.keySlot, sb.cellOffset, sb.tmpIds, sb.sortedHash);
+    k_scatter<<<(n + 255) / 256, 256, 0, s>>>(n, sb.keySlot, sb.cellOffset, sb.tmpIds, sb.sortedHash, sb.skip);
 }
 
 // ---------------------------------------------------------------------------
@@ -317,9 +322,10 @@ __global__ void k_rank_gather(int n, const int* __restrict__ sortedHash, const i
                               const int* __restrict__ tmpIds, const float4* __restrict__ pos,
                               const float4* __restrict__ vel, GridDev g_, const SceneDev* __restrict__ scenes,
                               int* __restrict__ sortedIds, int* __restrict__ workIds, int* __restrict__ halfOffset,
-                              float4* __restrict__ posS, float4* __restrict__ velS, float* __restrict__ xS) {
+                              float4* __restrict__ posS, float4* __restrict__ velS, float* __restrict__ xS,
+                              const int* __restrict__ skip) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
+    if (k >= n || (skip && *skip)) return;
     int c = sortedHash[k];
     int s = __ldg(cellOffset + c), e = __ldg(cellOffset + c + 1);
     int my = tmpIds[k];
@@ -353,15 +359,15 @@ void launch_rank_gather(int n, SortBuffers sb, const float4* pos, const float4* 
     if (sb.scenes)
         k_rank_gather<true, false><<<grid, 256, 0, s>>>(n, sb.sortedHash, sb.cellOffset, sb.tmpIds, pos, vel, g,
                                                         sb.scenes, sb.sortedIds, sb.workIds, sb.halfOffset, posS,
-                                                        velS, sb.xS);
+                                                        velS, sb.xS, sb.skip);
     else if (g.rel)
         k_rank_gather<false, true><<<grid, 256, 0, s>>>(n, sb.sortedHash, sb.cellOffset, sb.tmpIds, pos, vel, g,
                                                         nullptr, sb.sortedIds, sb.workIds, sb.halfOffset, posS, velS,
-                                                        sb.xS);
+                                                        sb.xS, sb.skip);
     else
         k_rank_gather<false, false><<<grid, 256, 0, s>>>(n, sb.sortedHash, sb.cellOffset, sb.tmpIds, pos, vel, g,
                                                          nullptr, sb.sortedIds, sb.workIds, sb.halfOffset, posS,
-                                                         velS, sb.xS);
+                                                         velS, sb.xS, sb.skip);
 }
 
 // ---------------------------------------------------------------------------

@@ -41,7 +41,7 @@ __global__ void __launch_bounds__(256)
 k_density(int n, const float4* __restrict__ posS, RowTables T, GridDev g_, PhysDev ph_, MapDev map_, int window,
           float4* __restrict__ rho4S, RowMasks M) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    if (i >= n || (T.skip && *T.skip)) return;
     const float4 xi = posS[i];
     // batched handles: the particle's own scene supplies grid, constants and maps
     const SceneDev* S = BATCH ? T.scenes + __float_as_int(xi.w) : nullptr;
