@@ -44,6 +44,18 @@ sph_status record_error(sph_status st, const char* file, int line, const std::st
 
 namespace sph {
 
+// The device address of page-locked host memory (pinned or registered),
+// which kernels read and write directly over the host link; NULL for
+// pageable memory, which goes through the staging buffer.
+void* host_device_ptr(const void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();  // pageable memory on older drivers: clear the error
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 RowTables rows_of(const sph_sim* s) {
     return RowTables{s->sb.cellOffset, s->sb.halfOffset, s->sb.scenes, s->sb.skip};
 }
@@ -409,6 +421,10 @@ sph_status latched_status(sph_sim* s) {
     SPH_CUDA(cudaMemcpyAsync(s->statusHost, s->status, sizeof(unsigned int), cudaMemcpyDeviceToHost,
                              s->stream));
     SPH_CUDA(cudaStreamSynchronize(s->stream));
+    return status_of_host_copy(s);
+}
+
+sph_status status_of_host_copy(const sph_sim* s) {
     unsigned int v = *s->statusHost;
     if (v & STATUS_NON_FINITE) SPH_FAIL(SPH_ERR_NON_FINITE, "a non-finite particle position entered the step");
     if (v & STATUS_OUT_OF_DOMAIN)
@@ -754,39 +770,43 @@ sph_status sph_read(sph_handle s, int field, void* dst, size_t bytes) {
         default: SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "unknown field");
     }
     if (bytes < need) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "destination too small");
-    sph_status st = latched_status(s);
-    if (st) return st;
     cudaStream_t q = s->stream;
+    // page-locked destinations are written by the kernels themselves
+    float* direct = static_cast<float*>(host_device_ptr(dst));
+    float* out = direct ? direct : s->staging;
     switch (field) {
         case SPH_FIELD_VERTEX_DATA:
-            if (s->O.cellRelative) launch_rel_to_abs(n, s->pos, grid_of(s), s->staging, 3, nullptr, q);
-            else launch_pack_aos(s->pos, n, s->staging, 3, 0, q);
+            if (s->O.cellRelative) launch_rel_to_abs(n, s->pos, grid_of(s), out, 3, nullptr, q);
+            else launch_pack_aos(s->pos, n, out, 3, 0, q);
             break;
-        case SPH_FIELD_VELOCITY: launch_pack_aos(s->vel, n, s->staging, 3, 0, q); break;
+        case SPH_FIELD_VELOCITY: launch_pack_aos(s->vel, n, out, 3, 0, q); break;
         case SPH_FIELD_ACCELERATION:
-            if (s->stepped) launch_unpermute(n, s->sb.workIds, s->accS, -1, s->staging, 3, 0, q);
-            else SPH_CUDA(cudaMemsetAsync(s->staging, 0, need, q));
+            if (s->stepped) launch_unpermute(n, s->sb.workIds, s->accS, -1, out, 3, 0, q);
+            else SPH_CUDA(cudaMemsetAsync(out, 0, need, q));
             break;
         case SPH_FIELD_DENSITY:
         case SPH_FIELD_PRESSURE:
             if (s->stepped)
-                launch_unpermute(n, s->sb.workIds, s->rho4S, field == SPH_FIELD_DENSITY ? 0 : 1, s->staging,
-                                 1, 0, q);
-            else SPH_CUDA(cudaMemsetAsync(s->staging, 0, need, q));
+                launch_unpermute(n, s->sb.workIds, s->rho4S, field == SPH_FIELD_DENSITY ? 0 : 1, out, 1, 0, q);
+            else SPH_CUDA(cudaMemsetAsync(out, 0, need, q));
             break;
         case SPH_FIELD_SIMULATION_DATA:
-            SPH_CUDA(cudaMemsetAsync(s->staging, 0, need, q));
+            SPH_CUDA(cudaMemsetAsync(out, 0, need, q));
             if (s->stepped) {
-                launch_unpermute(n, s->sb.workIds, s->rho4S, 0, s->staging, 10, 1, q);
-                launch_unpermute(n, s->sb.workIds, s->rho4S, 1, s->staging, 10, 2, q);
-                launch_unpermute(n, s->sb.workIds, s->accS, -1, s->staging, 10, 3, q);
+                launch_unpermute(n, s->sb.workIds, s->rho4S, 0, out, 10, 1, q);
+                launch_unpermute(n, s->sb.workIds, s->rho4S, 1, out, 10, 2, q);
+                launch_unpermute(n, s->sb.workIds, s->accS, -1, out, 10, 3, q);
             }
-            launch_pack_aos(s->vel, n, s->staging, 10, 6, q);
+            launch_pack_aos(s->vel, n, out, 10, 6, q);
             break;
     }
     SPH_CUDA(cudaGetLastError());
-    SPH_CUDA(cudaMemcpyAsync(dst, s->staging, need, cudaMemcpyDeviceToHost, q));
+    if (!direct) SPH_CUDA(cudaMemcpyAsync(dst, s->staging, need, cudaMemcpyDeviceToHost, q));
+    // one synchronisation: the status word comes back with the data
+    SPH_CUDA(cudaMemcpyAsync(s->statusHost, s->status, sizeof(unsigned int), cudaMemcpyDeviceToHost, q));
     SPH_CUDA(cudaStreamSynchronize(q));
+    sph_status st = status_of_host_copy(s);
+    if (st) return st;
     if (field == SPH_FIELD_SIMULATION_DATA) {
         float* f = static_cast<float*>(dst);
         for (int i = 0; i < n; i++) {
@@ -804,15 +824,21 @@ sph_status sph_write(sph_handle s, int field, const void* src, size_t bytes) {
     SPH_CUDA(cudaMemsetAsync(s->reuse, 0, sizeof(int), q));  // the state changes under the sorted copies
     switch (field) {
         case SPH_FIELD_VERTEX_DATA:
-        case SPH_FIELD_VELOCITY:
+        case SPH_FIELD_VELOCITY: {
             if (bytes < sizeof(float) * 3 * (size_t)n) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "source too small");
-            SPH_CUDA(cudaMemcpyAsync(s->staging, src, sizeof(float) * 3 * (size_t)n, cudaMemcpyHostToDevice, q));
-            launch_unpack_aos(s->staging, 3, 0, n, field == SPH_FIELD_VERTEX_DATA ? s->pos : s->vel, q);
+            // page-locked sources are read by the unpacking kernel itself
+            const float* in = static_cast<const float*>(host_device_ptr(src));
+            if (!in) {
+                SPH_CUDA(cudaMemcpyAsync(s->staging, src, sizeof(float) * 3 * (size_t)n, cudaMemcpyHostToDevice, q));
+                in = s->staging;
+            }
+            launch_unpack_aos(in, 3, 0, n, field == SPH_FIELD_VERTEX_DATA ? s->pos : s->vel, q);
             if (field == SPH_FIELD_VERTEX_DATA && s->O.cellRelative) launch_abs_to_rel(n, s->pos, grid_of(s), q);
             if (field == SPH_FIELD_VERTEX_DATA && s->numScenes > 1)  // restore the scene index lanes
                 for (int k = 0; k < s->numScenes; k++)
                     launch_set_scene(s->pos + s->sceneStart[k], (int)(s->sceneStart[k + 1] - s->sceneStart[k]), k, q);
             break;
+        }
         case SPH_FIELD_SIMULATION_DATA:
             if (bytes < sizeof(float) * 10 * (size_t)n) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "source too small");
             SPH_CUDA(cudaMemcpyAsync(s->staging, src, sizeof(float) * 10 * (size_t)n, cudaMemcpyHostToDevice, q));

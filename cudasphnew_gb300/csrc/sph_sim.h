@@ -136,6 +136,10 @@ sph_status corrector_step(sph_sim* s, int count, bool useGraph);
 void corrector_free(sph_sim* s);
 // Waits for the handle's stream and maps the latched device status.
 sph_status latched_status(sph_sim* s);
+// The status held in statusHost (already copied back and synchronised).
+sph_status status_of_host_copy(const sph_sim* s);
+// Device address of page-locked host memory, or NULL (pageable memory).
+void* host_device_ptr(const void* p);
 // Allocates the device state of n particles over C cells (zeroed counters,
 // velocities and per-step outputs) and the handle's stream.
 sph_status alloc_handle(sph_sim* s, int n, long long C);

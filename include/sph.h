@@ -265,11 +265,17 @@ sph_status sph_step_many(sph_handle h, int mode, int count);
 sph_status sph_synchronize(sph_handle h);
 
 /* Copies a field to host memory (GetParticleState, SaveParticleInfo,
- * :2238-2243, :2785-2852).  `bytes` must be at least the field's size. */
+ * :2238-2243, :2785-2852).  `bytes` must be at least the field's size.
+ * Returns when the data is in place.  A page-locked destination (pinned or
+ * registered) is written by the gathering kernel itself over the host link;
+ * pageable memory goes through a device staging buffer. */
 sph_status sph_read(sph_handle h, int field, void* dst, size_t bytes);
 
 /* Overwrites a field from host memory (SPH_FIELD_VERTEX_DATA,
- * SPH_FIELD_VELOCITY or SPH_FIELD_SIMULATION_DATA). */
+ * SPH_FIELD_VELOCITY or SPH_FIELD_SIMULATION_DATA).  A page-locked source of
+ * positions or velocities is read by the unpacking kernel itself, later on
+ * the handle's stream (as an asynchronous copy from pinned memory would be):
+ * keep it unchanged until the next synchronising call. */
 sph_status sph_write(sph_handle h, int field, const void* src, size_t bytes);
 
 /* The neighbour-search tables of the last step (SaveInfoTable, :2709-2783):
