@@ -631,7 +631,14 @@ sph_status sph_step(sph_handle s, int mode) {
         sph_status st = ensure_two_scale(s);
         if (st) return st;
     }
-    enqueue_step(s, mode, mode != SPH_STEP_SUB_ONLY && s->timingCap > 0);
+    // a step graph captured by sph_step_many for this mode replays as one launch
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    SPH_CUDA(cudaStreamIsCapturing(s->stream, &cs));
+    if (s->timingCap == 0 && s->graphValid && s->graphMode == mode && mode != SPH_STEP_SUB_ONLY &&
+        cs == cudaStreamCaptureStatusNone)
+        SPH_CUDA(cudaGraphLaunch(s->graphExec, s->stream));
+    else
+        enqueue_step(s, mode, mode != SPH_STEP_SUB_ONLY && s->timingCap > 0);
     SPH_CUDA(cudaGetLastError());
     if (mode != SPH_STEP_SUB_ONLY) {
         s->numTimeSteps++;
