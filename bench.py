@@ -73,6 +73,26 @@ def dist_setup(n_gpus):
     return rank, world, local, dist
 
 
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, x):
+    """The slowest rank's time: the job's time (replicas, no data exchange)."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_value(world, n, steps, ms):
+    """Particle-steps per second of all replicas together over the slowest rank's time."""
+    return world * n * steps / (ms / 1e3)
+
+
 def load_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -501,17 +521,6 @@ def run_ours(args):
     sim = lib.ParticleSimulation(sc.params, sc.positions, sc.velocities, sc.options, sc.boundary)
     sim.set_stream(stream.cuda_stream)
 
-    def barrier():
-        if dist is not None:
-            dist.barrier()
-
-    def max_over_ranks(x):
-        if dist is None:
-            return x
-        t = torch.tensor([x], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
-
     # ---- warm-up (also captures the step graph) ---------------------------
     clocks = ClockSampler(local)
     clocks.start()
@@ -527,7 +536,7 @@ def run_ours(args):
     # ---- timed region: K graph-launched steps, device-resident ----------
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
-    barrier()
+    barrier(dist)
     torch.cuda.synchronize()
     t_wall0 = time.time()
     with torch.cuda.stream(stream):
@@ -536,12 +545,12 @@ def run_ours(args):
         e1.record()
     torch.cuda.synchronize()
     t_wall1 = time.time()
-    barrier()
+    barrier(dist)
     sim.synchronize()  # raises on a latched device error
-    ms = max_over_ranks(e0.elapsed_time(e1))
+    ms = max_over_ranks(dist, e0.elapsed_time(e1))
     clocks.stop()
     clk = clocks.summary(t_wall0, t_wall1)
-    value = world * n * args.steps / (ms / 1e3)
+    value = whole_job_value(world, n, args.steps, ms)
 
     # ---- per-kernel times (stage events on the same stream) ---------------
     kt = min(args.steps, 200)
@@ -567,15 +576,15 @@ def run_ours(args):
     import ctypes
     e2e_steps = max(1, min(args.steps, 100))
     torch.cuda.synchronize()
-    barrier()
+    barrier(dist)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         lib.check(L.sph_write(sim._h, lib.FIELD_VERTEX_DATA, ctypes.c_void_p(pin_pos.data_ptr()), n * 12))
         lib.check(L.sph_write(sim._h, lib.FIELD_VELOCITY, ctypes.c_void_p(pin_vel.data_ptr()), n * 12))
         lib.check(L.sph_step(sim._h, lib.SPH_STEP_PLAIN))
         lib.check(L.sph_read(sim._h, lib.FIELD_VERTEX_DATA, ctypes.c_void_p(pin_out.data_ptr()), n * 12))
-    el = max_over_ranks(time.perf_counter() - t0)
-    barrier()
+    el = max_over_ranks(dist, time.perf_counter() - t0)
+    barrier(dist)
     e2e_value = world * n * e2e_steps / el
     sim.close()
 
