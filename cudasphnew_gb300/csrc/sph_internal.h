@@ -135,7 +135,7 @@ struct StepConfig {
 };
 
 constexpr int SCAN_THREADS = 256;
-constexpr int SCAN_ITEMS = 8;
+constexpr int SCAN_ITEMS = 32;
 constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
 
 // ---------------------------------------------------------------------------

@@ -164,13 +164,17 @@ k_cell_scan(int total, int* __restrict__ cnt, int* __restrict__ out, unsigned lo
     const int tile = s_tile;
     const int base = tile * SCAN_TILE + threadIdx.x * SCAN_ITEMS;
     int v[SCAN_ITEMS];
+    static_assert(SCAN_ITEMS % 4 == 0, "vector loads of four counters");
     if (base + SCAN_ITEMS <= total) {
-        int4 a = *reinterpret_cast<const int4*>(cnt + base);
-        int4 b = *reinterpret_cast<const int4*>(cnt + base + 4);
-        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
-        v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
-        *reinterpret_cast<int4*>(cnt + base) = make_int4(0, 0, 0, 0);
-        *reinterpret_cast<int4*>(cnt + base + 4) = make_int4(0, 0, 0, 0);
+#pragma unroll
+        for (int c = 0; c < SCAN_ITEMS / 4; c++) {
+            const int4 a = *reinterpret_cast<const int4*>(cnt + base + 4 * c);
+            v[4 * c] = a.x;
+            v[4 * c + 1] = a.y;
+            v[4 * c + 2] = a.z;
+            v[4 * c + 3] = a.w;
+            *reinterpret_cast<int4*>(cnt + base + 4 * c) = make_int4(0, 0, 0, 0);
+        }
     } else {
 #pragma unroll
         for (int k = 0; k < SCAN_ITEMS; k++) {
@@ -253,14 +257,19 @@ k_cell_scan(int total, int* __restrict__ cnt, int* __restrict__ out, unsigned lo
     __syncthreads();
     int run = s_prefix + excl;
     if (base + SCAN_ITEMS <= total) {
-        int o[SCAN_ITEMS];
 #pragma unroll
-        for (int k = 0; k < SCAN_ITEMS; k++) {
-            o[k] = run;
-            run += v[k];
+        for (int c = 0; c < SCAN_ITEMS / 4; c++) {
+            int4 o;
+            o.x = run;
+            run += v[4 * c];
+            o.y = run;
+            run += v[4 * c + 1];
+            o.z = run;
+            run += v[4 * c + 2];
+            o.w = run;
+            run += v[4 * c + 3];
+            *reinterpret_cast<int4*>(out + base + 4 * c) = o;
         }
-        *reinterpret_cast<int4*>(out + base) = make_int4(o[0], o[1], o[2], o[3]);
-        *reinterpret_cast<int4*>(out + base + 4) = make_int4(o[4], o[5], o[6], o[7]);
     } else {
 #pragma unroll
         for (int k = 0; k < SCAN_ITEMS; k++) {
