@@ -134,6 +134,27 @@ struct StepConfig {
     int kahan = 1;
 };
 
+// Raises a kernel's dynamic shared memory limit once per device (the
+// attribute belongs to the current device); K is the kernel itself, so each
+// kernel keeps its own record.
+template <auto K>
+inline void ensure_dynamic_smem(int bytes) {
+    static unsigned long long done = 0ull;  // one bit per device ordinal below 64
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const unsigned long long bit = dev < 64 ? 1ull << dev : 0ull;
+    if (bit && (done & bit)) return;
+    if (cudaFuncSetAttribute(K, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) == cudaSuccess) done |= bit;
+}
+
+// The current device's multiprocessor count.
+inline int device_sms() {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return sms > 0 ? sms : 1;
+}
+
 constexpr int SCAN_THREADS = 256;
 constexpr int SCAN_ITEMS = 32;
 constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;

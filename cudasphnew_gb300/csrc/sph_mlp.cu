@@ -507,15 +507,9 @@ __global__ void k_audit_select(int n, const unsigned int* __restrict__ errBits, 
 
 void launch_mlp_apply(int n, const float* feat, MlpDev m, int mode, const int* workIds, float4* pos, float4* vel,
                       PhysDev ph, int collide, float* out, unsigned int* status, cudaStream_t s) {
-    static bool configured = false;
-    if (!configured) {
-        cudaFuncSetAttribute(k_mlp_apply, cudaFuncAttributeMaxDynamicSharedMemorySize, A_SMEM);
-        configured = true;
-    }
+    ensure_dynamic_smem<k_mlp_apply>(A_SMEM);
     const int tiles = (n + TILE - 1) / TILE;
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int sms = device_sms();
     const int grid = tiles < A_CTAS_PER_SM * sms ? tiles : A_CTAS_PER_SM * sms;
     if (grid > 0)
         k_mlp_apply<<<grid, TILE, A_SMEM, s>>>(n, feat, m, mode, workIds, pos, vel, ph, collide, out, status);
@@ -524,11 +518,7 @@ void launch_mlp_apply(int n, const float* feat, MlpDev m, int mode, const int* w
 void launch_mlp_grad(int ctas, int tilesPerCta, const int* tileList, const float* feat, const float* tgt,
                      long long count, float invScale, MlpDev m, float* partial, unsigned int* status,
                      cudaStream_t s) {
-    static bool configured = false;
-    if (!configured) {
-        cudaFuncSetAttribute(k_mlp_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, G_SMEM);
-        configured = true;
-    }
+    ensure_dynamic_smem<k_mlp_grad>(G_SMEM);
     k_mlp_grad<<<ctas, TILE, G_SMEM, s>>>(tilesPerCta, tileList, feat, tgt, count, invScale, m, partial, status);
 }
 

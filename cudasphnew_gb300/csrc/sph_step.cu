@@ -783,25 +783,14 @@ void launch_force(int n, const float4* posS, const float4* velS, const float4* r
 
 template <bool KAHAN, bool TENSION, int BLOCKS>
 static void force_learned_launch(const ForceArgs& F, MlpDev m, unsigned int* status, cudaStream_t s) {
-    static bool configured = false;
-    if (!configured) {
-        cudaFuncSetAttribute(k_force_learned<KAHAN, TENSION, BLOCKS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             L_SMEM);
-        configured = true;
-    }
+    ensure_dynamic_smem<k_force_learned<KAHAN, TENSION, BLOCKS>>(L_SMEM);
     k_force_learned<KAHAN, TENSION, BLOCKS><<<(F.n + L_THREADS - 1) / L_THREADS, L_THREADS, L_SMEM, s>>>(F, m,
                                                                                                        status);
 }
 
 template <bool KAHAN, bool TENSION>
 static void force_learned_dispatch(const ForceArgs& F, MlpDev m, unsigned int* status, cudaStream_t s) {
-    static int sms = 0;
-    if (!sms) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (sms <= 0) sms = 1;
-    }
+    const int sms = device_sms();
     const long long blocks = (F.n + L_THREADS - 1) / L_THREADS;
     if (blocks >= 2LL * L_BLOCKS_MAX * sms) force_learned_launch<KAHAN, TENSION, L_BLOCKS_MAX>(F, m, status, s);
     else force_learned_launch<KAHAN, TENSION, 3>(F, m, status, s);
