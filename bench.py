@@ -164,6 +164,35 @@ class ClockSampler:
                 "samples": len(inside), "window": window}
 
 
+def pair_count(pos, h):
+    """Ordered pairs (i, j), i != j, with |x_i - x_j| <= h: the force stage's interactions."""
+    import numpy as np
+    from scipy.spatial import cKDTree
+    t = cKDTree(np.asarray(pos, np.float64))
+    return int(t.count_neighbors(t, h)) - len(pos)
+
+
+def combined_roofline(sc, n, pairs, t_s, hbm_gbs, sms, max_mhz):
+    """The force kernel's bound over both resources: its compulsory bytes
+    (56 per particle, 8 per cell, 12 per boundary-map node) at the measured
+    HBM peak, and 40 FP32 operations per interacting pair at the CUDA cores'
+    nominal peak (SMs x 128 lanes x 2 (FMA) x clock).  frac = T* / T."""
+    C = sc.params.num_cells
+    g3 = 0
+    if sc.boundary is not None:
+        d = sc.boundary.dims()
+        g3 = d[0] * d[1] * d[2]
+    byts = 56 * n + 8 * C + 12 * g3
+    flop = 40.0 * pairs
+    fp32 = sms * 128 * 2 * max_mhz * 1e6
+    t_bytes, t_flop = byts / (hbm_gbs * 1e9), flop / fp32
+    t_star = max(t_bytes, t_flop)
+    return {"kernel": "k_force", "bytes": byts, "pairs": pairs, "flop": flop,
+            "hbm_peak_gbs": hbm_gbs, "fp32_peak_tflops": fp32 / 1e12,
+            "t_bytes_us": t_bytes * 1e6, "t_flop_us": t_flop * 1e6, "t_measured_us": t_s * 1e6,
+            "bound": "fp32" if t_flop >= t_bytes else "hbm", "frac": t_star / t_s}
+
+
 def make_scene(name):
     from cudasphnew_gb300 import scenes
     return getattr(scenes, name)()
@@ -565,6 +594,8 @@ def run_ours(args):
     C = sc.params.num_cells
     alg = n * FORCE_BYTES_PER_PARTICLE + 4 * (C + 1)
     achieved = alg / force_avg_s / 1e9
+    pairs = pair_count(sim.positions(), float(sc.params.compactSupport))
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
 
     # ---- e2e: host buffers through the C ABI, copies inside the region ----
     pin_pos = torch.empty((n, 3), dtype=torch.float32, pin_memory=True)
@@ -619,6 +650,8 @@ def run_ours(args):
                         "peak_source": peak_kind,
                         "algorithmic_bytes_per_launch": alg,
                         "avg_launch_us": force_avg_s * 1e6},
+           "roofline_combined": combined_roofline(sc, n, pairs, force_avg_s, peak, sms,
+                                                  clk.get("sm_max_mhz") or 2070.0),
            "stages_us": {k: round(v[0] / v[1] * 1e3, 2) for k, v in stages.items()}}
     if batched is not None:
         out["batched"] = batched
