@@ -157,6 +157,12 @@ __device__ __forceinline__ float dist2(float4 a, float4 b) {
     return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
 }
 
+// A pair interacts when 0 < r^2 <= h^2.  r^2 is a sum of squares (or NaN),
+// so its bits order as the values do: one integer compare.
+__device__ __forceinline__ bool neighbour_r2(float r2, float h2) {
+    return __float_as_uint(r2) - 1u < __float_as_uint(h2);
+}
+
 // Candidate range [s, e) of stencil row r (0..8: k outer, j inner).  Rows
 // outside the stencil and rows the window cut removes are empty (s == e).
 __device__ __forceinline__ void row_range(float4 xi, const Stencil& st, float h, const GridDev& g, RowTables T,

@@ -59,17 +59,16 @@ k_density(int n, const float4* __restrict__ posS, RowTables T, GridDev g_, PhysD
         if (REL) row_range_rel(xi, ci, st, ph.h, g, T, window != 0, r, s, e, dyo, dzo);
         else row_range(xi, st, ph.h, g, T, window != 0, r, s, e);
         float rs = 0.f;
-        unsigned int m = 0u, bit = 1u;
+        // neighbour bits, first candidate in the highest bit used (one
+        // multiply-add per candidate), turned around after the row
+        unsigned int m = 0u;
         for (int t = s; t < e; t++) {
             float4 xj = __ldg(posS + t);
             if (REL) xj = rel_in_frame(xj, ci.x, dyo, dzo, g.spacing);
             const float r2 = dist2(xi, xj);
             const float w = fmaxf(h2 - r2, 0.f);
             rs = fmaf(w * w, w, rs);
-            if (EMIT) {
-                m |= (r2 <= h2 && r2 > 0.f) ? bit : 0u;
-                bit <<= 1;
-            }
+            if (EMIT) m = m * 2u + (neighbour_r2(r2, h2) ? 1u : 0u);
         }
         if (KAHAN) {
             if (rs > 0.f) kahan_add(sum, comp, rs);
@@ -77,9 +76,11 @@ k_density(int n, const float4* __restrict__ posS, RowTables T, GridDev g_, PhysD
             sum += rs;
         }
         if (EMIT) {
-            const bool fits = e - s <= 32;
+            const int c = e - s;
+            const bool fits = c <= 32;
+            const unsigned int bits = (fits && c > 0) ? __brev(m) >> (32 - c) : 0u;  // bit k: candidate s + k
             M.start[(size_t)r * n + i] = fits ? s : (s | (int)0x80000000);
-            M.mask[(size_t)r * n + i] = fits ? m : (unsigned int)e;
+            M.mask[(size_t)r * n + i] = fits ? bits : (unsigned int)e;
         }
     }
     float rho = (KAHAN ? __fsub_rn(sum, comp) : sum) * ph.poly6m;
@@ -475,7 +476,7 @@ __global__ void __launch_bounds__(256, FEAT ? 3 : (BATCH ? 3 : 4)) k_force(Force
         for (int t = s; t < e; t++) {
             const float4 xj = neighbour(t);
             const float r2 = dist2(xi, xj);
-            if (r2 <= h2 && r2 > 0.f) {
+            if (neighbour_r2(r2, h2)) {
                 const float4 vj = __ldg(F.velS + t), rj = __ldg(F.rho4S + t);
                 const Pair p(ph, xi, vi, xj, vj);
                 R.add(ph, p, ri.z, rj);
@@ -518,7 +519,7 @@ __global__ void __launch_bounds__(256, FEAT ? 3 : (BATCH ? 3 : 4)) k_force(Force
                     unsigned int m = 0u;
                     for (int k = 0; k < cnt; k++) {
                         const float r2 = dist2(xi, neighbour(base + k));
-                        m |= (r2 <= h2 && r2 > 0.f) ? (1u << k) : 0u;
+                        m |= neighbour_r2(r2, h2) ? (1u << k) : 0u;
                     }
                     bits(R, base, m);
                 }
@@ -613,7 +614,7 @@ __global__ void __launch_bounds__(L_THREADS, BLOCKS) k_force_learned(ForceArgs F
                     for (int tt = sv & 0x7fffffff; tt < (int)mk; tt++) {
                         const float4 xj = __ldg(F.posS + tt);
                         const float r2 = dist2(xi, xj);
-                        if (r2 <= ph.h2 && r2 > 0.f) {
+                        if (neighbour_r2(r2, ph.h2)) {
                             const float4 vj = __ldg(F.velS + tt), rj = __ldg(F.rho4S + tt);
                             const Pair p(ph, xi, vi, xj, vj);
                             R.add(ph, p, ri.z, rj);
