@@ -1029,6 +1029,8 @@ sph_status sph_autotune(sph_handle s, int reps, sph_tuning* chosen) {
     const int n = s->n;
     const int C = (int)s->numCellsTotal;
     cudaStream_t st = s->stream;
+    // the trials rewrite the sorted copies and masks: no step may reuse them
+    SPH_CUDA(cudaMemsetAsync(s->reuse, 0, sizeof(int), st));
     SPH_CUDA(cudaStreamSynchronize(st));
     // keep the last step's sorted data (read-back) and write forces to scratch
     struct Buf {
