@@ -125,6 +125,9 @@ struct RowSums {
         cl = 0.f;
         hits = 0;
     }
+    // COUNT: count the pair here (a caller walking a neighbour mask adds the
+    // mask's population once instead)
+    template <bool COUNT = true>
     __device__ __forceinline__ void add(const PhysDev& ph, const Pair& p, float qi, float4 rj) {
         const float sp = (qi + rj.z) * p.hr * p.hr * p.rinv;  // (p_i/rho_i^2 + p_j/rho_j^2)(h-r)^2/r
         const float sv = rj.w * p.hr;                         // (h-r)/rho_j
@@ -142,7 +145,7 @@ struct RowSums {
             cg[2] = fmaf(sc, p.dz, cg[2]);
             cl = fmaf(rj.w * d2, 3.f * ph.h2 - 7.f * p.r2, cl);
         }
-        hits++;
+        if (COUNT) hits++;
     }
     __device__ __forceinline__ void add(const PhysDev& ph, float4 xi, float4 vi, float qi, float4 xj, float4 vj,
                                         float4 rj) {
@@ -485,12 +488,13 @@ __global__ void __launch_bounds__(256, FEAT ? 3 : (BATCH ? 3 : 4)) k_force(Force
         }
     };
     auto bits = [&](RowSums<TENSION>& R, int base, unsigned int m) {
+        R.hits += __popc(m);
         while (m) {
             const int t = base + __ffs(m) - 1;
             m &= m - 1u;
             const float4 xj = neighbour(t), vj = __ldg(F.velS + t), rj = __ldg(F.rho4S + t);
             const Pair p(ph, xi, vi, xj, vj);
-            R.add(ph, p, ri.z, rj);
+            R.template add<false>(ph, p, ri.z, rj);
             if (FEAT) fs.add(ph, p, rj);
         }
     };
@@ -622,12 +626,13 @@ __global__ void __launch_bounds__(L_THREADS, BLOCKS) k_force_learned(ForceArgs F
                         }
                     }
                 } else {
+                    R.hits += __popc(mk);
                     while (mk) {
                         const int tt = sv + __ffs(mk) - 1;
                         mk &= mk - 1u;
                         const float4 xj = __ldg(F.posS + tt), vj = __ldg(F.velS + tt), rj = __ldg(F.rho4S + tt);
                         const Pair p(ph, xi, vi, xj, vj);
-                        R.add(ph, p, ri.z, rj);
+                        R.template add<false>(ph, p, ri.z, rj);
                         fs.add(ph, p, rj);
                     }
                 }
