@@ -1012,7 +1012,7 @@ sph_status sph_set_tuning(sph_handle s, const sph_tuning* t) {
     auto okBlock = [](int b) { return b == 64 || b == 128 || b == 256; };
     if (!okBlock(t->densityBlock) || !okBlock(t->forceBlock))
         SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "block sizes must be 64, 128 or 256");
-    if (t->forceVariant < FORCE_DIRECT || t->forceVariant > FORCE_PRETESTED)
+    if (t->forceVariant < FORCE_DIRECT || t->forceVariant > FORCE_STAGED)
         SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "unknown force variant");
     s->cfg.densityBlock = t->densityBlock;
     s->cfg.forceBlock = t->forceBlock;
@@ -1114,10 +1114,10 @@ sph_status sph_autotune(sph_handle s, int reps, sph_tuning* chosen) {
     StepConfig best = current;
     float bestTotal = currentTotal;
     for (int prune = 0; prune <= 1; prune++)
-        for (int v = FORCE_DIRECT; v <= FORCE_PRETESTED; v++) {
+        for (int v = FORCE_DIRECT; v <= FORCE_STAGED; v++) {
             StepConfig c = s->cfg;
             c.prune = prune;
-            c.forceVariant = v;  // the density stage records masks for the pretested form
+            c.forceVariant = v;  // the density stage records masks for the pretested and staged forms
             float bestD = 3.0e38f;
             int bestDB = c.densityBlock;
             for (int b : blocks) {

@@ -124,7 +124,7 @@ struct RowTables {
 };
 
 // Launch configuration of the step (chosen per handle; see the autotuner).
-enum ForceVariant { FORCE_DIRECT = 0, FORCE_MASK = 1, FORCE_PRETESTED = 2 };
+enum ForceVariant { FORCE_DIRECT = 0, FORCE_MASK = 1, FORCE_PRETESTED = 2, FORCE_STAGED = 3 };
 
 struct StepConfig {
     int densityBlock = 128;

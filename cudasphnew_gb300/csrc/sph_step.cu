@@ -18,6 +18,8 @@
 //                records each row's window start and a 32-bit neighbour mask;
 //                the force stage runs the interactions of the set bits only
 //                (rows longer than 32 candidates fall back to testing).
+#include <climits>
+
 #include "sph_device.cuh"
 #include "sph_mlp_tile.cuh"
 
@@ -541,6 +543,103 @@ __global__ void __launch_bounds__(256, FEAT ? 3 : (BATCH ? 3 : 4)) k_force(Force
 }
 
 // ---------------------------------------------------------------------------
+// The pretested force form with each warp's neighbour rows staged in shared
+// memory (plain handles).  The 32 particles of a warp are consecutive in the
+// working order, so their windows into one stencil row overlap: the warp
+// takes the union of its lanes' windows, loads it once with coalesced loads
+// (sorted position, velocity and density records) and every lane reads its
+// neighbours from there instead of gathering them through L1.  A row whose
+// union exceeds ST_ROW candidates (a warp across a cell-row boundary, or a
+// window too long for a mask) is read from global memory as before.  The
+// same pairs in the same order: results are bit-identical to the other
+// forms.
+// ---------------------------------------------------------------------------
+constexpr int ST_ROW = 96;     // staged candidates per warp and row
+constexpr int ST_WARPS = 8;    // 256-thread blocks
+
+template <bool KAHAN, bool TENSION>
+__global__ void __launch_bounds__(ST_WARPS * 32, 4) k_force_staged(ForceArgs F) {
+    __shared__ float4 sP[ST_WARPS][ST_ROW], sV[ST_WARPS][ST_ROW], sR[ST_WARPS][ST_ROW];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = i < F.n;  // no early return: the warp loads its rows together
+    float4 xi = make_float4(0.f, 0.f, 0.f, 0.f), vi = xi, ri = xi;
+    if (valid) {
+        xi = F.posS[i];
+        vi = F.velS[i];
+        ri = F.rho4S[i];
+    }
+    const PhysDev& ph = F.ph;
+    ForceTotals<KAHAN, TENSION> A;
+    float4* P = sP[warp];
+    float4* V = sV[warp];
+    float4* Q = sR[warp];
+#pragma unroll 1
+    for (int r = 0; r < 9; r++) {
+        RowSums<TENSION> R;
+        R.clear();
+        int sv = 0, lo = INT_MAX, hi = INT_MIN;
+        unsigned int mk = 0u;
+        if (valid) {
+            sv = __ldg(F.M.start + (size_t)r * F.n + i);
+            mk = __ldg(F.M.mask + (size_t)r * F.n + i);
+            if (sv >= 0 && mk) {
+                lo = sv + __ffs(mk) - 1;
+                hi = sv + 32 - __clz(mk);
+            }
+        }
+        const int u0 = __reduce_min_sync(0xffffffffu, lo), u1 = __reduce_max_sync(0xffffffffu, hi);
+        const int len = u1 > u0 ? u1 - u0 : 0;
+        const bool staged = len <= ST_ROW;  // the same for the whole warp
+        if (staged) {
+            for (int k = lane; k < len; k += 32) {
+                P[k] = __ldg(F.posS + u0 + k);
+                V[k] = __ldg(F.velS + u0 + k);
+                Q[k] = __ldg(F.rho4S + u0 + k);
+            }
+            __syncwarp();
+        }
+        if (valid) {
+            if (sv < 0) {
+                // a window too long for a mask: test and interact from global memory
+                for (int t = sv & 0x7fffffff; t < (int)mk; t++) {
+                    const float4 xj = __ldg(F.posS + t);
+                    const float r2 = dist2(xi, xj);
+                    if (neighbour_r2(r2, ph.h2)) {
+                        const float4 vj = __ldg(F.velS + t), rj = __ldg(F.rho4S + t);
+                        R.add(ph, Pair(ph, xi, vi, xj, vj), ri.z, rj);
+                    }
+                }
+            } else {
+                R.hits += __popc(mk);
+                while (mk) {
+                    const int t = sv + __ffs(mk) - 1;
+                    mk &= mk - 1u;
+                    float4 xj, vj, rj;
+                    if (staged) {
+                        xj = P[t - u0];
+                        vj = V[t - u0];
+                        rj = Q[t - u0];
+                    } else {
+                        xj = __ldg(F.posS + t);
+                        vj = __ldg(F.velS + t);
+                        rj = __ldg(F.rho4S + t);
+                    }
+                    R.template add<false>(ph, Pair(ph, xi, vi, xj, vj), ri.z, rj);
+                }
+            }
+        }
+        if (staged) __syncwarp();  // the next row reuses the buffers
+        A.add(R);
+    }
+    if (valid) {
+        FeatSums fs;
+        force_epilogue<KAHAN, TENSION, false>(A, i, xi, vi, ri, ph, F.map, F.collide, F.workIds, F.pos, F.vel,
+                                              F.accS, fs, F.fo);
+    }
+}
+
+// ---------------------------------------------------------------------------
 // The learned step's force stage with the corrector fused in.  The pretested
 // pair loop, wall terms, integration and collision of k_force, then the
 // 24 features of each particle go straight to shared memory as a BF16 MMA
@@ -703,7 +802,7 @@ void launch_density(int n, const float4* posS, RowTables T, GridDev g, PhysDev p
     const int bs = cfg.densityBlock > 0 ? cfg.densityBlock : 128;
     const int grid = (n + bs - 1) / bs;
     const RowMasks M{rowStart, rowMask};
-    const bool emit = cfg.forceVariant == FORCE_PRETESTED;
+    const bool emit = cfg.forceVariant >= FORCE_PRETESTED;  // the pretested and staged forms read masks
 #define SPH_DENSITY(K, E, B) k_density<K, E, B, false><<<grid, bs, 0, s>>>(n, posS, T, g, ph, map, cfg.prune, rho4S, M)
 #define SPH_DENSITY_REL(K, E) k_density<K, E, false, true><<<grid, bs, 0, s>>>(n, posS, T, g, ph, map, cfg.prune, rho4S, M)
     if (g.rel) {
@@ -740,16 +839,18 @@ static void force_dispatch(const ForceArgs& F, const StepConfig& cfg, cudaStream
     const int bs = cfg.forceBlock > 0 ? cfg.forceBlock : 128;
     const int grid = (F.n + bs - 1) / bs;
     if (F.T.scenes) {
-        // batched scenes (plain steps only; no feature recording)
-        if (cfg.forceVariant == FORCE_PRETESTED)
+        // batched scenes (plain steps only; no feature recording); the staged
+        // form is the plain handles' only, the pretested one serves here
+        if (cfg.forceVariant >= FORCE_PRETESTED)
             k_force<KAHAN, TENSION, FORCE_PRETESTED, false, true><<<grid, bs, 0, s>>>(F);
         else if (cfg.forceVariant == FORCE_MASK)
             k_force<KAHAN, TENSION, FORCE_MASK, false, true><<<grid, bs, 0, s>>>(F);
         else
             k_force<KAHAN, TENSION, FORCE_DIRECT, false, true><<<grid, bs, 0, s>>>(F);
     } else if (F.g.rel) {
-        // cell-relative positions (plain steps only)
-        if (cfg.forceVariant == FORCE_PRETESTED)
+        // cell-relative positions (plain steps only; the pretested form stands
+        // in for the staged one)
+        if (cfg.forceVariant >= FORCE_PRETESTED)
             k_force<KAHAN, TENSION, FORCE_PRETESTED, false, false, true><<<grid, bs, 0, s>>>(F);
         else if (cfg.forceVariant == FORCE_MASK)
             k_force<KAHAN, TENSION, FORCE_MASK, false, false, true><<<grid, bs, 0, s>>>(F);
@@ -759,6 +860,8 @@ static void force_dispatch(const ForceArgs& F, const StepConfig& cfg, cudaStream
         // the learned step's force stage records the corrector's features; the
         // density stage has recorded the neighbour masks (pretested form)
         k_force<KAHAN, TENSION, FORCE_PRETESTED, true, false><<<grid, bs, 0, s>>>(F);
+    } else if (cfg.forceVariant == FORCE_STAGED) {
+        k_force_staged<KAHAN, TENSION><<<(F.n + ST_WARPS * 32 - 1) / (ST_WARPS * 32), ST_WARPS * 32, 0, s>>>(F);
     } else if (cfg.forceVariant == FORCE_PRETESTED) {
         k_force<KAHAN, TENSION, FORCE_PRETESTED, false, false><<<grid, bs, 0, s>>>(F);
     } else if (cfg.forceVariant == FORCE_MASK) {

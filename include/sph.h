@@ -491,7 +491,10 @@ typedef struct sph_tuning {
     int densityBlock;  /* 64, 128 or 256 */
     int forceBlock;    /* 64, 128 or 256 */
     int forceVariant;  /* 0: direct loop, 1: per-chunk hit mask, then interactions,
-                          2: neighbour masks recorded by the density stage */
+                          2: neighbour masks recorded by the density stage,
+                          3: as 2, each warp's neighbour rows staged in shared
+                          memory (plain handles; batched and cell-relative
+                          handles run 2) */
     int prune;         /* 1: cut stencil rows to the half-cells within reach of h */
     int kahan;         /* 1: compensated density and force sums */
 } sph_tuning;

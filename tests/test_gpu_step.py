@@ -264,7 +264,9 @@ def test_tunings_are_bit_identical(sphlib, kahan):
                dict(forceVariant=1, prune=0, forceBlock=256, densityBlock=64),
                dict(forceVariant=0, prune=1, forceBlock=256, densityBlock=128),
                dict(forceVariant=2, prune=1, forceBlock=128, densityBlock=128),
-               dict(forceVariant=2, prune=0, forceBlock=64, densityBlock=64)]
+               dict(forceVariant=2, prune=0, forceBlock=64, densityBlock=64),
+               dict(forceVariant=3, prune=1, forceBlock=128, densityBlock=128),
+               dict(forceVariant=3, prune=0, forceBlock=256, densityBlock=256)]
     outs = []
     for cfg in configs:
         with sphlib.ParticleSimulation(sc.params, sc.positions, sc.velocities, sc.options,
@@ -290,7 +292,7 @@ def test_autotune_leaves_state_untouched(sphlib):
                                         sphlib.FIELD_VERTEX_DATA, sphlib.FIELD_VELOCITY)]
         cells_before = sim.cells()
         t = sim.autotune(reps=2)
-        assert t.densityBlock in (64, 128, 256) and t.forceVariant in (0, 1, 2)
+        assert t.densityBlock in (64, 128, 256) and t.forceVariant in (0, 1, 2, 3)
         after = [sim.read(f) for f in (sphlib.FIELD_DENSITY, sphlib.FIELD_ACCELERATION,
                                        sphlib.FIELD_VERTEX_DATA, sphlib.FIELD_VELOCITY)]
         for a, b in zip(before, after):
