@@ -56,8 +56,8 @@ constexpr int A_H1 = A_X + 8192;        // 128 x 64
 constexpr int A_H2 = A_H1 + 16384;      // 128 x 64
 constexpr int A_BIAS = A_H2 + 16384;    // NBIAS floats
 constexpr int A_NORM = A_BIAS + 4 * NBIAS;
-constexpr int A_BAR = A_NORM + 4 * NNORM;
-constexpr int A_SMEM = A_BAR + 16;
+constexpr int A_BAR = A_NORM + 4 * NNORM;  // MMA barrier, TMEM slot, weight-copy barrier
+constexpr int A_SMEM = A_BAR + 32;
 // Three CTAs fit an SM's shared memory; their 128-column TMEM allocations
 // (3 x 128 <= 512) always fit beside each other.
 constexpr int A_CTAS_PER_SM = 3;
@@ -73,15 +73,23 @@ __global__ void __launch_bounds__(TILE, 1)
     const int t = threadIdx.x, warp = t >> 5;
     uint64_t* bar = reinterpret_cast<uint64_t*>(sm + A_BAR);
     uint32_t* slot = reinterpret_cast<uint32_t*>(sm + A_BAR + 8);
+    uint64_t* wbar = reinterpret_cast<uint64_t*>(sm + A_BAR + 16);
     float* sBias = reinterpret_cast<float*>(sm + A_BIAS);
     float* sNorm = reinterpret_cast<float*>(sm + A_NORM);
-    for (int i = t; i < IMG_FWD_BYTES / 16; i += TILE)
-        reinterpret_cast<uint4*>(sm + A_W)[i] = reinterpret_cast<const uint4*>(m.image)[i];
     for (int i = t; i < NBIAS; i += TILE) sBias[i] = epilogue_bias(m.bias, i);
     for (int i = t; i < NNORM; i += TILE) sNorm[i] = m.norm[i];
     if (t == 0) {
         mbar_init(bar, 1);
+        mbar_init(wbar, 1);
         sOk = 1;
+        // the weight image: one TMA bulk copy
+        mbar_arrive_expect_tx(wbar, IMG_FWD_BYTES);
+        bulk_g2s(sm + A_W, m.image, IMG_FWD_BYTES, wbar);
+        if (!mbar_wait(wbar, 0, WAIT_LIMIT)) {
+            sOk = 0;
+            atomicOr(status, STATUS_DEVICE_WAIT);
+            mbar_wait(wbar, 0, WAIT_LIMIT);  // once more for the copy in flight
+        }
     }
     if (warp == 0) tmem_alloc(slot, A_TMEM_COLS);
     cta_sync();
@@ -89,7 +97,7 @@ __global__ void __launch_bounds__(TILE, 1)
     const uint32_t sW = smem_u32(sm + A_W);
     uint32_t phase = 0;
     const int tiles = (n + TILE - 1) / TILE;
-    for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    for (int tile = blockIdx.x; sOk && tile < tiles; tile += gridDim.x) {
         const long long u = (long long)tile * TILE + t;
         const bool valid = u < n;
         const long long row = (mode == 0 && valid) ? (long long)workIds[u] : u;
@@ -151,8 +159,8 @@ constexpr int G_BIAS = G_Q + 16384;
 constexpr int G_NORM = G_BIAS + 4 * NBIAS;
 constexpr int G_DB = G_NORM + 4 * NNORM;  // [4 warps][NBIAS] bias-gradient sums
 constexpr int G_LOSS = G_DB + 4 * 4 * NBIAS;
-constexpr int G_BAR = G_LOSS + 16;
-constexpr int G_SMEM = G_BAR + 16;
+constexpr int G_BAR = G_LOSS + 16;  // MMA barrier, TMEM slot, weight-copy barrier
+constexpr int G_SMEM = G_BAR + 32;
 static_assert(G_SMEM <= 227 * 1024, "training shared memory");
 
 // TMEM columns (512 allocated; one CTA per SM).
@@ -184,19 +192,27 @@ __global__ void __launch_bounds__(TILE, 1)
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
     uint64_t* bar = reinterpret_cast<uint64_t*>(sm + G_BAR);
     uint32_t* slot = reinterpret_cast<uint32_t*>(sm + G_BAR + 8);
+    uint64_t* wbar = reinterpret_cast<uint64_t*>(sm + G_BAR + 16);
     float* sBias = reinterpret_cast<float*>(sm + G_BIAS);
     float* sNorm = reinterpret_cast<float*>(sm + G_NORM);
     float* sDb = reinterpret_cast<float*>(sm + G_DB);
     float* sLoss = reinterpret_cast<float*>(sm + G_LOSS);
-    for (int i = t; i < IMG_BYTES / 16; i += TILE)
-        reinterpret_cast<uint4*>(sm + G_IMG)[i] = reinterpret_cast<const uint4*>(m.image)[i];
     for (int i = t; i < NBIAS; i += TILE) sBias[i] = m.bias[i];
     for (int i = t; i < NNORM; i += TILE) sNorm[i] = m.norm[i];
     for (int i = t; i < 4 * NBIAS; i += TILE) sDb[i] = 0.f;
     if (t < 4) sLoss[t] = 0.f;
     if (t == 0) {
         mbar_init(bar, 1);
+        mbar_init(wbar, 1);
         sOk = 1;
+        // the weight image (with the transposes the backward pass reads): one TMA bulk copy
+        mbar_arrive_expect_tx(wbar, IMG_BYTES);
+        bulk_g2s(sm + G_IMG, m.image, IMG_BYTES, wbar);
+        if (!mbar_wait(wbar, 0, WAIT_LIMIT)) {
+            sOk = 0;
+            atomicOr(status, STATUS_DEVICE_WAIT);
+            mbar_wait(wbar, 0, WAIT_LIMIT);  // once more for the copy in flight
+        }
     }
     if (warp == 0) tmem_alloc(slot, 512);
     cta_sync();
@@ -204,7 +220,7 @@ __global__ void __launch_bounds__(TILE, 1)
     const uint32_t sImg = smem_u32(sm + G_IMG);
     float* dbRow = sDb + warp * NBIAS;
     uint32_t phase = 0;
-    bool ok = true;
+    bool ok = sOk != 0;
     for (int j = 0; j < tilesPerCta && ok; j++) {
         const int tile = tileList[(size_t)blockIdx.x * tilesPerCta + j];
         const long long row = (long long)tile * TILE + t;

@@ -660,8 +660,8 @@ constexpr int L_X = mlp::IMG_FWD_BYTES;       // operand region: two 128 x 32 fe
 constexpr int L_H = L_X;                      // ... later two 128 x 64 hidden tiles
 constexpr int L_BIAS = L_H + 2 * 16384;
 constexpr int L_NORM = L_BIAS + 4 * mlp::NBIAS;
-constexpr int L_BAR = L_NORM + 4 * mlp::NNORM;
-constexpr int L_SMEM = L_BAR + 16;
+constexpr int L_BAR = L_NORM + 4 * mlp::NNORM;  // MMA barrier, TMEM slot, weight-copy barrier
+constexpr int L_SMEM = L_BAR + 32;
 constexpr int L_TMEM = 128;                   // 4 blocks x 128 = 512 columns
 constexpr int L_THREADS = 256;
 // Resident blocks per SM: four (64 registers, a few spilled) when the grid
@@ -680,15 +680,18 @@ __global__ void __launch_bounds__(L_THREADS, BLOCKS) k_force_learned(ForceArgs F
     const int t = threadIdx.x, warp = t >> 5, half = t >> 7, r = t & 127;
     uint64_t* bar = reinterpret_cast<uint64_t*>(sm + L_BAR);
     uint32_t* slot = reinterpret_cast<uint32_t*>(sm + L_BAR + 8);
+    uint64_t* wbar = reinterpret_cast<uint64_t*>(sm + L_BAR + 16);
     float* sBias = reinterpret_cast<float*>(sm + L_BIAS);
     float* sNorm = reinterpret_cast<float*>(sm + L_NORM);
-    for (int k = t; k < IMG_FWD_BYTES / 16; k += L_THREADS)
-        reinterpret_cast<uint4*>(sm + L_W)[k] = reinterpret_cast<const uint4*>(m.image)[k];
     for (int k = t; k < NBIAS; k += L_THREADS) sBias[k] = epilogue_bias(m.bias, k);
     for (int k = t; k < NNORM; k += L_THREADS) sNorm[k] = m.norm[k];
     if (t == 0) {
         tc::mbar_init(bar, 1);
+        tc::mbar_init(wbar, 1);
         sOk = 1;
+        // the weight image arrives by one TMA bulk copy while the pair loop runs
+        tc::mbar_arrive_expect_tx(wbar, IMG_FWD_BYTES);
+        tc::bulk_g2s(sm + L_W, m.image, IMG_FWD_BYTES, wbar);
     }
     if (warp == 0) tc::tmem_alloc(slot, L_TMEM);
     tc::cta_sync();
@@ -752,7 +755,13 @@ __global__ void __launch_bounds__(L_THREADS, BLOCKS) k_force_learned(ForceArgs F
     unsigned char* myH = sm + L_H + half * 16384;
     const uint32_t tl = tc::tmem_at(tb, 32 * (warp & 3), 64 * half);  // this warp's lanes of its tile
     uint32_t phase = 0;
-    do {
+    // sOk: 1 running, 0 an MMA wait gave up, 2 the weight copy never landed
+    if (t == 0 && !tc::mbar_wait(wbar, 0, WAIT_LIMIT)) {
+        sOk = 2;
+        atomicOr(status, STATUS_DEVICE_WAIT);
+    }
+    tc::cta_sync();
+    if (sOk == 1) do {
         tc::cta_sync();
         if (t == 0) {
             tc::mma_chain(tb, sX, sW + IMG_W1, INP, HID, false);
@@ -788,7 +797,8 @@ __global__ void __launch_bounds__(L_THREADS, BLOCKS) k_force_learned(ForceArgs F
         }
     } while (false);
     tc::cta_sync();
-    if (!sOk) drain(bar, phase, t, status);
+    if (sOk == 0) drain(bar, phase, t, status);
+    if (sOk == 2 && t == 0) tc::mbar_wait(wbar, 0, WAIT_LIMIT);  // once more for the copy in flight
     tc::cta_sync();
     if (warp == 0) tc::tmem_dealloc(tb, L_TMEM);
 }
