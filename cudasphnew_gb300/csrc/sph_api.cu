@@ -274,7 +274,7 @@ void enqueue_coarse(sph_sim* s, const GridDev& g, const PhysDev& ph, int collide
     mark(ST_FORCE);
     if (!force) return;
     launch_force(n, s->posS, s->velS, s->rho4S, s->sb.workIds, rows_of(s), g, ph, s->map, collide, s->rowStart,
-                 s->rowMask, s->pos, s->vel, s->accS, cfg, st, feat);
+                 s->rowMask, s->pos, s->vel, s->accS, cfg, st, feat, s->status);
     mark(ST_COUNT);
 }
 
@@ -1106,7 +1106,7 @@ sph_status sph_autotune(sph_handle s, int reps, sph_tuning* chosen) {
             [&] {
                 launch_force(n, s->posS, s->velS, s->rho4S, s->sb.workIds, rows_of(s), g, ph, s->map,
                              s->O.boxCollision, s->rowStart, s->rowMask, scratch, scratch + n,
-                             scratch + 2 * (size_t)n, c, st);
+                             scratch + 2 * (size_t)n, c, st, nullptr, s->status);
             });
         return d + f;
     };
@@ -1140,7 +1140,7 @@ sph_status sph_autotune(sph_handle s, int reps, sph_tuning* chosen) {
                 float t = timeit(beforeForce, [&] {
                     launch_force(n, s->posS, s->velS, s->rho4S, s->sb.workIds, rows_of(s), g, ph, s->map,
                                  s->O.boxCollision, s->rowStart, s->rowMask, scratch, scratch + n,
-                                 scratch + 2 * (size_t)n, c, st);
+                                 scratch + 2 * (size_t)n, c, st, nullptr, s->status);
                 });
                 if (bestD + t < bestTotal) {
                     bestTotal = bestD + t;

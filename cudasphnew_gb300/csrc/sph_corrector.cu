@@ -181,7 +181,8 @@ void enqueue_audit(sph_sim* s, Corrector* C) {
     // still hold the start state), so only its force stage runs; it writes
     // every particle's new state.
     launch_force(s->n, s->posS, s->velS, s->rho4S, s->sb.workIds, rows_of(s), grid_of(s), make_phys(s->P, s->O),
-                 s->map, s->O.boxCollision, s->rowStart, s->rowMask, s->pos, s->vel, s->accS, s->cfg, q);
+                 s->map, s->O.boxCollision, s->rowStart, s->rowMask, s->pos, s->vel, s->accS, s->cfg, q, nullptr,
+                 s->status);
     for (int k = 1; k < C->cfg.stride; k++) enqueue_step(s, SPH_STEP_PLAIN, false);
     enqueue_density_only(s, s->pos, s->vel);
     launch_unpermute(s->n, s->sb.workIds, s->rho4S, 0, C->rhoB, 1, 0, q);

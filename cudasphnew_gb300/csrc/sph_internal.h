@@ -190,7 +190,8 @@ struct FeatureOut {
 void launch_force(int n, const float4* posS, const float4* velS, const float4* rho4S,
                   const int* workIds, RowTables T, GridDev g, PhysDev ph, MapDev map, int collide,
                   const int* rowStart, const unsigned int* rowMask, float4* pos, float4* vel,
-                  float4* accS, const StepConfig& cfg, cudaStream_t s, const FeatureOut* feat = nullptr);
+                  float4* accS, const StepConfig& cfg, cudaStream_t s, const FeatureOut* feat = nullptr,
+                  unsigned int* status = nullptr);
 void launch_unpermute(int n, const int* sortedIds, const float4* srcS, int comp, float* dst,
                       int stride, int offset, cudaStream_t s);
 void launch_cell_tables(int numCells, const int* cellOffset, int* start, int* end, cudaStream_t s);

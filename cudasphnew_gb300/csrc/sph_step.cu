@@ -544,25 +544,38 @@ __global__ void __launch_bounds__(256, FEAT ? 3 : (BATCH ? 3 : 4)) k_force(Force
 
 // ---------------------------------------------------------------------------
 // The pretested force form with each warp's neighbour rows staged in shared
-// memory (plain handles).  The 32 particles of a warp are consecutive in the
-// working order, so their windows into one stencil row overlap: the warp
-// takes the union of its lanes' windows, loads it once with coalesced loads
-// (sorted position, velocity and density records) and every lane reads its
-// neighbours from there instead of gathering them through L1.  A row whose
-// union exceeds ST_ROW candidates (a warp across a cell-row boundary, or a
-// window too long for a mask) is read from global memory as before.  The
-// same pairs in the same order: results are bit-identical to the other
-// forms.
+// memory by TMA (plain handles).  The 32 particles of a warp are consecutive
+// in the working order, so their windows into one stencil row overlap: the
+// warp takes the union of its lanes' windows and one lane copies it into
+// shared memory with three bulk copies (sorted position, velocity and
+// density records, cp.async.bulk completing on an mbarrier).  Rows are
+// double-buffered: row r + 1's copies are issued before row r is processed.
+// Every lane then reads its neighbours from shared memory instead of
+// gathering them through L1.  A row whose union exceeds ST_ROW candidates (a
+// warp across a cell-row boundary, or a window too long for a mask) is read
+// from global memory as before.  The same pairs in the same order: results
+// are bit-identical to the other forms.  Each wait is bounded; a wait that
+// gives up latches STATUS_DEVICE_WAIT, the warp reads global memory from
+// then on and waits once more, bounded, for its copies still in flight.
 // ---------------------------------------------------------------------------
-constexpr int ST_ROW = 96;     // staged candidates per warp and row
+constexpr int ST_ROW = 72;     // staged candidates per warp, row and buffer
 constexpr int ST_WARPS = 8;    // 256-thread blocks
+constexpr int ST_SMEM = ST_WARPS * 2 * 3 * ST_ROW * 16 + ST_WARPS * 2 * 8;
+constexpr uint32_t ST_WAIT_LIMIT = 1u << 22;
 
 template <bool KAHAN, bool TENSION>
-__global__ void __launch_bounds__(ST_WARPS * 32, 4) k_force_staged(ForceArgs F) {
-    __shared__ float4 sP[ST_WARPS][ST_ROW], sV[ST_WARPS][ST_ROW], sR[ST_WARPS][ST_ROW];
+__global__ void __launch_bounds__(ST_WARPS * 32, 4) k_force_staged(ForceArgs F, unsigned int* status) {
+    extern __shared__ __align__(128) unsigned char stsm[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float4* buf = reinterpret_cast<float4*>(stsm) + warp * (2 * 3 * ST_ROW);  // [buffer][P, V, Q][ST_ROW]
+    uint64_t* bars = reinterpret_cast<uint64_t*>(stsm + ST_WARPS * 2 * 3 * ST_ROW * 16) + 2 * warp;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool valid = i < F.n;  // no early return: the warp loads its rows together
+    const bool valid = i < F.n;  // no early return: the warp stages its rows together
+    if (lane == 0) {
+        tc::mbar_init(bars, 1);
+        tc::mbar_init(bars + 1, 1);
+    }
+    __syncwarp();
     float4 xi = make_float4(0.f, 0.f, 0.f, 0.f), vi = xi, ri = xi;
     if (valid) {
         xi = F.posS[i];
@@ -571,15 +584,11 @@ __global__ void __launch_bounds__(ST_WARPS * 32, 4) k_force_staged(ForceArgs F) 
     }
     const PhysDev& ph = F.ph;
     ForceTotals<KAHAN, TENSION> A;
-    float4* P = sP[warp];
-    float4* V = sV[warp];
-    float4* Q = sR[warp];
-#pragma unroll 1
-    for (int r = 0; r < 9; r++) {
-        RowSums<TENSION> R;
-        R.clear();
-        int sv = 0, lo = INT_MAX, hi = INT_MIN;
-        unsigned int mk = 0u;
+    // a row: this lane's window (start, mask) and the warp's staged union [u0, u0 + len)
+    auto row_info = [&](int r, int& sv, unsigned int& mk, int& u0, int& len) {
+        sv = 0;
+        mk = 0u;
+        int lo = INT_MAX, hi = INT_MIN;
         if (valid) {
             sv = __ldg(F.M.start + (size_t)r * F.n + i);
             mk = __ldg(F.M.mask + (size_t)r * F.n + i);
@@ -588,17 +597,52 @@ __global__ void __launch_bounds__(ST_WARPS * 32, 4) k_force_staged(ForceArgs F) 
                 hi = sv + 32 - __clz(mk);
             }
         }
-        const int u0 = __reduce_min_sync(0xffffffffu, lo), u1 = __reduce_max_sync(0xffffffffu, hi);
-        const int len = u1 > u0 ? u1 - u0 : 0;
-        const bool staged = len <= ST_ROW;  // the same for the whole warp
-        if (staged) {
-            for (int k = lane; k < len; k += 32) {
-                P[k] = __ldg(F.posS + u0 + k);
-                V[k] = __ldg(F.velS + u0 + k);
-                Q[k] = __ldg(F.rho4S + u0 + k);
-            }
-            __syncwarp();
+        u0 = __reduce_min_sync(0xffffffffu, lo);
+        const int u1 = __reduce_max_sync(0xffffffffu, hi);
+        len = u1 > u0 ? u1 - u0 : 0;
+        if (len > ST_ROW) len = -1;  // not staged
+    };
+    unsigned int phase = 0u, pending = 0u;  // per buffer: wait parity, copy in flight
+    bool broken = false;
+    auto issue = [&](int b, int u0, int len) {
+        if (lane == 0) {
+            float4* d = buf + b * 3 * ST_ROW;
+            const uint32_t bytes = (uint32_t)len * 16u;
+            tc::fence_async_smem();  // this warp's reads of the buffer come first
+            tc::mbar_arrive_expect_tx(bars + b, 3u * bytes);
+            tc::bulk_g2s(d, F.posS + u0, bytes, bars + b);
+            tc::bulk_g2s(d + ST_ROW, F.velS + u0, bytes, bars + b);
+            tc::bulk_g2s(d + 2 * ST_ROW, F.rho4S + u0, bytes, bars + b);
         }
+        pending |= 1u << b;
+    };
+    int sv, u0, len;
+    unsigned int mk;
+    row_info(0, sv, mk, u0, len);
+    if (len > 0) issue(0, u0, len);
+#pragma unroll 1
+    for (int r = 0; r < 9; r++) {
+        const int b = r & 1;
+        int svN = 0, u0N = 0, lenN = 0;
+        unsigned int mkN = 0u;
+        if (r + 1 < 9) {
+            row_info(r + 1, svN, mkN, u0N, lenN);
+            if (lenN > 0 && !broken) issue(b ^ 1, u0N, lenN);
+        }
+        bool staged = len > 0 && (pending >> b & 1u);
+        if (staged) {
+            const bool ok = __all_sync(0xffffffffu, tc::mbar_wait(bars + b, phase >> b & 1u, ST_WAIT_LIMIT));
+            if (ok) {
+                phase ^= 1u << b;
+                pending &= ~(1u << b);
+            } else {
+                if (lane == 0 && status) atomicOr(status, STATUS_DEVICE_WAIT);
+                broken = true;
+                staged = false;
+            }
+        }
+        RowSums<TENSION> R;
+        R.clear();
         if (valid) {
             if (sv < 0) {
                 // a window too long for a mask: test and interact from global memory
@@ -611,6 +655,7 @@ __global__ void __launch_bounds__(ST_WARPS * 32, 4) k_force_staged(ForceArgs F) 
                     }
                 }
             } else {
+                const float4* P = buf + b * 3 * ST_ROW;
                 R.hits += __popc(mk);
                 while (mk) {
                     const int t = sv + __ffs(mk) - 1;
@@ -618,8 +663,8 @@ __global__ void __launch_bounds__(ST_WARPS * 32, 4) k_force_staged(ForceArgs F) 
                     float4 xj, vj, rj;
                     if (staged) {
                         xj = P[t - u0];
-                        vj = V[t - u0];
-                        rj = Q[t - u0];
+                        vj = P[ST_ROW + t - u0];
+                        rj = P[2 * ST_ROW + t - u0];
                     } else {
                         xj = __ldg(F.posS + t);
                         vj = __ldg(F.velS + t);
@@ -629,9 +674,17 @@ __global__ void __launch_bounds__(ST_WARPS * 32, 4) k_force_staged(ForceArgs F) 
                 }
             }
         }
-        if (staged) __syncwarp();  // the next row reuses the buffers
+        __syncwarp();  // the buffer is refilled two rows on
         A.add(R);
+        sv = svN;
+        mk = mkN;
+        u0 = u0N;
+        len = lenN;
     }
+    if (broken && lane == 0)  // copies still in flight land before the block leaves
+        for (int b = 0; b < 2; b++)
+            if (pending >> b & 1u) tc::mbar_wait(bars + b, phase >> b & 1u, ST_WAIT_LIMIT);
+    __syncwarp();
     if (valid) {
         FeatSums fs;
         force_epilogue<KAHAN, TENSION, false>(A, i, xi, vi, ri, ph, F.map, F.collide, F.workIds, F.pos, F.vel,
@@ -845,7 +898,7 @@ void launch_density(int n, const float4* posS, RowTables T, GridDev g, PhysDev p
 }
 
 template <bool KAHAN, bool TENSION>
-static void force_dispatch(const ForceArgs& F, const StepConfig& cfg, cudaStream_t s) {
+static void force_dispatch(const ForceArgs& F, const StepConfig& cfg, unsigned int* status, cudaStream_t s) {
     const int bs = cfg.forceBlock > 0 ? cfg.forceBlock : 128;
     const int grid = (F.n + bs - 1) / bs;
     if (F.T.scenes) {
@@ -871,7 +924,9 @@ static void force_dispatch(const ForceArgs& F, const StepConfig& cfg, cudaStream
         // density stage has recorded the neighbour masks (pretested form)
         k_force<KAHAN, TENSION, FORCE_PRETESTED, true, false><<<grid, bs, 0, s>>>(F);
     } else if (cfg.forceVariant == FORCE_STAGED) {
-        k_force_staged<KAHAN, TENSION><<<(F.n + ST_WARPS * 32 - 1) / (ST_WARPS * 32), ST_WARPS * 32, 0, s>>>(F);
+        ensure_dynamic_smem<k_force_staged<KAHAN, TENSION>>(ST_SMEM);
+        k_force_staged<KAHAN, TENSION>
+            <<<(F.n + ST_WARPS * 32 - 1) / (ST_WARPS * 32), ST_WARPS * 32, ST_SMEM, s>>>(F, status);
     } else if (cfg.forceVariant == FORCE_PRETESTED) {
         k_force<KAHAN, TENSION, FORCE_PRETESTED, false, false><<<grid, bs, 0, s>>>(F);
     } else if (cfg.forceVariant == FORCE_MASK) {
@@ -884,7 +939,7 @@ static void force_dispatch(const ForceArgs& F, const StepConfig& cfg, cudaStream
 void launch_force(int n, const float4* posS, const float4* velS, const float4* rho4S, const int* workIds,
                   RowTables T, GridDev g, PhysDev ph, MapDev map, int collide, const int* rowStart,
                   const unsigned int* rowMask, float4* pos, float4* vel, float4* accS, const StepConfig& cfg,
-                  cudaStream_t s, const FeatureOut* feat) {
+                  cudaStream_t s, const FeatureOut* feat, unsigned int* status) {
     if (n <= 0) return;
     FeatOut fo{nullptr, 0, 0, 0.f};
     if (feat) fo = FeatOut{feat->feat, feat->byId, feat->boxWalls, feat->dtL};
@@ -892,11 +947,11 @@ void launch_force(int n, const float4* posS, const float4* velS, const float4* r
                 RowMasks{const_cast<int*>(rowStart), const_cast<unsigned int*>(rowMask)}, pos, vel, accS, fo};
     const bool tension = ph.tension != 0.0f;
     if (cfg.kahan) {
-        if (tension) force_dispatch<true, true>(F, cfg, s);
-        else force_dispatch<true, false>(F, cfg, s);
+        if (tension) force_dispatch<true, true>(F, cfg, status, s);
+        else force_dispatch<true, false>(F, cfg, status, s);
     } else {
-        if (tension) force_dispatch<false, true>(F, cfg, s);
-        else force_dispatch<false, false>(F, cfg, s);
+        if (tension) force_dispatch<false, true>(F, cfg, status, s);
+        else force_dispatch<false, false>(F, cfg, status, s);
     }
 }
 
