@@ -183,7 +183,11 @@ __device__ __forceinline__ void row_range(float4 xi, const Stencil& st, float h,
     const float g2 = gy * gy + gz * gz;
     if (g2 > h2) return;
     const float inv = 1.0f / g.spacing;
-    const float rx = sqrtf(h2 - g2) + eps;
+    // the reach in x: an approximate square root (relative error ~2^-22) is
+    // far inside the eps margin
+    float rx;
+    asm("sqrt.approx.f32 %0, %1;" : "=f"(rx) : "f"(h2 - g2));
+    rx += eps;
     const float xl = xi.x - rx, xr = xi.x + rx;
     const int cl = max(st.x0, (int)floorf((xl - g.origin[0]) * inv));
     const int cr = min(st.x1, (int)floorf((xr - g.origin[0]) * inv));
@@ -292,7 +296,11 @@ __device__ __forceinline__ void row_range_rel(float4 xi, int3 c, const Stencil& 
     const float g2 = gy * gy + gz * gz;
     if (g2 > h2) return;
     const float inv = 1.0f / g.spacing;
-    const float rx = sqrtf(h2 - g2) + eps;
+    // the reach in x: an approximate square root (relative error ~2^-22) is
+    // far inside the eps margin
+    float rx;
+    asm("sqrt.approx.f32 %0, %1;" : "=f"(rx) : "f"(h2 - g2));
+    rx += eps;
     const float xl = xi.x - rx, xr = xi.x + rx;
     const int cl = max(st.x0, c.x + (int)floorf(xl * inv));
     const int cr = min(st.x1, c.x + (int)floorf(xr * inv));
