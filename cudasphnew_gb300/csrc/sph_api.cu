@@ -163,7 +163,7 @@ void free_all(sph_sim* s) {
     for (cudaEvent_t e : s->events) cudaEventDestroy(e);
     void* ptrs[] = {s->pos, s->vel, s->posS, s->velS, s->rho4S, s->accS, s->sb.cnt, s->sb.cellOffset,
                     s->sb.keySlot, s->sb.tmpIds, s->sb.sortedHash, s->sb.sortedIds, s->sb.workIds,
-                    s->sb.xS, s->sb.halfOffset, s->scanBlock,
+                    s->sb.halfOffset, s->scanBlock,
                     s->status, s->staging, s->map4, s->mapDist, s->rowStart, s->rowMask, s->diagBuf,
                     s->scenesDev, s->reuse};
     for (void* p : ptrs)
@@ -371,7 +371,6 @@ sph_status alloc_handle(sph_sim* s, int n, long long C) {
     SPH_CUDA(dalloc(&s->sb.sortedHash, n));
     SPH_CUDA(dalloc(&s->sb.sortedIds, n));
     SPH_CUDA(dalloc(&s->sb.workIds, n));
-    SPH_CUDA(dalloc(&s->sb.xS, n));
     SPH_CUDA(dalloc(&s->sb.halfOffset, (size_t)C + 1));
     SPH_CUDA(cudaMemsetAsync(s->sb.halfOffset, 0, sizeof(int) * ((size_t)C + 1), s->stream));
     SPH_CUDA(dalloc(&s->scanBlock, (size_t)tiles + 2));
@@ -1040,7 +1039,7 @@ sph_status sph_autotune(sph_handle s, int reps, sph_tuning* chosen) {
     } bufs[] = {{s->posS, nullptr, sizeof(float4) * n},       {s->velS, nullptr, sizeof(float4) * n},
                 {s->rho4S, nullptr, sizeof(float4) * n},      {s->sb.sortedHash, nullptr, sizeof(int) * n},
                 {s->sb.sortedIds, nullptr, sizeof(int) * n},  {s->sb.cellOffset, nullptr, sizeof(int) * ((size_t)C + 1)},
-                {s->sb.workIds, nullptr, sizeof(int) * n},    {s->sb.xS, nullptr, sizeof(float) * n},
+                {s->sb.workIds, nullptr, sizeof(int) * n},
                 {s->sb.halfOffset, nullptr, sizeof(int) * ((size_t)C + 1)}};
     float4* scratch = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;

@@ -79,7 +79,6 @@ struct SortBuffers {
     int* sortedHash;          // [n]
     int* sortedIds;           // [n]   the reference's permutation (cell, id)
     int* workIds;             // [n]   the working order (cell, x, id) of the sorted arrays
-    float* xS;                // [n]   x coordinate in the working order
     int* halfOffset;          // [C+1] first working index of each cell's upper x-half
                               //       (meaningful for occupied cells only)
     unsigned long long* scanFlags;  // decoupled look-back tile states

@@ -311,10 +311,9 @@ void launch_scatter(int n, SortBuffers sb, cudaStream_t s) {
 // Two orders come out of one pass over the cell segment:
 //   by particle id   -> sortedIds, the reference's permutation (stable sort
 //                       by hash, particle_simulation.cu:2340), kept for the API;
-//   by (x, id)       -> workIds, the order the neighbour kernels use.  A row of
-//                       three x-adjacent cells is then sorted by x as a whole,
-//                       so a binary search narrows it to the particles within
-//                       reach of a given x.
+//   by (x, id)       -> workIds, the order the neighbour kernels use: a cell's
+//                       members sorted by x, so the lower and upper x-halves of
+//                       a cell are two contiguous ranges (halfOffset below).
 // Ranks count the smaller keys in the segment; x is compared through its
 // order-preserving integer image so the order is total (NaN included).
 // ---------------------------------------------------------------------------
@@ -331,8 +330,7 @@ __global__ void k_rank_gather(int n, const int* __restrict__ sortedHash, const i
                               const int* __restrict__ tmpIds, const float4* __restrict__ pos,
                               const float4* __restrict__ vel, GridDev g_, const SceneDev* __restrict__ scenes,
                               int* __restrict__ sortedIds, int* __restrict__ workIds, int* __restrict__ halfOffset,
-                              float4* __restrict__ posS, float4* __restrict__ velS, float* __restrict__ xS,
-                              const int* __restrict__ skip) {
+                              float4* __restrict__ posS, float4* __restrict__ velS, const int* __restrict__ skip) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n || (skip && *skip)) return;
     int c = sortedHash[k];
@@ -357,7 +355,6 @@ __global__ void k_rank_gather(int n, const int* __restrict__ sortedHash, const i
     workIds[s + rX] = my;
     posS[s + rX] = p;
     velS[s + rX] = __ldg(vel + my);
-    xS[s + rX] = p.x;
     if (rX == 0) halfOffset[c] = s + below;
 }
 
@@ -368,15 +365,15 @@ void launch_rank_gather(int n, SortBuffers sb, const float4* pos, const float4* 
     if (sb.scenes)
         k_rank_gather<true, false><<<grid, 256, 0, s>>>(n, sb.sortedHash, sb.cellOffset, sb.tmpIds, pos, vel, g,
                                                         sb.scenes, sb.sortedIds, sb.workIds, sb.halfOffset, posS,
-                                                        velS, sb.xS, sb.skip);
+                                                        velS, sb.skip);
     else if (g.rel)
         k_rank_gather<false, true><<<grid, 256, 0, s>>>(n, sb.sortedHash, sb.cellOffset, sb.tmpIds, pos, vel, g,
                                                         nullptr, sb.sortedIds, sb.workIds, sb.halfOffset, posS, velS,
-                                                        sb.xS, sb.skip);
+                                                        sb.skip);
     else
         k_rank_gather<false, false><<<grid, 256, 0, s>>>(n, sb.sortedHash, sb.cellOffset, sb.tmpIds, pos, vel, g,
                                                          nullptr, sb.sortedIds, sb.workIds, sb.halfOffset, posS,
-                                                         velS, sb.xS, sb.skip);
+                                                         velS, sb.skip);
 }
 
 // ---------------------------------------------------------------------------
