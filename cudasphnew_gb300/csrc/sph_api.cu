@@ -1159,6 +1159,51 @@ sph_status sph_autotune(sph_handle s, int reps, sph_tuning* chosen) {
     return SPH_OK;
 }
 
+sph_status sph_time_kernel(sph_handle s, int stage, int reps, float* microseconds) {
+    if (!s || !microseconds) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (stage != ST_DENSITY && stage != ST_FORCE)
+        SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "only the density and force stages repeat on one sorted state");
+    if (reps < 1) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "reps must be positive");
+    if (!s->stepped) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "no step has run yet");
+    cudaStream_t st = s->stream;
+    const int n = s->n;
+    GridDev g = grid_of(s);
+    PhysDev ph = make_phys(s->P, s->O);
+    // the density stage rewrites what it wrote (and the masks the force form
+    // reads); the force stage rewrites the state the last step wrote
+    SPH_CUDA(cudaMemsetAsync(s->reuse, 0, sizeof(int), st));
+    auto launch = [&]() {
+        if (stage == ST_DENSITY)
+            launch_density(n, s->posS, rows_of(s), g, ph, s->map, s->rho4S, s->rowStart, s->rowMask, s->cfg, st);
+        else
+            launch_force(n, s->posS, s->velS, s->rho4S, s->sb.workIds, rows_of(s), g, ph, s->map,
+                         s->O.boxCollision, s->rowStart, s->rowMask, s->pos, s->vel, s->accS, s->cfg, st, nullptr,
+                         s->status);
+    };
+    if (stage == ST_FORCE) {  // the masks of the current tuning
+        StepConfig c = s->cfg;
+        launch_density(n, s->posS, rows_of(s), g, ph, s->map, s->rho4S, s->rowStart, s->rowMask, c, st);
+    }
+    launch();  // warm
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    SPH_CUDA(cudaEventCreate(&e0));
+    cudaError_t e = cudaEventCreate(&e1);
+    if (e == cudaSuccess) e = cudaEventRecord(e0, st);
+    if (e == cudaSuccess) {
+        for (int r = 0; r < reps; r++) launch();
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(e1, st);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    SPH_CUDA(e);
+    *microseconds = 1e3f * ms / (float)reps;
+    return latched_status(s);
+}
+
 sph_status sph_stage_times(sph_handle s, float* ms, int* counts, int capacity, int* numStages) {
     if (!s) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "handle is NULL");
     if (numStages) *numStages = ST_COUNT;

@@ -73,6 +73,7 @@ SIGNATURES = {
     "sph_sdf_load": (_i, [ctypes.c_char_p, _vp]),
     "sph_sdf_free": (None, [_vp]),
     "sph_surface_particles": (_i, [_vp, _vp]),
+    "sph_time_kernel": (_i, [_vp, ctypes.c_int, ctypes.c_int, _vp]),
     "sph_camera_look_at": (_i, [_vp, _vp, _vp, _vp]),
     "sph_camera_perspective": (_i, [_vp, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float]),
     "sph_render": (_i, [_vp, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, _vp]),
@@ -487,6 +488,12 @@ class ParticleSimulation:
         check(load().sph_render(self._h, ctypes.byref(camera), width, height, what, img.ctypes.data,
                                 dep.ctypes.data if dep is not None else None))
         return (img, dep) if depth else img
+
+    def time_kernel(self, stage: str, reps: int = 20) -> float:
+        """sph_time_kernel: microseconds per launch of 'density' or 'force'."""
+        us = ctypes.c_float()
+        check(load().sph_time_kernel(self._h, {"density": 4, "force": 5}[stage], reps, ctypes.byref(us)))
+        return us.value
 
     def surface_particles(self) -> np.ndarray:
         """CreateIsParticleSurfaceList: 1 for surface particles (particle order)."""

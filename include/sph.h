@@ -516,6 +516,15 @@ sph_status sph_set_stage_timing(sph_handle h, int enable);
 sph_status sph_stage_times(sph_handle h, float* ms, int* counts, int capacity, int* numStages);
 const char* sph_stage_name(int stage);
 
+/* Average device time of one launch of a stage's kernel (stage 4: density,
+ * 5: force; see sph_stage_name), launched `reps` times back to back on the
+ * last step's sorted state between two CUDA events on the handle's stream,
+ * with the current tuning.  Both kernels rewrite what they wrote: after a
+ * plain step the force stage leaves the state that step left (after another
+ * kind of step it replaces that step's result with the plain step's).  No
+ * reference counterpart. */
+sph_status sph_time_kernel(sph_handle h, int stage, int reps, float* microseconds);
+
 /* Largest inputs sph_cell_tables_noalloc() accepts. */
 #define SPH_NOALLOC_MAX_PARTICLES 65536
 #define SPH_NOALLOC_MAX_CELLS 262144
