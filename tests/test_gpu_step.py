@@ -362,3 +362,21 @@ def test_surface_particles(sphlib):
     # the GPU tests r^2 in float: a pair exactly at h may count differently
     assert (flags != ref).sum() <= 2
     assert 0 < flags.sum() < len(flags)
+
+
+def test_time_kernel_leaves_the_plain_step_state(sphlib):
+    """sph_time_kernel repeats the density and force kernels on the last
+    step's sorted state: the state after it is the state after the step."""
+    sc = scenes.config1()
+    with sphlib.ParticleSimulation(sc.params, sc.positions, sc.velocities, sc.options) as sim, \
+            sphlib.ParticleSimulation(sc.params, sc.positions, sc.velocities, sc.options) as ref:
+        for s in (sim, ref):
+            s.step(count=4)
+        assert sim.time_kernel("density", 5) > 0.0
+        assert sim.time_kernel("force", 5) > 0.0
+        np.testing.assert_array_equal(sim.positions(), ref.positions())
+        np.testing.assert_array_equal(sim.velocities(), ref.velocities())
+        np.testing.assert_array_equal(sim.read(sphlib.FIELD_DENSITY), ref.read(sphlib.FIELD_DENSITY))
+        sim.step(count=2)
+        ref.step(count=2)
+        np.testing.assert_array_equal(sim.positions(), ref.positions())
