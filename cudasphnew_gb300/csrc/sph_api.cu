@@ -9,6 +9,7 @@
 #include <new>
 #include <sstream>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "sph_sim.h"
@@ -1039,7 +1040,7 @@ sph_status sph_autotune(sph_handle s, int reps, sph_tuning* chosen) {
     } bufs[] = {{s->posS, nullptr, sizeof(float4) * n},       {s->velS, nullptr, sizeof(float4) * n},
                 {s->rho4S, nullptr, sizeof(float4) * n},      {s->sb.sortedHash, nullptr, sizeof(int) * n},
                 {s->sb.sortedIds, nullptr, sizeof(int) * n},  {s->sb.cellOffset, nullptr, sizeof(int) * ((size_t)C + 1)},
-                {s->sb.workIds, nullptr, sizeof(int) * n},
+                {s->sb.workIds, nullptr, sizeof(int) * n},    {s->accS, nullptr, sizeof(float4) * n},
                 {s->sb.halfOffset, nullptr, sizeof(int) * ((size_t)C + 1)}};
     float4* scratch = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -1112,6 +1113,7 @@ sph_status sph_autotune(sph_handle s, int reps, sph_tuning* chosen) {
     const float currentTotal = stepTime(current);
     StepConfig best = current;
     float bestTotal = currentTotal;
+    std::vector<std::pair<float, StepConfig>> shapes;  // the best block sizes of each form and cut
     for (int prune = 0; prune <= 1; prune++)
         for (int v = FORCE_DIRECT; v <= FORCE_STAGED; v++) {
             StepConfig c = s->cfg;
@@ -1134,6 +1136,8 @@ sph_status sph_autotune(sph_handle s, int reps, sph_tuning* chosen) {
                 sortStages();
                 launch_density(n, s->posS, rows_of(s), g, ph, s->map, s->rho4S, s->rowStart, s->rowMask, c, st);
             };
+            float bestF = 3.0e38f;
+            StepConfig bestC = c;
             for (int b : blocks) {
                 c.forceBlock = b;
                 float t = timeit(beforeForce, [&] {
@@ -1141,19 +1145,74 @@ sph_status sph_autotune(sph_handle s, int reps, sph_tuning* chosen) {
                                  s->O.boxCollision, s->rowStart, s->rowMask, scratch, scratch + n,
                                  scratch + 2 * (size_t)n, c, st, nullptr, s->status);
                 });
+                if (t < bestF) {
+                    bestF = t;
+                    bestC = c;
+                }
                 if (bestD + t < bestTotal) {
                     bestTotal = bestD + t;
                     best = c;
                 }
             }
+            shapes.push_back({bestD + bestF, bestC});
         }
     if (bestTotal > 0.98f * currentTotal) best = current;
     TUNE_CUDA(cudaGetLastError());
     for (auto& b : bufs) TUNE_CUDA(cudaMemcpyAsync(b.dst, b.save, b.bytes, cudaMemcpyDeviceToDevice, st));
     TUNE_CUDA(cudaStreamSynchronize(st));
+
+    // Whole steps decide between the leading shapes: the stage estimates miss
+    // how the stages share the caches and overlap inside a step graph.  The
+    // particle state is saved and put back around each trial.
+    std::sort(shapes.begin(), shapes.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
+    std::vector<StepConfig> finalists{best, current};
+    for (size_t k = 0; k < shapes.size() && finalists.size() < 5; k++) finalists.push_back(shapes[k].second);
+    float4 *savePos = nullptr, *saveVel = nullptr;
+    TUNE_CUDA(cudaMalloc((void**)&savePos, sizeof(float4) * n));
+    TUNE_CUDA(cudaMalloc((void**)&saveVel, sizeof(float4) * n));
+    TUNE_CUDA(cudaMemcpyAsync(savePos, s->pos, sizeof(float4) * n, cudaMemcpyDeviceToDevice, st));
+    TUNE_CUDA(cudaMemcpyAsync(saveVel, s->vel, sizeof(float4) * n, cudaMemcpyDeviceToDevice, st));
+    const unsigned int steps0 = s->numTimeSteps;
+    const bool stepped0 = s->stepped;
+    float bestStep = 3.0e38f;
+    StepConfig chosenCfg = best;
+    cudaError_t te = cudaSuccess;
+    for (const StepConfig& c : finalists) {
+        s->cfg = c;
+        invalidate_graphs(s);
+        float fastest = 3.0e38f;
+        for (int r = 0; r < 3 && te == cudaSuccess; r++) {
+            te = cudaMemcpyAsync(s->pos, savePos, sizeof(float4) * n, cudaMemcpyDeviceToDevice, st);
+            if (te == cudaSuccess) te = cudaMemcpyAsync(s->vel, saveVel, sizeof(float4) * n, cudaMemcpyDeviceToDevice, st);
+            if (te == cudaSuccess && sph_step_many(s, SPH_STEP_PLAIN, 2) != SPH_OK) te = cudaErrorUnknown;  // capture
+            if (te == cudaSuccess) te = cudaEventRecord(e0, st);
+            if (te == cudaSuccess && sph_step_many(s, SPH_STEP_PLAIN, 8) != SPH_OK) te = cudaErrorUnknown;
+            if (te == cudaSuccess) te = cudaEventRecord(e1, st);
+            if (te == cudaSuccess) te = cudaEventSynchronize(e1);
+            float ms = 0.f;
+            if (te == cudaSuccess) te = cudaEventElapsedTime(&ms, e0, e1);
+            if (te == cudaSuccess) fastest = std::min(fastest, ms);
+        }
+        // keep the incumbent unless beaten by 2 %
+        if (te == cudaSuccess && fastest < (&c == &finalists[0] ? bestStep : 0.98f * bestStep)) {
+            bestStep = fastest;
+            chosenCfg = c;
+        }
+    }
+    if (te == cudaSuccess) te = cudaMemcpyAsync(s->pos, savePos, sizeof(float4) * n, cudaMemcpyDeviceToDevice, st);
+    if (te == cudaSuccess) te = cudaMemcpyAsync(s->vel, saveVel, sizeof(float4) * n, cudaMemcpyDeviceToDevice, st);
+    if (te == cudaSuccess) te = cudaMemsetAsync(s->reuse, 0, sizeof(int), st);
+    for (auto& b : bufs)
+        if (te == cudaSuccess) te = cudaMemcpyAsync(b.dst, b.save, b.bytes, cudaMemcpyDeviceToDevice, st);
+    if (te == cudaSuccess) te = cudaStreamSynchronize(st);
+    cudaFree(savePos);
+    cudaFree(saveVel);
+    s->numTimeSteps = steps0;
+    s->stepped = stepped0;
+    TUNE_CUDA(te);
 #undef TUNE_CUDA
     cleanup();
-    s->cfg = best;
+    s->cfg = chosenCfg;
     invalidate_graphs(s);
     if (chosen) return sph_get_tuning(s, chosen);
     return SPH_OK;
