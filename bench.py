@@ -6,7 +6,7 @@ boundary map.  A "step" is one plain SPH step of that scene (hash, sort, cell
 table, density, forces + wall terms + integration + box collision).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-  python bench.py --leg batched|learned_1m --steps K     (one leg alone, for profiling)
+  python bench.py --leg batched|learned_1m|two_scale --steps K     (one leg alone, for profiling)
 
 --impl reference times the reference algorithm on the host cores (the oracle's
 FP32 restatement: the reference itself does not build here) on the same scene.
@@ -53,10 +53,10 @@ def parse():
                     help="skip the 64-scene batched leg and the two-scale leg")
     ap.add_argument("--no-learned", action="store_true",
                     help="skip the learned-corrector legs (16,384-particle scene and the 1M scene)")
-    ap.add_argument("--leg", choices=["batched", "learned_1m"], default=None,
+    ap.add_argument("--leg", choices=["batched", "learned_1m", "two_scale"], default=None,
                     help="run only this leg (batched: the 64-scene batch; learned_1m: train the corrector on the "
-                         "16,384-particle scene, then the learned leg of the 1M scene) and print its JSON object; "
-                         "for profiling")
+                         "16,384-particle scene, then the learned leg of the 1M scene; two_scale: the two-scale "
+                         "run) and print its JSON object; for profiling")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the library's default launch shapes (for profiling runs)")
     return ap.parse_args()
@@ -542,6 +542,8 @@ def run_ours(args):
         if rank == 0:
             if args.leg == "batched":
                 res = batched_leg(lib, torch, stream, steps=args.steps)
+            elif args.leg == "two_scale":
+                res = two_scale_leg(lib, torch, stream, steps=args.steps)
             else:
                 model, lcfg = train_corrector_16k(lib, stream)
                 res = learned_leg_1m(lib, torch, stream, model, lcfg, sc, args.steps)
