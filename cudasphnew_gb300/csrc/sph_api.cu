@@ -173,7 +173,8 @@ void free_all(sph_sim* s) {
                       s->ts.splitIds,  s->ts.boundaryIds, s->ts.defaultIds,  s->ts.subIds,
                       s->ts.subPos,    s->ts.subVel,      s->ts.subAcc,      s->ts.subRho,
                       s->ts.subCnt,    s->ts.subOffset,   s->ts.subKeySlot,  s->ts.subTmp,
-                      s->ts.subSortedHash, s->ts.subSortedIds, s->subScanBlock};
+                      s->ts.subSortedHash, s->ts.subSortedIds, s->ts.subPosS, s->ts.markList,
+                      s->subScanBlock};
     for (void* p : tsPtrs)
         if (p) cudaFree(p);
     if (s->statusHost) cudaFreeHost(s->statusHost);
@@ -208,7 +209,8 @@ sph_status ensure_two_scale(sph_sim* s) {
     SPH_CUDA(dalloc(&T.state, n4));
     SPH_CUDA(dalloc(&T.blockCounts, 3 * nb));
     SPH_CUDA(dalloc(&T.blockOffsets, 3 * nb));
-    SPH_CUDA(dalloc(&T.counts, 4));
+    SPH_CUDA(dalloc(&T.counts, 5));
+    SPH_CUDA(dalloc(&T.markList, n));
     SPH_CUDA(dalloc(&T.splitIds, n));
     SPH_CUDA(dalloc(&T.boundaryIds, n));
     SPH_CUDA(dalloc(&T.defaultIds, n));
@@ -223,10 +225,11 @@ sph_status ensure_two_scale(sph_sim* s) {
     SPH_CUDA(dalloc(&T.subTmp, 8 * n));
     SPH_CUDA(dalloc(&T.subSortedHash, 8 * n));
     SPH_CUDA(dalloc(&T.subSortedIds, 8 * n));
+    SPH_CUDA(dalloc(&T.subPosS, 8 * n));
     SPH_CUDA(dalloc(&s->subScanBlock, tiles + 2));
     cudaStream_t q = s->stream;
     SPH_CUDA(cudaMemsetAsync(T.state, 0, n4, q));
-    SPH_CUDA(cudaMemsetAsync(T.counts, 0, sizeof(int) * 4, q));
+    SPH_CUDA(cudaMemsetAsync(T.counts, 0, sizeof(int) * 5, q));
     SPH_CUDA(cudaMemsetAsync(T.subPos, 0, sizeof(float4) * 8 * n, q));
     SPH_CUDA(cudaMemsetAsync(T.subVel, 0, sizeof(float4) * 8 * n, q));
     SPH_CUDA(cudaMemsetAsync(T.subAcc, 0, sizeof(float4) * 8 * n, q));

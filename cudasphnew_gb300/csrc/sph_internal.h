@@ -95,7 +95,9 @@ struct TwoScaleDev {
     unsigned char* state;       // [n rounded up to 4] 2-bit history per particle
     int* blockCounts;           // [3 * blocks] per-block class counts
     int* blockOffsets;          // [3 * blocks]
-    int* counts;                // [4] split, boundary, default, children (device side)
+    int* counts;                // [5] split, boundary, default, children (device side); [4]: length
+                                //     of markList, zero between steps
+    int* markList;              // [n] working-order indices of split particles, any order
     int* splitIds;              // [n]
     int* boundaryIds;           // [n]
     int* defaultIds;            // [n]
@@ -110,6 +112,7 @@ struct TwoScaleDev {
     int* subTmp;                // [8n]
     int* subSortedHash;         // [8n]
     int* subSortedIds;          // [8n] slots in (fine cell, list position) order
+    float4* subPosS;            // [8n] child positions in that order
     float splitMin[3], splitMax[3];
     int childMode;              // sph_options.childMode
 };

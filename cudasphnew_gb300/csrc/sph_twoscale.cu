@@ -43,61 +43,107 @@ inline int stride_grid(long long work, int bs) {
     return (int)(g < 1 ? 1 : (g > 4096 ? 4096 : g));
 }
 
-// The neighbour loops of the two-scale pass run over few particles (a few
-// thousand split parents, tens of thousands of children), so each particle
-// gets a group of TS_G lanes that stride through its candidates; the
-// group's partial sums are combined by a fixed shuffle tree, so results do
-// not depend on scheduling.  Groups are aligned to TS_G lanes of a warp and
-// all lanes of a group take the same branches.
-constexpr int TS_G = 8;
+// The neighbour loops of the two-scale pass (marking, projection, the fine
+// level's density and forces) run over few particles (a few thousand split
+// parents, tens of thousands of children), so each particle gets a warp.
+// Lane l < 27 takes row l / 3 of the particle's 3 x 3 stencil rows and every
+// third candidate of it, from the row's start + l % 3, and loads TS_BATCH
+// candidates before it tests any; lanes 27..31 take none.  So a particle
+// waits for one round of row offsets and a few rounds of candidate loads,
+// not for its rows one after the other.  Partial sums are combined by a
+// fixed butterfly (every lane ends with the same bits), so results do not
+// depend on scheduling.
+constexpr int TS_BATCH = 4;
+constexpr int TS_WARP_BLOCK = 128;
 
-__device__ __forceinline__ unsigned int group_mask() { return 0xFFu << (threadIdx.x & 24u); }
+__device__ __forceinline__ void lane_row(const Stencil& st, const GridDev& g, const int* __restrict__ offs, int lane,
+                                         int& t, int& e) {
+    t = e = 0;
+    if (lane >= 27) return;
+    const int r = lane / 3;
+    const int z = st.z0 + r / 3, y = st.y0 + r % 3;
+    if (z > st.z1 || y > st.y1) return;
+    const int row = g.dim[0] * (g.dim[1] * z + y);
+    t = __ldg(offs + row + st.x0) + lane % 3;
+    e = __ldg(offs + row + st.x1 + 1);
+}
 
-__device__ __forceinline__ float group_sum(float v, unsigned int m) {
-    v += __shfl_xor_sync(m, v, 4);
-    v += __shfl_xor_sync(m, v, 2);
-    v += __shfl_xor_sync(m, v, 1);
+// Calls visit(t, x_t) for the lane's candidates t, with x_t = load(t).
+template <class Load, class Visit>
+__device__ __forceinline__ void walk_lane(int t, int e, Load load, Visit visit) {
+    for (; t < e; t += 3 * TS_BATCH) {
+        float4 x[TS_BATCH];
+#pragma unroll
+        for (int u = 0; u < TS_BATCH; u++)
+            if (t + 3 * u < e) x[u] = load(t + 3 * u);
+#pragma unroll
+        for (int u = 0; u < TS_BATCH; u++)
+            if (t + 3 * u < e) visit(t + 3 * u, x[u]);
+    }
+}
+
+__device__ __forceinline__ float warp_total(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
+}
+
+inline int warp_grid(long long items) {
+    const long long per = TS_WARP_BLOCK / 32;
+    long long b = (items + per - 1) / per;
+    const long long cap = 16LL * device_sms();
+    return (int)(b < 1 ? 1 : (b > cap ? cap : b));
 }
 
 // ---------------------------------------------------------------------------
 // shift_state + find_split_particles (:730-740, 932-952)
 // ---------------------------------------------------------------------------
+// Also lists the split particles' working-order indices for the marking
+// (warp-aggregated appends, in no fixed order: the marks do not depend on it).
 __global__ void k_ts_state(int n, const float4* __restrict__ posS, const int* __restrict__ workIds, TwoScaleDev T) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    const int id = workIds[k];
-    unsigned int s = ((unsigned int)T.state[id] << 2) & 0xFFu;
-    if (in_region(T, posS[k])) s |= 1u;
-    T.state[id] = (unsigned char)s;
+    const int lane = threadIdx.x & 31;
+    bool split = false;
+    if (k < n) {
+        const int id = workIds[k];
+        unsigned int s = ((unsigned int)T.state[id] << 2) & 0xFFu;
+        split = in_region(T, posS[k]);
+        if (split) s |= 1u;
+        T.state[id] = (unsigned char)s;
+    }
+    const unsigned int m = __ballot_sync(0xffffffffu, split);
+    if (!m) return;
+    int base = 0;
+    if (lane == 0) base = atomicAdd(T.counts + 4, __popc(m));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (split) T.markList[base + __popc(m & ((1u << lane) - 1u))] = k;
 }
 
 // find_boundary_particles (:954-1017) as a race-free scatter: every split
 // particle (decided from its position, not from a state other threads are
 // changing) marks all particles of its 27-cell stencil within compactSupport,
-// itself included, with a word-wide atomic OR.
-__global__ void k_ts_mark(int n, const float4* __restrict__ posS, const int* __restrict__ workIds,
-                          const int* __restrict__ cellOffset, GridDev g, float h, TwoScaleDev T) {
-    const long long gid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) / TS_G;
-    const int lane = threadIdx.x & (TS_G - 1);
-    if (gid >= n) return;
-    const int k = (int)gid;
-    const float4 xs = posS[k];
-    if (!in_region(T, xs)) return;
-    const Stencil st = stencil(xs, h, g);
+// itself included, with a word-wide atomic OR.  One warp per listed split
+// particle.
+__global__ void __launch_bounds__(TS_WARP_BLOCK) k_ts_mark(const float4* __restrict__ posS,
+                                                           const int* __restrict__ workIds,
+                                                           const int* __restrict__ cellOffset, GridDev g, float h,
+                                                           TwoScaleDev T) {
+    const int count = T.counts[4];
+    const int lane = threadIdx.x & 31;
+    const int warps = gridDim.x * (TS_WARP_BLOCK / 32);
     const float h2 = __fmul_rn(h, h);
     unsigned int* words = reinterpret_cast<unsigned int*>(T.state);
-    for (int z = st.z0; z <= st.z1; z++)
-        for (int y = st.y0; y <= st.y1; y++) {
-            const int row = g.dim[0] * (g.dim[1] * z + y);
-            const int s = __ldg(cellOffset + row + st.x0), e = __ldg(cellOffset + row + st.x1 + 1);
-            for (int t = s + lane; t < e; t += TS_G) {
-                if (ref_r2(xs, __ldg(posS + t)) <= h2) {
-                    const int v = workIds[t];
-                    atomicOr(words + (v >> 2), 2u << (8 * (v & 3)));
-                }
+    for (int idx = (blockIdx.x * TS_WARP_BLOCK + threadIdx.x) >> 5; idx < count; idx += warps) {
+        const float4 xs = posS[T.markList[idx]];
+        int t, e;
+        lane_row(stencil(xs, h, g), g, cellOffset, lane, t, e);
+        walk_lane(t, e, [&](int c) { return __ldg(posS + c); }, [&](int c, float4 xc) {
+            if (ref_r2(xs, xc) <= h2) {
+                const int v = workIds[c];
+                atomicOr(words + (v >> 2), 2u << (8 * (v & 3)));
             }
-        }
+        });
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -167,6 +213,7 @@ __global__ void __launch_bounds__(TS_BLOCK) k_ts_scan_blocks(int nb, TwoScaleDev
         T.counts[1] = s_carry[1];
         T.counts[2] = s_carry[2];
         T.counts[3] = 8 * (s_carry[0] + s_carry[1]);
+        T.counts[4] = 0;  // the marking has read the split list: empty for the next step
     }
 }
 
@@ -289,37 +336,35 @@ __global__ void k_ts_merge(int n, float4* __restrict__ posS, float4* __restrict_
 // 0 by 0).  Coarse positions come from `coarsePos` in the working order, or
 // through workIds from the particle-order state when `byId` is set.
 // ---------------------------------------------------------------------------
-__global__ void k_ts_project(const float4* __restrict__ coarsePos, const int* __restrict__ workIds, int byId,
-                             const float4* __restrict__ rho4S, const int* __restrict__ cellOffset, GridDev g,
-                             float hs, TwoScaleDev T) {
+__global__ void __launch_bounds__(TS_WARP_BLOCK) k_ts_project(const float4* __restrict__ coarsePos,
+                                                              const int* __restrict__ workIds, int byId,
+                                                              const float4* __restrict__ rho4S,
+                                                              const int* __restrict__ cellOffset, GridDev g,
+                                                              float hs, TwoScaleDev T) {
     const int nSplit = T.counts[0];
     const int nSub = T.counts[3];
     const float hs2 = __fmul_rn(hs, hs);
-    const int lane = threadIdx.x & (TS_G - 1);
-    const unsigned int gm = group_mask();
-    const int groups = gridDim.x * blockDim.x / TS_G;
-    for (int idx = 8 * nSplit + (blockIdx.x * blockDim.x + threadIdx.x) / TS_G; idx < nSub; idx += groups) {
+    const int lane = threadIdx.x & 31;
+    const int warps = gridDim.x * (TS_WARP_BLOCK / 32);
+    for (int idx = 8 * nSplit + ((blockIdx.x * TS_WARP_BLOCK + threadIdx.x) >> 5); idx < nSub; idx += warps) {
         const int slot = T.subIds[idx];
         const float4 x = T.subPos[slot];
-        const Stencil st = stencil(x, hs, g);
+        int t, e;
+        lane_row(stencil(x, hs, g), g, cellOffset, lane, t, e);
         float d = 0.f, p = 0.f, cnt = 0.f;
-        for (int z = st.z0; z <= st.z1; z++)
-            for (int y = st.y0; y <= st.y1; y++) {
-                const int row = g.dim[0] * (g.dim[1] * z + y);
-                const int s = __ldg(cellOffset + row + st.x0), e = __ldg(cellOffset + row + st.x1 + 1);
-                for (int t = s + lane; t < e; t += TS_G) {
-                    const float4 xj = byId ? coarsePos[workIds[t]] : coarsePos[t];
-                    if (ref_r2(x, xj) <= hs2) {
-                        const float4 rj = rho4S[t];
-                        d += rj.x;
-                        p += rj.y;
-                        cnt += 1.f;
-                    }
+        walk_lane(
+            t, e, [&](int c) { return byId ? __ldg(coarsePos + __ldg(workIds + c)) : __ldg(coarsePos + c); },
+            [&](int c, float4 xc) {
+                if (ref_r2(x, xc) <= hs2) {
+                    const float4 rj = __ldg(rho4S + c);
+                    d += rj.x;
+                    p += rj.y;
+                    cnt += 1.f;
                 }
-            }
-        d = group_sum(d, gm);
-        p = group_sum(p, gm);
-        cnt = group_sum(cnt, gm);
+            });
+        d = warp_total(d);
+        p = warp_total(p);
+        cnt = warp_total(cnt);
         if (lane == 0) T.subRho[slot] = cnt > 0.f ? make_float2(d / cnt, p / cnt) : make_float2(0.f, 0.f);
     }
 }
@@ -361,36 +406,38 @@ __global__ void k_ts_subrank(TwoScaleDev T) {
         const int my = T.subTmp[k];
         int r = 0;
         for (int t = s; t < e; t++) r += T.subTmp[t] < my;
-        T.subSortedIds[s + r] = T.subIds[my];
+        const int slot = T.subIds[my];
+        T.subSortedIds[s + r] = slot;
+        T.subPosS[s + r] = T.subPos[slot];
     }
 }
 
 // ---------------------------------------------------------------------------
 // compute_sub_particle_density_pressure (:259-313) for regular children.
 // ---------------------------------------------------------------------------
-__global__ void k_ts_subdensity(GridDev g, PhysDev ph, TwoScaleDev T) {
+__global__ void __launch_bounds__(TS_WARP_BLOCK) k_ts_subdensity(GridDev g, PhysDev ph, TwoScaleDev T) {
     const int nReg = 8 * T.counts[0];
-    const int lane = threadIdx.x & (TS_G - 1);
-    const unsigned int gm = group_mask();
-    const int groups = gridDim.x * blockDim.x / TS_G;
-    for (int idx = (blockIdx.x * blockDim.x + threadIdx.x) / TS_G; idx < nReg; idx += groups) {
+    const int lane = threadIdx.x & 31;
+    const int warps = gridDim.x * (TS_WARP_BLOCK / 32);
+    for (int idx = (blockIdx.x * TS_WARP_BLOCK + threadIdx.x) >> 5; idx < nReg; idx += warps) {
         const int slot = T.subIds[idx];
         const float4 x = T.subPos[slot];
-        const Stencil st = stencil(x, ph.h, g);
+        int t, e;
+        lane_row(stencil(x, ph.h, g), g, T.subOffset, lane, t, e);
+        float part = 0.f;
+        walk_lane(t, e, [&](int c) { return __ldg(T.subPosS + c); }, [&](int, float4 xc) {
+            const float w = fmaxf(ph.h2 - dist2(x, xc), 0.f);
+            part = fmaf(w * w, w, part);
+        });
+        // row sums (lanes 3r, 3r+1, 3r+2), then compensated over the rows in order
+        const float p1 = __shfl_down_sync(0xffffffffu, part, 1), p2 = __shfl_down_sync(0xffffffffu, part, 2);
+        const float rowSum = (part + p1) + p2;
         float sum = 0.f, comp = 0.f;
-        for (int z = st.z0; z <= st.z1; z++)
-            for (int y = st.y0; y <= st.y1; y++) {
-                const int row = g.dim[0] * (g.dim[1] * z + y);
-                const int s = __ldg(T.subOffset + row + st.x0), e = __ldg(T.subOffset + row + st.x1 + 1);
-                float rs = 0.f;
-                for (int t = s + lane; t < e; t += TS_G) {
-                    const float r2 = dist2(x, T.subPos[T.subSortedIds[t]]);
-                    const float w = fmaxf(ph.h2 - r2, 0.f);
-                    rs = fmaf(w * w, w, rs);
-                }
-                rs = group_sum(rs, gm);  // every lane of the group holds the row sum
-                if (rs > 0.f) kahan_add(sum, comp, rs);
-            }
+#pragma unroll
+        for (int r = 0; r < 9; r++) {
+            const float rs = __shfl_sync(0xffffffffu, rowSum, 3 * r);
+            if (rs > 0.f) kahan_add(sum, comp, rs);
+        }
         const float rho = __fsub_rn(sum, comp) * ph.poly6m;
         if (lane == 0) T.subRho[slot] = make_float2(rho, ph.stiffness * (rho - ph.restDensity));
     }
@@ -401,56 +448,50 @@ __global__ void k_ts_subdensity(GridDev g, PhysDev ph, TwoScaleDev T) {
 // colour field of the regular children; surface tension is always tested
 // (no wall terms at this level).
 // ---------------------------------------------------------------------------
-__global__ void k_ts_subforce(GridDev g, PhysDev ph, TwoScaleDev T) {
+__global__ void __launch_bounds__(TS_WARP_BLOCK) k_ts_subforce(GridDev g, PhysDev ph, TwoScaleDev T) {
     const int nReg = 8 * T.counts[0];
-    const int lane = threadIdx.x & (TS_G - 1);
-    const unsigned int gm = group_mask();
-    const int groups = gridDim.x * blockDim.x / TS_G;
-    for (int idx = (blockIdx.x * blockDim.x + threadIdx.x) / TS_G; idx < nReg; idx += groups) {
+    const int lane = threadIdx.x & 31;
+    const int warps = gridDim.x * (TS_WARP_BLOCK / 32);
+    for (int idx = (blockIdx.x * TS_WARP_BLOCK + threadIdx.x) >> 5; idx < nReg; idx += warps) {
         const int slot = T.subIds[idx];
         const float4 xi = T.subPos[slot], vi = T.subVel[slot];
         const float2 ri = T.subRho[slot];
         const float rhoi = ri.x;
         const float qi = ri.y / (rhoi * rhoi);
-        const Stencil st = stencil(xi, ph.h, g);
+        int t, e;
+        lane_row(stencil(xi, ph.h, g), g, T.subOffset, lane, t, e);
         float fp[3] = {0.f, 0.f, 0.f}, fv[3] = {0.f, 0.f, 0.f}, cg[3] = {0.f, 0.f, 0.f}, cl = 0.f;
-        for (int z = st.z0; z <= st.z1; z++)
-            for (int y = st.y0; y <= st.y1; y++) {
-                const int row = g.dim[0] * (g.dim[1] * z + y);
-                const int s = __ldg(T.subOffset + row + st.x0), e = __ldg(T.subOffset + row + st.x1 + 1);
-                for (int t = s + lane; t < e; t += TS_G) {
-                    const int j = T.subSortedIds[t];
-                    const float4 xj = T.subPos[j];
-                    const float r2 = dist2(xi, xj);
-                    if (!(r2 <= ph.h2 && r2 > 0.f)) continue;
-                    const float4 vj = T.subVel[j];
-                    const float2 rj = T.subRho[j];
-                    const float invj = 1.0f / rj.x;
-                    const float dx = __fsub_rn(xi.x, xj.x), dy = __fsub_rn(xi.y, xj.y), dz = __fsub_rn(xi.z, xj.z);
-                    const float rinv = rsqrtf(r2);
-                    const float hr = ph.h - r2 * rinv;
-                    const float sp = (qi + rj.y * invj * invj) * hr * hr * rinv;
-                    const float sv = invj * hr;
-                    fp[0] = fmaf(sp, dx, fp[0]);
-                    fp[1] = fmaf(sp, dy, fp[1]);
-                    fp[2] = fmaf(sp, dz, fp[2]);
-                    fv[0] = fmaf(sv, vj.x - vi.x, fv[0]);
-                    fv[1] = fmaf(sv, vj.y - vi.y, fv[1]);
-                    fv[2] = fmaf(sv, vj.z - vi.z, fv[2]);
-                    const float d2 = ph.h2 - r2;
-                    const float sc = invj * d2 * d2;
-                    cg[0] = fmaf(sc, dx, cg[0]);
-                    cg[1] = fmaf(sc, dy, cg[1]);
-                    cg[2] = fmaf(sc, dz, cg[2]);
-                    cl = fmaf(invj * d2, 3.f * ph.h2 - 7.f * r2, cl);
-                }
-            }
+        walk_lane(t, e, [&](int c) { return __ldg(T.subPosS + c); }, [&](int c, float4 xj) {
+            const float r2 = dist2(xi, xj);
+            if (!(r2 <= ph.h2 && r2 > 0.f)) return;
+            const int j = __ldg(T.subSortedIds + c);
+            const float4 vj = T.subVel[j];
+            const float2 rj = T.subRho[j];
+            const float invj = 1.0f / rj.x;
+            const float dx = __fsub_rn(xi.x, xj.x), dy = __fsub_rn(xi.y, xj.y), dz = __fsub_rn(xi.z, xj.z);
+            const float rinv = rsqrtf(r2);
+            const float hr = ph.h - r2 * rinv;
+            const float sp = (qi + rj.y * invj * invj) * hr * hr * rinv;
+            const float sv = invj * hr;
+            fp[0] = fmaf(sp, dx, fp[0]);
+            fp[1] = fmaf(sp, dy, fp[1]);
+            fp[2] = fmaf(sp, dz, fp[2]);
+            fv[0] = fmaf(sv, vj.x - vi.x, fv[0]);
+            fv[1] = fmaf(sv, vj.y - vi.y, fv[1]);
+            fv[2] = fmaf(sv, vj.z - vi.z, fv[2]);
+            const float d2 = ph.h2 - r2;
+            const float sc = invj * d2 * d2;
+            cg[0] = fmaf(sc, dx, cg[0]);
+            cg[1] = fmaf(sc, dy, cg[1]);
+            cg[2] = fmaf(sc, dz, cg[2]);
+            cl = fmaf(invj * d2, 3.f * ph.h2 - 7.f * r2, cl);
+        });
         for (int a = 0; a < 3; a++) {
-            fp[a] = group_sum(fp[a], gm);
-            fv[a] = group_sum(fv[a], gm);
-            cg[a] = group_sum(cg[a], gm);
+            fp[a] = warp_total(fp[a]);
+            fv[a] = warp_total(fv[a]);
+            cg[a] = warp_total(cg[a]);
         }
-        cl = group_sum(cl, gm);
+        cl = warp_total(cl);
         if (lane != 0) continue;
         const float pc = ph.pressCoef * rhoi;
         float force[3];
@@ -520,8 +561,7 @@ void launch_ts_states(int n, const float4* posS, const int* workIds, const int* 
                       const TwoScaleDev& T, cudaStream_t s) {
     if (n <= 0) return;
     k_ts_state<<<(n + 255) / 256, 256, 0, s>>>(n, posS, workIds, T);
-    k_ts_mark<<<(unsigned int)(((long long)n * TS_G + 255) / 256), 256, 0, s>>>(n, posS, workIds, cellOffset, g, h,
-                                                                              T);
+    k_ts_mark<<<warp_grid(n), TS_WARP_BLOCK, 0, s>>>(posS, workIds, cellOffset, g, h, T);
     const int nb = (n + TS_BLOCK - 1) / TS_BLOCK;
     k_ts_count<<<nb, TS_BLOCK, 0, s>>>(n, T);
     k_ts_scan_blocks<<<1, TS_BLOCK, 0, s>>>(nb, T);
@@ -542,8 +582,8 @@ void launch_ts_merge(int n, float4* posS, float4* velS, const float4* accS, cons
 void launch_ts_project(const float4* coarsePos, const int* workIds, int byId, const float4* rho4S,
                        const int* cellOffset, GridDev g, float hs, const TwoScaleDev& T, int capacity,
                        cudaStream_t s) {
-    k_ts_project<<<stride_grid((long long)capacity * TS_G, 128), 128, 0, s>>>(coarsePos, workIds, byId, rho4S,
-                                                                              cellOffset, g, hs, T);
+    k_ts_project<<<warp_grid(capacity), TS_WARP_BLOCK, 0, s>>>(coarsePos, workIds, byId, rho4S, cellOffset, g, hs,
+                                                                T);
 }
 
 void launch_ts_sub_sort(GridDev sg, const TwoScaleDev& T, SortBuffers subSb, int capacity, unsigned int* status,
@@ -555,11 +595,11 @@ void launch_ts_sub_sort(GridDev sg, const TwoScaleDev& T, SortBuffers subSb, int
 }
 
 void launch_ts_sub_density(GridDev sg, PhysDev sph, const TwoScaleDev& T, int capacity, cudaStream_t s) {
-    k_ts_subdensity<<<stride_grid((long long)capacity * TS_G, 128), 128, 0, s>>>(sg, sph, T);
+    k_ts_subdensity<<<warp_grid(capacity), TS_WARP_BLOCK, 0, s>>>(sg, sph, T);
 }
 
 void launch_ts_sub_force(GridDev sg, PhysDev sph, const TwoScaleDev& T, int capacity, cudaStream_t s) {
-    k_ts_subforce<<<stride_grid((long long)capacity * TS_G, 128), 128, 0, s>>>(sg, sph, T);
+    k_ts_subforce<<<warp_grid(capacity), TS_WARP_BLOCK, 0, s>>>(sg, sph, T);
 }
 
 void launch_ts_sub_integrate(PhysDev sph, const TwoScaleDev& T, int capacity, cudaStream_t s) {
