@@ -56,6 +56,28 @@ inline int stride_grid(long long work, int bs) {
 constexpr int TS_BATCH = 4;
 constexpr int TS_WARP_BLOCK = 128;
 
+// stencil() with its six bounds computed by lanes 0..5 (lane 2a + 1 the high
+// bound of axis a) and handed to the whole warp; the same values, at a sixth
+// of the warp's instructions.
+__device__ __forceinline__ Stencil warp_stencil(float4 x, float h, const GridDev& g, int lane) {
+    int c = 0;
+    if (lane < 6) {
+        const int ax = lane >> 1;
+        const float p = ax == 0 ? x.x : (ax == 1 ? x.y : x.z);
+        const float o = ax == 0 ? g.origin[0] : (ax == 1 ? g.origin[1] : g.origin[2]);
+        const int d = ax == 0 ? g.dim[0] : (ax == 1 ? g.dim[1] : g.dim[2]);
+        c = grid_coord(p, (lane & 1) ? h : -h, o, g.spacing, d);
+    }
+    Stencil s;
+    s.x0 = __shfl_sync(0xffffffffu, c, 0);
+    s.x1 = __shfl_sync(0xffffffffu, c, 1);
+    s.y0 = __shfl_sync(0xffffffffu, c, 2);
+    s.y1 = __shfl_sync(0xffffffffu, c, 3);
+    s.z0 = __shfl_sync(0xffffffffu, c, 4);
+    s.z1 = __shfl_sync(0xffffffffu, c, 5);
+    return s;
+}
+
 __device__ __forceinline__ void lane_row(const Stencil& st, const GridDev& g, const int* __restrict__ offs, int lane,
                                          int& t, int& e) {
     t = e = 0;
@@ -136,7 +158,7 @@ __global__ void __launch_bounds__(TS_WARP_BLOCK) k_ts_mark(const float4* __restr
     for (int idx = (blockIdx.x * TS_WARP_BLOCK + threadIdx.x) >> 5; idx < count; idx += warps) {
         const float4 xs = posS[T.markList[idx]];
         int t, e;
-        lane_row(stencil(xs, h, g), g, cellOffset, lane, t, e);
+        lane_row(warp_stencil(xs, h, g, lane), g, cellOffset, lane, t, e);
         walk_lane(t, e, [&](int c) { return __ldg(posS + c); }, [&](int c, float4 xc) {
             if (ref_r2(xs, xc) <= h2) {
                 const int v = workIds[c];
@@ -350,18 +372,25 @@ __global__ void __launch_bounds__(TS_WARP_BLOCK) k_ts_project(const float4* __re
         const int slot = T.subIds[idx];
         const float4 x = T.subPos[slot];
         int t, e;
-        lane_row(stencil(x, hs, g), g, cellOffset, lane, t, e);
+        lane_row(warp_stencil(x, hs, g, lane), g, cellOffset, lane, t, e);
         float d = 0.f, p = 0.f, cnt = 0.f;
-        walk_lane(
-            t, e, [&](int c) { return byId ? __ldg(coarsePos + __ldg(workIds + c)) : __ldg(coarsePos + c); },
-            [&](int c, float4 xc) {
-                if (ref_r2(x, xc) <= hs2) {
-                    const float4 rj = __ldg(rho4S + c);
-                    d += rj.x;
-                    p += rj.y;
+        for (; t < e; t += 3 * TS_BATCH) {
+            float4 xc[TS_BATCH], rc[TS_BATCH];
+#pragma unroll
+            for (int u = 0; u < TS_BATCH; u++)
+                if (t + 3 * u < e) {
+                    const int c = t + 3 * u;
+                    xc[u] = byId ? __ldg(coarsePos + __ldg(workIds + c)) : __ldg(coarsePos + c);
+                    rc[u] = __ldg(rho4S + c);
+                }
+#pragma unroll
+            for (int u = 0; u < TS_BATCH; u++)
+                if (t + 3 * u < e && ref_r2(x, xc[u]) <= hs2) {
+                    d += rc[u].x;
+                    p += rc[u].y;
                     cnt += 1.f;
                 }
-            });
+        }
         d = warp_total(d);
         p = warp_total(p);
         cnt = warp_total(cnt);
@@ -423,7 +452,7 @@ __global__ void __launch_bounds__(TS_WARP_BLOCK) k_ts_subdensity(GridDev g, Phys
         const int slot = T.subIds[idx];
         const float4 x = T.subPos[slot];
         int t, e;
-        lane_row(stencil(x, ph.h, g), g, T.subOffset, lane, t, e);
+        lane_row(warp_stencil(x, ph.h, g, lane), g, T.subOffset, lane, t, e);
         float part = 0.f;
         walk_lane(t, e, [&](int c) { return __ldg(T.subPosS + c); }, [&](int, float4 xc) {
             const float w = fmaxf(ph.h2 - dist2(x, xc), 0.f);
@@ -449,8 +478,11 @@ __global__ void __launch_bounds__(TS_WARP_BLOCK) k_ts_subdensity(GridDev g, Phys
 // (no wall terms at this level).
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(TS_WARP_BLOCK) k_ts_subforce(GridDev g, PhysDev ph, TwoScaleDev T) {
+    __shared__ int s_queue[TS_WARP_BLOCK / 32][32 * TS_BATCH];
     const int nReg = 8 * T.counts[0];
     const int lane = threadIdx.x & 31;
+    const unsigned int below = (1u << lane) - 1u;
+    int* queue = s_queue[threadIdx.x >> 5];
     const int warps = gridDim.x * (TS_WARP_BLOCK / 32);
     for (int idx = (blockIdx.x * TS_WARP_BLOCK + threadIdx.x) >> 5; idx < nReg; idx += warps) {
         const int slot = T.subIds[idx];
@@ -459,33 +491,57 @@ __global__ void __launch_bounds__(TS_WARP_BLOCK) k_ts_subforce(GridDev g, PhysDe
         const float rhoi = ri.x;
         const float qi = ri.y / (rhoi * rhoi);
         int t, e;
-        lane_row(stencil(xi, ph.h, g), g, T.subOffset, lane, t, e);
+        lane_row(warp_stencil(xi, ph.h, g, lane), g, T.subOffset, lane, t, e);
         float fp[3] = {0.f, 0.f, 0.f}, fv[3] = {0.f, 0.f, 0.f}, cg[3] = {0.f, 0.f, 0.f}, cl = 0.f;
-        walk_lane(t, e, [&](int c) { return __ldg(T.subPosS + c); }, [&](int c, float4 xj) {
-            const float r2 = dist2(xi, xj);
-            if (!(r2 <= ph.h2 && r2 > 0.f)) return;
-            const int j = __ldg(T.subSortedIds + c);
-            const float4 vj = T.subVel[j];
-            const float2 rj = T.subRho[j];
-            const float invj = 1.0f / rj.x;
-            const float dx = __fsub_rn(xi.x, xj.x), dy = __fsub_rn(xi.y, xj.y), dz = __fsub_rn(xi.z, xj.z);
-            const float rinv = rsqrtf(r2);
-            const float hr = ph.h - r2 * rinv;
-            const float sp = (qi + rj.y * invj * invj) * hr * hr * rinv;
-            const float sv = invj * hr;
-            fp[0] = fmaf(sp, dx, fp[0]);
-            fp[1] = fmaf(sp, dy, fp[1]);
-            fp[2] = fmaf(sp, dz, fp[2]);
-            fv[0] = fmaf(sv, vj.x - vi.x, fv[0]);
-            fv[1] = fmaf(sv, vj.y - vi.y, fv[1]);
-            fv[2] = fmaf(sv, vj.z - vi.z, fv[2]);
-            const float d2 = ph.h2 - r2;
-            const float sc = invj * d2 * d2;
-            cg[0] = fmaf(sc, dx, cg[0]);
-            cg[1] = fmaf(sc, dy, cg[1]);
-            cg[2] = fmaf(sc, dz, cg[2]);
-            cl = fmaf(invj * d2, 3.f * ph.h2 - 7.f * r2, cl);
-        });
+        // rounds of TS_BATCH candidates per lane: test, list the hits in the
+        // warp's queue, then all lanes take the listed pairs
+        while (__any_sync(0xffffffffu, t < e)) {
+            float4 xc[TS_BATCH];
+#pragma unroll
+            for (int u = 0; u < TS_BATCH; u++)
+                if (t + 3 * u < e) xc[u] = __ldg(T.subPosS + t + 3 * u);
+            int listed = 0;
+#pragma unroll
+            for (int u = 0; u < TS_BATCH; u++) {
+                bool hit = false;
+                if (t + 3 * u < e) {
+                    const float r2 = dist2(xi, xc[u]);
+                    hit = r2 <= ph.h2 && r2 > 0.f;
+                }
+                const unsigned int m = __ballot_sync(0xffffffffu, hit);
+                if (hit) queue[listed + __popc(m & below)] = t + 3 * u;
+                listed += __popc(m);
+            }
+            __syncwarp();
+            for (int q = lane; q < listed; q += 32) {
+                const int c = queue[q];
+                const float4 xj = __ldg(T.subPosS + c);
+                const int j = __ldg(T.subSortedIds + c);
+                const float r2 = dist2(xi, xj);
+                const float4 vj = T.subVel[j];
+                const float2 rj = T.subRho[j];
+                const float invj = 1.0f / rj.x;
+                const float dx = __fsub_rn(xi.x, xj.x), dy = __fsub_rn(xi.y, xj.y), dz = __fsub_rn(xi.z, xj.z);
+                const float rinv = rsqrtf(r2);
+                const float hr = ph.h - r2 * rinv;
+                const float sp = (qi + rj.y * invj * invj) * hr * hr * rinv;
+                const float sv = invj * hr;
+                fp[0] = fmaf(sp, dx, fp[0]);
+                fp[1] = fmaf(sp, dy, fp[1]);
+                fp[2] = fmaf(sp, dz, fp[2]);
+                fv[0] = fmaf(sv, vj.x - vi.x, fv[0]);
+                fv[1] = fmaf(sv, vj.y - vi.y, fv[1]);
+                fv[2] = fmaf(sv, vj.z - vi.z, fv[2]);
+                const float d2 = ph.h2 - r2;
+                const float sc = invj * d2 * d2;
+                cg[0] = fmaf(sc, dx, cg[0]);
+                cg[1] = fmaf(sc, dy, cg[1]);
+                cg[2] = fmaf(sc, dz, cg[2]);
+                cl = fmaf(invj * d2, 3.f * ph.h2 - 7.f * r2, cl);
+            }
+            __syncwarp();
+            t += 3 * TS_BATCH;
+        }
         for (int a = 0; a < 3; a++) {
             fp[a] = warp_total(fp[a]);
             fv[a] = warp_total(fv[a]);
