@@ -173,7 +173,7 @@ void free_all(sph_sim* s) {
                       s->ts.splitIds,  s->ts.boundaryIds, s->ts.defaultIds,  s->ts.subIds,
                       s->ts.subPos,    s->ts.subVel,      s->ts.subAcc,      s->ts.subRho,
                       s->ts.subCnt,    s->ts.subOffset,   s->ts.subKeySlot,  s->ts.subTmp,
-                      s->ts.subSortedHash, s->ts.subSortedIds, s->ts.subPosS, s->ts.markList,
+                      s->ts.subSortedHash, s->ts.subSortedIds, s->ts.subPosS, s->ts.subVelS, s->ts.markList,
                       s->subScanBlock};
     for (void* p : tsPtrs)
         if (p) cudaFree(p);
@@ -226,6 +226,7 @@ sph_status ensure_two_scale(sph_sim* s) {
     SPH_CUDA(dalloc(&T.subSortedHash, 8 * n));
     SPH_CUDA(dalloc(&T.subSortedIds, 8 * n));
     SPH_CUDA(dalloc(&T.subPosS, 8 * n));
+    SPH_CUDA(dalloc(&T.subVelS, 8 * n));
     SPH_CUDA(dalloc(&s->subScanBlock, tiles + 2));
     cudaStream_t q = s->stream;
     SPH_CUDA(cudaMemsetAsync(T.state, 0, n4, q));
@@ -315,7 +316,6 @@ void enqueue_step(sph_sim* s, int mode, bool timing) {
             launch_ts_project(s->pos, s->sb.workIds, 1, s->rho4S, s->sb.cellOffset, make_grid(s->P, false),
                               s->P.compactSupportSub, s->ts, cap, st);
         launch_ts_sub_force(sg, sph, s->ts, cap, st);
-        launch_ts_sub_integrate(sph, s->ts, cap, st);
         return;
     }
     const bool twoScale = mode == SPH_STEP_TWO_SCALE;
@@ -337,9 +337,8 @@ void enqueue_step(sph_sim* s, int mode, bool timing) {
         // (:2157-2160) from the pre-integration sorted state, which the force
         // stage leaves as it was (it writes the new state in particle order)
         launch_ts_states(n, s->posS, s->sb.workIds, s->sb.cellOffset, g, s->P.compactSupport, s->ts, st);
-        if (s->O.childMode == 1)
-            launch_ts_merge(n, s->posS, s->velS, s->accS, s->sb.workIds, ph, collide, s->pos, s->vel, s->ts, st);
-        launch_ts_children(n, s->posS, s->velS, s->rho4S, s->sb.workIds, s->P.particleMass, s->ts, st);
+        launch_ts_children(n, s->posS, s->velS, s->accS, s->rho4S, s->sb.workIds, s->P.particleMass, ph, collide,
+                           s->pos, s->vel, s->ts, st);
         launch_ts_project(s->posS, s->sb.workIds, 0, s->rho4S, s->sb.cellOffset, g, s->P.compactSupportSub,
                           s->ts, 8 * n, st);
         // the fine level (:2162-2171)
@@ -349,7 +348,6 @@ void enqueue_step(sph_sim* s, int mode, bool timing) {
         launch_ts_sub_sort(sg, s->ts, s->subSb, cap, s->status, st);
         launch_ts_sub_density(sg, sph, s->ts, cap, st);
         launch_ts_sub_force(sg, sph, s->ts, cap, st);
-        launch_ts_sub_integrate(sph, s->ts, cap, st);
     }
 }
 

@@ -113,6 +113,7 @@ struct TwoScaleDev {
     int* subSortedHash;         // [8n]
     int* subSortedIds;          // [8n] slots in (fine cell, list position) order
     float4* subPosS;            // [8n] child positions in that order
+    float4* subVelS;            // [8n] child velocities in that order
     float splitMin[3], splitMax[3];
     int childMode;              // sph_options.childMode
 };
@@ -201,10 +202,9 @@ void launch_cell_tables(int numCells, const int* cellOffset, int* start, int* en
 // Two-scale pass (sph_twoscale.cu).
 void launch_ts_states(int n, const float4* posS, const int* workIds, const int* cellOffset, GridDev g, float h,
                       const TwoScaleDev& T, cudaStream_t s);
-void launch_ts_children(int n, const float4* posS, const float4* velS, const float4* rho4S, const int* workIds,
-                        float mass, const TwoScaleDev& T, cudaStream_t s);
-void launch_ts_merge(int n, float4* posS, float4* velS, const float4* accS, const int* workIds, PhysDev ph,
-                     int collide, float4* pos, float4* vel, const TwoScaleDev& T, cudaStream_t s);
+void launch_ts_children(int n, float4* posS, float4* velS, const float4* accS, const float4* rho4S,
+                        const int* workIds, float mass, PhysDev ph, int collide, float4* pos, float4* vel,
+                        const TwoScaleDev& T, cudaStream_t s);
 void launch_ts_project(const float4* coarsePos, const int* workIds, int byId, const float4* rho4S,
                        const int* cellOffset, GridDev g, float hs, const TwoScaleDev& T, int capacity,
                        cudaStream_t s);
@@ -212,7 +212,6 @@ void launch_ts_sub_sort(GridDev sg, const TwoScaleDev& T, SortBuffers subSb, int
                         cudaStream_t s);
 void launch_ts_sub_density(GridDev sg, PhysDev sph, const TwoScaleDev& T, int capacity, cudaStream_t s);
 void launch_ts_sub_force(GridDev sg, PhysDev sph, const TwoScaleDev& T, int capacity, cudaStream_t s);
-void launch_ts_sub_integrate(PhysDev sph, const TwoScaleDev& T, int capacity, cudaStream_t s);
 void launch_ts_pack_sd(const TwoScaleDev& T, int slots, float* dst, cudaStream_t s);
 
 // FP64 diagnostics (sph_diag.cu): out[DIAG_TERMS] in this order; the maximum

@@ -286,16 +286,50 @@ __global__ void __launch_bounds__(TS_BLOCK) k_ts_lists(int n, TwoScaleDev T) {
 // float once; pos + dir*radius is one fused multiply-add, as the reference's
 // kernel compiles it.
 // ---------------------------------------------------------------------------
-__global__ void k_ts_init(int n, const float4* __restrict__ posS, const float4* __restrict__ velS,
-                          const float4* __restrict__ rho4S, const int* __restrict__ workIds, float mass,
-                          TwoScaleDev T) {
+//
+// Merge-back (childMode 1, no reference counterpart) comes first, in the same
+// thread: a parent whose class went from split to boundary or default takes
+// the mean of its eight children (summed in slot order, times 1/8) as its
+// pre-integration position and velocity -- written to the sorted copies,
+// which seeding and projection read -- and is integrated and collided again
+// from there with the acceleration the force stage computed at its own
+// position.
+// ---------------------------------------------------------------------------
+__global__ void k_ts_children(int n, float4* __restrict__ posS, float4* __restrict__ velS,
+                              const float4* __restrict__ accS, const float4* __restrict__ rho4S,
+                              const int* __restrict__ workIds, float mass, PhysDev ph, int collideFlag,
+                              float4* __restrict__ pos, float4* __restrict__ vel, TwoScaleDev T) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const int id = workIds[k];
     const unsigned int code = T.state[id] & 15u;
+    const int was = state_class(code >> 2), now = state_class(code & 3u);
+    if (T.childMode == 1 && was == 1 && now != 1) {
+        float sx = 0.f, sy = 0.f, sz = 0.f, ux = 0.f, uy = 0.f, uz = 0.f;
+        for (int c = 0; c < 8; c++) {
+            const float4 a = T.subPos[8 * (size_t)id + c], b = T.subVel[8 * (size_t)id + c];
+            sx = __fadd_rn(sx, a.x);
+            sy = __fadd_rn(sy, a.y);
+            sz = __fadd_rn(sz, a.z);
+            ux = __fadd_rn(ux, b.x);
+            uy = __fadd_rn(uy, b.y);
+            uz = __fadd_rn(uz, b.z);
+        }
+        const float4 x0 = posS[k], v0 = velS[k];
+        const float3 xm = make_float3(sx * 0.125f, sy * 0.125f, sz * 0.125f);
+        const float3 vm = make_float3(ux * 0.125f, uy * 0.125f, uz * 0.125f);
+        posS[k] = make_float4(xm.x, xm.y, xm.z, x0.w);
+        velS[k] = make_float4(vm.x, vm.y, vm.z, v0.w);
+        const float4 a = accS[k];
+        float3 v = make_float3(vm.x + ph.dt * a.x, vm.y + ph.dt * a.y, vm.z + ph.dt * a.z);
+        float3 x = make_float3(xm.x + ph.dt * v.x, xm.y + ph.dt * v.y, xm.z + ph.dt * v.z);
+        if (collideFlag) collide(ph, x, v);
+        pos[id] = make_float4(x.x, x.y, x.z, x0.w);
+        vel[id] = make_float4(v.x, v.y, v.z, 0.f);
+    }
     if ((code & 3u) == 0) return;
     // childMode 1: seed only on a class change (:1052-1055)
-    if (T.childMode == 1 && state_class(code >> 2) == state_class(code & 3u)) return;
+    if (T.childMode == 1 && was == now) return;
     const double rad = (double)(3.0f * mass) / (4.0 * 3.14159265358979323846 * (double)rho4S[k].x);
     const float radicand = (float)rad;
     const float radius = (float)pow((double)radicand, (double)(1.0f / 3.0f));
@@ -309,46 +343,6 @@ __global__ void k_ts_init(int n, const float4* __restrict__ posS, const float4* 
                                      __fmaf_rn(sz, radius, x.z), 0.f);
         T.subVel[slot] = make_float4(v.x, v.y, v.z, 0.f);
     }
-}
-
-// ---------------------------------------------------------------------------
-// Merge-back (childMode 1, no reference counterpart).  Runs after the coarse
-// force stage, before the children are re-seeded: a parent whose class went
-// from split to boundary or default takes the mean of its eight children
-// (summed in slot order, times 1/8) as its pre-integration position and
-// velocity -- written to the sorted copies, which seeding and projection read
-// next -- and is integrated and collided again from there with the
-// acceleration the force stage computed at its own position.
-// ---------------------------------------------------------------------------
-__global__ void k_ts_merge(int n, float4* __restrict__ posS, float4* __restrict__ velS,
-                           const float4* __restrict__ accS, const int* __restrict__ workIds, PhysDev ph,
-                           int collideFlag, float4* __restrict__ pos, float4* __restrict__ vel, TwoScaleDev T) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    const int id = workIds[k];
-    const unsigned int code = T.state[id] & 15u;
-    if (state_class(code >> 2) != 1 || state_class(code & 3u) == 1) return;
-    float sx = 0.f, sy = 0.f, sz = 0.f, ux = 0.f, uy = 0.f, uz = 0.f;
-    for (int c = 0; c < 8; c++) {
-        const float4 a = T.subPos[8 * (size_t)id + c], b = T.subVel[8 * (size_t)id + c];
-        sx = __fadd_rn(sx, a.x);
-        sy = __fadd_rn(sy, a.y);
-        sz = __fadd_rn(sz, a.z);
-        ux = __fadd_rn(ux, b.x);
-        uy = __fadd_rn(uy, b.y);
-        uz = __fadd_rn(uz, b.z);
-    }
-    const float4 x0 = posS[k], v0 = velS[k];
-    const float3 xm = make_float3(sx * 0.125f, sy * 0.125f, sz * 0.125f);
-    const float3 vm = make_float3(ux * 0.125f, uy * 0.125f, uz * 0.125f);
-    posS[k] = make_float4(xm.x, xm.y, xm.z, x0.w);
-    velS[k] = make_float4(vm.x, vm.y, vm.z, v0.w);
-    const float4 a = accS[k];
-    float3 v = make_float3(vm.x + ph.dt * a.x, vm.y + ph.dt * a.y, vm.z + ph.dt * a.z);
-    float3 x = make_float3(xm.x + ph.dt * v.x, xm.y + ph.dt * v.y, xm.z + ph.dt * v.z);
-    if (collideFlag) collide(ph, x, v);
-    pos[id] = make_float4(x.x, x.y, x.z, x0.w);
-    vel[id] = make_float4(v.x, v.y, v.z, 0.f);
 }
 
 // ---------------------------------------------------------------------------
@@ -438,6 +432,7 @@ __global__ void k_ts_subrank(TwoScaleDev T) {
         const int slot = T.subIds[my];
         T.subSortedIds[s + r] = slot;
         T.subPosS[s + r] = T.subPos[slot];
+        T.subVelS[s + r] = T.subVel[slot];
     }
 }
 
@@ -475,11 +470,34 @@ __global__ void __launch_bounds__(TS_WARP_BLOCK) k_ts_subdensity(GridDev g, Phys
 // ---------------------------------------------------------------------------
 // compute_sub_particle_acceleration (:477-568): pressure, viscosity and the
 // colour field of the regular children; surface tension is always tested
-// (no wall terms at this level).
+// (no wall terms at this level).  Then integrate_sub_particles_euler
+// (:667-696) + collision_handling_sub_particles (:836-930) for every child
+// of the list, in the same launch: neighbours are read from the sorted
+// copies only, so a child can be moved as soon as its own sums are done.
+// Children of boundary particles use whatever acceleration their slot holds
+// (the reference computes none for them).
 // ---------------------------------------------------------------------------
+__device__ __forceinline__ void integrate_child(const PhysDev& ph, const TwoScaleDev& T, int slot, float4 a,
+                                                float4 x0, float4 v0) {
+    float3 v = make_float3(v0.x + ph.dt * a.x, v0.y + ph.dt * a.y, v0.z + ph.dt * a.z);
+    float3 x = make_float3(x0.x + ph.dt * v.x, x0.y + ph.dt * v.y, x0.z + ph.dt * v.z);
+    collide(ph, x, v);
+    T.subPos[slot] = make_float4(x.x, x.y, x.z, 0.f);
+    T.subVel[slot] = make_float4(v.x, v.y, v.z, 0.f);
+}
+
+// Hit queue of one warp: a round adds at most 32 * TS_BATCH pairs to fewer
+// than 32 left over.
+constexpr int TS_QUEUE = 32 * TS_BATCH + 32;
+
 __global__ void __launch_bounds__(TS_WARP_BLOCK) k_ts_subforce(GridDev g, PhysDev ph, TwoScaleDev T) {
-    __shared__ int s_queue[TS_WARP_BLOCK / 32][32 * TS_BATCH];
+    __shared__ int s_queue[TS_WARP_BLOCK / 32][TS_QUEUE];
     const int nReg = 8 * T.counts[0];
+    const int nSub = T.counts[3];
+    for (int idx = nReg + blockIdx.x * TS_WARP_BLOCK + threadIdx.x; idx < nSub; idx += gridDim.x * TS_WARP_BLOCK) {
+        const int slot = T.subIds[idx];
+        integrate_child(ph, T, slot, T.subAcc[slot], T.subPos[slot], T.subVel[slot]);
+    }
     const int lane = threadIdx.x & 31;
     const unsigned int below = (1u << lane) - 1u;
     int* queue = s_queue[threadIdx.x >> 5];
@@ -493,14 +511,15 @@ __global__ void __launch_bounds__(TS_WARP_BLOCK) k_ts_subforce(GridDev g, PhysDe
         int t, e;
         lane_row(warp_stencil(xi, ph.h, g, lane), g, T.subOffset, lane, t, e);
         float fp[3] = {0.f, 0.f, 0.f}, fv[3] = {0.f, 0.f, 0.f}, cg[3] = {0.f, 0.f, 0.f}, cl = 0.f;
-        // rounds of TS_BATCH candidates per lane: test, list the hits in the
-        // warp's queue, then all lanes take the listed pairs
-        while (__any_sync(0xffffffffu, t < e)) {
+        // rounds of TS_BATCH candidates per lane: test and list the hits in
+        // the warp's queue; all lanes take the listed pairs 32 at a time
+        int listed = 0;
+        bool more = __any_sync(0xffffffffu, t < e);
+        while (more) {
             float4 xc[TS_BATCH];
 #pragma unroll
             for (int u = 0; u < TS_BATCH; u++)
                 if (t + 3 * u < e) xc[u] = __ldg(T.subPosS + t + 3 * u);
-            int listed = 0;
 #pragma unroll
             for (int u = 0; u < TS_BATCH; u++) {
                 bool hit = false;
@@ -512,14 +531,15 @@ __global__ void __launch_bounds__(TS_WARP_BLOCK) k_ts_subforce(GridDev g, PhysDe
                 if (hit) queue[listed + __popc(m & below)] = t + 3 * u;
                 listed += __popc(m);
             }
+            t += 3 * TS_BATCH;
+            more = __any_sync(0xffffffffu, t < e);
+            const int take = more ? (listed & ~31) : listed;
             __syncwarp();
-            for (int q = lane; q < listed; q += 32) {
+            for (int q = lane; q < take; q += 32) {
                 const int c = queue[q];
-                const float4 xj = __ldg(T.subPosS + c);
-                const int j = __ldg(T.subSortedIds + c);
+                const float4 xj = __ldg(T.subPosS + c), vj = __ldg(T.subVelS + c);
+                const float2 rj = T.subRho[__ldg(T.subSortedIds + c)];
                 const float r2 = dist2(xi, xj);
-                const float4 vj = T.subVel[j];
-                const float2 rj = T.subRho[j];
                 const float invj = 1.0f / rj.x;
                 const float dx = __fsub_rn(xi.x, xj.x), dy = __fsub_rn(xi.y, xj.y), dz = __fsub_rn(xi.z, xj.z);
                 const float rinv = rsqrtf(r2);
@@ -539,8 +559,13 @@ __global__ void __launch_bounds__(TS_WARP_BLOCK) k_ts_subforce(GridDev g, PhysDe
                 cg[2] = fmaf(sc, dz, cg[2]);
                 cl = fmaf(invj * d2, 3.f * ph.h2 - 7.f * r2, cl);
             }
+            // fewer than 32 left: to the front of the queue
+            const int left = listed - take;
+            const int keep = lane < left ? queue[take + lane] : 0;
             __syncwarp();
-            t += 3 * TS_BATCH;
+            if (lane < left) queue[lane] = keep;
+            listed = left;
+            __syncwarp();
         }
         for (int a = 0; a < 3; a++) {
             fp[a] = warp_total(fp[a]);
@@ -564,25 +589,9 @@ __global__ void __launch_bounds__(TS_WARP_BLOCK) k_ts_subforce(GridDev g, PhysDe
         acc[0] -= ph.gravityAxis == 0 ? ph.gravity : 0.f;
         acc[1] -= ph.gravityAxis == 1 ? ph.gravity : 0.f;
         acc[2] -= ph.gravityAxis == 2 ? ph.gravity : 0.f;
-        T.subAcc[slot] = make_float4(acc[0], acc[1], acc[2], 0.f);
-    }
-}
-
-// integrate_sub_particles_euler (:667-696) + collision_handling_sub_particles
-// (:836-930) for every child of the list.  Children of boundary particles use
-// whatever acceleration their slot holds (the reference computes none for
-// them).
-__global__ void k_ts_subintegrate(PhysDev ph, TwoScaleDev T) {
-    const int nSub = T.counts[3];
-    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < nSub; idx += gridDim.x * blockDim.x) {
-        const int slot = T.subIds[idx];
-        const float4 a = T.subAcc[slot];
-        const float4 v0 = T.subVel[slot], x0 = T.subPos[slot];
-        float3 v = make_float3(v0.x + ph.dt * a.x, v0.y + ph.dt * a.y, v0.z + ph.dt * a.z);
-        float3 x = make_float3(x0.x + ph.dt * v.x, x0.y + ph.dt * v.y, x0.z + ph.dt * v.z);
-        collide(ph, x, v);
-        T.subPos[slot] = make_float4(x.x, x.y, x.z, 0.f);
-        T.subVel[slot] = make_float4(v.x, v.y, v.z, 0.f);
+        const float4 a4 = make_float4(acc[0], acc[1], acc[2], 0.f);
+        T.subAcc[slot] = a4;
+        integrate_child(ph, T, slot, a4, xi, vi);
     }
 }
 
@@ -624,15 +633,12 @@ void launch_ts_states(int n, const float4* posS, const int* workIds, const int* 
     k_ts_lists<<<nb, TS_BLOCK, 0, s>>>(n, T);
 }
 
-void launch_ts_children(int n, const float4* posS, const float4* velS, const float4* rho4S, const int* workIds,
-                        float mass, const TwoScaleDev& T, cudaStream_t s) {
+void launch_ts_children(int n, float4* posS, float4* velS, const float4* accS, const float4* rho4S,
+                        const int* workIds, float mass, PhysDev ph, int collide, float4* pos, float4* vel,
+                        const TwoScaleDev& T, cudaStream_t s) {
     if (n <= 0) return;
-    k_ts_init<<<(n + 127) / 128, 128, 0, s>>>(n, posS, velS, rho4S, workIds, mass, T);
-}
-
-void launch_ts_merge(int n, float4* posS, float4* velS, const float4* accS, const int* workIds, PhysDev ph,
-                     int collide, float4* pos, float4* vel, const TwoScaleDev& T, cudaStream_t s) {
-    k_ts_merge<<<(n + 255) / 256, 256, 0, s>>>(n, posS, velS, accS, workIds, ph, collide, pos, vel, T);
+    k_ts_children<<<(n + 127) / 128, 128, 0, s>>>(n, posS, velS, accS, rho4S, workIds, mass, ph, collide, pos, vel,
+                                                  T);
 }
 
 void launch_ts_project(const float4* coarsePos, const int* workIds, int byId, const float4* rho4S,
@@ -658,8 +664,5 @@ void launch_ts_sub_force(GridDev sg, PhysDev sph, const TwoScaleDev& T, int capa
     k_ts_subforce<<<warp_grid(capacity), TS_WARP_BLOCK, 0, s>>>(sg, sph, T);
 }
 
-void launch_ts_sub_integrate(PhysDev sph, const TwoScaleDev& T, int capacity, cudaStream_t s) {
-    k_ts_subintegrate<<<stride_grid(capacity, 256), 256, 0, s>>>(sph, T);
-}
 
 }  // namespace sph
