@@ -43,16 +43,12 @@ inline int stride_grid(long long work, int bs) {
     return (int)(g < 1 ? 1 : (g > 4096 ? 4096 : g));
 }
 
-// The neighbour loops of the two-scale pass (marking, projection, the fine
-// level's density and forces) run over few particles (a few thousand split
-// parents, tens of thousands of children), so each particle gets a warp.
-// Lane l < 27 takes row l / 3 of the particle's 3 x 3 stencil rows and every
+// The marking runs over a few thousand split parents, so each gets a warp:
+// lane l < 27 takes row l / 3 of the particle's 3 x 3 stencil rows and every
 // third candidate of it, from the row's start + l % 3, and loads TS_BATCH
 // candidates before it tests any; lanes 27..31 take none.  So a particle
 // waits for one round of row offsets and a few rounds of candidate loads,
-// not for its rows one after the other.  Partial sums are combined by a
-// fixed butterfly (every lane ends with the same bits), so results do not
-// depend on scheduling.
+// not for its rows one after the other.
 constexpr int TS_BATCH = 4;
 constexpr int TS_WARP_BLOCK = 128;
 
@@ -104,17 +100,84 @@ __device__ __forceinline__ void walk_lane(int t, int e, Load load, Visit visit) 
     }
 }
 
-__device__ __forceinline__ float warp_total(float v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
-
 inline int warp_grid(long long items) {
     const long long per = TS_WARP_BLOCK / 32;
     long long b = (items + per - 1) / per;
     const long long cap = 16LL * device_sms();
     return (int)(b < 1 ? 1 : (b > cap ? cap : b));
+}
+
+// The projection and the fine level's loops run over tens of thousands of
+// children: there a particle gets a group of TS_G = 8 lanes (4 per warp), so
+// that its setup, stencil and epilogue are shared four ways.  Lane g of a
+// group walks stencil row g from its start, then every eighth candidate of
+// row 8 from its start + g, TS_BATCH loads at a time.  Group sums use a
+// fixed xor tree (every lane of the group ends with the same bits).
+constexpr int TS_G = 8;
+
+inline int group_grid(long long items) { return warp_grid((items + 32 / TS_G - 1) / (32 / TS_G)); }
+
+__device__ __forceinline__ Stencil group_stencil(float4 x, float h, const GridDev& g, int gl) {
+    int c = 0;
+    if (gl < 6) {
+        const int ax = gl >> 1;
+        const float p = ax == 0 ? x.x : (ax == 1 ? x.y : x.z);
+        const float o = ax == 0 ? g.origin[0] : (ax == 1 ? g.origin[1] : g.origin[2]);
+        const int d = ax == 0 ? g.dim[0] : (ax == 1 ? g.dim[1] : g.dim[2]);
+        c = grid_coord(p, (gl & 1) ? h : -h, o, g.spacing, d);
+    }
+    Stencil s;
+    s.x0 = __shfl_sync(0xffffffffu, c, 0, TS_G);
+    s.x1 = __shfl_sync(0xffffffffu, c, 1, TS_G);
+    s.y0 = __shfl_sync(0xffffffffu, c, 2, TS_G);
+    s.y1 = __shfl_sync(0xffffffffu, c, 3, TS_G);
+    s.z0 = __shfl_sync(0xffffffffu, c, 4, TS_G);
+    s.z1 = __shfl_sync(0xffffffffu, c, 5, TS_G);
+    return s;
+}
+
+struct RowWalk {
+    int t, e;    // own row
+    int t8, e8;  // this lane's share of row 8
+};
+
+__device__ __forceinline__ void row_bounds(const Stencil& st, const GridDev& g, const int* __restrict__ offs, int r,
+                                           int& s, int& e) {
+    s = e = 0;
+    const int z = st.z0 + r / 3, y = st.y0 + r % 3;
+    if (z > st.z1 || y > st.y1) return;
+    const int row = g.dim[0] * (g.dim[1] * z + y);
+    s = __ldg(offs + row + st.x0);
+    e = __ldg(offs + row + st.x1 + 1);
+}
+
+__device__ __forceinline__ RowWalk group_rows(const Stencil& st, const GridDev& g, const int* __restrict__ offs,
+                                              int gl) {
+    RowWalk w;
+    row_bounds(st, g, offs, gl, w.t, w.e);
+    row_bounds(st, g, offs, 8, w.t8, w.e8);
+    w.t8 += gl;
+    return w;
+}
+
+__device__ __forceinline__ bool walking(const RowWalk& w) { return w.t < w.e || w.t8 < w.e8; }
+
+// The lane's next candidate (own row first), -1 when it has none left.
+__device__ __forceinline__ int next_candidate(RowWalk& w) {
+    if (w.t < w.e) return w.t++;
+    if (w.t8 < w.e8) {
+        const int c = w.t8;
+        w.t8 += TS_G;
+        return c;
+    }
+    return -1;
+}
+
+__device__ __forceinline__ float group_total(float v) {
+    v += __shfl_xor_sync(0xffffffffu, v, 4);
+    v += __shfl_xor_sync(0xffffffffu, v, 2);
+    v += __shfl_xor_sync(0xffffffffu, v, 1);
+    return v;
 }
 
 // ---------------------------------------------------------------------------
@@ -357,38 +420,45 @@ __global__ void __launch_bounds__(TS_WARP_BLOCK) k_ts_project(const float4* __re
                                                               const float4* __restrict__ rho4S,
                                                               const int* __restrict__ cellOffset, GridDev g,
                                                               float hs, TwoScaleDev T) {
-    const int nSplit = T.counts[0];
+    const int first = 8 * T.counts[0];
     const int nSub = T.counts[3];
     const float hs2 = __fmul_rn(hs, hs);
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, gl = lane & (TS_G - 1), grp = lane / TS_G;
     const int warps = gridDim.x * (TS_WARP_BLOCK / 32);
-    for (int idx = 8 * nSplit + ((blockIdx.x * TS_WARP_BLOCK + threadIdx.x) >> 5); idx < nSub; idx += warps) {
-        const int slot = T.subIds[idx];
-        const float4 x = T.subPos[slot];
-        int t, e;
-        lane_row(warp_stencil(x, hs, g, lane), g, cellOffset, lane, t, e);
+    constexpr int per = 32 / TS_G;
+    for (int base = first + per * ((blockIdx.x * TS_WARP_BLOCK + threadIdx.x) >> 5); base < nSub;
+         base += per * warps) {
+        const int idx = base + grp;
+        const bool valid = idx < nSub;
+        const int slot = valid ? T.subIds[idx] : 0;
+        const float4 x = valid ? T.subPos[slot] : make_float4(g.origin[0], g.origin[1], g.origin[2], 0.f);
+        const Stencil st = group_stencil(x, hs, g, gl);
+        RowWalk w = {0, 0, 0, 0};
+        if (valid) w = group_rows(st, g, cellOffset, gl);
         float d = 0.f, p = 0.f, cnt = 0.f;
-        for (; t < e; t += 3 * TS_BATCH) {
+        while (__any_sync(0xffffffffu, walking(w))) {
+            int c[TS_BATCH];
             float4 xc[TS_BATCH], rc[TS_BATCH];
 #pragma unroll
-            for (int u = 0; u < TS_BATCH; u++)
-                if (t + 3 * u < e) {
-                    const int c = t + 3 * u;
-                    xc[u] = byId ? __ldg(coarsePos + __ldg(workIds + c)) : __ldg(coarsePos + c);
-                    rc[u] = __ldg(rho4S + c);
+            for (int u = 0; u < TS_BATCH; u++) {
+                c[u] = next_candidate(w);
+                if (c[u] >= 0) {
+                    xc[u] = byId ? __ldg(coarsePos + __ldg(workIds + c[u])) : __ldg(coarsePos + c[u]);
+                    rc[u] = __ldg(rho4S + c[u]);
                 }
+            }
 #pragma unroll
             for (int u = 0; u < TS_BATCH; u++)
-                if (t + 3 * u < e && ref_r2(x, xc[u]) <= hs2) {
+                if (c[u] >= 0 && ref_r2(x, xc[u]) <= hs2) {
                     d += rc[u].x;
                     p += rc[u].y;
                     cnt += 1.f;
                 }
         }
-        d = warp_total(d);
-        p = warp_total(p);
-        cnt = warp_total(cnt);
-        if (lane == 0) T.subRho[slot] = cnt > 0.f ? make_float2(d / cnt, p / cnt) : make_float2(0.f, 0.f);
+        d = group_total(d);
+        p = group_total(p);
+        cnt = group_total(cnt);
+        if (valid && gl == 0) T.subRho[slot] = cnt > 0.f ? make_float2(d / cnt, p / cnt) : make_float2(0.f, 0.f);
     }
 }
 
@@ -441,29 +511,46 @@ __global__ void k_ts_subrank(TwoScaleDev T) {
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(TS_WARP_BLOCK) k_ts_subdensity(GridDev g, PhysDev ph, TwoScaleDev T) {
     const int nReg = 8 * T.counts[0];
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, gl = lane & (TS_G - 1), grp = lane / TS_G;
     const int warps = gridDim.x * (TS_WARP_BLOCK / 32);
-    for (int idx = (blockIdx.x * TS_WARP_BLOCK + threadIdx.x) >> 5; idx < nReg; idx += warps) {
-        const int slot = T.subIds[idx];
-        const float4 x = T.subPos[slot];
-        int t, e;
-        lane_row(warp_stencil(x, ph.h, g, lane), g, T.subOffset, lane, t, e);
-        float part = 0.f;
-        walk_lane(t, e, [&](int c) { return __ldg(T.subPosS + c); }, [&](int, float4 xc) {
-            const float w = fmaxf(ph.h2 - dist2(x, xc), 0.f);
-            part = fmaf(w * w, w, part);
-        });
-        // row sums (lanes 3r, 3r+1, 3r+2), then compensated over the rows in order
-        const float p1 = __shfl_down_sync(0xffffffffu, part, 1), p2 = __shfl_down_sync(0xffffffffu, part, 2);
-        const float rowSum = (part + p1) + p2;
+    constexpr int per = 32 / TS_G;
+    for (int base = per * ((blockIdx.x * TS_WARP_BLOCK + threadIdx.x) >> 5); base < nReg; base += per * warps) {
+        const int idx = base + grp;
+        const bool valid = idx < nReg;
+        const int slot = valid ? T.subIds[idx] : 0;
+        const float4 x = valid ? T.subPos[slot] : make_float4(g.origin[0], g.origin[1], g.origin[2], 0.f);
+        const Stencil st = group_stencil(x, ph.h, g, gl);
+        RowWalk w = {0, 0, 0, 0};
+        if (valid) w = group_rows(st, g, T.subOffset, gl);
+        float own = 0.f, share = 0.f;  // sums over row gl and over this lane's share of row 8
+        while (__any_sync(0xffffffffu, walking(w))) {
+            int c[TS_BATCH];
+            bool mine[TS_BATCH];
+            float4 xc[TS_BATCH];
+#pragma unroll
+            for (int u = 0; u < TS_BATCH; u++) {
+                mine[u] = w.t < w.e;
+                c[u] = next_candidate(w);
+                if (c[u] >= 0) xc[u] = __ldg(T.subPosS + c[u]);
+            }
+#pragma unroll
+            for (int u = 0; u < TS_BATCH; u++)
+                if (c[u] >= 0) {
+                    const float q = fmaxf(ph.h2 - dist2(x, xc[u]), 0.f);
+                    if (mine[u]) own = fmaf(q * q, q, own);
+                    else share = fmaf(q * q, q, share);
+                }
+        }
+        // row sums, compensated over the rows in order
+        const float row8 = group_total(share);
         float sum = 0.f, comp = 0.f;
 #pragma unroll
         for (int r = 0; r < 9; r++) {
-            const float rs = __shfl_sync(0xffffffffu, rowSum, 3 * r);
+            const float rs = r < 8 ? __shfl_sync(0xffffffffu, own, r, TS_G) : row8;
             if (rs > 0.f) kahan_add(sum, comp, rs);
         }
         const float rho = __fsub_rn(sum, comp) * ph.poly6m;
-        if (lane == 0) T.subRho[slot] = make_float2(rho, ph.stiffness * (rho - ph.restDensity));
+        if (valid && gl == 0) T.subRho[slot] = make_float2(rho, ph.stiffness * (rho - ph.restDensity));
     }
 }
 
@@ -486,94 +573,102 @@ __device__ __forceinline__ void integrate_child(const PhysDev& ph, const TwoScal
     T.subVel[slot] = make_float4(v.x, v.y, v.z, 0.f);
 }
 
-// Hit queue of one warp: a round adds at most 32 * TS_BATCH pairs to fewer
-// than 32 left over.
-constexpr int TS_QUEUE = 32 * TS_BATCH + 32;
+// Hit queue of one group: a round adds at most TS_G * TS_BATCH pairs to
+// fewer than TS_G left over.
+constexpr int TS_QUEUE = TS_G * TS_BATCH + TS_G;
 
 __global__ void __launch_bounds__(TS_WARP_BLOCK) k_ts_subforce(GridDev g, PhysDev ph, TwoScaleDev T) {
-    __shared__ int s_queue[TS_WARP_BLOCK / 32][TS_QUEUE];
+    __shared__ int s_queue[TS_WARP_BLOCK / TS_G][TS_QUEUE];
     const int nReg = 8 * T.counts[0];
     const int nSub = T.counts[3];
     for (int idx = nReg + blockIdx.x * TS_WARP_BLOCK + threadIdx.x; idx < nSub; idx += gridDim.x * TS_WARP_BLOCK) {
         const int slot = T.subIds[idx];
         integrate_child(ph, T, slot, T.subAcc[slot], T.subPos[slot], T.subVel[slot]);
     }
-    const int lane = threadIdx.x & 31;
-    const unsigned int below = (1u << lane) - 1u;
-    int* queue = s_queue[threadIdx.x >> 5];
+    const int lane = threadIdx.x & 31, gl = lane & (TS_G - 1), grp = lane / TS_G;
+    const unsigned int below = (1u << gl) - 1u;
+    int* queue = s_queue[threadIdx.x / TS_G];
     const int warps = gridDim.x * (TS_WARP_BLOCK / 32);
-    for (int idx = (blockIdx.x * TS_WARP_BLOCK + threadIdx.x) >> 5; idx < nReg; idx += warps) {
-        const int slot = T.subIds[idx];
-        const float4 xi = T.subPos[slot], vi = T.subVel[slot];
-        const float2 ri = T.subRho[slot];
+    constexpr int per = 32 / TS_G;
+    for (int base = per * ((blockIdx.x * TS_WARP_BLOCK + threadIdx.x) >> 5); base < nReg; base += per * warps) {
+        const int idx = base + grp;
+        const bool valid = idx < nReg;
+        const int slot = valid ? T.subIds[idx] : 0;
+        const float4 xi = valid ? T.subPos[slot] : make_float4(g.origin[0], g.origin[1], g.origin[2], 0.f);
+        const float4 vi = valid ? T.subVel[slot] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float2 ri = valid ? T.subRho[slot] : make_float2(1.f, 0.f);
         const float rhoi = ri.x;
         const float qi = ri.y / (rhoi * rhoi);
-        int t, e;
-        lane_row(warp_stencil(xi, ph.h, g, lane), g, T.subOffset, lane, t, e);
+        const Stencil st = group_stencil(xi, ph.h, g, gl);
+        RowWalk w = {0, 0, 0, 0};
+        if (valid) w = group_rows(st, g, T.subOffset, gl);
         float fp[3] = {0.f, 0.f, 0.f}, fv[3] = {0.f, 0.f, 0.f}, cg[3] = {0.f, 0.f, 0.f}, cl = 0.f;
+        auto pair = [&](int c) {
+            const float4 xj = __ldg(T.subPosS + c), vj = __ldg(T.subVelS + c);
+            const float2 rj = T.subRho[__ldg(T.subSortedIds + c)];
+            const float r2 = dist2(xi, xj);
+            const float invj = 1.0f / rj.x;
+            const float dx = __fsub_rn(xi.x, xj.x), dy = __fsub_rn(xi.y, xj.y), dz = __fsub_rn(xi.z, xj.z);
+            const float rinv = rsqrtf(r2);
+            const float hr = ph.h - r2 * rinv;
+            const float sp = (qi + rj.y * invj * invj) * hr * hr * rinv;
+            const float sv = invj * hr;
+            fp[0] = fmaf(sp, dx, fp[0]);
+            fp[1] = fmaf(sp, dy, fp[1]);
+            fp[2] = fmaf(sp, dz, fp[2]);
+            fv[0] = fmaf(sv, vj.x - vi.x, fv[0]);
+            fv[1] = fmaf(sv, vj.y - vi.y, fv[1]);
+            fv[2] = fmaf(sv, vj.z - vi.z, fv[2]);
+            const float d2 = ph.h2 - r2;
+            const float sc = invj * d2 * d2;
+            cg[0] = fmaf(sc, dx, cg[0]);
+            cg[1] = fmaf(sc, dy, cg[1]);
+            cg[2] = fmaf(sc, dz, cg[2]);
+            cl = fmaf(invj * d2, 3.f * ph.h2 - 7.f * r2, cl);
+        };
         // rounds of TS_BATCH candidates per lane: test and list the hits in
-        // the warp's queue; all lanes take the listed pairs 32 at a time
+        // the group's queue; the group's lanes take the listed pairs TS_G at
+        // a time
         int listed = 0;
-        bool more = __any_sync(0xffffffffu, t < e);
-        while (more) {
+        while (__any_sync(0xffffffffu, walking(w))) {
+            int c[TS_BATCH];
             float4 xc[TS_BATCH];
 #pragma unroll
-            for (int u = 0; u < TS_BATCH; u++)
-                if (t + 3 * u < e) xc[u] = __ldg(T.subPosS + t + 3 * u);
+            for (int u = 0; u < TS_BATCH; u++) {
+                c[u] = next_candidate(w);
+                if (c[u] >= 0) xc[u] = __ldg(T.subPosS + c[u]);
+            }
 #pragma unroll
             for (int u = 0; u < TS_BATCH; u++) {
                 bool hit = false;
-                if (t + 3 * u < e) {
+                if (c[u] >= 0) {
                     const float r2 = dist2(xi, xc[u]);
                     hit = r2 <= ph.h2 && r2 > 0.f;
                 }
-                const unsigned int m = __ballot_sync(0xffffffffu, hit);
-                if (hit) queue[listed + __popc(m & below)] = t + 3 * u;
+                const unsigned int m = (__ballot_sync(0xffffffffu, hit) >> (TS_G * grp)) & 0xFFu;
+                if (hit) queue[listed + __popc(m & below)] = c[u];
                 listed += __popc(m);
             }
-            t += 3 * TS_BATCH;
-            more = __any_sync(0xffffffffu, t < e);
-            const int take = more ? (listed & ~31) : listed;
+            const int take = listed & ~(TS_G - 1);
             __syncwarp();
-            for (int q = lane; q < take; q += 32) {
-                const int c = queue[q];
-                const float4 xj = __ldg(T.subPosS + c), vj = __ldg(T.subVelS + c);
-                const float2 rj = T.subRho[__ldg(T.subSortedIds + c)];
-                const float r2 = dist2(xi, xj);
-                const float invj = 1.0f / rj.x;
-                const float dx = __fsub_rn(xi.x, xj.x), dy = __fsub_rn(xi.y, xj.y), dz = __fsub_rn(xi.z, xj.z);
-                const float rinv = rsqrtf(r2);
-                const float hr = ph.h - r2 * rinv;
-                const float sp = (qi + rj.y * invj * invj) * hr * hr * rinv;
-                const float sv = invj * hr;
-                fp[0] = fmaf(sp, dx, fp[0]);
-                fp[1] = fmaf(sp, dy, fp[1]);
-                fp[2] = fmaf(sp, dz, fp[2]);
-                fv[0] = fmaf(sv, vj.x - vi.x, fv[0]);
-                fv[1] = fmaf(sv, vj.y - vi.y, fv[1]);
-                fv[2] = fmaf(sv, vj.z - vi.z, fv[2]);
-                const float d2 = ph.h2 - r2;
-                const float sc = invj * d2 * d2;
-                cg[0] = fmaf(sc, dx, cg[0]);
-                cg[1] = fmaf(sc, dy, cg[1]);
-                cg[2] = fmaf(sc, dz, cg[2]);
-                cl = fmaf(invj * d2, 3.f * ph.h2 - 7.f * r2, cl);
-            }
-            // fewer than 32 left: to the front of the queue
+            for (int q = gl; q < take; q += TS_G) pair(queue[q]);
+            // fewer than TS_G left: to the front of the queue
             const int left = listed - take;
-            const int keep = lane < left ? queue[take + lane] : 0;
+            const int keep = gl < left ? queue[take + gl] : 0;
             __syncwarp();
-            if (lane < left) queue[lane] = keep;
+            if (gl < left) queue[gl] = keep;
             listed = left;
             __syncwarp();
         }
+        if (gl < listed) pair(queue[gl]);
+        __syncwarp();
         for (int a = 0; a < 3; a++) {
-            fp[a] = warp_total(fp[a]);
-            fv[a] = warp_total(fv[a]);
-            cg[a] = warp_total(cg[a]);
+            fp[a] = group_total(fp[a]);
+            fv[a] = group_total(fv[a]);
+            cg[a] = group_total(cg[a]);
         }
-        cl = warp_total(cl);
-        if (lane != 0) continue;
+        cl = group_total(cl);
+        if (!valid || gl != 0) continue;
         const float pc = ph.pressCoef * rhoi;
         float force[3];
         for (int a = 0; a < 3; a++) force[a] = ph.viscCoef * fv[a] + pc * fp[a];
@@ -644,7 +739,7 @@ void launch_ts_children(int n, float4* posS, float4* velS, const float4* accS, c
 void launch_ts_project(const float4* coarsePos, const int* workIds, int byId, const float4* rho4S,
                        const int* cellOffset, GridDev g, float hs, const TwoScaleDev& T, int capacity,
                        cudaStream_t s) {
-    k_ts_project<<<warp_grid(capacity), TS_WARP_BLOCK, 0, s>>>(coarsePos, workIds, byId, rho4S, cellOffset, g, hs,
+    k_ts_project<<<group_grid(capacity), TS_WARP_BLOCK, 0, s>>>(coarsePos, workIds, byId, rho4S, cellOffset, g, hs,
                                                                 T);
 }
 
@@ -657,11 +752,11 @@ void launch_ts_sub_sort(GridDev sg, const TwoScaleDev& T, SortBuffers subSb, int
 }
 
 void launch_ts_sub_density(GridDev sg, PhysDev sph, const TwoScaleDev& T, int capacity, cudaStream_t s) {
-    k_ts_subdensity<<<warp_grid(capacity), TS_WARP_BLOCK, 0, s>>>(sg, sph, T);
+    k_ts_subdensity<<<group_grid(capacity), TS_WARP_BLOCK, 0, s>>>(sg, sph, T);
 }
 
 void launch_ts_sub_force(GridDev sg, PhysDev sph, const TwoScaleDev& T, int capacity, cudaStream_t s) {
-    k_ts_subforce<<<warp_grid(capacity), TS_WARP_BLOCK, 0, s>>>(sg, sph, T);
+    k_ts_subforce<<<group_grid(capacity), TS_WARP_BLOCK, 0, s>>>(sg, sph, T);
 }
 
 
