@@ -109,10 +109,12 @@ inline int warp_grid(long long items) {
 
 // The projection and the fine level's loops run over tens of thousands of
 // children: there a particle gets a group of TS_G = 8 lanes (4 per warp), so
-// that its setup, stencil and epilogue are shared four ways.  Lane g of a
-// group walks stencil row g from its start, then every eighth candidate of
-// row 8 from its start + g, TS_BATCH loads at a time.  Group sums use a
-// fixed xor tree (every lane of the group ends with the same bits).
+// that its setup, stencil and epilogue are shared four ways.  The group
+// fetches the bounds of its 9 stencil rows in one round (lane g row g, every
+// lane row 8) and walks the rows in order; within a row lane g takes
+// candidates start + g, + 8, ... (consecutive lanes read consecutive
+// addresses), TS_BATCH loads in flight.  Group sums use a fixed xor tree
+// (every lane of the group ends with the same bits).
 constexpr int TS_G = 8;
 
 inline int group_grid(long long items) { return warp_grid((items + 32 / TS_G - 1) / (32 / TS_G)); }
@@ -136,11 +138,6 @@ __device__ __forceinline__ Stencil group_stencil(float4 x, float h, const GridDe
     return s;
 }
 
-struct RowWalk {
-    int t, e;    // own row
-    int t8, e8;  // this lane's share of row 8
-};
-
 __device__ __forceinline__ void row_bounds(const Stencil& st, const GridDev& g, const int* __restrict__ offs, int r,
                                            int& s, int& e) {
     s = e = 0;
@@ -151,26 +148,26 @@ __device__ __forceinline__ void row_bounds(const Stencil& st, const GridDev& g, 
     e = __ldg(offs + row + st.x1 + 1);
 }
 
-__device__ __forceinline__ RowWalk group_rows(const Stencil& st, const GridDev& g, const int* __restrict__ offs,
-                                              int gl) {
-    RowWalk w;
-    row_bounds(st, g, offs, gl, w.t, w.e);
-    row_bounds(st, g, offs, 8, w.t8, w.e8);
-    w.t8 += gl;
-    return w;
+struct GroupRows {
+    int s, e;    // row gl
+    int s8, e8;  // row 8
+};
+
+// All-empty rows for a group without a particle.
+__device__ __forceinline__ GroupRows group_rows(const Stencil& st, const GridDev& g, const int* __restrict__ offs,
+                                               int gl, bool valid) {
+    GroupRows R = {0, 0, 0, 0};
+    if (!valid) return R;
+    row_bounds(st, g, offs, gl, R.s, R.e);
+    row_bounds(st, g, offs, 8, R.s8, R.e8);
+    return R;
 }
 
-__device__ __forceinline__ bool walking(const RowWalk& w) { return w.t < w.e || w.t8 < w.e8; }
-
-// The lane's next candidate (own row first), -1 when it has none left.
-__device__ __forceinline__ int next_candidate(RowWalk& w) {
-    if (w.t < w.e) return w.t++;
-    if (w.t8 < w.e8) {
-        const int c = w.t8;
-        w.t8 += TS_G;
-        return c;
-    }
-    return -1;
+// Bounds of row r (the same in every lane of the group; all lanes call it).
+__device__ __forceinline__ void group_row(const GroupRows& R, int r, int& s, int& e) {
+    const int a = __shfl_sync(0xffffffffu, R.s, r & 7, TS_G), b = __shfl_sync(0xffffffffu, R.e, r & 7, TS_G);
+    s = r < 8 ? a : R.s8;
+    e = r < 8 ? b : R.e8;
 }
 
 __device__ __forceinline__ float group_total(float v) {
@@ -432,28 +429,29 @@ __global__ void __launch_bounds__(TS_WARP_BLOCK) k_ts_project(const float4* __re
         const bool valid = idx < nSub;
         const int slot = valid ? T.subIds[idx] : 0;
         const float4 x = valid ? T.subPos[slot] : make_float4(g.origin[0], g.origin[1], g.origin[2], 0.f);
-        const Stencil st = group_stencil(x, hs, g, gl);
-        RowWalk w = {0, 0, 0, 0};
-        if (valid) w = group_rows(st, g, cellOffset, gl);
+        const GroupRows R = group_rows(group_stencil(x, hs, g, gl), g, cellOffset, gl, valid);
         float d = 0.f, p = 0.f, cnt = 0.f;
-        while (__any_sync(0xffffffffu, walking(w))) {
-            int c[TS_BATCH];
-            float4 xc[TS_BATCH], rc[TS_BATCH];
+        for (int r = 0; r < 9; r++) {
+            int s0, e;
+            group_row(R, r, s0, e);
+            for (int t = s0 + gl; t < e; t += TS_G * TS_BATCH) {
+                float4 xc[TS_BATCH], rc[TS_BATCH];
 #pragma unroll
-            for (int u = 0; u < TS_BATCH; u++) {
-                c[u] = next_candidate(w);
-                if (c[u] >= 0) {
-                    xc[u] = byId ? __ldg(coarsePos + __ldg(workIds + c[u])) : __ldg(coarsePos + c[u]);
-                    rc[u] = __ldg(rho4S + c[u]);
+                for (int u = 0; u < TS_BATCH; u++) {
+                    const int c = t + TS_G * u;
+                    if (c < e) {
+                        xc[u] = byId ? __ldg(coarsePos + __ldg(workIds + c)) : __ldg(coarsePos + c);
+                        rc[u] = __ldg(rho4S + c);
+                    }
                 }
+#pragma unroll
+                for (int u = 0; u < TS_BATCH; u++)
+                    if (t + TS_G * u < e && ref_r2(x, xc[u]) <= hs2) {
+                        d += rc[u].x;
+                        p += rc[u].y;
+                        cnt += 1.f;
+                    }
             }
-#pragma unroll
-            for (int u = 0; u < TS_BATCH; u++)
-                if (c[u] >= 0 && ref_r2(x, xc[u]) <= hs2) {
-                    d += rc[u].x;
-                    p += rc[u].y;
-                    cnt += 1.f;
-                }
         }
         d = group_total(d);
         p = group_total(p);
@@ -519,34 +517,26 @@ __global__ void __launch_bounds__(TS_WARP_BLOCK) k_ts_subdensity(GridDev g, Phys
         const bool valid = idx < nReg;
         const int slot = valid ? T.subIds[idx] : 0;
         const float4 x = valid ? T.subPos[slot] : make_float4(g.origin[0], g.origin[1], g.origin[2], 0.f);
-        const Stencil st = group_stencil(x, ph.h, g, gl);
-        RowWalk w = {0, 0, 0, 0};
-        if (valid) w = group_rows(st, g, T.subOffset, gl);
-        float own = 0.f, share = 0.f;  // sums over row gl and over this lane's share of row 8
-        while (__any_sync(0xffffffffu, walking(w))) {
-            int c[TS_BATCH];
-            bool mine[TS_BATCH];
-            float4 xc[TS_BATCH];
-#pragma unroll
-            for (int u = 0; u < TS_BATCH; u++) {
-                mine[u] = w.t < w.e;
-                c[u] = next_candidate(w);
-                if (c[u] >= 0) xc[u] = __ldg(T.subPosS + c[u]);
-            }
-#pragma unroll
-            for (int u = 0; u < TS_BATCH; u++)
-                if (c[u] >= 0) {
-                    const float q = fmaxf(ph.h2 - dist2(x, xc[u]), 0.f);
-                    if (mine[u]) own = fmaf(q * q, q, own);
-                    else share = fmaf(q * q, q, share);
-                }
-        }
-        // row sums, compensated over the rows in order
-        const float row8 = group_total(share);
+        const GroupRows R = group_rows(group_stencil(x, ph.h, g, gl), g, T.subOffset, gl, valid);
         float sum = 0.f, comp = 0.f;
-#pragma unroll
         for (int r = 0; r < 9; r++) {
-            const float rs = r < 8 ? __shfl_sync(0xffffffffu, own, r, TS_G) : row8;
+            int s0, e;
+            group_row(R, r, s0, e);
+            float part = 0.f;
+            for (int t = s0 + gl; t < e; t += TS_G * TS_BATCH) {
+                float4 xc[TS_BATCH];
+#pragma unroll
+                for (int u = 0; u < TS_BATCH; u++)
+                    if (t + TS_G * u < e) xc[u] = __ldg(T.subPosS + t + TS_G * u);
+#pragma unroll
+                for (int u = 0; u < TS_BATCH; u++)
+                    if (t + TS_G * u < e) {
+                        const float q = fmaxf(ph.h2 - dist2(x, xc[u]), 0.f);
+                        part = fmaf(q * q, q, part);
+                    }
+            }
+            // the row's sum, compensated over the rows in order
+            const float rs = group_total(part);
             if (rs > 0.f) kahan_add(sum, comp, rs);
         }
         const float rho = __fsub_rn(sum, comp) * ph.poly6m;
@@ -599,9 +589,7 @@ __global__ void __launch_bounds__(TS_WARP_BLOCK) k_ts_subforce(GridDev g, PhysDe
         const float2 ri = valid ? T.subRho[slot] : make_float2(1.f, 0.f);
         const float rhoi = ri.x;
         const float qi = ri.y / (rhoi * rhoi);
-        const Stencil st = group_stencil(xi, ph.h, g, gl);
-        RowWalk w = {0, 0, 0, 0};
-        if (valid) w = group_rows(st, g, T.subOffset, gl);
+        const GroupRows R = group_rows(group_stencil(xi, ph.h, g, gl), g, T.subOffset, gl, valid);
         float fp[3] = {0.f, 0.f, 0.f}, fv[3] = {0.f, 0.f, 0.f}, cg[3] = {0.f, 0.f, 0.f}, cl = 0.f;
         auto pair = [&](int c) {
             const float4 xj = __ldg(T.subPosS + c), vj = __ldg(T.subVelS + c);
@@ -626,39 +614,40 @@ __global__ void __launch_bounds__(TS_WARP_BLOCK) k_ts_subforce(GridDev g, PhysDe
             cg[2] = fmaf(sc, dz, cg[2]);
             cl = fmaf(invj * d2, 3.f * ph.h2 - 7.f * r2, cl);
         };
-        // rounds of TS_BATCH candidates per lane: test and list the hits in
-        // the group's queue; the group's lanes take the listed pairs TS_G at
-        // a time
+        // row by row, rounds of TS_BATCH candidates per lane: test and list
+        // the hits in the group's queue; the group's lanes take the listed
+        // pairs TS_G at a time
         int listed = 0;
-        while (__any_sync(0xffffffffu, walking(w))) {
-            int c[TS_BATCH];
-            float4 xc[TS_BATCH];
+        for (int r = 0; r < 9; r++) {
+            int s0, e;
+            group_row(R, r, s0, e);
+            for (int t = s0 + gl; __any_sync(0xffffffffu, t < e); t += TS_G * TS_BATCH) {
+                float4 xc[TS_BATCH];
 #pragma unroll
-            for (int u = 0; u < TS_BATCH; u++) {
-                c[u] = next_candidate(w);
-                if (c[u] >= 0) xc[u] = __ldg(T.subPosS + c[u]);
-            }
+                for (int u = 0; u < TS_BATCH; u++)
+                    if (t + TS_G * u < e) xc[u] = __ldg(T.subPosS + t + TS_G * u);
 #pragma unroll
-            for (int u = 0; u < TS_BATCH; u++) {
-                bool hit = false;
-                if (c[u] >= 0) {
-                    const float r2 = dist2(xi, xc[u]);
-                    hit = r2 <= ph.h2 && r2 > 0.f;
+                for (int u = 0; u < TS_BATCH; u++) {
+                    bool hit = false;
+                    if (t + TS_G * u < e) {
+                        const float r2 = dist2(xi, xc[u]);
+                        hit = r2 <= ph.h2 && r2 > 0.f;
+                    }
+                    const unsigned int m = (__ballot_sync(0xffffffffu, hit) >> (TS_G * grp)) & 0xFFu;
+                    if (hit) queue[listed + __popc(m & below)] = t + TS_G * u;
+                    listed += __popc(m);
                 }
-                const unsigned int m = (__ballot_sync(0xffffffffu, hit) >> (TS_G * grp)) & 0xFFu;
-                if (hit) queue[listed + __popc(m & below)] = c[u];
-                listed += __popc(m);
+                const int take = listed & ~(TS_G - 1);
+                __syncwarp();
+                for (int q = gl; q < take; q += TS_G) pair(queue[q]);
+                // fewer than TS_G left: to the front of the queue
+                const int left = listed - take;
+                const int keep = gl < left ? queue[take + gl] : 0;
+                __syncwarp();
+                if (gl < left) queue[gl] = keep;
+                listed = left;
+                __syncwarp();
             }
-            const int take = listed & ~(TS_G - 1);
-            __syncwarp();
-            for (int q = gl; q < take; q += TS_G) pair(queue[q]);
-            // fewer than TS_G left: to the front of the queue
-            const int left = listed - take;
-            const int keep = gl < left ? queue[take + gl] : 0;
-            __syncwarp();
-            if (gl < left) queue[gl] = keep;
-            listed = left;
-            __syncwarp();
         }
         if (gl < listed) pair(queue[gl]);
         __syncwarp();
