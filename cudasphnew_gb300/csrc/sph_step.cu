@@ -38,8 +38,11 @@ struct RowMasks {
 
 // With REL the positions are cell-relative: every neighbour is moved into
 // particle i's cell frame before its distance is taken.
+// Occupancy: 40 registers (six 256-thread blocks per SM) cost no spills
+// outside the batched form's setup, and the stage runs ~1 % faster than at
+// 48; the cell-relative forms keep 48.
 template <bool KAHAN, bool EMIT, bool BATCH, bool REL>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, REL ? 5 : 6)
 k_density(int n, const float4* __restrict__ posS, RowTables T, GridDev g_, PhysDev ph_, MapDev map_, int window,
           float4* __restrict__ rho4S, RowMasks M) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -447,14 +450,16 @@ struct ForceArgs {
     FeatOut fo;
 };
 
-// Occupancy: the plain forms fit 64 registers without spilling, so four
-// 256-thread blocks share an SM (the force stage is latency bound: 210 ->
-// 150 us per million particles against two blocks); the feature and batched
-// forms take up to 80 registers, three blocks.
+// Occupancy: the force stage is latency bound, so it runs as many warps as
+// fit without heavy spilling.  The pretested form without surface tension
+// fits 48 registers with a few spilled bytes outside the pair loop: five
+// 256-thread blocks per SM (145 -> 140 us per million particles against
+// four).  The other plain forms fit 64 registers, four blocks (210 -> 150 us
+// against two); the feature and batched forms take up to 80, three blocks.
 // REL: cell-relative positions (plain forms only): neighbours are moved into
 // particle i's cell frame, the step is integrated there and re-binned.
 template <bool KAHAN, bool TENSION, int FORM, bool FEAT, bool BATCH, bool REL = false>
-__global__ void __launch_bounds__(256, FEAT ? 3 : (BATCH ? 3 : 4)) k_force(ForceArgs F) {
+__global__ void __launch_bounds__(256, FEAT || BATCH ? 3 : (TENSION || REL || FORM != FORCE_PRETESTED ? 4 : 5)) k_force(ForceArgs F) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= F.n) return;
     const float4 xi = F.posS[i];
