@@ -1166,7 +1166,8 @@ sph_status sph_autotune(sph_handle s, int reps, sph_tuning* chosen) {
     // how the stages share the caches and overlap inside a step graph.  The
     // particle state is saved and put back around each trial.
     std::sort(shapes.begin(), shapes.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
-    std::vector<StepConfig> finalists{best, current};
+    // the configuration in use is the incumbent
+    std::vector<StepConfig> finalists{current, best};
     for (size_t k = 0; k < shapes.size() && finalists.size() < 5; k++) finalists.push_back(shapes[k].second);
     float4 *savePos = nullptr, *saveVel = nullptr;
     TUNE_CUDA(cudaMalloc((void**)&savePos, sizeof(float4) * n));
@@ -1176,7 +1177,7 @@ sph_status sph_autotune(sph_handle s, int reps, sph_tuning* chosen) {
     const unsigned int steps0 = s->numTimeSteps;
     const bool stepped0 = s->stepped;
     float bestStep = 3.0e38f;
-    StepConfig chosenCfg = best;
+    StepConfig chosenCfg = current;
     cudaError_t te = cudaSuccess;
     for (const StepConfig& c : finalists) {
         s->cfg = c;
