@@ -454,12 +454,13 @@ struct ForceArgs {
 // fit without heavy spilling.  The pretested form without surface tension
 // fits 48 registers with a few spilled bytes outside the pair loop: five
 // 256-thread blocks per SM (145 -> 140 us per million particles against
-// four).  The other plain forms fit 64 registers, four blocks (210 -> 150 us
-// against two); the feature and batched forms take up to 80, three blocks.
+// four).  The other plain forms and the batched forms fit 64 registers, four
+// blocks (210 -> 150 us against two; the 64-scene batch 1.55 -> 1.44 ms per
+// step against three); the feature form takes up to 80, three blocks.
 // REL: cell-relative positions (plain forms only): neighbours are moved into
 // particle i's cell frame, the step is integrated there and re-binned.
 template <bool KAHAN, bool TENSION, int FORM, bool FEAT, bool BATCH, bool REL = false>
-__global__ void __launch_bounds__(256, FEAT || BATCH ? 3 : (TENSION || REL || FORM != FORCE_PRETESTED ? 4 : 5)) k_force(ForceArgs F) {
+__global__ void __launch_bounds__(256, FEAT ? 3 : (BATCH || TENSION || REL || FORM != FORCE_PRETESTED ? 4 : 5)) k_force(ForceArgs F) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= F.n) return;
     const float4 xi = F.posS[i];
