@@ -58,7 +58,7 @@ void* host_device_ptr(const void* p) {
 }
 
 RowTables rows_of(const sph_sim* s) {
-    return RowTables{s->sb.cellOffset, s->sb.quarterCuts, s->sb.scenes, s->sb.skip};
+    return RowTables{s->sb.cellOffset, s->sb.halfOffset, s->sb.scenes, s->sb.skip};
 }
 
 GridDev make_grid(const SimulationParameters& P, bool sub) {
@@ -164,7 +164,7 @@ void free_all(sph_sim* s) {
     for (cudaEvent_t e : s->events) cudaEventDestroy(e);
     void* ptrs[] = {s->pos, s->vel, s->posS, s->velS, s->rho4S, s->accS, s->sb.cnt, s->sb.cellOffset,
                     s->sb.keySlot, s->sb.tmpIds, s->sb.sortedHash, s->sb.sortedIds, s->sb.workIds,
-                    s->sb.quarterCuts, s->scanBlock,
+                    s->sb.halfOffset, s->scanBlock,
                     s->status, s->staging, s->map4, s->mapDist, s->rowStart, s->rowMask, s->diagBuf,
                     s->scenesDev, s->reuse};
     for (void* p : ptrs)
@@ -373,8 +373,8 @@ sph_status alloc_handle(sph_sim* s, int n, long long C) {
     SPH_CUDA(dalloc(&s->sb.sortedHash, n));
     SPH_CUDA(dalloc(&s->sb.sortedIds, n));
     SPH_CUDA(dalloc(&s->sb.workIds, n));
-    SPH_CUDA(dalloc(&s->sb.quarterCuts, (size_t)C + 1));
-    SPH_CUDA(cudaMemsetAsync(s->sb.quarterCuts, 0, sizeof(int) * ((size_t)C + 1), s->stream));
+    SPH_CUDA(dalloc(&s->sb.halfOffset, (size_t)C + 1));
+    SPH_CUDA(cudaMemsetAsync(s->sb.halfOffset, 0, sizeof(int) * ((size_t)C + 1), s->stream));
     SPH_CUDA(dalloc(&s->scanBlock, (size_t)tiles + 2));
     s->sb.tileCounter = reinterpret_cast<unsigned int*>(s->scanBlock);
     s->sb.scanFlags = s->scanBlock + 2;
@@ -1042,7 +1042,7 @@ sph_status sph_autotune(sph_handle s, int reps, sph_tuning* chosen) {
                 {s->rho4S, nullptr, sizeof(float4) * n},      {s->sb.sortedHash, nullptr, sizeof(int) * n},
                 {s->sb.sortedIds, nullptr, sizeof(int) * n},  {s->sb.cellOffset, nullptr, sizeof(int) * ((size_t)C + 1)},
                 {s->sb.workIds, nullptr, sizeof(int) * n},    {s->accS, nullptr, sizeof(float4) * n},
-                {s->sb.quarterCuts, nullptr, sizeof(int) * ((size_t)C + 1)}};
+                {s->sb.halfOffset, nullptr, sizeof(int) * ((size_t)C + 1)}};
     float4* scratch = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     auto cleanup = [&]() {

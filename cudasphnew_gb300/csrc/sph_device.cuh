@@ -120,10 +120,10 @@ __device__ __forceinline__ void map_uvw(const MapDev& m, float4 x, float* uvw) {
 // arrays, visited in the reference's k, j, i order.
 //
 // With `window`, a row whose (y, z) cell rectangle lies farther than h from
-// the particle is skipped, and the others are cut to the quarter-cells (in x)
+// the particle is skipped, and the others are cut to the half-cells (in x)
 // that the sphere of radius h reaches at that (y, z) gap: the working order
-// sorts each cell by x and records how many members lie below each of its
-// quarter-planes, so the cut is a table lookup.  The gap is shrunk and the reach grown by 1e-3 h -- far
+// sorts each cell by x and records where its upper half starts, so the cut
+// is a table lookup.  The gap is shrunk and the reach grown by 1e-3 h -- far
 // more than the rounding of any cell boundary or distance -- so every particle
 // within h stays a candidate; the candidates dropped all lie beyond h and
 // contribute exactly nothing in the reference either.
@@ -165,35 +165,6 @@ __device__ __forceinline__ bool neighbour_r2(float r2, float h2) {
 
 // Candidate range [s, e) of stencil row r (0..8: k outer, j inner).  Rows
 // outside the stencil and rows the window cut removes are empty (s == e).
-// The cut of a row [a0 .. b1) whose end cells are cl (members [a0, a1)) and
-// cr (members [b0, b1)) to the reach [xl, xr]: the start skips the members of
-// cl below the highest quarter-plane at or below xl, the end drops the
-// members of cr at or above the lowest quarter-plane above xr.  A plane k of
-// cell c sits at base + (cf + k/4) spacing (cf the cell's x index in the
-// frame of xl and xr), the expression k_rank_gather counted against.  Cut
-// words of empty cells are stale; the clamps keep the range inside the cell.
-__device__ __forceinline__ void quarter_cut(const unsigned int* cuts, int row, int cl, int cr, float xl, float xr,
-                                            float base, float cfl, float cfr, float spacing, int a0, int a1, int b0,
-                                            int b1, int& s, int& e) {
-    int kl = 0, kr = 0;
-#pragma unroll
-    for (int j = 1; j <= 3; j++) {
-        kl += xl >= base + (cfl + 0.25f * (float)j) * spacing;
-        kr += xr >= base + (cfr + 0.25f * (float)j) * spacing;
-    }
-    s = a0;
-    e = b1;
-    if (kl > 0) {
-        const int q = (int)((__ldg(cuts + row + cl) >> (8 * (kl - 1))) & 0xFFu);
-        if (q != 255) s = min(a0 + q, a1);
-    }
-    if (kr < 3) {
-        const int q = (int)((__ldg(cuts + row + cr) >> (8 * kr)) & 0xFFu);
-        if (q != 255) e = min(b0 + q, b1);
-    }
-    if (e < s) e = s;
-}
-
 __device__ __forceinline__ void row_range(float4 xi, const Stencil& st, float h, const GridDev& g, RowTables T,
                                           bool window, int r, int& s, int& e) {
     s = e = 0;
@@ -223,8 +194,13 @@ __device__ __forceinline__ void row_range(float4 xi, const Stencil& st, float h,
     if (cl > cr) return;
     const int a0 = __ldg(T.cellOffset + row + cl), a1 = __ldg(T.cellOffset + row + cl + 1);
     const int b0 = __ldg(T.cellOffset + row + cr), b1 = __ldg(T.cellOffset + row + cr + 1);
-    quarter_cut(T.quarterCuts, row, cl, cr, xl, xr, g.origin[0], (float)cl, (float)cr, g.spacing, a0, a1, b0, b1, s,
-                e);
+    const float midL = g.origin[0] + ((float)cl + 0.5f) * g.spacing;
+    const float midR = g.origin[0] + ((float)cr + 0.5f) * g.spacing;
+    s = a0;
+    e = b1;
+    if (xl >= midL) s = min(max(__ldg(T.halfOffset + row + cl), a0), a1);
+    if (xr < midR) e = min(max(__ldg(T.halfOffset + row + cr), b0), b1);
+    if (e < s) e = s;
 }
 
 // ---------------------------------------------------------------------------
@@ -296,7 +272,7 @@ __device__ __forceinline__ Stencil stencil_rel(float4 x, int3 c, float h, const 
     return s;
 }
 
-// row_range for a cell-relative particle: the same rows and quarter-cell cut,
+// row_range for a cell-relative particle: the same rows and half-cell cut,
 // with every boundary taken in the particle's own cell frame.  Also returns
 // the row's y and z offsets (times spacing) for rel_in_frame.
 __device__ __forceinline__ void row_range_rel(float4 xi, int3 c, const Stencil& st, float h, const GridDev& g,
@@ -331,8 +307,13 @@ __device__ __forceinline__ void row_range_rel(float4 xi, int3 c, const Stencil& 
     if (cl > cr) return;
     const int a0 = __ldg(T.cellOffset + row + cl), a1 = __ldg(T.cellOffset + row + cl + 1);
     const int b0 = __ldg(T.cellOffset + row + cr), b1 = __ldg(T.cellOffset + row + cr + 1);
-    quarter_cut(T.quarterCuts, row, cl, cr, xl, xr, 0.f, (float)(cl - c.x), (float)(cr - c.x), g.spacing, a0, a1, b0,
-                b1, s, e);
+    const float midL = ((float)(cl - c.x) + 0.5f) * g.spacing;
+    const float midR = ((float)(cr - c.x) + 0.5f) * g.spacing;
+    s = a0;
+    e = b1;
+    if (xl >= midL) s = min(max(__ldg(T.halfOffset + row + cl), a0), a1);
+    if (xr < midR) e = min(max(__ldg(T.halfOffset + row + cr), b0), b1);
+    if (e < s) e = s;
 }
 
 __device__ __forceinline__ void kahan_add(float& sum, float& comp, float term) {

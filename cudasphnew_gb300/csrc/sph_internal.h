@@ -79,7 +79,7 @@ struct SortBuffers {
     int* sortedHash;          // [n]
     int* sortedIds;           // [n]   the reference's permutation (cell, id)
     int* workIds;             // [n]   the working order (cell, x, id) of the sorted arrays
-    unsigned int* quarterCuts;  // [C+1] per cell: members below its x quarter-planes (sph_device.cuh)
+    int* halfOffset;          // [C+1] first working index of each cell's upper x-half
                               //       (meaningful for occupied cells only)
     unsigned long long* scanFlags;  // decoupled look-back tile states
     unsigned int* tileCounter;
@@ -121,7 +121,7 @@ struct TwoScaleDev {
 // Per-row lookup tables of the neighbour search.
 struct RowTables {
     const int* cellOffset;  // [C+1]
-    const unsigned int* quarterCuts;  // [C+1], valid for occupied cells
+    const int* halfOffset;  // [C+1], valid for occupied cells
     const SceneDev* scenes; // batched handles: per-scene grids, constants, maps (else NULL)
     const int* skip;        // as SortBuffers::skip, read by the density stage only
 };
@@ -133,7 +133,7 @@ struct StepConfig {
     int densityBlock = 128;
     int forceBlock = 128;
     int forceVariant = FORCE_PRETESTED;
-    int prune = 1;   // row / quarter-cell window cut (sph_device.cuh)
+    int prune = 1;   // row / half-cell window cut (sph_device.cuh)
     int kahan = 1;
 };
 

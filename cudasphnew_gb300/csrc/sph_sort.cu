@@ -312,8 +312,8 @@ void launch_scatter(int n, SortBuffers sb, cudaStream_t s) {
 //   by particle id   -> sortedIds, the reference's permutation (stable sort
 //                       by hash, particle_simulation.cu:2340), kept for the API;
 //   by (x, id)       -> workIds, the order the neighbour kernels use: a cell's
-//                       members sorted by x, so the members on either side of
-//                       any x-plane are two contiguous ranges (quarterCuts below).
+//                       members sorted by x, so the lower and upper x-halves of
+//                       a cell are two contiguous ranges (halfOffset below).
 // Ranks count the smaller keys in the segment; x is compared through its
 // order-preserving integer image so the order is total (NaN included).
 // ---------------------------------------------------------------------------
@@ -322,15 +322,14 @@ __device__ __forceinline__ unsigned int ordered_bits(float x) {
     return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
 }
 
-// The same pass records, per cell, how many of its members lie below its
-// x quarter-planes (origin + (cx + k/4) spacing, k = 1, 2, 3; byte k-1 of
-// quarterCuts[c], 255 when the count exceeds 254), so a neighbour search can
-// cut a row at quarter-cell granularity from a table.
+// The same pass records, per cell, where its upper x-half starts in the
+// working order (halfOffset[c] = first index with x >= the cell's mid-plane),
+// so a neighbour search can cut a row at half-cell granularity from a table.
 template <bool BATCH, bool REL>
 __global__ void k_rank_gather(int n, const int* __restrict__ sortedHash, const int* __restrict__ cellOffset,
                               const int* __restrict__ tmpIds, const float4* __restrict__ pos,
                               const float4* __restrict__ vel, GridDev g_, const SceneDev* __restrict__ scenes,
-                              int* __restrict__ sortedIds, int* __restrict__ workIds, unsigned int* __restrict__ quarterCuts,
+                              int* __restrict__ sortedIds, int* __restrict__ workIds, int* __restrict__ halfOffset,
                               float4* __restrict__ posS, float4* __restrict__ velS, const int* __restrict__ skip) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n || (skip && *skip)) return;
@@ -340,31 +339,23 @@ __global__ void k_rank_gather(int n, const int* __restrict__ sortedHash, const i
     float4 p = __ldg(pos + my);
     const GridDev& g = BATCH ? scenes[__float_as_int(p.w)].g : g_;
     unsigned int key = ordered_bits(p.x);
-    // the cell's quarter-planes, in the frame its members' x is stored in
-    // (the expressions row_range compares against)
-    const float base = REL ? 0.f : g.origin[0];
-    const float cf = REL ? 0.f : (float)((c - g.cellBase) % g.dim[0]);
-    const float q1 = base + (cf + 0.25f) * g.spacing, q2 = base + (cf + 0.5f) * g.spacing,
-                q3 = base + (cf + 0.75f) * g.spacing;
-    int rId = 0, rX = 0, b1 = 0, b2 = 0, b3 = 0;
+    // the cell's mid-plane, in the frame its members' x is stored in
+    const float mid = REL ? 0.5f * g.spacing
+                          : g.origin[0] + ((float)((c - g.cellBase) % g.dim[0]) + 0.5f) * g.spacing;
+    int rId = 0, rX = 0, below = 0;
     for (int t = s; t < e; t++) {
         int o = __ldg(tmpIds + t);
         float xo = __ldg(&pos[o].x);
         unsigned int ko = ordered_bits(xo);
         rId += o < my;
         rX += (ko < key) || (ko == key && o < my);
-        b1 += xo < q1;
-        b2 += xo < q2;
-        b3 += xo < q3;
+        below += xo < mid;
     }
     sortedIds[s + rId] = my;
     workIds[s + rX] = my;
     posS[s + rX] = p;
     velS[s + rX] = __ldg(vel + my);
-    if (rX == 0) {
-        auto byte = [](int b) { return (unsigned int)(b > 254 ? 255 : b); };
-        quarterCuts[c] = byte(b1) | (byte(b2) << 8) | (byte(b3) << 16);
-    }
+    if (rX == 0) halfOffset[c] = s + below;
 }
 
 void launch_rank_gather(int n, SortBuffers sb, const float4* pos, const float4* vel, GridDev g, float4* posS,
@@ -373,15 +364,15 @@ void launch_rank_gather(int n, SortBuffers sb, const float4* pos, const float4* 
     const int grid = (n + 255) / 256;
     if (sb.scenes)
         k_rank_gather<true, false><<<grid, 256, 0, s>>>(n, sb.sortedHash, sb.cellOffset, sb.tmpIds, pos, vel, g,
-                                                        sb.scenes, sb.sortedIds, sb.workIds, sb.quarterCuts, posS,
+                                                        sb.scenes, sb.sortedIds, sb.workIds, sb.halfOffset, posS,
                                                         velS, sb.skip);
     else if (g.rel)
         k_rank_gather<false, true><<<grid, 256, 0, s>>>(n, sb.sortedHash, sb.cellOffset, sb.tmpIds, pos, vel, g,
-                                                        nullptr, sb.sortedIds, sb.workIds, sb.quarterCuts, posS, velS,
+                                                        nullptr, sb.sortedIds, sb.workIds, sb.halfOffset, posS, velS,
                                                         sb.skip);
     else
         k_rank_gather<false, false><<<grid, 256, 0, s>>>(n, sb.sortedHash, sb.cellOffset, sb.tmpIds, pos, vel, g,
-                                                         nullptr, sb.sortedIds, sb.workIds, sb.quarterCuts, posS,
+                                                         nullptr, sb.sortedIds, sb.workIds, sb.halfOffset, posS,
                                                          velS, sb.skip);
 }
 

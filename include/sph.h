@@ -495,7 +495,7 @@ typedef struct sph_tuning {
                           3: as 2, each warp's neighbour rows staged in shared
                           memory (plain handles; batched and cell-relative
                           handles run 2) */
-    int prune;         /* 1: cut stencil rows to the quarter-cells within reach of h */
+    int prune;         /* 1: cut stencil rows to the half-cells within reach of h */
     int kahan;         /* 1: compensated density and force sums */
 } sph_tuning;
 
