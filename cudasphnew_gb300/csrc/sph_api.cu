@@ -779,9 +779,10 @@ sph_status sph_read(sph_handle s, int field, void* dst, size_t bytes) {
     }
     if (bytes < need) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "destination too small");
     cudaStream_t q = s->stream;
-    // page-locked destinations are written by the kernels themselves
-    float* direct = static_cast<float*>(host_device_ptr(dst));
-    float* out = direct ? direct : s->staging;
+    // the fields are packed in device memory and copied back by one DMA copy:
+    // faster than kernels writing a page-locked destination over the host
+    // link (12 MB: 87 against 95 us)
+    float* out = s->staging;
     switch (field) {
         case SPH_FIELD_VERTEX_DATA:
             if (s->O.cellRelative) launch_rel_to_abs(n, s->pos, grid_of(s), out, 3, nullptr, q);
@@ -809,7 +810,7 @@ sph_status sph_read(sph_handle s, int field, void* dst, size_t bytes) {
             break;
     }
     SPH_CUDA(cudaGetLastError());
-    if (!direct) SPH_CUDA(cudaMemcpyAsync(dst, s->staging, need, cudaMemcpyDeviceToHost, q));
+    SPH_CUDA(cudaMemcpyAsync(dst, s->staging, need, cudaMemcpyDeviceToHost, q));
     // one synchronisation: the status word comes back with the data
     SPH_CUDA(cudaMemcpyAsync(s->statusHost, s->status, sizeof(unsigned int), cudaMemcpyDeviceToHost, q));
     SPH_CUDA(cudaStreamSynchronize(q));

@@ -266,9 +266,9 @@ sph_status sph_synchronize(sph_handle h);
 
 /* Copies a field to host memory (GetParticleState, SaveParticleInfo,
  * :2238-2243, :2785-2852).  `bytes` must be at least the field's size.
- * Returns when the data is in place.  A page-locked destination (pinned or
- * registered) is written by the gathering kernel itself over the host link;
- * pageable memory goes through a device staging buffer. */
+ * Returns when the data is in place.  The field is gathered into a device
+ * staging buffer and copied back by one DMA copy (the fastest route to a
+ * page-locked destination as well). */
 sph_status sph_read(sph_handle h, int field, void* dst, size_t bytes);
 
 /* Overwrites a field from host memory (SPH_FIELD_VERTEX_DATA,
