@@ -248,62 +248,57 @@ __global__ void __launch_bounds__(TS_BLOCK) k_ts_count(int n, TwoScaleDev T) {
     if (threadIdx.x < 3) T.blockCounts[3 * blockIdx.x + threadIdx.x] = s_cnt[threadIdx.x];
 }
 
-// Exclusive scan of the per-block counts (one block, looping), totals into
-// the device counters.
-__global__ void __launch_bounds__(TS_BLOCK) k_ts_scan_blocks(int nb, TwoScaleDev T) {
+// collect_ids (:1118-1162): id lists, and the child list -- split children
+// first, then boundary children, 8 consecutive slots per parent.  Each block
+// adds up the class counts of the blocks before it (and the split total, the
+// boundary children's base) from k_ts_count's table itself, so no separate
+// scan launch is needed; the last block writes the totals to the device
+// counters.  listBase[i] is particle i's first child-list position (-1 for a
+// default particle), for the child seeding that hashes the children next.
+__global__ void __launch_bounds__(TS_BLOCK) k_ts_lists(int n, TwoScaleDev T) {
     __shared__ int s_warp[3][TS_BLOCK / 32];
-    __shared__ int s_carry[3];
+    __shared__ int s_red[4][TS_BLOCK / 32];
+    __shared__ int s_base[4];  // split, boundary, default before this block; split total
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (threadIdx.x < 3) s_carry[threadIdx.x] = 0;
-    __syncthreads();
-    for (int base = 0; base < nb; base += TS_BLOCK) {
-        const int b = base + threadIdx.x;
-        int x[3], incl[3];
-        for (int c = 0; c < 3; c++) {
-            x[c] = b < nb ? T.blockCounts[3 * b + c] : 0;
-            incl[c] = x[c];
-            for (int o = 1; o < 32; o <<= 1) {
-                int t = __shfl_up_sync(0xffffffffu, incl[c], o);
-                if (lane >= o) incl[c] += t;
+    const int nb = gridDim.x;
+    {
+        int v[4] = {0, 0, 0, 0};
+        for (int b = threadIdx.x; b < nb; b += TS_BLOCK) {
+            const int c0 = T.blockCounts[3 * b], c1 = T.blockCounts[3 * b + 1], c2 = T.blockCounts[3 * b + 2];
+            if (b < (int)blockIdx.x) {
+                v[0] += c0;
+                v[1] += c1;
+                v[2] += c2;
             }
-            if (lane == 31) s_warp[c][warp] = incl[c];
+            v[3] += c0;
+        }
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v[c] += __shfl_xor_sync(0xffffffffu, v[c], o);
+            if (lane == 0) s_red[c][warp] = v[c];
         }
         __syncthreads();
         if (warp == 0) {
-            for (int c = 0; c < 3; c++) {
-                int w = s_warp[c][lane];
-                for (int o = 1; o < 32; o <<= 1) {
-                    int t = __shfl_up_sync(0xffffffffu, w, o);
-                    if (lane >= o) w += t;
-                }
-                s_warp[c][lane] = w;
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+                int w = s_red[c][lane];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) w += __shfl_xor_sync(0xffffffffu, w, o);
+                if (lane == 0) s_base[c] = w;
             }
         }
         __syncthreads();
-        int excl[3];
-        for (int c = 0; c < 3; c++) {
-            excl[c] = s_carry[c] + (warp > 0 ? s_warp[c][warp - 1] : 0) + incl[c] - x[c];
-            if (b < nb) T.blockOffsets[3 * b + c] = excl[c];
-        }
-        __syncthreads();
-        if (threadIdx.x == TS_BLOCK - 1)
-            for (int c = 0; c < 3; c++) s_carry[c] = excl[c] + x[c];
-        __syncthreads();
     }
-    if (threadIdx.x == 0) {
-        T.counts[0] = s_carry[0];
-        T.counts[1] = s_carry[1];
-        T.counts[2] = s_carry[2];
-        T.counts[3] = 8 * (s_carry[0] + s_carry[1]);
+    if (blockIdx.x == nb - 1 && threadIdx.x == 0) {
+        const int tot[3] = {s_base[0] + T.blockCounts[3 * blockIdx.x], s_base[1] + T.blockCounts[3 * blockIdx.x + 1],
+                            s_base[2] + T.blockCounts[3 * blockIdx.x + 2]};
+        T.counts[0] = tot[0];
+        T.counts[1] = tot[1];
+        T.counts[2] = tot[2];
+        T.counts[3] = 8 * (tot[0] + tot[1]);
         T.counts[4] = 0;  // the marking has read the split list: empty for the next step
     }
-}
-
-// collect_ids (:1118-1162): id lists, and the child list -- split children
-// first, then boundary children, 8 consecutive slots per parent.
-__global__ void __launch_bounds__(TS_BLOCK) k_ts_lists(int n, TwoScaleDev T) {
-    __shared__ int s_warp[3][TS_BLOCK / 32];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int i = blockIdx.x * TS_BLOCK + threadIdx.x;
     const int cls = i < n ? ts_class(T.state[i]) : -1;
     int rank[3];
@@ -326,17 +321,34 @@ __global__ void __launch_bounds__(TS_BLOCK) k_ts_lists(int n, TwoScaleDev T) {
     }
     __syncthreads();
     if (cls < 0) return;
-    const int r = T.blockOffsets[3 * blockIdx.x + cls] + s_warp[cls][warp] + rank[cls];
+    const int r = s_base[cls] + s_warp[cls][warp] + rank[cls];
     if (cls == 0) {
         T.splitIds[r] = i;
         for (int k = 0; k < 8; k++) T.subIds[8 * r + k] = 8 * i + k;
+        T.listBase[i] = 8 * r;
     } else if (cls == 1) {
         T.boundaryIds[r] = i;
-        const int base = 8 * (T.counts[0] + r);
+        const int base = 8 * (s_base[3] + r);
         for (int k = 0; k < 8; k++) T.subIds[base + k] = 8 * i + k;
+        T.listBase[i] = base;
     } else {
         T.defaultIds[r] = i;
+        T.listBase[i] = -1;
     }
+}
+
+// compute_sub_particle_hash (:121-153) of the child at list position idx,
+// with its arrival slot in its fine cell (the counting sort's first stage).
+__device__ __forceinline__ void hash_child(float4 x, const GridDev& sg, const TwoScaleDev& T, int idx,
+                                           unsigned int* status) {
+    bool outside = false;
+    if (!(isfinite(x.x) && isfinite(x.y) && isfinite(x.z))) {
+        atomicOr(status, STATUS_NON_FINITE);
+        x = make_float4(sg.origin[0], sg.origin[1], sg.origin[2], 0.f);
+    }
+    const int h = particle_hash(x, sg, &outside);
+    if (outside) atomicOr(status, STATUS_OUT_OF_DOMAIN);
+    T.subKeySlot[idx] = make_int2(h, atomicAdd(T.subCnt + h, 1));
 }
 
 // ---------------------------------------------------------------------------
@@ -354,11 +366,16 @@ __global__ void __launch_bounds__(TS_BLOCK) k_ts_lists(int n, TwoScaleDev T) {
 // which seeding and projection read -- and is integrated and collided again
 // from there with the acceleration the force stage computed at its own
 // position.
+//
+// Every child of a split or boundary parent (seeded now or kept) is then
+// hashed on the fine grid at its list position, so the fine level's sort
+// starts from the cell scan.
 // ---------------------------------------------------------------------------
 __global__ void k_ts_children(int n, float4* __restrict__ posS, float4* __restrict__ velS,
                               const float4* __restrict__ accS, const float4* __restrict__ rho4S,
                               const int* __restrict__ workIds, float mass, PhysDev ph, int collideFlag,
-                              float4* __restrict__ pos, float4* __restrict__ vel, TwoScaleDev T) {
+                              float4* __restrict__ pos, float4* __restrict__ vel, GridDev sg, unsigned int* status,
+                              TwoScaleDev T) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const int id = workIds[k];
@@ -388,8 +405,13 @@ __global__ void k_ts_children(int n, float4* __restrict__ posS, float4* __restri
         vel[id] = make_float4(v.x, v.y, v.z, 0.f);
     }
     if ((code & 3u) == 0) return;
+    const int base = T.listBase[id];
     // childMode 1: seed only on a class change (:1052-1055)
-    if (T.childMode == 1 && was == now) return;
+    if (T.childMode == 1 && was == now) {
+#pragma unroll
+        for (int c = 0; c < 8; c++) hash_child(T.subPos[8 * (size_t)id + c], sg, T, base + c, status);
+        return;
+    }
     const double rad = (double)(3.0f * mass) / (4.0 * 3.14159265358979323846 * (double)rho4S[k].x);
     const float radicand = (float)rad;
     const float radius = (float)pow((double)radicand, (double)(1.0f / 3.0f));
@@ -399,9 +421,11 @@ __global__ void k_ts_children(int n, float4* __restrict__ posS, float4* __restri
     for (int c = 0; c < 8; c++) {
         const float sx = (c & 4) ? -d : d, sy = (c & 2) ? -d : d, sz = (c & 1) ? -d : d;
         const size_t slot = 8 * (size_t)id + c;
-        T.subPos[slot] = make_float4(__fmaf_rn(sx, radius, x.x), __fmaf_rn(sy, radius, x.y),
-                                     __fmaf_rn(sz, radius, x.z), 0.f);
+        const float4 xc = make_float4(__fmaf_rn(sx, radius, x.x), __fmaf_rn(sy, radius, x.y),
+                                      __fmaf_rn(sz, radius, x.z), 0.f);
+        T.subPos[slot] = xc;
         T.subVel[slot] = make_float4(v.x, v.y, v.z, 0.f);
+        hash_child(xc, sg, T, base + c, status);
     }
 }
 
@@ -464,19 +488,11 @@ __global__ void __launch_bounds__(TS_WARP_BLOCK) k_ts_project(const float4* __re
 // The fine level's sort: compute_sub_particle_hash (:121-153) over the child
 // list, then the same counting sort as the coarse level, stable in list order.
 // ---------------------------------------------------------------------------
+// The sub-only step hashes the children of the current lists on its own.
 __global__ void k_ts_subhash(GridDev g, TwoScaleDev T, unsigned int* status) {
     const int nSub = T.counts[3];
-    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < nSub; idx += gridDim.x * blockDim.x) {
-        float4 x = T.subPos[T.subIds[idx]];
-        bool outside = false;
-        if (!(isfinite(x.x) && isfinite(x.y) && isfinite(x.z))) {
-            atomicOr(status, STATUS_NON_FINITE);
-            x = make_float4(g.origin[0], g.origin[1], g.origin[2], 0.f);
-        }
-        const int h = particle_hash(x, g, &outside);
-        if (outside) atomicOr(status, STATUS_OUT_OF_DOMAIN);
-        T.subKeySlot[idx] = make_int2(h, atomicAdd(T.subCnt + h, 1));
-    }
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < nSub; idx += gridDim.x * blockDim.x)
+        hash_child(T.subPos[T.subIds[idx]], g, T, idx, status);
 }
 
 __global__ void k_ts_subscatter(TwoScaleDev T) {
@@ -713,16 +729,15 @@ void launch_ts_states(int n, const float4* posS, const int* workIds, const int* 
     k_ts_mark<<<warp_grid(n), TS_WARP_BLOCK, 0, s>>>(posS, workIds, cellOffset, g, h, T);
     const int nb = (n + TS_BLOCK - 1) / TS_BLOCK;
     k_ts_count<<<nb, TS_BLOCK, 0, s>>>(n, T);
-    k_ts_scan_blocks<<<1, TS_BLOCK, 0, s>>>(nb, T);
     k_ts_lists<<<nb, TS_BLOCK, 0, s>>>(n, T);
 }
 
 void launch_ts_children(int n, float4* posS, float4* velS, const float4* accS, const float4* rho4S,
                         const int* workIds, float mass, PhysDev ph, int collide, float4* pos, float4* vel,
-                        const TwoScaleDev& T, cudaStream_t s) {
+                        GridDev sg, unsigned int* status, const TwoScaleDev& T, cudaStream_t s) {
     if (n <= 0) return;
     k_ts_children<<<(n + 127) / 128, 128, 0, s>>>(n, posS, velS, accS, rho4S, workIds, mass, ph, collide, pos, vel,
-                                                  T);
+                                                  sg, status, T);
 }
 
 void launch_ts_project(const float4* coarsePos, const int* workIds, int byId, const float4* rho4S,
@@ -733,8 +748,8 @@ void launch_ts_project(const float4* coarsePos, const int* workIds, int byId, co
 }
 
 void launch_ts_sub_sort(GridDev sg, const TwoScaleDev& T, SortBuffers subSb, int capacity, unsigned int* status,
-                        cudaStream_t s) {
-    k_ts_subhash<<<stride_grid(capacity, 256), 256, 0, s>>>(sg, T, status);
+                        bool hashed, cudaStream_t s) {
+    if (!hashed) k_ts_subhash<<<stride_grid(capacity, 256), 256, 0, s>>>(sg, T, status);
     launch_cell_scan(sg.numCells, subSb, status, s);
     k_ts_subscatter<<<stride_grid(capacity, 256), 256, 0, s>>>(T);
     k_ts_subrank<<<stride_grid(capacity, 256), 256, 0, s>>>(T);
