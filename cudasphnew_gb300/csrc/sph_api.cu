@@ -169,7 +169,7 @@ void free_all(sph_sim* s) {
                     s->scenesDev, s->reuse};
     for (void* p : ptrs)
         if (p) cudaFree(p);
-    void* tsPtrs[] = {s->ts.state,     s->ts.blockCounts, s->ts.listBase, s->ts.counts,
+    void* tsPtrs[] = {s->ts.state,     s->ts.blockCounts, s->ts.counts,
                       s->ts.splitIds,  s->ts.boundaryIds, s->ts.defaultIds,  s->ts.subIds,
                       s->ts.subPos,    s->ts.subVel,      s->ts.subAcc,      s->ts.subRho,
                       s->ts.subCnt,    s->ts.subOffset,   s->ts.subKeySlot,  s->ts.subTmp,
@@ -208,7 +208,6 @@ sph_status ensure_two_scale(sph_sim* s) {
     TwoScaleDev& T = s->ts;
     SPH_CUDA(dalloc(&T.state, n4));
     SPH_CUDA(dalloc(&T.blockCounts, 3 * nb));
-    SPH_CUDA(dalloc(&T.listBase, n));
     SPH_CUDA(dalloc(&T.counts, 5));
     SPH_CUDA(dalloc(&T.markList, n));
     SPH_CUDA(dalloc(&T.splitIds, n));
@@ -310,7 +309,7 @@ void enqueue_step(sph_sim* s, int mode, bool timing) {
         const int cap = 8 * s->n;
         GridDev sg = make_grid(s->P, true);
         PhysDev sph = make_sub_phys(s->P, s->O);
-        launch_ts_sub_sort(sg, s->ts, s->subSb, cap, s->status, false, st);
+        launch_ts_sub_sort(sg, s->ts, s->subSb, cap, s->status, st);
         launch_ts_sub_density(sg, sph, s->ts, cap, st);
         if (s->stepped)
             launch_ts_project(s->pos, s->sb.workIds, 1, s->rho4S, s->sb.cellOffset, make_grid(s->P, false),
@@ -336,16 +335,16 @@ void enqueue_step(sph_sim* s, int mode, bool timing) {
         // computeParticleState, collect, initializeSubParticles, projectQuantities
         // (:2157-2160) from the pre-integration sorted state, which the force
         // stage leaves as it was (it writes the new state in particle order)
-        const GridDev sg = make_grid(s->P, true);
         launch_ts_states(n, s->posS, s->sb.workIds, s->sb.cellOffset, g, s->P.compactSupport, s->ts, st);
         launch_ts_children(n, s->posS, s->velS, s->accS, s->rho4S, s->sb.workIds, s->P.particleMass, ph, collide,
-                           s->pos, s->vel, sg, s->status, s->ts, st);
+                           s->pos, s->vel, s->ts, st);
         launch_ts_project(s->posS, s->sb.workIds, 0, s->rho4S, s->sb.cellOffset, g, s->P.compactSupportSub,
                           s->ts, 8 * n, st);
-        // the fine level (:2162-2171); the children were hashed with their seeding
+        // the fine level (:2162-2171)
         const int cap = 8 * n;
+        const GridDev sg = make_grid(s->P, true);
         PhysDev sph = make_sub_phys(s->P, s->O);
-        launch_ts_sub_sort(sg, s->ts, s->subSb, cap, s->status, true, st);
+        launch_ts_sub_sort(sg, s->ts, s->subSb, cap, s->status, st);
         launch_ts_sub_density(sg, sph, s->ts, cap, st);
         launch_ts_sub_force(sg, sph, s->ts, cap, st);
     }

@@ -94,7 +94,6 @@ struct SortBuffers {
 struct TwoScaleDev {
     unsigned char* state;       // [n rounded up to 4] 2-bit history per particle
     int* blockCounts;           // [3 * blocks] per-block class counts
-    int* listBase;              // [n] first child-list position of each particle, -1 if default
     int* counts;                // [5] split, boundary, default, children (device side); [4]: length
                                 //     of markList, zero between steps
     int* markList;              // [n] working-order indices of split particles, any order
@@ -202,16 +201,14 @@ void launch_cell_tables(int numCells, const int* cellOffset, int* start, int* en
 // Two-scale pass (sph_twoscale.cu).
 void launch_ts_states(int n, const float4* posS, const int* workIds, const int* cellOffset, GridDev g, float h,
                       const TwoScaleDev& T, cudaStream_t s);
-// Merge-back, child seeding and the children's fine-grid hash (the sort's
-// first stage; launch_ts_sub_sort then runs with hashed = true).
 void launch_ts_children(int n, float4* posS, float4* velS, const float4* accS, const float4* rho4S,
                         const int* workIds, float mass, PhysDev ph, int collide, float4* pos, float4* vel,
-                        GridDev sg, unsigned int* status, const TwoScaleDev& T, cudaStream_t s);
+                        const TwoScaleDev& T, cudaStream_t s);
 void launch_ts_project(const float4* coarsePos, const int* workIds, int byId, const float4* rho4S,
                        const int* cellOffset, GridDev g, float hs, const TwoScaleDev& T, int capacity,
                        cudaStream_t s);
 void launch_ts_sub_sort(GridDev sg, const TwoScaleDev& T, SortBuffers subSb, int capacity, unsigned int* status,
-                        bool hashed, cudaStream_t s);
+                        cudaStream_t s);
 void launch_ts_sub_density(GridDev sg, PhysDev sph, const TwoScaleDev& T, int capacity, cudaStream_t s);
 void launch_ts_sub_force(GridDev sg, PhysDev sph, const TwoScaleDev& T, int capacity, cudaStream_t s);
 void launch_ts_pack_sd(const TwoScaleDev& T, int slots, float* dst, cudaStream_t s);

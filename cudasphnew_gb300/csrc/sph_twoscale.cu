@@ -253,8 +253,7 @@ __global__ void __launch_bounds__(TS_BLOCK) k_ts_count(int n, TwoScaleDev T) {
 // adds up the class counts of the blocks before it (and the split total, the
 // boundary children's base) from k_ts_count's table itself, so no separate
 // scan launch is needed; the last block writes the totals to the device
-// counters.  listBase[i] is particle i's first child-list position (-1 for a
-// default particle), for the child seeding that hashes the children next.
+// counters.
 __global__ void __launch_bounds__(TS_BLOCK) k_ts_lists(int n, TwoScaleDev T) {
     __shared__ int s_warp[3][TS_BLOCK / 32];
     __shared__ int s_red[4][TS_BLOCK / 32];
@@ -325,15 +324,12 @@ __global__ void __launch_bounds__(TS_BLOCK) k_ts_lists(int n, TwoScaleDev T) {
     if (cls == 0) {
         T.splitIds[r] = i;
         for (int k = 0; k < 8; k++) T.subIds[8 * r + k] = 8 * i + k;
-        T.listBase[i] = 8 * r;
     } else if (cls == 1) {
         T.boundaryIds[r] = i;
         const int base = 8 * (s_base[3] + r);
         for (int k = 0; k < 8; k++) T.subIds[base + k] = 8 * i + k;
-        T.listBase[i] = base;
     } else {
         T.defaultIds[r] = i;
-        T.listBase[i] = -1;
     }
 }
 
@@ -366,16 +362,11 @@ __device__ __forceinline__ void hash_child(float4 x, const GridDev& sg, const Tw
 // which seeding and projection read -- and is integrated and collided again
 // from there with the acceleration the force stage computed at its own
 // position.
-//
-// Every child of a split or boundary parent (seeded now or kept) is then
-// hashed on the fine grid at its list position, so the fine level's sort
-// starts from the cell scan.
 // ---------------------------------------------------------------------------
 __global__ void k_ts_children(int n, float4* __restrict__ posS, float4* __restrict__ velS,
                               const float4* __restrict__ accS, const float4* __restrict__ rho4S,
                               const int* __restrict__ workIds, float mass, PhysDev ph, int collideFlag,
-                              float4* __restrict__ pos, float4* __restrict__ vel, GridDev sg, unsigned int* status,
-                              TwoScaleDev T) {
+                              float4* __restrict__ pos, float4* __restrict__ vel, TwoScaleDev T) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const int id = workIds[k];
@@ -405,13 +396,8 @@ __global__ void k_ts_children(int n, float4* __restrict__ posS, float4* __restri
         vel[id] = make_float4(v.x, v.y, v.z, 0.f);
     }
     if ((code & 3u) == 0) return;
-    const int base = T.listBase[id];
     // childMode 1: seed only on a class change (:1052-1055)
-    if (T.childMode == 1 && was == now) {
-#pragma unroll
-        for (int c = 0; c < 8; c++) hash_child(T.subPos[8 * (size_t)id + c], sg, T, base + c, status);
-        return;
-    }
+    if (T.childMode == 1 && was == now) return;
     const double rad = (double)(3.0f * mass) / (4.0 * 3.14159265358979323846 * (double)rho4S[k].x);
     const float radicand = (float)rad;
     const float radius = (float)pow((double)radicand, (double)(1.0f / 3.0f));
@@ -421,11 +407,9 @@ __global__ void k_ts_children(int n, float4* __restrict__ posS, float4* __restri
     for (int c = 0; c < 8; c++) {
         const float sx = (c & 4) ? -d : d, sy = (c & 2) ? -d : d, sz = (c & 1) ? -d : d;
         const size_t slot = 8 * (size_t)id + c;
-        const float4 xc = make_float4(__fmaf_rn(sx, radius, x.x), __fmaf_rn(sy, radius, x.y),
-                                      __fmaf_rn(sz, radius, x.z), 0.f);
-        T.subPos[slot] = xc;
+        T.subPos[slot] = make_float4(__fmaf_rn(sx, radius, x.x), __fmaf_rn(sy, radius, x.y),
+                                     __fmaf_rn(sz, radius, x.z), 0.f);
         T.subVel[slot] = make_float4(v.x, v.y, v.z, 0.f);
-        hash_child(xc, sg, T, base + c, status);
     }
 }
 
@@ -488,7 +472,6 @@ __global__ void __launch_bounds__(TS_WARP_BLOCK) k_ts_project(const float4* __re
 // The fine level's sort: compute_sub_particle_hash (:121-153) over the child
 // list, then the same counting sort as the coarse level, stable in list order.
 // ---------------------------------------------------------------------------
-// The sub-only step hashes the children of the current lists on its own.
 __global__ void k_ts_subhash(GridDev g, TwoScaleDev T, unsigned int* status) {
     const int nSub = T.counts[3];
     for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < nSub; idx += gridDim.x * blockDim.x)
@@ -734,10 +717,10 @@ void launch_ts_states(int n, const float4* posS, const int* workIds, const int* 
 
 void launch_ts_children(int n, float4* posS, float4* velS, const float4* accS, const float4* rho4S,
                         const int* workIds, float mass, PhysDev ph, int collide, float4* pos, float4* vel,
-                        GridDev sg, unsigned int* status, const TwoScaleDev& T, cudaStream_t s) {
+                        const TwoScaleDev& T, cudaStream_t s) {
     if (n <= 0) return;
     k_ts_children<<<(n + 127) / 128, 128, 0, s>>>(n, posS, velS, accS, rho4S, workIds, mass, ph, collide, pos, vel,
-                                                  sg, status, T);
+                                                  T);
 }
 
 void launch_ts_project(const float4* coarsePos, const int* workIds, int byId, const float4* rho4S,
@@ -748,8 +731,8 @@ void launch_ts_project(const float4* coarsePos, const int* workIds, int byId, co
 }
 
 void launch_ts_sub_sort(GridDev sg, const TwoScaleDev& T, SortBuffers subSb, int capacity, unsigned int* status,
-                        bool hashed, cudaStream_t s) {
-    if (!hashed) k_ts_subhash<<<stride_grid(capacity, 256), 256, 0, s>>>(sg, T, status);
+                        cudaStream_t s) {
+    k_ts_subhash<<<stride_grid(capacity, 256), 256, 0, s>>>(sg, T, status);
     launch_cell_scan(sg.numCells, subSb, status, s);
     k_ts_subscatter<<<stride_grid(capacity, 256), 256, 0, s>>>(T);
     k_ts_subrank<<<stride_grid(capacity, 256), 256, 0, s>>>(T);
