@@ -346,7 +346,7 @@ sph_status sph_get_diagnostics(sph_handle h, sph_diagnostics* out);
  * weights and activations and FP32 accumulation on the tensor cores, corrects
  * one plain step of stride*dt (SPH_STEP_LEARNED) towards `stride` plain steps
  * of dt.  It is trained on the device from the plain solver's own trajectory.
- * The plain solver is the fallback and the judge: every auditInterval-th
+ * The plain solver is the fallback and the arbiter: every auditInterval-th
  * learned step is also run as `stride` plain steps from the same state, and
  * when the largest per-particle relative density difference between the two
  * results exceeds densityTolerance the plain result is kept (a rollback).

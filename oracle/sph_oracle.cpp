@@ -11,7 +11,7 @@
 //    R = float  : the reference's FP32 operation order ("ref32"), used for the
 //                 bit-exact integer outputs (hash, permutation, cell table) and
 //                 as the timed CPU baseline;
-//    R = double : the same formulas in FP64 ("oracle64"), used as the judge of
+//    R = double : the same formulas in FP64 ("oracle64"), used as the yardstick for
 //                 densities, pressures and accelerations, together with the
 //                 per-particle magnitude scales the tolerances are quoted on.
 //
