@@ -113,9 +113,10 @@ inline int warp_grid(long long items) {
 // fetches the bounds of its 9 stencil rows in one round (lane g row g, every
 // lane row 8) and walks the rows in order; within a row lane g takes
 // candidates start + g, + 8, ... (consecutive lanes read consecutive
-// addresses), TS_BATCH loads in flight.  Group sums use a fixed xor tree
+// addresses), TS_GBATCH loads in flight.  Group sums use a fixed xor tree
 // (every lane of the group ends with the same bits).
 constexpr int TS_G = 8;
+constexpr int TS_GBATCH = 4;
 
 inline int group_grid(long long items) { return warp_grid((items + 32 / TS_G - 1) / (32 / TS_G)); }
 
@@ -442,10 +443,10 @@ __global__ void __launch_bounds__(TS_WARP_BLOCK) k_ts_project(const float4* __re
         for (int r = 0; r < 9; r++) {
             int s0, e;
             group_row(R, r, s0, e);
-            for (int t = s0 + gl; t < e; t += TS_G * TS_BATCH) {
-                float4 xc[TS_BATCH], rc[TS_BATCH];
+            for (int t = s0 + gl; t < e; t += TS_G * TS_GBATCH) {
+                float4 xc[TS_GBATCH], rc[TS_GBATCH];
 #pragma unroll
-                for (int u = 0; u < TS_BATCH; u++) {
+                for (int u = 0; u < TS_GBATCH; u++) {
                     const int c = t + TS_G * u;
                     if (c < e) {
                         xc[u] = byId ? __ldg(coarsePos + __ldg(workIds + c)) : __ldg(coarsePos + c);
@@ -453,7 +454,7 @@ __global__ void __launch_bounds__(TS_WARP_BLOCK) k_ts_project(const float4* __re
                     }
                 }
 #pragma unroll
-                for (int u = 0; u < TS_BATCH; u++)
+                for (int u = 0; u < TS_GBATCH; u++)
                     if (t + TS_G * u < e && ref_r2(x, xc[u]) <= hs2) {
                         d += rc[u].x;
                         p += rc[u].y;
@@ -522,13 +523,13 @@ __global__ void __launch_bounds__(TS_WARP_BLOCK) k_ts_subdensity(GridDev g, Phys
             int s0, e;
             group_row(R, r, s0, e);
             float part = 0.f;
-            for (int t = s0 + gl; t < e; t += TS_G * TS_BATCH) {
-                float4 xc[TS_BATCH];
+            for (int t = s0 + gl; t < e; t += TS_G * TS_GBATCH) {
+                float4 xc[TS_GBATCH];
 #pragma unroll
-                for (int u = 0; u < TS_BATCH; u++)
+                for (int u = 0; u < TS_GBATCH; u++)
                     if (t + TS_G * u < e) xc[u] = __ldg(T.subPosS + t + TS_G * u);
 #pragma unroll
-                for (int u = 0; u < TS_BATCH; u++)
+                for (int u = 0; u < TS_GBATCH; u++)
                     if (t + TS_G * u < e) {
                         const float q = fmaxf(ph.h2 - dist2(x, xc[u]), 0.f);
                         part = fmaf(q * q, q, part);
@@ -562,9 +563,9 @@ __device__ __forceinline__ void integrate_child(const PhysDev& ph, const TwoScal
     T.subVel[slot] = make_float4(v.x, v.y, v.z, 0.f);
 }
 
-// Hit queue of one group: a round adds at most TS_G * TS_BATCH pairs to
+// Hit queue of one group: a round adds at most TS_G * TS_GBATCH pairs to
 // fewer than TS_G left over.
-constexpr int TS_QUEUE = TS_G * TS_BATCH + TS_G;
+constexpr int TS_QUEUE = TS_G * TS_GBATCH + TS_G;
 
 __global__ void __launch_bounds__(TS_WARP_BLOCK) k_ts_subforce(GridDev g, PhysDev ph, TwoScaleDev T) {
     __shared__ int s_queue[TS_WARP_BLOCK / TS_G][TS_QUEUE];
@@ -613,20 +614,20 @@ __global__ void __launch_bounds__(TS_WARP_BLOCK) k_ts_subforce(GridDev g, PhysDe
             cg[2] = fmaf(sc, dz, cg[2]);
             cl = fmaf(invj * d2, 3.f * ph.h2 - 7.f * r2, cl);
         };
-        // row by row, rounds of TS_BATCH candidates per lane: test and list
+        // row by row, rounds of TS_GBATCH candidates per lane: test and list
         // the hits in the group's queue; the group's lanes take the listed
         // pairs TS_G at a time
         int listed = 0;
         for (int r = 0; r < 9; r++) {
             int s0, e;
             group_row(R, r, s0, e);
-            for (int t = s0 + gl; __any_sync(0xffffffffu, t < e); t += TS_G * TS_BATCH) {
-                float4 xc[TS_BATCH];
+            for (int t = s0 + gl; __any_sync(0xffffffffu, t < e); t += TS_G * TS_GBATCH) {
+                float4 xc[TS_GBATCH];
 #pragma unroll
-                for (int u = 0; u < TS_BATCH; u++)
+                for (int u = 0; u < TS_GBATCH; u++)
                     if (t + TS_G * u < e) xc[u] = __ldg(T.subPosS + t + TS_G * u);
 #pragma unroll
-                for (int u = 0; u < TS_BATCH; u++) {
+                for (int u = 0; u < TS_GBATCH; u++) {
                     bool hit = false;
                     if (t + TS_G * u < e) {
                         const float r2 = dist2(xi, xc[u]);
