@@ -1,0 +1,71 @@
+"""CPU known-answer checks of the oracle's two-scale restatement (particle
+states, the three-way lists, the child list and the child seeding), against
+a numpy restatement of find_split_particles / find_boundary_particles /
+collect / initialize_sub_particles (particle_simulation.cu:932-1090,
+2509-2567) on a small lattice."""
+import numpy as np
+
+from cudasphnew_gb300 import scenes
+
+
+def ref_r2(a, b):
+    """r^2 as find_boundary_particles forms it: FP32 differences, products and
+    a left-to-right sum, each rounded."""
+    d = (a.astype(np.float32) - b.astype(np.float32)).astype(np.float32)
+    p = (d * d).astype(np.float32)
+    return ((p[..., 0] + p[..., 1]).astype(np.float32) + p[..., 2]).astype(np.float32)
+
+
+def run_first_pass(orc):
+    sc = scenes.two_scale(nb=12, region=(0.05, 0.1), box=0.5, name="two_scale_kat")
+    x0, v0 = sc.positions, sc.velocities
+    coarse = orc.step_plain(sc.params, sc.options, None, x0, v0)
+    T = orc.TwoScale(sc.n)
+    T.part(sc.params, sc.options, x0, v0, coarse["rho"], coarse["p"], coarse["ids"], coarse["start"],
+           coarse["end"])
+    return sc, x0, v0, coarse, T
+
+
+def test_states_and_lists(orc):
+    sc, x0, _, _, T = run_first_pass(orc)
+    lo, hi = np.float32(sc.options.splitMin[0]), np.float32(sc.options.splitMax[0])
+    split = np.all((x0 >= lo) & (x0 <= hi), axis=1)
+    h2 = np.float32(sc.params.compactSupport) * np.float32(sc.params.compactSupport)
+    near = (ref_r2(x0[:, None, :], x0[None, split, :]) <= h2).any(axis=1)
+    assert 0 < split.sum() < near.sum() < sc.n
+    # first step from the zero history: split particles also mark themselves
+    want_state = np.where(split, 3, np.where(near, 2, 0)).astype(np.uint8)
+    np.testing.assert_array_equal(T.get("state"), want_state)
+    ids = np.arange(sc.n)
+    np.testing.assert_array_equal(T.get("split"), ids[split])
+    np.testing.assert_array_equal(T.get("boundary"), ids[near & ~split])
+    np.testing.assert_array_equal(T.get("default"), ids[~near])
+    parents = np.concatenate([ids[split], ids[near & ~split]])
+    np.testing.assert_array_equal(T.get("sub_ids"), (8 * parents[:, None] + np.arange(8)).ravel())
+    c = T.counts()
+    assert (c["split"], c["boundary"], c["sub"]) == (split.sum(), (near & ~split).sum(), 8 * len(parents))
+
+
+def test_child_seeding_geometry(orc):
+    sc, x0, v0, coarse, T = run_first_pass(orc)
+    parents = np.concatenate([T.get("split"), T.get("boundary")])
+    m = np.float32(sc.params.particleMass)
+    rho = coarse["rho"][parents].astype(np.float64)
+    # radius (3m / (4 pi rho))^(1/3): 3m in float, the quotient in double,
+    # the radicand rounded to float once
+    three_m = float(np.float32(3.0) * m)
+    radicand = (three_m / (4.0 * np.pi * rho)).astype(np.float32)
+    radius = np.cbrt(radicand.astype(np.float64)).astype(np.float32)
+    signs = np.array([[1 - 2 * ((c >> 2) & 1), 1 - 2 * ((c >> 1) & 1), 1 - 2 * (c & 1)] for c in range(8)],
+                     np.float64)
+    d = float(np.float32(0.577350269))
+    seeded = x0[parents][:, None, :].astype(np.float64) + signs[None] * d * radius[:, None, None]
+    got = T.get("sub_pos").reshape(sc.n, 8, 3)[parents].astype(np.float64)
+    # the fine step has already moved the children by dt_sub (v + dt_sub a)
+    # from rest: far below a micrometre against a radius of ~8 mm
+    assert np.abs(got - seeded).max() < 2e-6
+    assert radius.min() > 0.007 and radius.max() < 0.009
+    # every child keeps its parent's start velocity plus one fine-step kick
+    vel = T.get("sub_vel").reshape(sc.n, 8, 3)[parents]
+    kick = float(sc.params.timeStepSubParticles) * 1e3
+    assert np.abs(vel - v0[parents][:, None, :]).max() < kick
