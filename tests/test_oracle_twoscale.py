@@ -1,7 +1,8 @@
 """CPU known-answer checks of the oracle's two-scale restatement (particle
-states, the three-way lists, the child list and the child seeding), against
-a numpy restatement of find_split_particles / find_boundary_particles /
-collect / initialize_sub_particles (particle_simulation.cu:932-1090,
+states, the three-way lists, the child list, the child seeding and the
+projection), against a numpy restatement of find_split_particles /
+find_boundary_particles / collect / initialize_sub_particles /
+project_quantities (particle_simulation.cu:570-622, 932-1090, 1328-1381,
 2509-2567) on a small lattice."""
 import numpy as np
 
@@ -69,3 +70,35 @@ def test_child_seeding_geometry(orc):
     vel = T.get("sub_vel").reshape(sc.n, 8, 3)[parents]
     kick = float(sc.params.timeStepSubParticles) * 1e3
     assert np.abs(vel - v0[parents][:, None, :]).max() < kick
+
+
+def test_projection_means(orc):
+    """project_quantities (:570-622, 1328-1381): a boundary child takes the
+    unweighted mean coarse density and pressure of the coarse particles within
+    compactSupportSub of its seeded position."""
+    sc, x0, _, coarse, T = run_first_pass(orc)
+    bnd = T.get("boundary")
+    m = np.float32(sc.params.particleMass)
+    rho = coarse["rho"][bnd].astype(np.float64)
+    radicand = (float(np.float32(3.0) * m) / (4.0 * np.pi * rho)).astype(np.float32)
+    radius = np.cbrt(radicand.astype(np.float64)).astype(np.float32).astype(np.float64)
+    d = float(np.float32(0.577350269))
+    signs = np.array([[1 - 2 * ((c >> 2) & 1), 1 - 2 * ((c >> 1) & 1), 1 - 2 * (c & 1)] for c in range(8)],
+                     np.float64)
+    seeded = (x0[bnd][:, None, :].astype(np.float64) + signs[None] * d * radius[:, None, None]).astype(np.float32)
+    seeded = seeded.reshape(-1, 3)
+    hs = np.float32(sc.params.compactSupportSub)
+    r2 = ref_r2(seeded[:, None, :], x0[None, :, :]).astype(np.float64)
+    inside = r2 <= float(hs * hs)
+    # children with a coarse particle within a relative 1e-5 of the cut are
+    # left out: the seeded position above is a double-rounded restatement
+    clear = ~(np.abs(r2 - float(hs * hs)) <= 1e-5 * float(hs * hs)).any(axis=1)
+    cnt = inside.sum(axis=1)
+    sel = clear & (cnt > 0)
+    assert sel.sum() > 0.9 * len(sel)
+    mean_rho = (inside * coarse["rho"][None, :].astype(np.float64)).sum(1) / np.maximum(cnt, 1)
+    mean_p = (inside * coarse["p"][None, :].astype(np.float64)).sum(1) / np.maximum(cnt, 1)
+    slots = (8 * bnd[:, None] + np.arange(8)).ravel()
+    got_rho, got_p = T.get("sub_rho")[slots], T.get("sub_p")[slots]
+    np.testing.assert_allclose(got_rho[sel], mean_rho[sel], rtol=1e-5)
+    np.testing.assert_allclose(got_p[sel], mean_p[sel], rtol=1e-4, atol=1e-3)
