@@ -1,9 +1,10 @@
 """CPU known-answer checks of the oracle's two-scale restatement (particle
-states, the three-way lists, the child list, the child seeding and the
-projection), against a numpy restatement of find_split_particles /
-find_boundary_particles / collect / initialize_sub_particles /
-project_quantities (particle_simulation.cu:570-622, 932-1090, 1328-1381,
-2509-2567) on a small lattice."""
+states, the three-way lists, the child list, the child seeding, the
+projection and the fine density), against a numpy restatement of
+find_split_particles / find_boundary_particles / collect /
+initialize_sub_particles / project_quantities /
+compute_sub_particle_density_pressure (particle_simulation.cu:259-313,
+570-622, 932-1090, 1328-1381, 2509-2567) on a small lattice."""
 import numpy as np
 
 from cudasphnew_gb300 import scenes
@@ -102,3 +103,34 @@ def test_projection_means(orc):
     got_rho, got_p = T.get("sub_rho")[slots], T.get("sub_p")[slots]
     np.testing.assert_allclose(got_rho[sel], mean_rho[sel], rtol=1e-5)
     np.testing.assert_allclose(got_p[sel], mean_p[sel], rtol=1e-4, atol=1e-3)
+
+
+def test_fine_density_of_regular_children(orc):
+    """compute_sub_particle_density_pressure (:259-313): a regular child's
+    density is (m/8) poly6_sub sum (h_s^2 - r^2)^3 over every child (regular
+    and boundary) within h_s, itself included; checked on the FP64 oracle
+    against a brute-force sum over the seeded children."""
+    sc = scenes.two_scale(nb=12, region=(0.05, 0.1), box=0.5, name="two_scale_kat")
+    x0, v0 = sc.positions, sc.velocities
+    coarse = orc.step_plain(sc.params, sc.options, None, x0, v0, fp64=True)
+    T = orc.TwoScale(sc.n, fp64=True)
+    T.part(sc.params, sc.options, x0, v0, coarse["rho"], coarse["p"], coarse["ids"], coarse["start"],
+           coarse["end"])
+    split, bnd = T.get("split"), T.get("boundary")
+    parents = np.concatenate([split, bnd])
+    m = float(np.float32(sc.params.particleMass))
+    rho = coarse["rho"][parents].astype(np.float64)
+    radius = np.cbrt(3.0 * m / (4.0 * np.pi * rho))
+    d = 0.577350269
+    signs = np.array([[1 - 2 * ((c >> 2) & 1), 1 - 2 * ((c >> 1) & 1), 1 - 2 * (c & 1)] for c in range(8)],
+                     np.float64)
+    kids = (x0[parents][:, None, :].astype(np.float64) + signs[None] * d * radius[:, None, None]).reshape(-1, 3)
+    hs = float(sc.params.compactSupportSub)
+    nreg = 8 * len(split)
+    r2 = ((kids[:nreg, None, :] - kids[None, :, :]) ** 2).sum(-1)
+    w = np.clip(hs * hs - r2, 0.0, None) ** 3
+    want = float(sc.params.subParticleMass) * float(sc.params.poly6Sub) * w.sum(1)
+    slots = (8 * split[:, None] + np.arange(8)).ravel()
+    got = T.get("sub_rho")[slots]
+    np.testing.assert_allclose(got, want, rtol=1e-5)
+    assert want.min() > 0.5 * float(sc.params.restDensity)
