@@ -4,7 +4,8 @@ projection and the fine density), against a numpy restatement of
 find_split_particles / find_boundary_particles / collect /
 initialize_sub_particles / project_quantities /
 compute_sub_particle_density_pressure (particle_simulation.cu:259-313,
-570-622, 932-1090, 1328-1381, 2509-2567) on a small lattice."""
+570-622, 932-1090, 1328-1381, 2509-2567) on a small lattice, and the
+merge-back of persistent children."""
 import numpy as np
 
 from cudasphnew_gb300 import scenes
@@ -175,3 +176,34 @@ def test_fine_acceleration_of_regular_children(orc):
     scale = np.abs(acc).max() + float(P_.gravity)
     assert np.abs(got - acc).max() <= 1e-9 * scale
     assert np.abs(acc[:, :2]).max() > 1.0  # the pair terms are there, not just gravity
+
+
+def test_merge_back_takes_the_childrens_mean(orc):
+    """childMode 1 (no reference counterpart): a parent leaving the split
+    class takes its eight children's mean position and velocity (slot order,
+    times 1/8) and is integrated from there with the acceleration computed at
+    its own position (symplectic Euler, away from the walls)."""
+    sc = scenes.two_scale(nb=12, region=(0.056, 0.1), box=0.5, name="two_scale_merge_kat")
+    sc.options.childMode = 1
+    sc.velocities[:, 2] = -1.0
+    T = orc.TwoScale(sc.n, fp64=True)
+    x, v = sc.positions.astype(np.float64), sc.velocities.astype(np.float64)
+    dt = float(sc.params.timeStep)
+    merged = 0
+    for _ in range(6):
+        kids_x = T.get("sub_pos").reshape(sc.n, 8, 3).copy()
+        kids_v = T.get("sub_vel").reshape(sc.n, 8, 3).copy()
+        r = T.step(sc.params, sc.options, None, x, v)
+        code = T.get("state").astype(np.int64) & 15
+        was, now = code >> 2, code & 3
+        left = ((was & 1) == 1) & ((now & 1) == 0)
+        if left.any():
+            mx = kids_x[left].sum(1) * 0.125
+            mv = kids_v[left].sum(1) * 0.125
+            v_new = mv + dt * r["acc"][left]
+            x_new = mx + dt * v_new
+            np.testing.assert_allclose(r["vel"][left], v_new, rtol=0, atol=1e-12)
+            np.testing.assert_allclose(r["pos"][left], x_new, rtol=0, atol=1e-12)
+            merged += int(left.sum())
+        x, v = r["pos"], r["vel"]
+    assert merged > 0
