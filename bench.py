@@ -30,15 +30,23 @@ METRIC = "particle-steps/s @1M: plain vs learned-4×dt at ≤1% density err; HBM
 UNIT = "particle-steps/s"
 L2_BYTES = 129 * 1024 * 1024
 
-# Algorithmic bytes per particle of the force kernel (k_force): reads sorted
-# position, velocity, (rho, p, p/rho^2, 1/rho) float4s and the sorted id
-# (16+16+16+4), writes position, velocity and acceleration float4s (3*16).
-FORCE_BYTES_PER_PARTICLE = 100
-# Per launch it also reads the (C+1)-entry cell-offset table once (4 B/cell).
-# DRAM bytes (read + write) of one k_force launch of the 1,048,576-particle
-# obstacle scene, pretested form, measured with ncu (dram__bytes_read.sum +
-# dram__bytes_write.sum).  Other scenes report no traffic figure.
-FORCE_DRAM_BYTES_1M = 130.137088e6 + 29.085440e6
+# Algorithmic (compulsory) bytes and flops of the two neighbour kernels, per
+# particle and per interacting pair:
+#   k_density: reads a position (12 B of xyz + 4 B), writes rho and p: 24 B;
+#              15 flop per pair within h, the particle itself included;
+#   k_force:   reads position, velocity, rho and p, writes position, velocity
+#              and acceleration: 56 B, plus 8 B per cell (start/end) and 12 B
+#              per boundary-map node (distance, wall density, wall viscosity);
+#              40 flop per interacting pair (0 < r <= h).
+DENSITY_BYTES_PER_PARTICLE = 24
+FORCE_BYTES_PER_PARTICLE = 56
+DENSITY_FLOP_PER_PAIR = 15
+FORCE_FLOP_PER_PAIR = 40
+# The source files the neighbour kernels are compiled from: a DRAM traffic
+# figure recorded under profiles/ holds only while their hash is unchanged.
+KERNEL_SOURCES = ["cudasphnew_gb300/csrc/" + f for f in
+                  ("sph_step.cu", "sph_device.cuh", "sph_internal.h", "sph_sim.h", "sph_mlp_tile.cuh",
+                   "sph_tc.cuh")] + ["include/sph.h"]
 
 
 def parse():
@@ -53,10 +61,11 @@ def parse():
                     help="skip the 64-scene batched leg and the two-scale leg")
     ap.add_argument("--no-learned", action="store_true",
                     help="skip the learned-corrector legs (16,384-particle scene and the 1M scene)")
-    ap.add_argument("--leg", choices=["batched", "learned_1m", "two_scale"], default=None,
-                    help="run only this leg (batched: the 64-scene batch; learned_1m: train the corrector on the "
-                         "16,384-particle scene, then the learned leg of the 1M scene; two_scale: the two-scale "
-                         "run) and print its JSON object; for profiling")
+    ap.add_argument("--leg", choices=["plain", "batched", "learned_1m", "two_scale"], default=None,
+                    help="run only this leg (plain: W warm-up and K graph-launched plain steps of the scene, "
+                         "library default launch shapes; batched: the 64-scene batch; learned_1m: train the "
+                         "corrector on the 16,384-particle scene, then the learned leg of the 1M scene; "
+                         "two_scale: the two-scale run) and print its JSON object; for profiling")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the library's default launch shapes (for profiling runs)")
     return ap.parse_args()
@@ -172,30 +181,92 @@ def pair_count(pos, h):
     return int(t.count_neighbors(t, h)) - len(pos)
 
 
-def combined_roofline(sc, n, pairs, t_s, hbm_gbs, sms, max_mhz):
-    """The force kernel's bound over both resources: its compulsory bytes
-    (56 per particle, 8 per cell, 12 per boundary-map node) at the measured
-    HBM peak, and 40 FP32 operations per interacting pair at the CUDA cores'
-    nominal peak (SMs x 128 lanes x 2 (FMA) x clock).  frac = T* / T."""
-    C = sc.params.num_cells
-    g3 = 0
-    if sc.boundary is not None:
-        d = sc.boundary.dims()
-        g3 = d[0] * d[1] * d[2]
-    byts = 56 * n + 8 * C + 12 * g3
-    flop = 40.0 * pairs
-    fp32 = sms * 128 * 2 * max_mhz * 1e6
+def kernel_sources_sha16():
+    """Hash of the neighbour kernels' source files (see KERNEL_SOURCES)."""
+    import hashlib
+    d = hashlib.sha256()
+    for f in KERNEL_SOURCES:
+        with open(os.path.join(ROOT, f), "rb") as fh:
+            d.update(fh.read())
+    return d.hexdigest()[:16]
+
+
+def profiled_traffic(workload):
+    """DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of
+    k_density and k_force from profiles/traffic_<workload>.md, for the kernel
+    sources that capture was made from; {} when there is no capture or the
+    sources have changed since."""
+    path = os.path.join(ROOT, "profiles", f"traffic_{workload}.md")
+    out = {}
+    try:
+        lines = open(path).read().splitlines()
+    except OSError:
+        return out
+    sha = kernel_sources_sha16()
+    for line in lines:
+        cells = [c.strip() for c in line.strip().strip("|").split("|")]
+        if len(cells) >= 4 and cells[0] in ("k_density", "k_force") and cells[3] == sha:
+            try:
+                out[cells[0]] = float(cells[1])
+            except ValueError:
+                pass
+    return out
+
+
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo), for the CPU baselines."""
+    try:
+        r = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10)
+        for line in r.stdout.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith("model name"):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+    return platform.machine() or "unknown"
+
+
+def fp32_peak(sms, max_mhz):
+    """Nominal FP32 rate: SMs x 128 lanes x 2 (FMA) x clock, flop/s."""
+    return sms * 128 * 2 * max_mhz * 1e6
+
+
+def kernel_roofline(kernel, n, C, g3, pairs, t_s, hbm_gbs, fp32, traffic=None):
+    """Roofline of one launch of a neighbour kernel (k_density or k_force):
+    its compulsory bytes at the measured HBM peak and its flops at the FP32
+    peak; `frac` is the HBM fraction (the contract's bound), `combined_frac`
+    = max(T_bytes, T_flop) / T."""
+    if kernel == "k_density":
+        byts = DENSITY_BYTES_PER_PARTICLE * n
+        flop = DENSITY_FLOP_PER_PAIR * (pairs + n)
+    else:
+        byts = FORCE_BYTES_PER_PARTICLE * n + 8 * C + 12 * g3
+        flop = FORCE_FLOP_PER_PAIR * pairs
     t_bytes, t_flop = byts / (hbm_gbs * 1e9), flop / fp32
-    t_star = max(t_bytes, t_flop)
-    return {"kernel": "k_force", "bytes": byts, "pairs": pairs, "flop": flop,
-            "hbm_peak_gbs": hbm_gbs, "fp32_peak_tflops": fp32 / 1e12,
-            "t_bytes_us": t_bytes * 1e6, "t_flop_us": t_flop * 1e6, "t_measured_us": t_s * 1e6,
-            "bound": "fp32" if t_flop >= t_bytes else "hbm", "frac": t_star / t_s}
+    achieved = byts / t_s / 1e9
+    return {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": hbm_gbs, "unit": "GB/s",
+            "frac": achieved / hbm_gbs, "traffic": traffic, "algorithmic_bytes_per_launch": byts,
+            "flop_per_launch": flop, "pairs": pairs, "avg_launch_us": t_s * 1e6,
+            "t_bytes_us": t_bytes * 1e6, "t_flop_us": t_flop * 1e6, "fp32_peak_tflops": fp32 / 1e12,
+            "limiter": "fp32" if t_flop >= t_bytes else "hbm",
+            "combined_frac": max(t_bytes, t_flop) / t_s}
 
 
 def make_scene(name):
     from cudasphnew_gb300 import scenes
     return getattr(scenes, name)()
+
+
+def scenes_config4():
+    from cudasphnew_gb300 import scenes
+    return scenes.config4()
 
 
 def working_set_bytes(sc):
@@ -208,15 +279,22 @@ def working_set_bytes(sc):
     return n * (16 * 6 + 8 + 4 * 3) + 8 * (C + 1) + maps
 
 
-def cpu_baseline(sc, max_seconds=20.0):
-    """The oracle's FP32 restatement of the reference step on all host cores,
-    on a bounded number of full steps of the same scene."""
+def load_oracle():
+    """The oracle's shared library (the reference algorithm restated for the
+    CPU), built if needed, on all host cores."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle  # the reference algorithm restated for the CPU
+    import oracle
     if not os.path.exists(oracle.LIB_PATH):
         oracle.build()
     cores = os.cpu_count() or 1
     oracle.set_threads(cores)
+    return oracle, cores
+
+
+def cpu_baseline(sc, max_seconds=20.0, max_steps=50):
+    """The oracle's FP32 restatement of the reference step on all host cores,
+    on a bounded number of full steps of the same scene."""
+    oracle, cores = load_oracle()
     bm = oracle.boundary_maps(sc.boundary) if sc.boundary is not None else None
     x, v = sc.positions, sc.velocities
     r = oracle.step_plain(sc.params, sc.options, bm, x, v)  # warm-up step
@@ -227,11 +305,54 @@ def cpu_baseline(sc, max_seconds=20.0):
         x, v = r["pos"], r["vel"]
         steps += 1
         el = time.perf_counter() - t0
-        if el > max_seconds or steps >= 50:
+        if el > max_seconds or steps >= max_steps:
             break
-    return {"value": sc.n * steps / el, "unit": UNIT, "cores": cores, "kind": "port",
+    return {"value": sc.n * steps / el, "unit": UNIT, "cores": cores, "cpu": cpu_model(), "kind": "port",
             "sample": f"{steps} full steps of the {sc.n}-particle scene after 1 warm-up step "
                       f"({el:.1f} s, FP32 restatement of the reference, OpenMP over particles)"}
+
+
+def cpu_baseline_two_scale(sc, max_seconds=15.0, max_steps=20):
+    """AdvanceTwoScale restated on the CPU (oracle, FP32, all host cores) on a
+    bounded number of full two-scale steps of the same scene."""
+    oracle, cores = load_oracle()
+    T = oracle.TwoScale(sc.n)
+    x, v = sc.positions, sc.velocities
+    r = T.step(sc.params, sc.options, None, x, v)  # warm-up step
+    x, v = r["pos"], r["vel"]
+    steps, t0 = 0, time.perf_counter()
+    while True:
+        r = T.step(sc.params, sc.options, None, x, v)
+        x, v = r["pos"], r["vel"]
+        steps += 1
+        el = time.perf_counter() - t0
+        if el > max_seconds or steps >= max_steps:
+            break
+    return {"value": sc.n * steps / el, "unit": UNIT, "cores": cores, "cpu": cpu_model(), "kind": "port",
+            "sample": f"{steps} full two-scale steps of the {sc.n}-particle scene after 1 warm-up step "
+                      f"({el:.1f} s, FP32 restatement of AdvanceTwoScale, OpenMP over particles)"}
+
+
+def cpu_baseline_batch(scs, max_seconds=20.0):
+    """The batched workload on the CPU: every scene stepped in turn by the
+    oracle's FP32 plain step (all host cores), whole rounds over the 64
+    scenes until the time bound."""
+    oracle, cores = load_oracle()
+    bms = [oracle.boundary_maps(sc.boundary) for sc in scs]
+    state = [(sc.positions, sc.velocities) for sc in scs]
+    rounds, t0 = 0, time.perf_counter()
+    while True:
+        for k, sc in enumerate(scs):
+            r = oracle.step_plain(sc.params, sc.options, bms[k], *state[k])
+            state[k] = (r["pos"], r["vel"])
+        rounds += 1
+        el = time.perf_counter() - t0
+        if el > max_seconds or rounds >= 5:
+            break
+    n = sum(sc.n for sc in scs)
+    return {"value": n * rounds / el, "unit": UNIT, "cores": cores, "cpu": cpu_model(), "kind": "port",
+            "sample": f"{rounds} step(s) of each of the {len(scs)} scenes ({n} particles, {el:.1f} s, "
+                      f"FP32 restatement of the reference step, OpenMP over particles)"}
 
 
 def run_reference(args):
@@ -239,17 +360,12 @@ def run_reference(args):
     if rank != 0:
         return
     sc = make_scene(args.config)
-    # each step is one full CPU step of the workload; the run is kept to a few
-    # minutes by bounding the number of steps actually timed
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle
-    if not os.path.exists(oracle.LIB_PATH):
-        oracle.build()
-    cores = os.cpu_count() or 1
-    oracle.set_threads(cores)
+    # each step is one full CPU step of the workload; W warm-up steps, then K
+    # timed steps, bounded to ~2 minutes of CPU time
+    oracle, cores = load_oracle()
     bm = oracle.boundary_maps(sc.boundary) if sc.boundary is not None else None
     x, v = sc.positions, sc.velocities
-    for _ in range(min(args.warmup, 2)):
+    for _ in range(args.warmup):
         r = oracle.step_plain(sc.params, sc.options, bm, x, v)
         x, v = r["pos"], r["vel"]
     steps, t0 = 0, time.perf_counter()
@@ -262,14 +378,15 @@ def run_reference(args):
     el = time.perf_counter() - t0
     val = sc.n * steps / el
     out = {"metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus, "steps": steps,
-           "warmup": min(args.warmup, 2), "ms_per_step": el / steps * 1e3, "higher_is_better": True,
+           "warmup": args.warmup, "ms_per_step": el / steps * 1e3, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
            "impl": "reference",
            "config": {"workload": sc.name, "particles": sc.n, "cells": sc.params.num_cells,
-                      "parallelism": "replicas"},
-           "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores, "kind": "port",
-                            "sample": f"{steps} of {args.steps} requested full steps "
-                                      f"(bounded to ~2 min), FP32 restatement of the reference "
+                      "boundary_map": list(sc.boundary.dims()) if sc.boundary is not None else None,
+                      "parallelism": "replicas" if world > 1 else "single"},
+           "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores, "cpu": cpu_model(), "kind": "port",
+                            "sample": f"{steps} of {args.steps} requested full steps after {args.warmup} "
+                                      f"warm-up steps (bounded to ~2 min), FP32 restatement of the reference "
                                       f"(the reference itself does not build: Windows/GL headers, "
                                       f"removed CUDA texture references)"},
            "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -461,6 +578,18 @@ def learned_leg_1m(lib, torch, stream, model, cfg, sc, steps):
             "audits": after.audits - before.audits, "rollbacks": after.rollbacks - before.rollbacks}
 
 
+def plain_leg(lib, torch, stream, sc, warmup, steps):
+    """W warm-up and K graph-launched plain steps of `sc` with the library's
+    default launch shapes (the command the ncu captures under profiles/ run)."""
+    with lib.ParticleSimulation(sc.params, sc.positions, sc.velocities, sc.options, sc.boundary) as sim:
+        sim.set_stream(stream.cuda_stream)
+        sim.step(count=max(warmup, 1))
+        ms = time_steps(torch, stream, sim, lib.SPH_STEP_PLAIN, steps)
+        tuning = sim.tuning().as_dict()
+    return {"workload": sc.name, "particles": sc.n, "steps": steps, "warmup": max(warmup, 1),
+            "ms_per_step": ms / steps, "tuning": tuning}
+
+
 def batched_leg(lib, torch, stream, steps=200):
     """The 64-scene batched workload (about 4.4M particles, seeded sizes and
     sphere obstacles): one handle, one launch per stage, one CUDA graph per
@@ -540,7 +669,9 @@ def run_ours(args):
     stream = torch.cuda.Stream()
     if args.leg is not None:
         if rank == 0:
-            if args.leg == "batched":
+            if args.leg == "plain":
+                res = plain_leg(lib, torch, stream, sc, args.warmup, args.steps)
+            elif args.leg == "batched":
                 res = batched_leg(lib, torch, stream, steps=args.steps)
             elif args.leg == "two_scale":
                 res = two_scale_leg(lib, torch, stream, steps=args.steps)
@@ -590,16 +721,29 @@ def run_ours(args):
         sim.Advance()
     stages = sim.stage_times()
     sim.set_stage_timing(0)
-    # the force kernel's own launch time: back-to-back launches on the last
-    # step's sorted state (the stage events above also hold launch gaps)
+    # the neighbour kernels' own launch times: back-to-back launches on the
+    # last step's sorted state (the stage events above also hold launch gaps)
     sim.step(count=1)
+    pos_now = sim.positions()  # the state both timed kernels work on
+    density_avg_s = sim.time_kernel("density", 50) / 1e6
     force_avg_s = sim.time_kernel("force", 50) / 1e6
     peak, peak_kind = load_peaks()
     C = sc.params.num_cells
-    alg = n * FORCE_BYTES_PER_PARTICLE + 4 * (C + 1)
-    achieved = alg / force_avg_s / 1e9
-    pairs = pair_count(sim.positions(), float(sc.params.compactSupport))
+    g3 = int(np.prod(sc.boundary.dims())) if sc.boundary is not None else 0
+    pairs = pair_count(pos_now, float(sc.params.compactSupport))
     sms = torch.cuda.get_device_properties(local).multi_processor_count
+    fp32 = fp32_peak(sms, clk.get("sm_max_mhz") or 2070.0)
+    traffic = profiled_traffic(sc.name)
+    roofs = {k: kernel_roofline(k, n, C, g3, pairs, t, peak, fp32, traffic.get(k))
+             for k, t in (("k_density", density_avg_s), ("k_force", force_avg_s))}
+    for r in roofs.values():
+        r["peak_source"] = peak_kind
+        r["timing"] = (f"50 back-to-back launches of {r['kernel']} on one step's sorted state, CUDA events on "
+                       f"the library's stream")
+        r["traffic_source"] = (f"profiles/traffic_{sc.name}.md (ncu dram__bytes_read.sum + "
+                               f"dram__bytes_write.sum, one launch, same kernel sources)"
+                               if r["traffic"] is not None else "no ncu capture of the current kernel sources")
+    dominant = max(roofs, key=lambda k: roofs[k]["avg_launch_us"])
 
     # ---- e2e: host buffers through the C ABI, copies inside the region ----
     pin_pos = torch.empty((n, 3), dtype=torch.float32, pin_memory=True)
@@ -630,7 +774,9 @@ def run_ours(args):
     learned = learned_1m = None
     if rank == 0 and not args.no_learned:
         learned, lcfg, model = learned_leg(lib, torch, stream)
-        learned_1m = learned_leg_1m(lib, torch, stream, model, lcfg, sc, min(args.steps, 500))
+        # the scene's 500 plain steps against 125 learned ones, whatever --steps is: the
+        # learned run then holds several audits (one per auditInterval learned steps)
+        learned_1m = learned_leg_1m(lib, torch, stream, model, lcfg, sc, 500)
 
     if rank != 0:
         return
@@ -648,16 +794,9 @@ def run_ours(args):
            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * n * 12,
                    "d2h_bytes_per_step": n * 12, "steps": e2e_steps,
                    "path": "sph_write(VD, VEL) + sph_step + sph_read(VD), pinned host buffers"},
-           "roofline": {"bound": "hbm", "kernel": "k_force", "achieved": achieved, "peak": peak,
-                        "unit": "GB/s", "frac": achieved / peak,
-                        "traffic": FORCE_DRAM_BYTES_1M if (n == 1048576 and tuning["forceVariant"] == 2) else None,
-                        "peak_source": peak_kind,
-                        "algorithmic_bytes_per_launch": alg,
-                        "avg_launch_us": force_avg_s * 1e6,
-                        "timing": "50 back-to-back launches of k_force on one step's sorted state, CUDA events "
-                                  "on the library's stream"},
-           "roofline_combined": combined_roofline(sc, n, pairs, force_avg_s, peak, sms,
-                                                  clk.get("sm_max_mhz") or 2070.0),
+           "roofline": roofs[dominant],
+           "roofline_density": roofs["k_density"],
+           "roofline_force": roofs["k_force"],
            "stages_us": {k: round(v[0] / v[1] * 1e3, 2) for k, v in stages.items()}}
     if batched is not None:
         out["batched"] = batched
@@ -667,6 +806,9 @@ def run_ours(args):
         out["learned_1m"] = learned_1m
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(sc)
+        if batched is not None:
+            batched["cpu_baseline"] = cpu_baseline_batch(scenes_config4())
+            two_scale["cpu_baseline"] = cpu_baseline_two_scale(make_scene("config3"))
     print(json.dumps(out), flush=True)
 
 

@@ -2,9 +2,10 @@
 recorded boundary-map images (CUDASPHNEW/distances.ppm, viscosities.ppm:
 mid-z slices of Example01's box maps written by
 SphInComplexShapes::SaveSliced{Distance,Viscosity}MapToPpm via
-particle_simulation.cu:2613-2614).  Run once where the reference is mounted:
+particle_simulation.cu:2613-2614).  Run once where the reference checkout is
+available, with the path of its CUDASPHNEW directory:
 
-    python tests/golden/make_golden.py /root/reference/CUDASPHNEW
+    python tests/golden/make_golden.py <reference checkout>/CUDASPHNEW
 """
 import os
 import sys

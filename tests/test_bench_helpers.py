@@ -28,28 +28,53 @@ def fake_scene(num_cells, dims=None):
     return types.SimpleNamespace(params=params, boundary=boundary)
 
 
-def test_combined_roofline_arithmetic():
-    sc = fake_scene(1000, (4, 5, 6))
-    n, pairs, t = 2000, 30000, 10e-6
-    r = bench.combined_roofline(sc, n, pairs, t, hbm_gbs=1000.0, sms=2, max_mhz=1000.0)
-    assert r["bytes"] == 56 * n + 8 * 1000 + 12 * 120
-    assert r["flop"] == 40.0 * pairs
-    fp32 = 2 * 128 * 2 * 1000.0 * 1e6
-    assert r["fp32_peak_tflops"] == pytest.approx(fp32 / 1e12)
-    t_bytes = r["bytes"] / 1e12
-    t_flop = r["flop"] / fp32
+@pytest.mark.parametrize("kernel", ["k_density", "k_force"])
+def test_kernel_roofline_arithmetic(kernel):
+    n, C, g3, pairs, t = 2000, 1000, 120, 30000, 10e-6
+    fp32 = bench.fp32_peak(2, 1000.0)
+    assert fp32 == 2 * 128 * 2 * 1000.0 * 1e6
+    r = bench.kernel_roofline(kernel, n, C, g3, pairs, t, hbm_gbs=1000.0, fp32=fp32, traffic=123.0)
+    if kernel == "k_density":
+        assert r["algorithmic_bytes_per_launch"] == 24 * n
+        assert r["flop_per_launch"] == 15 * (pairs + n)
+    else:
+        assert r["algorithmic_bytes_per_launch"] == 56 * n + 8 * C + 12 * g3
+        assert r["flop_per_launch"] == 40 * pairs
+    t_bytes = r["algorithmic_bytes_per_launch"] / 1e12
+    t_flop = r["flop_per_launch"] / fp32
+    assert r["achieved"] == pytest.approx(r["algorithmic_bytes_per_launch"] / t / 1e9)
+    assert r["frac"] == pytest.approx(r["achieved"] / 1000.0)
     assert r["t_bytes_us"] == pytest.approx(t_bytes * 1e6)
     assert r["t_flop_us"] == pytest.approx(t_flop * 1e6)
-    assert r["bound"] == ("fp32" if t_flop >= t_bytes else "hbm")
-    assert r["frac"] == pytest.approx(max(t_bytes, t_flop) / t)
+    assert r["limiter"] == ("fp32" if t_flop >= t_bytes else "hbm")
+    assert r["combined_frac"] == pytest.approx(max(t_bytes, t_flop) / t)
+    assert r["traffic"] == 123.0 and r["bound"] == "hbm" and r["unit"] == "GB/s"
 
 
-def test_combined_roofline_picks_the_binding_resource():
-    sc = fake_scene(10)
-    # no pairs: the bytes bind
-    assert bench.combined_roofline(sc, 100, 0, 1e-6, 1000.0, 1, 1000.0)["bound"] == "hbm"
-    # many pairs on a tiny GPU: the flops bind
-    assert bench.combined_roofline(sc, 100, 10**9, 1e-6, 1000.0, 1, 1000.0)["bound"] == "fp32"
+def test_kernel_roofline_picks_the_binding_resource():
+    # no pairs: the bytes bind; many pairs on a tiny GPU: the flops bind
+    assert bench.kernel_roofline("k_force", 100, 10, 0, 0, 1e-6, 1000.0, 1e9)["limiter"] == "hbm"
+    assert bench.kernel_roofline("k_force", 100, 10, 0, 10**9, 1e-6, 1000.0, 1e9)["limiter"] == "fp32"
+
+
+def test_profiled_traffic_only_for_the_current_sources(tmp_path, monkeypatch):
+    sha = bench.kernel_sources_sha16()
+    (tmp_path / "profiles").mkdir()
+    (tmp_path / "profiles" / "traffic_w.md").write_text(
+        "| kernel | dram bytes / launch | launches | kernel sources |\n|---|---:|---:|---|\n"
+        f"| k_density | 1.5e8 | 2 | {sha} |\n| k_force | 2.5e8 | 2 | 0000000000000000 |\n")
+    real = bench.kernel_sources_sha16
+    monkeypatch.setattr(bench, "ROOT", str(tmp_path))
+    monkeypatch.setattr(bench, "kernel_sources_sha16", real)
+    monkeypatch.setattr(bench, "KERNEL_SOURCES", [])
+    assert bench.profiled_traffic("w") == {}  # the hash of no files differs
+    monkeypatch.setattr(bench, "kernel_sources_sha16", lambda: sha)
+    assert bench.profiled_traffic("w") == {"k_density": 1.5e8}  # the stale k_force row is dropped
+    assert bench.profiled_traffic("missing") == {}
+
+
+def test_cpu_model_is_named():
+    assert isinstance(bench.cpu_model(), str) and bench.cpu_model()
 
 
 def test_working_set_counts_state_tables_and_maps():

@@ -36,7 +36,8 @@ def run_batch(sphlib, scs, steps, autotune=False):
         fp, fc = sim.scene_ranges()
         h, ids, start, end = sim.cells()
         return fp, fc, dict(pos=sim.positions(), vel=sim.velocities(), rho=sim.read(sphlib.FIELD_DENSITY),
-                            acc=sim.read(sphlib.FIELD_ACCELERATION), hash=h, ids=ids, start=start, end=end)
+                            p=sim.read(sphlib.FIELD_PRESSURE), acc=sim.read(sphlib.FIELD_ACCELERATION),
+                            hash=h, ids=ids, start=start, end=end)
 
 
 def check_scene(k, fp, fc, b, a):
@@ -111,3 +112,39 @@ def test_batched_workload_runs(sphlib):
         lo = np.asarray(sc.params.boxCen) - np.asarray(sc.params.boxDim)
         hi = np.asarray(sc.params.boxCen) + np.asarray(sc.params.boxDim)
         assert (p >= lo - 1e-6).all() and (p <= hi + 1e-6).all()
+
+
+def spread(scs, count):
+    """Indices of `count` scenes spread over the size range (smallest to largest)."""
+    order = np.argsort([sc.n for sc in scs], kind="stable")
+    return sorted({int(order[int(round(q))]) for q in np.linspace(0, len(scs) - 1, count)})
+
+
+def scene_slice(k, fp, fc, b):
+    """Scene k's part of a batch result, with the particle and cell offsets removed."""
+    p0, p1, c0, c1 = int(fp[k]), int(fp[k + 1]), int(fc[k]), int(fc[k + 1])
+    st, en = b["start"][c0:c1].copy(), b["end"][c0:c1].copy()
+    occ = st != EMPTY
+    st[occ] -= p0
+    en[occ] -= p0
+    return dict(hash=b["hash"][p0:p1] - c0, ids=b["ids"][p0:p1] - p0, start=st, end=en,
+                **{key: b[key][p0:p1] for key in ("rho", "p", "acc", "pos", "vel")})
+
+
+def test_batched_workload_matches_oracle_and_scenes_alone(sphlib, orc):
+    """The full 64-scene workload (about 4.4M particles): after one step a
+    mid-size scene matches the oracle (tables bit-exact, rho, p, a within the
+    plain step's FP64 bars); after three steps eight scenes spread over the
+    size range are bit-identical to the same scenes run alone."""
+    from test_gpu_step import check_step, maps_for
+    scs = scenes.config4()
+    fp, fc, b = run_batch(sphlib, scs, 1)
+    k = spread(scs, 3)[1]
+    assert 20000 < scs[k].n < 120000
+    check_step(orc, scs[k], scene_slice(k, fp, fc, b), maps_for(orc, scs[k]))
+    steps = 3
+    fp, fc, b = run_batch(sphlib, scs, steps)
+    picked = spread(scs, 8)
+    assert len(picked) == 8
+    for k in picked:
+        check_scene(k, fp, fc, b, run_alone(sphlib, scs[k], steps))

@@ -225,3 +225,34 @@ def test_config3_runs(sphlib):
         pos = sim.read(sphlib.FIELD_SUB_VERTEX_DATA)
     assert c.numParticlesSplit > 3000 and c.numSubParticles == 8 * (c.numParticlesSplit + c.numParticlesBoundary)
     assert np.isfinite(pos[sub]).all()
+
+
+def test_config3_matches_oracle(sphlib, orc):
+    """The 262,144-particle two-scale configuration (persistent children,
+    merge-back) at full size: coarse tables, states, lists, child list and the
+    fine level's tables bit-exact against the FP32 restatement, fine
+    densities and accelerations within 1e-5 of the FP64 scale, over two steps
+    (the second with the children the first one left)."""
+    sc = scenes.config3()
+    n = sc.n
+    o32 = orc.TwoScale(n)
+    o64 = orc.TwoScale(n, fp64=True)
+    with sphlib.ParticleSimulation(sc.params, sc.positions, sc.velocities, sc.options) as sim:
+        for step in range(2):
+            x0, v0 = sim.positions(), sim.velocities()
+            if step > 0:
+                sp = sim.read(sphlib.FIELD_SUB_VERTEX_DATA)
+                sv = sim.read(sphlib.FIELD_SUB_SIMULATION_DATA)[:, 6:9].copy()
+                for T in (o32, o64):
+                    T.set_children(sp, sv)
+            sim.AdvanceTwoScale()
+            co = coarse_inputs(sphlib, sim)
+            r32 = orc.step_plain(sc.params, sc.options, None, x0, v0)
+            h, _, _, _ = sim.cells(0)
+            for key, got in (("hash", h), ("ids", co["ids"]), ("start", co["start"]), ("end", co["end"])):
+                np.testing.assert_array_equal(got, r32[key], err_msg=f"coarse {key}, step {step}")
+            g = gpu_two_scale(sphlib, sim)
+            c = g["counts"]
+            assert c.numParticlesSplit > 3000
+            assert c.numSubParticles == 8 * (c.numParticlesSplit + c.numParticlesBoundary)
+            check_against_oracle(orc, sc, g, o32, o64, x0, v0, co)
