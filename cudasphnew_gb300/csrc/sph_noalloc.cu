@@ -18,7 +18,16 @@
 //
 // The first call on each device looks up the array's device address with
 // cudaGetSymbolAddress while that device is current; make that first call
-// before capturing work into a CUDA graph on that device.
+// before any stream capture on that device.  Every call waits for its own
+// work to finish (it reads the input-check flags back), so a call on a
+// stream that is being captured is refused with SPH_ERR_NOT_SUPPORTED before
+// anything is enqueued.
+//
+// Cost: the stable order inside a cell compares every particle of the cell
+// with every other (k^2 work for a cell of k particles).  At a few particles
+// per cell that is nothing, but positions crowded into one cell make it
+// quadratic: 65,536 particles in one cell take about 4e9 comparisons (seconds).
+// Inputs that fail the checks (non-finite or outside the grid) skip that pass.
 #include <mutex>
 #include <string>
 
@@ -128,9 +137,11 @@ __global__ void k_na_scatter(int n, NaView v, int* __restrict__ sortedHash) {
 }
 
 // Stable order inside each cell: rank = number of smaller ids in the segment.
+// Skipped when the input checks failed: the call returns an error then, and
+// inputs clamped into one cell would make this pass quadratic in n.
 __global__ void k_na_rank(int n, NaView v, const int* __restrict__ sortedHash, int* __restrict__ sortedIds) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
+    if (k >= n || *v.flags) return;
     int c = sortedHash[k];
     int s = v.offsets[c], e = v.offsets[c + 1];
     int my = v.tmpIds[k];
@@ -180,8 +191,14 @@ extern "C" sph_status sph_cell_tables_noalloc(const SimulationParameters* params
         NA_FAIL(SPH_ERR_INVALID_ARGUMENT, "gridDim[0]*gridDim[1]*gridDim[2] exceeds SPH_NOALLOC_MAX_CELLS = " +
                                               std::to_string(NA_MAX_CELLS));
     if (!(params->gridSpacing > 0.0f)) NA_FAIL(SPH_ERR_INVALID_ARGUMENT, "gridSpacing must be positive");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    cudaError_t e = cudaStreamIsCapturing(st, &cap);
+    if (e != cudaSuccess) NA_FAIL(SPH_ERR_CUDA, cudaGetErrorString(e));
+    if (cap != cudaStreamCaptureStatusNone)
+        NA_FAIL(SPH_ERR_NOT_SUPPORTED, "the stream is being captured: this call waits for its own work");
     int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
+    e = cudaGetDevice(&dev);
     if (e != cudaSuccess) NA_FAIL(SPH_ERR_CUDA, cudaGetErrorString(e));
     if (dev < 0 || dev >= NA_MAX_DEVICES) NA_FAIL(SPH_ERR_NOT_SUPPORTED, "device index too large");
     unsigned char* base = nullptr;
@@ -195,7 +212,6 @@ extern "C" sph_status sph_cell_tables_noalloc(const SimulationParameters* params
         }
         base = g_naBase[dev];
     }
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
     sph::GridDev g;
     for (int a = 0; a < 3; a++) {
         g.origin[a] = params->gridOrigin[a];

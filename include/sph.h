@@ -547,9 +547,13 @@ sph_status sph_time_kernel(sph_handle h, int stage, int reps, float* microsecond
  * rejected with SPH_ERR_INVALID_ARGUMENT.  Calls share that array: calls whose
  * work overlaps on the GPU race and must be serialised by the caller.  The
  * first call on a device looks the array up for that device; make it before
- * capturing work on that device into a CUDA graph.  The call enqueues its
- * work on `stream` (a cudaStream_t, NULL for the default stream) and returns
- * once that work is done. */
+ * any stream capture on that device.  The call enqueues its work on `stream`
+ * (a cudaStream_t, NULL for the default stream) and returns once that work is
+ * done; on a stream that is being captured it enqueues nothing and returns
+ * SPH_ERR_NOT_SUPPORTED.  A non-finite position gives SPH_ERR_NON_FINITE and
+ * one hashed outside the grid SPH_ERR_OUT_OF_DOMAIN; the outputs are then
+ * unspecified.  The stable order inside a cell costs k^2 comparisons for a
+ * cell of k particles, so positions crowded into a few cells are slow. */
 sph_status sph_cell_tables_noalloc(const SimulationParameters* params, const float* devVertexData,
                                    unsigned int n, int* devSortedHash, int* devSortedIds,
                                    int* devCellStart, int* devCellEnd, void* stream);
