@@ -590,6 +590,44 @@ def plain_leg(lib, torch, stream, sc, warmup, steps):
             "ms_per_step": ms / steps, "tuning": tuning}
 
 
+def with_skin(sc, skin):
+    """The scene's options with another neighbourSkin (0: the neighbour search
+    in every step)."""
+    o = type(sc.options).from_buffer_copy(bytes(sc.options))
+    o.neighbourSkin = skin
+    return o
+
+
+def lists_leg(lib, torch, stream, sc, steps, tuning, late_start=1000, late_steps=200):
+    """The reused neighbour lists against the per-step search on the same
+    scene and launch shapes: the first `steps` steps from the initial state,
+    and a later window (`late_steps` steps after `late_start` steps, when the
+    fluid moves fast and the lists are built every few steps)."""
+    import numpy as np
+    out = {"skin": float(sc.options.neighbourSkin),
+           "rebuild_distance_m": 0.45 * float(sc.options.neighbourSkin) * float(sc.params.compactSupport)}
+    for label, skin in (("lists", float(sc.options.neighbourSkin)), ("per_step_search", 0.0)):
+        with lib.ParticleSimulation(sc.params, sc.positions, sc.velocities, with_skin(sc, skin),
+                                    sc.boundary) as sim:
+            sim.set_stream(stream.cuda_stream)
+            sim.set_tuning(**{k: v for k, v in tuning.items() if k in ("densityBlock", "forceBlock", "kahan")})
+            sim.step(count=3)
+            sim.write_state(sc.positions, sc.velocities)
+            b0 = sim.neighbour_builds()
+            ms = time_steps(torch, stream, sim, lib.SPH_STEP_PLAIN, steps)
+            b1 = sim.neighbour_builds()
+            sim.step(count=max(late_start - steps, 1))
+            b2 = sim.neighbour_builds()
+            ms_late = time_steps(torch, stream, sim, lib.SPH_STEP_PLAIN, late_steps)
+            b3 = sim.neighbour_builds()
+            vmax = float(np.linalg.norm(sim.velocities(), axis=1).max())
+        out[label] = {"first_steps": steps, "ms_per_step": ms / steps, "builds": b1 - b0,
+                      "late_window": f"steps {late_start}..{late_start + late_steps}",
+                      "late_ms_per_step": ms_late / late_steps, "late_builds": b3 - b2,
+                      "late_max_speed_m_s": vmax}
+    return out
+
+
 def batched_leg(lib, torch, stream, steps=200):
     """The 64-scene batched workload (about 4.4M particles, seeded sizes and
     sphere obstacles): one handle, one launch per stage, one CUDA graph per
@@ -696,6 +734,7 @@ def run_ours(args):
     sim.synchronize()
 
     # ---- timed region: K graph-launched steps, device-resident ----------
+    builds0 = sim.neighbour_builds()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     barrier(dist)
@@ -709,6 +748,7 @@ def run_ours(args):
     t_wall1 = time.time()
     barrier(dist)
     sim.synchronize()  # raises on a latched device error
+    builds_timed = sim.neighbour_builds() - builds0
     ms = max_over_ranks(dist, e0.elapsed_time(e1))
     clocks.stop()
     clk = clocks.summary(t_wall0, t_wall1)
@@ -767,6 +807,9 @@ def run_ours(args):
     e2e_value = world * n * e2e_steps / el
     sim.close()
 
+    lists = None
+    if rank == 0 and float(sc.options.neighbourSkin) > 0:
+        lists = lists_leg(lib, torch, stream, sc, args.steps, tuning)
     batched = two_scale = None
     if rank == 0 and not args.no_batched:
         batched = batched_leg(lib, torch, stream)
@@ -790,7 +833,12 @@ def run_ours(args):
                             f"> {L2_BYTES / 2**20:.0f} MiB L2",
                       "graph": "one CUDA graph launch per step", "tuning": tuning},
            "clocks": clk,
-           "gpu_launches": 6 * args.steps,
+           "gpu_launches": (7 if float(sc.options.neighbourSkin) > 0 else 6) * args.steps,
+           "neighbour_lists": {"skin": float(sc.options.neighbourSkin), "builds_in_timed_region": builds_timed,
+                               "note": "cell tables, hash and permutation are rebuilt in every step; the "
+                                       "neighbour candidates within (1 + skin) h are rebuilt when a particle "
+                                       "has moved 0.45 skin h since the last build",
+                               "comparison": lists},
            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * n * 12,
                    "d2h_bytes_per_step": n * 12, "steps": e2e_steps,
                    "path": "sph_write(VD, VEL) + sph_step + sph_read(VD), pinned host buffers"},

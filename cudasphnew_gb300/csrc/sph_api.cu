@@ -120,6 +120,10 @@ sph_status validate_params(const SimulationParameters* P, const sph_options* O) 
     if (O && (O->childMode < 0 || O->childMode > 1)) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "childMode must be 0 or 1");
     if (O && (O->cellRelative < 0 || O->cellRelative > 1))
         SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "cellRelative must be 0 or 1");
+    // at most 0.4: the skin sphere then spans at most 4 cells per axis (compactSupport <= gridSpacing),
+    // so a particle's rows fit the lists' VL_SLOTS = 16 entries
+    if (O && !(O->neighbourSkin >= 0.0f && O->neighbourSkin <= 0.4f))
+        SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "neighbourSkin must be in [0, 0.4]");
     if (O && O->cellRelative &&
         (P->gridDim[0] > REL_MAX_X || P->gridDim[1] > REL_MAX_Y || P->gridDim[2] > REL_MAX_Z))
         SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "cellRelative needs gridDim of at most 2048 x 2048 x 1024");
@@ -166,7 +170,8 @@ void free_all(sph_sim* s) {
                     s->sb.keySlot, s->sb.tmpIds, s->sb.sortedHash, s->sb.sortedIds, s->sb.workIds,
                     s->sb.halfOffset, s->scanBlock,
                     s->status, s->staging, s->map4, s->mapDist, s->rowStart, s->rowMask, s->diagBuf,
-                    s->scenesDev, s->reuse};
+                    s->scenesDev, s->reuse, s->vl.start, s->vl.skin, s->vl.exact, s->vl.rows, s->vl.posB,
+                    s->vl.flags};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     void* tsPtrs[] = {s->ts.state,     s->ts.blockCounts, s->ts.counts,
@@ -252,10 +257,71 @@ sph_status ensure_two_scale(sph_sim* s) {
 }
 
 // Enqueues one step of `mode` (no host synchronisation).
+void request_list_build(sph_sim* s) {
+    if (s->vlOn) cudaMemsetAsync(s->vl.flags + VL_BUILD, 1, sizeof(unsigned int), s->stream);
+    s->lastStepLists = false;
+}
+
+void set_list_radius(sph_sim* s) {
+    const float h = s->P.compactSupport, skin = s->O.neighbourSkin;
+    s->vl.radius = (1.0f + skin) * h;
+    s->vl.radius2 = s->vl.radius * s->vl.radius;
+    const float lim = 0.45f * skin * h;
+    s->vl.dispLimit2 = lim * lim;
+}
+
+sph_status alloc_lists(sph_sim* s) {
+    if (!(s->O.neighbourSkin > 0.0f) || s->O.cellRelative || s->numScenes > 1) return SPH_OK;
+    const size_t n = (size_t)s->n;
+    SPH_CUDA(dalloc(&s->vl.start, VL_SLOTS * n));
+    SPH_CUDA(dalloc(&s->vl.skin, VL_SLOTS * n));
+    SPH_CUDA(dalloc(&s->vl.exact, VL_SLOTS * n));
+    SPH_CUDA(dalloc(&s->vl.rows, n));
+    SPH_CUDA(dalloc(&s->vl.posB, n));
+    SPH_CUDA(dalloc(&s->vl.flags, VL_FLAGS));
+    SPH_CUDA(cudaMemsetAsync(s->vl.flags, 0, sizeof(unsigned int) * VL_FLAGS, s->stream));
+    SPH_CUDA(cudaMemsetAsync(s->vl.rows, 0, n, s->stream));
+    set_list_radius(s);
+    s->vlOn = true;
+    request_list_build(s);
+    return SPH_OK;
+}
+
+// A plain step over the reused neighbour lists: the reference's hash, sort
+// and cell tables as in every step, the state gathered into the lists'
+// working order, then the density stage (building the lists when this step
+// must) and the force stage over them.
+static void enqueue_lists(sph_sim* s, const GridDev& g, const PhysDev& ph, int collide, cudaEvent_t* ev) {
+    cudaStream_t st = s->stream;
+    const int n = s->n;
+    auto mark = [&](int k) {
+        if (ev) cudaEventRecord(ev[k], st);
+    };
+    mark(ST_HASH);
+    launch_hash_count(n, s->pos, g, s->sb, s->status, st, &s->vl);
+    mark(ST_SCAN);
+    launch_cell_scan(g.numCells, s->sb, s->status, st);
+    mark(ST_SCATTER);
+    launch_scatter(n, s->sb, st);
+    mark(ST_RANK);
+    launch_rank_gather(n, s->sb, s->pos, s->vel, g, s->posS, s->velS, st, &s->vl);
+    mark(ST_DENSITY);
+    launch_density_lists(n, s->posS, rows_of(s), g, ph, s->map, s->rho4S, s->vl, s->cfg, true, true, st);
+    // the sorted copies are now this step's own: a reuse the audit granted is used up
+    cudaMemsetAsync(s->reuse, 0, sizeof(int), st);
+    mark(ST_FORCE);
+    launch_force_lists(n, s->posS, s->velS, s->rho4S, s->sb.workIds, ph, s->map, collide, s->vl, s->pos, s->vel,
+                       s->accS, s->cfg, st);
+    mark(ST_COUNT);
+    s->lastStepLists = true;
+}
+
 void enqueue_coarse(sph_sim* s, const GridDev& g, const PhysDev& ph, int collide, cudaEvent_t* ev,
                     const FeatureOut* feat, bool force) {
     cudaStream_t st = s->stream;
     const int n = s->n;
+    // the per-step search rewrites the sorted copies and the working order
+    request_list_build(s);
     StepConfig cfg = s->cfg;
     // the feature form and the fused learned form read the density stage's masks
     if (feat || !force) cfg.forceVariant = FORCE_PRETESTED;
@@ -285,6 +351,7 @@ void enqueue_coarse(sph_sim* s, const GridDev& g, const PhysDev& ph, int collide
 void enqueue_density_only(sph_sim* s, const float4* pos, const float4* vel, bool masks) {
     cudaStream_t st = s->stream;
     const int n = s->n;
+    request_list_build(s);
     GridDev g = grid_of(s);
     PhysDev ph = make_phys(s->P, s->O);
     launch_hash_count(n, pos, g, s->sb, s->status, st);
@@ -301,7 +368,7 @@ void invalidate_graphs(sph_sim* s) {
     s->graphGen++;
 }
 
-void enqueue_step(sph_sim* s, int mode, bool timing) {
+void enqueue_step(sph_sim* s, int mode, bool timing, bool lists) {
     if (mode == SPH_STEP_SUB_ONLY) {
         if (!s->tsReady) return;
         // AdvanceSubParticles (:2119-2143) on the current lists
@@ -330,6 +397,10 @@ void enqueue_step(sph_sim* s, int mode, bool timing) {
     }
     // AdvanceTwoScale always runs handleCollisions (:2170)
     const int collide = twoScale ? 1 : s->O.boxCollision;
+    if (!twoScale && lists && s->vlOn) {
+        enqueue_lists(s, g, ph, collide, ev);
+        return;
+    }
     enqueue_coarse(s, g, ph, collide, ev);
     if (twoScale) {
         // computeParticleState, collect, initializeSubParticles, projectQuantities
@@ -448,6 +519,7 @@ void sph_default_options(sph_options* o) {
         o->splitMin[a] = -3.0e38f;
         o->splitMax[a] = 3.0e38f;
     }
+    o->neighbourSkin = 0.1f;
 }
 
 const char* sph_last_error(void) { return g_lastError.c_str(); }
@@ -522,6 +594,7 @@ sph_status sph_create(const SimulationParameters* params, const sph_options* opt
     const int n = (int)params->numParticles;
     const long long C = (long long)params->gridDim[0] * params->gridDim[1] * params->gridDim[2];
     st = alloc_handle(s, n, C);
+    if (!st) st = alloc_lists(s);
     if (st) {
         free_all(s);
         delete s;
@@ -607,6 +680,8 @@ sph_status sph_bind(sph_handle s, const SimulationParameters* params) {
     }
     SPH_CUDA(cudaMemsetAsync(s->reuse, 0, sizeof(int), s->stream));
     s->P = *params;
+    if (s->vlOn) set_list_radius(s);
+    request_list_build(s);
     invalidate_graphs(s);
     return SPH_OK;
 }
@@ -841,6 +916,10 @@ sph_status sph_write(sph_handle s, int field, const void* src, size_t bytes) {
                 in = s->staging;
             }
             launch_unpack_aos(in, 3, 0, n, field == SPH_FIELD_VERTEX_DATA ? s->pos : s->vel, q);
+            // the lists stay valid while every particle is within the rebuild
+            // distance of where it was at their build (velocities do not matter)
+            if (field == SPH_FIELD_VERTEX_DATA && s->vlOn && s->lastStepLists)
+                launch_list_displacement(n, s->pos, s->sb.workIds, s->vl, q);
             if (field == SPH_FIELD_VERTEX_DATA && s->O.cellRelative) launch_abs_to_rel(n, s->pos, grid_of(s), q);
             if (field == SPH_FIELD_VERTEX_DATA && s->numScenes > 1)  // restore the scene index lanes
                 for (int k = 0; k < s->numScenes; k++)
@@ -1024,9 +1103,101 @@ sph_status sph_set_tuning(sph_handle s, const sph_tuning* t) {
     return SPH_OK;
 }
 
+// The autotuner of a handle with reused neighbour lists: the list kernels
+// have one form each, so only their block sizes are tried, by whole steps
+// from the current state.  The state, the sorted copies and tables, and the
+// lists with their flags are saved first and put back afterwards, so the
+// next step is the one that would have come without the tuning.
+static sph_status autotune_lists(sph_sim* s, int reps, sph_tuning* chosen) {
+    const int n = s->n;
+    const size_t C1 = (size_t)s->numCellsTotal + 1;
+    cudaStream_t st = s->stream;
+    struct Buf {
+        void* dst;
+        void* save;
+        size_t bytes;
+    } bufs[] = {{s->pos, nullptr, sizeof(float4) * n},          {s->vel, nullptr, sizeof(float4) * n},
+                {s->posS, nullptr, sizeof(float4) * n},         {s->velS, nullptr, sizeof(float4) * n},
+                {s->rho4S, nullptr, sizeof(float4) * n},        {s->accS, nullptr, sizeof(float4) * n},
+                {s->sb.sortedHash, nullptr, sizeof(int) * n},   {s->sb.sortedIds, nullptr, sizeof(int) * n},
+                {s->sb.workIds, nullptr, sizeof(int) * n},      {s->sb.cellOffset, nullptr, sizeof(int) * C1},
+                {s->sb.halfOffset, nullptr, sizeof(int) * C1},  {s->vl.flags, nullptr, sizeof(unsigned int) * VL_FLAGS},
+                {s->vl.start, nullptr, sizeof(int) * VL_SLOTS * n},
+                {s->vl.skin, nullptr, sizeof(uint2) * VL_SLOTS * n},
+                {s->vl.exact, nullptr, sizeof(uint2) * VL_SLOTS * n},
+                {s->vl.rows, nullptr, (size_t)n},               {s->vl.posB, nullptr, sizeof(float4) * n}};
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    auto cleanup = [&]() {
+        for (auto& b : bufs)
+            if (b.save) cudaFree(b.save);
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+    };
+    cudaError_t te = cudaStreamSynchronize(st);
+    for (auto& b : bufs) {
+        if (te == cudaSuccess) te = cudaMalloc(&b.save, b.bytes);
+        if (te == cudaSuccess) te = cudaMemcpyAsync(b.save, b.dst, b.bytes, cudaMemcpyDeviceToDevice, st);
+    }
+    if (te == cudaSuccess) te = cudaEventCreate(&e0);
+    if (te == cudaSuccess) te = cudaEventCreate(&e1);
+    const unsigned int steps0 = s->numTimeSteps;
+    const bool stepped0 = s->stepped;
+    const bool lists0 = s->lastStepLists;
+    const StepConfig current = s->cfg;
+    std::vector<StepConfig> trials{current};
+    for (int db : {64, 128, 256})
+        for (int fb : {64, 128, 256}) {
+            StepConfig c = current;
+            c.densityBlock = db;
+            c.forceBlock = fb;
+            if (db != current.densityBlock || fb != current.forceBlock) trials.push_back(c);
+        }
+    float bestStep = 3.0e38f;
+    StepConfig chosenCfg = current;
+    for (size_t k = 0; k < trials.size() && te == cudaSuccess; k++) {
+        s->cfg = trials[k];
+        invalidate_graphs(s);
+        float fastest = 3.0e38f;
+        for (int r = 0; r < std::max(reps, 1) && te == cudaSuccess; r++) {
+            te = cudaMemcpyAsync(s->pos, bufs[0].save, bufs[0].bytes, cudaMemcpyDeviceToDevice, st);
+            if (te == cudaSuccess) te = cudaMemcpyAsync(s->vel, bufs[1].save, bufs[1].bytes, cudaMemcpyDeviceToDevice, st);
+            request_list_build(s);
+            // capture and the build step, then list steps only
+            if (te == cudaSuccess && sph_step_many(s, SPH_STEP_PLAIN, 2) != SPH_OK) te = cudaErrorUnknown;
+            if (te == cudaSuccess) te = cudaEventRecord(e0, st);
+            if (te == cudaSuccess && sph_step_many(s, SPH_STEP_PLAIN, 8) != SPH_OK) te = cudaErrorUnknown;
+            if (te == cudaSuccess) te = cudaEventRecord(e1, st);
+            if (te == cudaSuccess) te = cudaEventSynchronize(e1);
+            float ms = 0.f;
+            if (te == cudaSuccess) te = cudaEventElapsedTime(&ms, e0, e1);
+            if (te == cudaSuccess) fastest = std::min(fastest, ms);
+        }
+        // keep the incumbent unless beaten by 2 %
+        if (te == cudaSuccess && fastest < (k == 0 ? bestStep : 0.98f * bestStep)) {
+            bestStep = fastest;
+            chosenCfg = trials[k];
+        }
+    }
+    for (auto& b : bufs)
+        if (te == cudaSuccess && b.save) te = cudaMemcpyAsync(b.dst, b.save, b.bytes, cudaMemcpyDeviceToDevice, st);
+    if (te == cudaSuccess) te = cudaStreamSynchronize(st);
+    cleanup();
+    s->numTimeSteps = steps0;
+    s->stepped = stepped0;
+    s->cfg = te == cudaSuccess ? chosenCfg : current;
+    // the lists, their flags and the sorted copies are as the last step left them
+    s->lastStepLists = lists0;
+    if (te != cudaSuccess) request_list_build(s);
+    invalidate_graphs(s);
+    SPH_CUDA(te);
+    if (chosen) return sph_get_tuning(s, chosen);
+    return SPH_OK;
+}
+
 sph_status sph_autotune(sph_handle s, int reps, sph_tuning* chosen) {
     if (!s) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "handle is NULL");
     reps = std::max(reps, 1);
+    if (s->vlOn) return autotune_lists(s, reps, chosen);
     const int n = s->n;
     const int C = (int)s->numCellsTotal;
     cudaStream_t st = s->stream;
@@ -1233,17 +1404,32 @@ sph_status sph_time_kernel(sph_handle s, int stage, int reps, float* microsecond
     // the density stage rewrites what it wrote (and the masks the force form
     // reads); the force stage rewrites the state the last step wrote
     SPH_CUDA(cudaMemsetAsync(s->reuse, 0, sizeof(int), st));
+    // after a step over the reused neighbour lists the list forms are timed
+    // (the density stage's list form: the lists match the sorted copies)
+    const bool lists = s->vlOn && s->lastStepLists;
+    if (lists) SPH_CUDA(cudaMemsetAsync(s->vl.flags + VL_BUILD_NOW, 0, sizeof(unsigned int), st));
     auto launch = [&]() {
-        if (stage == ST_DENSITY)
+        if (lists) {
+            if (stage == ST_DENSITY)
+                launch_density_lists(n, s->posS, rows_of(s), g, ph, s->map, s->rho4S, s->vl, s->cfg, false, true,
+                                     st);
+            else
+                launch_force_lists(n, s->posS, s->velS, s->rho4S, s->sb.workIds, ph, s->map, s->O.boxCollision,
+                                   s->vl, s->pos, s->vel, s->accS, s->cfg, st);
+        } else if (stage == ST_DENSITY) {
             launch_density(n, s->posS, rows_of(s), g, ph, s->map, s->rho4S, s->rowStart, s->rowMask, s->cfg, st);
-        else
+        } else {
             launch_force(n, s->posS, s->velS, s->rho4S, s->sb.workIds, rows_of(s), g, ph, s->map,
                          s->O.boxCollision, s->rowStart, s->rowMask, s->pos, s->vel, s->accS, s->cfg, st, nullptr,
                          s->status);
+        }
     };
     if (stage == ST_FORCE) {  // the masks of the current tuning
         StepConfig c = s->cfg;
-        launch_density(n, s->posS, rows_of(s), g, ph, s->map, s->rho4S, s->rowStart, s->rowMask, c, st);
+        if (lists)
+            launch_density_lists(n, s->posS, rows_of(s), g, ph, s->map, s->rho4S, s->vl, c, false, true, st);
+        else
+            launch_density(n, s->posS, rows_of(s), g, ph, s->map, s->rho4S, s->rowStart, s->rowMask, c, st);
     }
     launch();  // warm
     cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -1262,6 +1448,17 @@ sph_status sph_time_kernel(sph_handle s, int stage, int reps, float* microsecond
     if (e1) cudaEventDestroy(e1);
     SPH_CUDA(e);
     *microseconds = 1e3f * ms / (float)reps;
+    return latched_status(s);
+}
+
+sph_status sph_neighbour_builds(sph_handle s, unsigned int* builds) {
+    if (!s || !builds) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "NULL argument");
+    *builds = 0;
+    if (!s->vlOn) return SPH_OK;
+    SPH_CUDA(cudaMemcpyAsync(s->statusHost, s->vl.flags + VL_COUNT, sizeof(unsigned int), cudaMemcpyDeviceToHost,
+                             s->stream));
+    SPH_CUDA(cudaStreamSynchronize(s->stream));
+    *builds = *s->statusHost;
     return latched_status(s);
 }
 

@@ -203,6 +203,48 @@ __device__ __forceinline__ void row_range(float4 xi, const Stencil& st, float h,
     if (e < s) e = s;
 }
 
+// Candidate window [s, e) of the grid row (y, z) for a sphere of radius R
+// around xi: the row is skipped when its (y, z) cell rectangle lies farther
+// than R, and otherwise cut to the half-cells in x that the sphere reaches at
+// that gap, clamped to the grid (not to the 27-cell stencil: R may exceed a
+// cell).  The same margins as row_range, so every particle within R is a
+// candidate.  Used to build the reused neighbour lists.
+__device__ __forceinline__ bool row_window(float4 xi, int y, int z, float R, float eps, const GridDev& g,
+                                           RowTables T, int& s, int& e) {
+    s = e = 0;
+    const float R2 = R * R;
+    const float gz = cell_gap(xi.z, z, g.origin[2], g.spacing, eps);
+    const float gy = cell_gap(xi.y, y, g.origin[1], g.spacing, eps);
+    const float g2 = gy * gy + gz * gz;
+    if (g2 > R2) return false;
+    const float inv = 1.0f / g.spacing;
+    float rx;
+    asm("sqrt.approx.f32 %0, %1;" : "=f"(rx) : "f"(R2 - g2));
+    rx += eps;
+    const float xl = xi.x - rx, xr = xi.x + rx;
+    const int cl = max(0, (int)floorf((xl - g.origin[0]) * inv));
+    const int cr = min(g.dim[0] - 1, (int)floorf((xr - g.origin[0]) * inv));
+    if (cl > cr) return false;
+    const int row = g.cellBase + g.dim[0] * (g.dim[1] * z + y);
+    const int a0 = __ldg(T.cellOffset + row + cl), a1 = __ldg(T.cellOffset + row + cl + 1);
+    const int b0 = __ldg(T.cellOffset + row + cr), b1 = __ldg(T.cellOffset + row + cr + 1);
+    const float midL = g.origin[0] + ((float)cl + 0.5f) * g.spacing;
+    const float midR = g.origin[0] + ((float)cr + 0.5f) * g.spacing;
+    s = a0;
+    e = b1;
+    if (xl >= midL) s = min(max(__ldg(T.halfOffset + row + cl), a0), a1);
+    if (xr < midR) e = min(max(__ldg(T.halfOffset + row + cr), b0), b1);
+    if (e < s) e = s;
+    return e > s;
+}
+
+// The cell range [lo, hi] of axis `a` that [p - r, p + r] touches, clamped to the grid.
+__device__ __forceinline__ void cell_span(float p, float r, const GridDev& g, int a, int& lo, int& hi) {
+    const float inv = 1.0f / g.spacing;
+    lo = max(0, (int)floorf((p - r - g.origin[a]) * inv));
+    hi = min(g.dim[a] - 1, (int)floorf((p + r - g.origin[a]) * inv));
+}
+
 // ---------------------------------------------------------------------------
 // Cell-relative positions (sph_options.cellRelative): .xyz is the offset from
 // the low corner of the particle's cell, .w carries the cell's integer

@@ -125,6 +125,40 @@ struct RowTables {
     const int* skip;        // as SortBuffers::skip, read by the density stage only
 };
 
+// Reused neighbour lists (sph_options.neighbourSkin).  When the lists are
+// built, every particle records the stencil rows of the reference grid that
+// its skin sphere (radius R = (1 + skin) h) reaches: per row a window start
+// in the working order and a 64-bit mask of the candidates within R.  Later
+// steps keep that working order (the state is gathered into it) and visit
+// only those candidates, until some particle has moved farther than 0.45 skin
+// h from where it was at the build.  Slots 0-8 hold the reference's own 3 x 3
+// rows in its order (an empty row: start 0, no bits), so a build step sums
+// exactly what the per-step search sums; the further rows the skin reaches
+// follow from slot 9.  A window whose candidates within R span more than 64
+// places is kept unmasked: bit 31 of `start` set and the window end in the
+// low word of its masks.
+constexpr int VL_SLOTS = 16;  // rows within R <= 1.4 gridSpacing: at most 4 x 4
+constexpr int VL_INNER = 9;
+enum : int {
+    VL_BUILD = 0,      // a build is requested (state written, another kind of step ran)
+    VL_BUILD_NOW = 1,  // this step builds the lists (decided at the start of the step)
+    VL_DISP = 2,       // largest squared displacement since the build (float bits)
+    VL_COUNT = 3,      // builds so far
+    VL_FLAGS = 4,
+};
+struct NeighbourLists {
+    int* start;            // [VL_SLOTS][n] window start (bit 31: unmasked window)
+    uint2* skin;           // [VL_SLOTS][n] candidates within R (bit k: start + k; .x bits 0-31), or
+                           //               .x = the window end
+    uint2* exact;          // [VL_SLOTS][n] this step's neighbours (0 < r <= h) over the same window, or
+                           //               .x = the window end
+    unsigned char* rows;   // [n] slots in use (9 + the further rows)
+    float4* posB;          // [n] positions at the build, working order
+    unsigned int* flags;   // [VL_FLAGS]
+    float radius, radius2; // R and R^2
+    float dispLimit2;      // (0.45 skin h)^2
+};
+
 // Launch configuration of the step (chosen per handle; see the autotuner).
 enum ForceVariant { FORCE_DIRECT = 0, FORCE_MASK = 1, FORCE_PRETESTED = 2, FORCE_STAGED = 3 };
 
@@ -172,12 +206,31 @@ void launch_pack_aos(const float4* in, int n, float* aos, int stride, int offset
 // back to absolute (AoS with `stride` floats per particle and/or float4s).
 void launch_abs_to_rel(int n, float4* pos, GridDev g, cudaStream_t s);
 void launch_rel_to_abs(int n, const float4* pos, GridDev g, float* aos, int stride, float4* out4, cudaStream_t s);
+// With `lists`, the first thread also decides whether this step builds the
+// neighbour lists (VL_BUILD_NOW).
 void launch_hash_count(int n, const float4* pos, GridDev g, SortBuffers sb, unsigned int* status,
-                       cudaStream_t s);
+                       cudaStream_t s, const NeighbourLists* lists = nullptr);
 void launch_cell_scan(int numCells, SortBuffers sb, unsigned int* status, cudaStream_t s);
 void launch_scatter(int n, SortBuffers sb, cudaStream_t s);
+// With `lists` and no build in this step, only the reference permutation is
+// ranked and the state is gathered into the kept working order (workIds).
 void launch_rank_gather(int n, SortBuffers sb, const float4* pos, const float4* vel, GridDev g,
-                        float4* posS, float4* velS, cudaStream_t s);
+                        float4* posS, float4* velS, cudaStream_t s, const NeighbourLists* lists = nullptr);
+// Density stage over reused neighbour lists: the build form (the reference's
+// rows and the skin rows, recording the lists) and the list form; each
+// returns at once unless the step is of its kind.
+void launch_density_lists(int n, const float4* posS, RowTables T, GridDev g, PhysDev ph, MapDev map,
+                          float4* rho4S, const NeighbourLists& L, const StepConfig& cfg, bool build, bool reuse,
+                          cudaStream_t s);
+// After a write of the positions: the largest distance from the build
+// positions, measured afresh (the lists stay if it is within the limit).
+void launch_list_displacement(int n, const float4* pos, const int* workIds, const NeighbourLists& L,
+                              cudaStream_t s);
+// Force stage over the lists' neighbour masks; also records the largest
+// displacement since the build.
+void launch_force_lists(int n, const float4* posS, const float4* velS, const float4* rho4S, const int* workIds,
+                        PhysDev ph, MapDev map, int collide, const NeighbourLists& L, float4* pos, float4* vel,
+                        float4* accS, const StepConfig& cfg, cudaStream_t s);
 void launch_density(int n, const float4* posS, RowTables T, GridDev g, PhysDev ph, MapDev map,
                     float4* rho4S, int* rowStart, unsigned int* rowMask, const StepConfig& cfg,
                     cudaStream_t s);

@@ -99,6 +99,12 @@ struct sph_sim {
     // FP64 diagnostics scratch: partial rows then the DIAG_TERMS results
     double* diagBuf = nullptr;
 
+    // reused neighbour lists (sph_options.neighbourSkin > 0 on a single-scene
+    // handle with absolute positions): plain steps build and reuse them
+    sph::NeighbourLists vl{};
+    bool vlOn = false;
+    bool lastStepLists = false;  // the last step ran over the lists (they match the sorted copies)
+
     // stage timing ring
     int timingCap = 0, timingNext = 0, timingFilled = 0;
     std::vector<cudaEvent_t> events;  // timingCap * (sph::ST_COUNT + 1)
@@ -115,8 +121,16 @@ sph_status validate_params(const SimulationParameters* P, const sph_options* O);
 sph_status check_desc(const sph_boundary_desc* d, unsigned int dims[3]);
 void free_all(sph_sim* s);
 sph_status ensure_two_scale(sph_sim* s);
-// Enqueues one step of `mode` (no host synchronisation).
-void enqueue_step(sph_sim* s, int mode, bool timing);
+// Enqueues one step of `mode` (no host synchronisation).  A plain step runs
+// over the reused neighbour lists when the handle has them and `lists`.
+void enqueue_step(sph_sim* s, int mode, bool timing, bool lists = true);
+// Asks the next plain step over the lists to build them (the sorted copies
+// and the working order changed under them).
+void request_list_build(sph_sim* s);
+// Allocates the reused neighbour lists when the handle's options ask for them.
+sph_status alloc_lists(sph_sim* s);
+// Radius and displacement limit of the lists from the handle's parameters.
+void set_list_radius(sph_sim* s);
 // Hash, sort, density and force + integration (+ box collision) of the
 // coarse particles with the given constants; stage events when `ev`; the
 // force stage also records the corrector's features when `feat`.  With

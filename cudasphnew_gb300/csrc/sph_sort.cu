@@ -101,11 +101,25 @@ void launch_pack_aos(const float4* in, int n, float* aos, int stride, int offset
 // start at that scene's cellBase in the concatenated cell space.
 // With REL the position is cell-relative and the hash comes from its packed
 // cell coordinates.
+// With `vl` (reused neighbour lists) the first thread decides whether this
+// step builds them: on request, or when some particle has moved farther than
+// the skin allows since the last build (or the displacement is not finite).
+// The kernels after this one read the decision.
 template <bool BATCH, bool REL>
 __global__ void k_hash_count(int n, const float4* __restrict__ pos, GridDev g_, const SceneDev* __restrict__ scenes,
                              int* __restrict__ cnt, int2* __restrict__ keySlot, unsigned int* status,
-                             const int* __restrict__ skip) {
+                             const int* __restrict__ skip, unsigned int* vl, float dispLimit2) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (vl && i == 0) {
+        const float d2 = __uint_as_float(vl[VL_DISP]);
+        const bool build = vl[VL_BUILD] != 0u || !(d2 <= dispLimit2);
+        vl[VL_BUILD_NOW] = build ? 1u : 0u;
+        vl[VL_BUILD] = 0u;
+        if (build) {
+            vl[VL_DISP] = 0u;
+            vl[VL_COUNT] += 1u;
+        }
+    }
     if (i >= n || (skip && *skip)) return;
     float4 p = pos[i];
     const GridDev& g = BATCH ? scenes[__float_as_int(p.w)].g : g_;
@@ -128,17 +142,19 @@ __global__ void k_hash_count(int n, const float4* __restrict__ pos, GridDev g_, 
 }
 
 void launch_hash_count(int n, const float4* pos, GridDev g, SortBuffers sb, unsigned int* status,
-                       cudaStream_t s) {
+                       cudaStream_t s, const NeighbourLists* L) {
     if (n <= 0) return;
+    unsigned int* vl = L ? L->flags : nullptr;
+    const float lim = L ? L->dispLimit2 : 0.f;
     if (sb.scenes)
         k_hash_count<true, false><<<(n + 255) / 256, 256, 0, s>>>(n, pos, g, sb.scenes, sb.cnt, sb.keySlot, status,
-                                                                  sb.skip);
+                                                                  sb.skip, nullptr, 0.f);
     else if (g.rel)
         k_hash_count<false, true><<<(n + 255) / 256, 256, 0, s>>>(n, pos, g, nullptr, sb.cnt, sb.keySlot, status,
-                                                                  sb.skip);
+                                                                  sb.skip, nullptr, 0.f);
     else
         k_hash_count<false, false><<<(n + 255) / 256, 256, 0, s>>>(n, pos, g, nullptr, sb.cnt, sb.keySlot, status,
-                                                                  sb.skip);
+                                                                   sb.skip, vl, lim);
 }
 
 // ---------------------------------------------------------------------------
@@ -325,17 +341,30 @@ __device__ __forceinline__ unsigned int ordered_bits(float x) {
 // The same pass records, per cell, where its upper x-half starts in the
 // working order (halfOffset[c] = first index with x >= the cell's mid-plane),
 // so a neighbour search can cut a row at half-cell granularity from a table.
+// With reused neighbour lists (`vl`) and no build in this step, the working
+// order is the one kept since the build (workIds): only the reference
+// permutation is ranked, and the state is gathered into the kept order.
 template <bool BATCH, bool REL>
 __global__ void k_rank_gather(int n, const int* __restrict__ sortedHash, const int* __restrict__ cellOffset,
                               const int* __restrict__ tmpIds, const float4* __restrict__ pos,
                               const float4* __restrict__ vel, GridDev g_, const SceneDev* __restrict__ scenes,
                               int* __restrict__ sortedIds, int* __restrict__ workIds, int* __restrict__ halfOffset,
-                              float4* __restrict__ posS, float4* __restrict__ velS, const int* __restrict__ skip) {
+                              float4* __restrict__ posS, float4* __restrict__ velS, const int* __restrict__ skip,
+                              const unsigned int* __restrict__ vl) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n || (skip && *skip)) return;
     int c = sortedHash[k];
     int s = __ldg(cellOffset + c), e = __ldg(cellOffset + c + 1);
     int my = tmpIds[k];
+    if (vl && !vl[VL_BUILD_NOW]) {
+        int rId = 0;
+        for (int t = s; t < e; t++) rId += __ldg(tmpIds + t) < my;
+        sortedIds[s + rId] = my;
+        const int w = workIds[k];
+        posS[k] = __ldg(pos + w);
+        velS[k] = __ldg(vel + w);
+        return;
+    }
     float4 p = __ldg(pos + my);
     const GridDev& g = BATCH ? scenes[__float_as_int(p.w)].g : g_;
     unsigned int key = ordered_bits(p.x);
@@ -359,21 +388,21 @@ __global__ void k_rank_gather(int n, const int* __restrict__ sortedHash, const i
 }
 
 void launch_rank_gather(int n, SortBuffers sb, const float4* pos, const float4* vel, GridDev g, float4* posS,
-                        float4* velS, cudaStream_t s) {
+                        float4* velS, cudaStream_t s, const NeighbourLists* L) {
     if (n <= 0) return;
     const int grid = (n + 255) / 256;
     if (sb.scenes)
         k_rank_gather<true, false><<<grid, 256, 0, s>>>(n, sb.sortedHash, sb.cellOffset, sb.tmpIds, pos, vel, g,
                                                         sb.scenes, sb.sortedIds, sb.workIds, sb.halfOffset, posS,
-                                                        velS, sb.skip);
+                                                        velS, sb.skip, nullptr);
     else if (g.rel)
         k_rank_gather<false, true><<<grid, 256, 0, s>>>(n, sb.sortedHash, sb.cellOffset, sb.tmpIds, pos, vel, g,
                                                         nullptr, sb.sortedIds, sb.workIds, sb.halfOffset, posS, velS,
-                                                        sb.skip);
+                                                        sb.skip, nullptr);
     else
         k_rank_gather<false, false><<<grid, 256, 0, s>>>(n, sb.sortedHash, sb.cellOffset, sb.tmpIds, pos, vel, g,
                                                          nullptr, sb.sortedIds, sb.workIds, sb.halfOffset, posS,
-                                                         velS, sb.skip);
+                                                         velS, sb.skip, L ? L->flags : nullptr);
 }
 
 // ---------------------------------------------------------------------------

@@ -103,6 +103,179 @@ k_density(int n, const float4* __restrict__ posS, RowTables T, GridDev g_, PhysD
 }
 
 // ---------------------------------------------------------------------------
+// Density over reused neighbour lists (sph_options.neighbourSkin).
+//
+// Build form (steps that build the lists): the reference's 3 x 3 stencil
+// rows first, in its order, into slots 0-8, then the further rows the skin
+// sphere of radius R reaches; each row's window at R is walked in the working
+// order and the density terms are summed as in k_density (candidates beyond
+// h add exactly nothing, so the reference's rows give the same row sums).
+// Each row is recorded with two 64-bit masks over its candidates, starting at
+// its first candidate within R: the candidates within R (the lists) and the
+// neighbours within h (this step's force stage).  A row whose candidates
+// within R span more than 64 places is kept unmasked.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool within_r2(float r2, float R2) {  // r2 >= 0 or NaN
+    return __float_as_uint(r2) <= __float_as_uint(R2);
+}
+
+template <bool KAHAN>
+__global__ void __launch_bounds__(256, 4)
+k_density_build(int n, const float4* __restrict__ posS, RowTables T, GridDev g, PhysDev ph, MapDev map,
+                float4* __restrict__ rho4S, NeighbourLists L) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || !L.flags[VL_BUILD_NOW]) return;
+    const float4 xi = posS[i];
+    const Stencil st = stencil(xi, ph.h, g);
+    const float h2 = ph.h2, R = L.radius, R2 = L.radius2, eps = 1e-3f * ph.h;
+    float sum = 0.f, comp = 0.f;
+    int extra = VL_INNER;  // next slot of a further row
+    // `slot` >= 0: a fixed slot, written even when the row is empty
+    auto visit = [&](int y, int z, int slot) {
+        int s0 = 0, e0 = 0;
+        const bool any = y >= 0 && row_window(xi, y, z, R, eps, g, T, s0, e0);
+        float rs = 0.f;
+        unsigned long long ms = 0ull, me = 0ull;  // bit t - first, for the first 64
+        int first = -1, last = -1;
+        if (any) {
+            for (int t = s0; t < e0; t++) {
+                const float4 xj = __ldg(posS + t);
+                const float r2 = dist2(xi, xj);
+                const float w = fmaxf(h2 - r2, 0.f);
+                rs = fmaf(w * w, w, rs);
+                if (within_r2(r2, R2)) {
+                    if (first < 0) first = t;
+                    last = t;
+                    const int k = t - first;
+                    if (k < 64) {
+                        ms |= 1ull << k;
+                        if (neighbour_r2(r2, h2)) me |= 1ull << k;
+                    }
+                }
+            }
+        }
+        if (KAHAN) {
+            if (rs > 0.f) kahan_add(sum, comp, rs);
+        } else {
+            sum += rs;
+        }
+        if (slot < 0) {
+            if (first < 0 || extra >= VL_SLOTS) return;  // nothing within R to record
+            slot = extra++;
+        }
+        const size_t at = (size_t)slot * n + i;
+        if (first < 0) {
+            L.start[at] = 0;
+            L.skin[at] = make_uint2(0u, 0u);
+            L.exact[at] = make_uint2(0u, 0u);
+        } else if (last - first < 64) {
+            L.start[at] = first;
+            L.skin[at] = make_uint2((unsigned int)ms, (unsigned int)(ms >> 32));
+            L.exact[at] = make_uint2((unsigned int)me, (unsigned int)(me >> 32));
+        } else {
+            L.start[at] = first | (int)0x80000000;
+            L.skin[at] = make_uint2((unsigned int)(last + 1), 0u);
+            L.exact[at] = make_uint2((unsigned int)(last + 1), 0u);
+        }
+    };
+    // the reference's rows (k_density's order) into their slots, then the rest within R
+    const int y1 = min(st.y1, st.y0 + 2), z1 = min(st.z1, st.z0 + 2);
+#pragma unroll 1
+    for (int r = 0; r < VL_INNER; r++) {
+        const int z = st.z0 + r / 3, y = st.y0 + r % 3;
+        visit(z <= z1 && y <= y1 ? y : -1, z, r);
+    }
+    int ya, yb, za, zb;
+    cell_span(xi.y, R + eps, g, 1, ya, yb);
+    cell_span(xi.z, R + eps, g, 2, za, zb);
+#pragma unroll 1
+    for (int z = za; z <= zb; z++)
+#pragma unroll 1
+        for (int y = ya; y <= yb; y++)
+            if (z < st.z0 || z > z1 || y < st.y0 || y > y1) visit(y, z, -1);
+    L.rows[i] = (unsigned char)extra;
+    L.posB[i] = xi;
+    float rho = (KAHAN ? __fsub_rn(sum, comp) : sum) * ph.poly6m;
+    if (map.present) {
+        float uvw[3];
+        map_uvw(map, xi, uvw);
+        rho += tri_vec(map, uvw[0], uvw[1], uvw[2]).y;  // wall density, :242-248
+    }
+    const float p = ph.stiffness * (rho - ph.restDensity);
+    const float inv = 1.0f / rho;
+    rho4S[i] = make_float4(rho, p, p * inv * inv, inv);
+}
+
+// List form: each recorded row's candidates within R, in the recorded order;
+// the row's neighbours within h of this step are recorded for the force
+// stage over the same window (empty and unmasked rows keep what the build
+// wrote).  The next row's entries are loaded before the current row is walked.
+template <bool KAHAN>
+__global__ void __launch_bounds__(256, 8)
+k_density_lists(int n, const float4* __restrict__ posS, PhysDev ph, MapDev map, float4* __restrict__ rho4S,
+                NeighbourLists L) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || L.flags[VL_BUILD_NOW]) return;
+    const float4 xi = posS[i];
+    const float h2 = ph.h2;
+    const int rows = L.rows[i];
+    float sum = 0.f, comp = 0.f;
+    int svN = __ldg(L.start + i);
+    uint2 mN = __ldg(L.skin + i);
+#pragma unroll 1
+    for (int r = 0; r < rows; r++) {
+        const int sv = svN;
+        const uint2 m = mN;
+        if (r + 1 < rows) {
+            svN = __ldg(L.start + (size_t)(r + 1) * n + i);
+            mN = __ldg(L.skin + (size_t)(r + 1) * n + i);
+        }
+        float rs = 0.f;
+        if (sv < 0) {
+            for (int t = sv & 0x7fffffff; t < (int)m.x; t++) {
+                const float w = fmaxf(h2 - dist2(xi, __ldg(posS + t)), 0.f);
+                rs = fmaf(w * w, w, rs);
+            }
+        } else if (m.x | m.y) {
+            unsigned int e0 = 0u, e1 = 0u;
+            unsigned int b = m.x;
+            while (b) {
+                const int k = __ffs(b) - 1;
+                b &= b - 1u;
+                const float r2 = dist2(xi, __ldg(posS + sv + k));
+                const float w = fmaxf(h2 - r2, 0.f);
+                rs = fmaf(w * w, w, rs);
+                if (neighbour_r2(r2, h2)) e0 |= 1u << k;
+            }
+            b = m.y;
+            while (b) {
+                const int k = __ffs(b) - 1;
+                b &= b - 1u;
+                const float r2 = dist2(xi, __ldg(posS + sv + 32 + k));
+                const float w = fmaxf(h2 - r2, 0.f);
+                rs = fmaf(w * w, w, rs);
+                if (neighbour_r2(r2, h2)) e1 |= 1u << k;
+            }
+            L.exact[(size_t)r * n + i] = make_uint2(e0, e1);
+        }
+        if (KAHAN) {
+            if (rs > 0.f) kahan_add(sum, comp, rs);
+        } else {
+            sum += rs;
+        }
+    }
+    float rho = (KAHAN ? __fsub_rn(sum, comp) : sum) * ph.poly6m;
+    if (map.present) {
+        float uvw[3];
+        map_uvw(map, xi, uvw);
+        rho += tri_vec(map, uvw[0], uvw[1], uvw[2]).y;  // wall density, :242-248
+    }
+    const float p = ph.stiffness * (rho - ph.restDensity);
+    const float inv = 1.0f / rho;
+    rho4S[i] = make_float4(rho, p, p * inv * inv, inv);
+}
+
+// ---------------------------------------------------------------------------
 // Pair interaction (compute_viscosity_pressure_forces_and_ifsurf_cell,
 // :1459-1556), per-row partial sums, compensated totals.
 // ---------------------------------------------------------------------------
@@ -552,6 +725,86 @@ __global__ void __launch_bounds__(256, FEAT ? 3 : (BATCH || TENSION || REL || FO
 }
 
 // ---------------------------------------------------------------------------
+// Force stage over reused neighbour lists: the pretested form over the rows
+// the lists recorded (the density stage wrote this step's neighbour masks
+// over them), then wall terms, integration, collision and write-back as
+// k_force.  The next row's entries are loaded before the current row is
+// walked.  It also records, for the decision at the next step, the largest
+// squared distance of a particle from where it was when the lists were built.
+// Occupancy: 64 registers, four 256-thread blocks per SM, no spills (at 48
+// registers and five blocks the spills cost more than the warps gain).
+// ---------------------------------------------------------------------------
+template <bool KAHAN, bool TENSION>
+__global__ void __launch_bounds__(256, 4)
+k_force_lists(int n, const float4* __restrict__ posS, const float4* __restrict__ velS,
+              const float4* __restrict__ rho4S, const int* __restrict__ workIds, PhysDev ph, MapDev map,
+              int collideFlag, NeighbourLists L, float4* __restrict__ pos, float4* __restrict__ vel,
+              float4* __restrict__ accS) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    float d2 = 0.f;
+    if (i < n) {
+        const float4 xi = posS[i];
+        const float4 vi = velS[i];
+        const float4 ri = rho4S[i];
+        const float h2 = ph.h2;
+        ForceTotals<KAHAN, TENSION> A;
+        const int rows = L.rows[i];
+        int svN = __ldg(L.start + i);
+        uint2 mN = __ldg(L.exact + i);
+        auto pairs = [&](RowSums<TENSION>& R, int base, unsigned int m) {
+            R.hits += __popc(m);
+            while (m) {
+                const int t = base + __ffs(m) - 1;
+                m &= m - 1u;
+                R.template add<false>(ph, Pair(ph, xi, vi, __ldg(posS + t), __ldg(velS + t)), ri.z,
+                                      __ldg(rho4S + t));
+            }
+        };
+#pragma unroll 1
+        for (int r = 0; r < rows; r++) {
+            const int sv = svN;
+            const uint2 m = mN;
+            if (r + 1 < rows) {
+                svN = __ldg(L.start + (size_t)(r + 1) * n + i);
+                mN = __ldg(L.exact + (size_t)(r + 1) * n + i);
+            }
+            RowSums<TENSION> R;
+            R.clear();
+            if (sv < 0) {
+                for (int t = sv & 0x7fffffff; t < (int)m.x; t++) {
+                    const float4 xj = __ldg(posS + t);
+                    if (neighbour_r2(dist2(xi, xj), h2))
+                        R.add(ph, Pair(ph, xi, vi, xj, __ldg(velS + t)), ri.z, __ldg(rho4S + t));
+                }
+            } else {
+                pairs(R, sv, m.x);
+                pairs(R, sv + 32, m.y);
+            }
+            A.add(R);
+        }
+        float mapDist = 1e30f, mapN[3] = {0.f, 0.f, 0.f};
+        float3 x, v;
+        float acc[3];
+        force_finish<KAHAN, TENSION, false>(A, xi, vi, ri, ph, map, collideFlag, x, v, acc, mapDist, mapN, xi);
+        const int id = workIds[i];
+        pos[id] = make_float4(x.x, x.y, x.z, xi.w);
+        vel[id] = make_float4(v.x, v.y, v.z, 0.f);
+        accS[i] = make_float4(acc[0], acc[1], acc[2], 0.f);
+        const float4 b = __ldg(L.posB + i);
+        const float dx = x.x - b.x, dy = x.y - b.y, dz = x.z - b.z;
+        d2 = dx * dx + dy * dy + dz * dz;
+        if (!(d2 == d2)) d2 = __uint_as_float(0x7f800000u);  // NaN: as far as it gets
+    }
+    // squared distances are non-negative: their bits order as the values do.
+    // The recorded maximum only grows, so a warp that does not exceed the value
+    // it reads (possibly an older, smaller one) has nothing to add: this keeps
+    // the atomics on the one word to the few warps that raise it.
+    const unsigned int w = __reduce_max_sync(0xffffffffu, __float_as_uint(d2));
+    if ((threadIdx.x & 31) == 0 && w > 0u && w > *(volatile unsigned int*)(L.flags + VL_DISP))
+        atomicMax(L.flags + VL_DISP, w);
+}
+
+// ---------------------------------------------------------------------------
 // The pretested force form with each warp's neighbour rows staged in shared
 // memory by TMA (plain handles).  The 32 particles of a warp are consecutive
 // in the working order, so their windows into one stencil row overlap: the
@@ -995,6 +1248,65 @@ void launch_force_learned(int n, const float4* posS, const float4* velS, const f
         if (tension) force_learned_dispatch<false, true>(F, m, status, s);
         else force_learned_dispatch<false, false>(F, m, status, s);
     }
+}
+
+// After the positions were written: the largest squared distance of a
+// particle from where it was when the lists were built, in place of the one
+// the steps accumulated (the next step builds the lists again only if that
+// exceeds the rebuild distance).  flags[VL_DISP] must be zero on entry.
+__global__ void k_list_displacement(int n, const float4* __restrict__ pos, const int* __restrict__ workIds,
+                                    NeighbourLists L) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    float d2 = 0.f;
+    if (k < n) {
+        const float4 x = __ldg(pos + workIds[k]), b = __ldg(L.posB + k);
+        const float dx = x.x - b.x, dy = x.y - b.y, dz = x.z - b.z;
+        d2 = dx * dx + dy * dy + dz * dz;
+        if (!(d2 == d2)) d2 = __uint_as_float(0x7f800000u);
+    }
+    const unsigned int w = __reduce_max_sync(0xffffffffu, __float_as_uint(d2));
+    if ((threadIdx.x & 31) == 0 && w > 0u && w > *(volatile unsigned int*)(L.flags + VL_DISP))
+        atomicMax(L.flags + VL_DISP, w);
+}
+
+void launch_list_displacement(int n, const float4* pos, const int* workIds, const NeighbourLists& L, cudaStream_t s) {
+    if (n <= 0) return;
+    cudaMemsetAsync(L.flags + VL_DISP, 0, sizeof(unsigned int), s);
+    k_list_displacement<<<(n + 255) / 256, 256, 0, s>>>(n, pos, workIds, L);
+}
+
+void launch_density_lists(int n, const float4* posS, RowTables T, GridDev g, PhysDev ph, MapDev map, float4* rho4S,
+                          const NeighbourLists& L, const StepConfig& cfg, bool build, bool reuse, cudaStream_t s) {
+    if (n <= 0) return;
+    const int bs = cfg.densityBlock > 0 ? cfg.densityBlock : 128;
+    const int grid = (n + bs - 1) / bs;
+    if (build) {
+        if (cfg.kahan) k_density_build<true><<<grid, bs, 0, s>>>(n, posS, T, g, ph, map, rho4S, L);
+        else k_density_build<false><<<grid, bs, 0, s>>>(n, posS, T, g, ph, map, rho4S, L);
+    }
+    if (reuse) {
+        if (cfg.kahan) k_density_lists<true><<<grid, bs, 0, s>>>(n, posS, ph, map, rho4S, L);
+        else k_density_lists<false><<<grid, bs, 0, s>>>(n, posS, ph, map, rho4S, L);
+    }
+}
+
+void launch_force_lists(int n, const float4* posS, const float4* velS, const float4* rho4S, const int* workIds,
+                        PhysDev ph, MapDev map, int collide, const NeighbourLists& L, float4* pos, float4* vel,
+                        float4* accS, const StepConfig& cfg, cudaStream_t s) {
+    if (n <= 0) return;
+    const int bs = cfg.forceBlock > 0 ? cfg.forceBlock : 128;
+    const int grid = (n + bs - 1) / bs;
+    const bool tension = ph.tension != 0.0f;
+#define SPH_FORCE_LISTS(K, T) \
+    k_force_lists<K, T><<<grid, bs, 0, s>>>(n, posS, velS, rho4S, workIds, ph, map, collide, L, pos, vel, accS)
+    if (cfg.kahan) {
+        if (tension) SPH_FORCE_LISTS(true, true);
+        else SPH_FORCE_LISTS(true, false);
+    } else {
+        if (tension) SPH_FORCE_LISTS(false, true);
+        else SPH_FORCE_LISTS(false, false);
+    }
+#undef SPH_FORCE_LISTS
 }
 
 }  // namespace sph

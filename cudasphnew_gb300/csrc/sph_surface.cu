@@ -46,6 +46,45 @@ __global__ void k_surface(int n, const float4* __restrict__ posS, const int* __r
     flags[workIds[u]] = surface ? 1 : 0;
 }
 
+// The same test over the reused neighbour lists (after a step that ran over
+// them the sorted copies are in the lists' working order, which the cell
+// tables do not describe): the candidates within the skin radius are a
+// superset of those within h, visited in the lists' order.
+__global__ void k_surface_lists(int n, const float4* __restrict__ posS, const int* __restrict__ workIds,
+                                NeighbourLists L, float h, float cmThresh, float countThresh, int* __restrict__ flags) {
+    const int u = blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= n) return;
+    const float4 xi = posS[u];
+    const float h2 = h * h;
+    double sx = 0.0, sy = 0.0, sz = 0.0;
+    int cnt = 0;
+    const int rows = L.rows[u];
+    for (int r = 0; r < rows; r++) {
+        const size_t at = (size_t)r * n + u;
+        const int sv = L.start[at];
+        const uint2 m2 = L.skin[at];
+        const unsigned long long m = (unsigned long long)m2.x | ((unsigned long long)m2.y << 32);
+        const int t0 = sv & 0x7fffffff;
+        const int t1 = sv < 0 ? (int)m2.x : t0 + 64;
+        for (int t = t0; t < t1; t++) {
+            if (sv >= 0 && !((m >> (t - t0)) & 1ull)) continue;
+            const float4 xj = posS[t];
+            const float r2 = dist2(xi, xj);
+            if (t == u || !(r2 <= h2)) continue;
+            sx += xj.x;
+            sy += xj.y;
+            sz += xj.z;
+            cnt++;
+        }
+    }
+    bool surface = (float)cnt < countThresh;
+    if (cnt > 0) {
+        const double cx = sx / cnt - xi.x, cy = sy / cnt - xi.y, cz = sz / cnt - xi.z;
+        surface = surface || sqrt(cx * cx + cy * cy + cz * cz) > (double)cmThresh * h;
+    }
+    flags[workIds[u]] = surface ? 1 : 0;
+}
+
 }  // namespace
 }  // namespace sph
 
@@ -69,9 +108,14 @@ extern "C" sph_status sph_surface_particles(sph_handle s, int* flags) {
         posS = absS;
         g.rel = 0;
     }
-    k_surface<<<(s->n + 127) / 128, 128, 0, s->stream>>>(s->n, posS, s->sb.workIds, rows_of(s), g,
-                                                         s->P.compactSupport, s->P.cmDistanceThresh,
-                                                         s->P.nPartTresh, d);
+    if (s->vlOn && s->lastStepLists)
+        k_surface_lists<<<(s->n + 127) / 128, 128, 0, s->stream>>>(s->n, posS, s->sb.workIds, s->vl,
+                                                                   s->P.compactSupport, s->P.cmDistanceThresh,
+                                                                   s->P.nPartTresh, d);
+    else
+        k_surface<<<(s->n + 127) / 128, 128, 0, s->stream>>>(s->n, posS, s->sb.workIds, rows_of(s), g,
+                                                             s->P.compactSupport, s->P.cmDistanceThresh,
+                                                             s->P.nPartTresh, d);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemcpyAsync(flags, d, sizeof(int) * (size_t)s->n, cudaMemcpyDeviceToHost, s->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);

@@ -74,6 +74,7 @@ SIGNATURES = {
     "sph_sdf_free": (None, [_vp]),
     "sph_surface_particles": (_i, [_vp, _vp]),
     "sph_time_kernel": (_i, [_vp, ctypes.c_int, ctypes.c_int, _vp]),
+    "sph_neighbour_builds": (_i, [_vp, _vp]),
     "sph_camera_look_at": (_i, [_vp, _vp, _vp, _vp]),
     "sph_camera_perspective": (_i, [_vp, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float]),
     "sph_render": (_i, [_vp, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _vp, _vp]),
@@ -494,6 +495,12 @@ class ParticleSimulation:
         us = ctypes.c_float()
         check(load().sph_time_kernel(self._h, {"density": 4, "force": 5}[stage], reps, ctypes.byref(us)))
         return us.value
+
+    def neighbour_builds(self) -> int:
+        """How many times the plain steps have built the reused neighbour lists."""
+        b = ctypes.c_uint()
+        check(load().sph_neighbour_builds(self._h, ctypes.byref(b)))
+        return int(b.value)
 
     def surface_particles(self) -> np.ndarray:
         """CreateIsParticleSurfaceList: 1 for surface particles (particle order)."""

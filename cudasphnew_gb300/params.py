@@ -77,6 +77,7 @@ class Options(ctypes.Structure):
         ("cellRelative", ctypes.c_int),
         ("splitMin", F3),
         ("splitMax", F3),
+        ("neighbourSkin", ctypes.c_float),
     ]
 
 
@@ -268,6 +269,11 @@ def dam_break_params(box_lo, box_hi, num_particles: int, dt: float = 1e-4,
     return p
 
 
+# Default skin of the reused neighbour lists, as a fraction of compactSupport
+# (sph_options.neighbourSkin; the C default of sph_default_options).
+NEIGHBOUR_SKIN = 0.1
+
+
 def default_options(gravity_axis: int = 1, box_collision: bool = True) -> Options:
     o = Options()
     o.gravityAxis = gravity_axis
@@ -275,6 +281,7 @@ def default_options(gravity_axis: int = 1, box_collision: bool = True) -> Option
     for a, (lo, hi) in enumerate(zip((0.2, -3.0e38, -3.0e38), (0.5, 3.0e38, 3.0e38))):
         o.splitMin[a] = lo
         o.splitMax[a] = hi
+    o.neighbourSkin = NEIGHBOUR_SKIN
     return o
 
 

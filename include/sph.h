@@ -98,6 +98,20 @@ typedef struct sph_options {
                            1024.  No reference counterpart. */
     float splitMin[3];  /* two-scale split region; reference: 0.2 <= x <= 0.5 */
     float splitMax[3];  /* (find_split_particles, :948) */
+    float neighbourSkin; /* plain steps of single-scene handles: the neighbour
+                            candidates within (1 + neighbourSkin) * compactSupport
+                            are recorded when the lists are built and reused by
+                            later steps until some particle has moved more than
+                            0.45 * neighbourSkin * compactSupport since, when
+                            they are built again (a Verlet list; a pair that
+                            comes within compactSupport in the meantime was
+                            within the skin when they were built).  The cell
+                            tables, hash and permutation are still built, bit
+                            exact, in every step; only the order in which the
+                            neighbour sums are taken follows the lists.  0: the
+                            neighbour search runs in every step, as the
+                            reference does (compute_particle_density_pressure,
+                            :196-256).  In [0, 0.4].  No reference counterpart. */
 } sph_options;
 
 /* Boundary solids ("SPH in complex shapes", SphInComplexShapes.h:18-93). */
@@ -524,6 +538,11 @@ const char* sph_stage_name(int stage);
  * kind of step it replaces that step's result with the plain step's).  No
  * reference counterpart. */
 sph_status sph_time_kernel(sph_handle h, int stage, int reps, float* microseconds);
+
+/* How many times the handle's plain steps have built their reused neighbour
+ * lists (sph_options.neighbourSkin; 0 when the handle has none).  Waits for
+ * the handle's stream.  No reference counterpart. */
+sph_status sph_neighbour_builds(sph_handle h, unsigned int* builds);
 
 /* Largest inputs sph_cell_tables_noalloc() accepts. */
 #define SPH_NOALLOC_MAX_PARTICLES 65536

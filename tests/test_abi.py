@@ -99,6 +99,20 @@ def test_default_options_are_the_reference_values(sphlib):
     sphlib.load().sph_default_options(ctypes.byref(o))
     assert o.gravityAxis == 1 and o.boxCollision == 0
     assert (o.splitMin[0], o.splitMax[0]) == pytest.approx((0.2, 0.5))
+    # reused neighbour lists are on by default for plain steps; the Python scenes agree
+    assert o.neighbourSkin == pytest.approx(0.1) == P.default_options().neighbourSkin
+
+
+def test_neighbour_skin_range_without_gpu(sphlib):
+    L = sphlib.load()
+    p = P.dam_break_params((0, 0, 0), (1, 1, 1), 4)
+    buf = (ctypes.c_float * 12)()
+    h = ctypes.c_void_p()
+    for bad in (-0.1, 0.41, float("nan")):
+        o = P.default_options()
+        o.neighbourSkin = bad
+        st = L.sph_create(ctypes.byref(p), ctypes.byref(o), buf, None, None, ctypes.byref(h))
+        assert st == 1 and h.value is None and b"neighbourSkin" in L.sph_last_error()
 
 
 def test_status_strings_and_errors_without_gpu(sphlib):

@@ -21,7 +21,10 @@ def small_batch():
 
 
 def run_alone(sphlib, sc, steps):
-    with sphlib.ParticleSimulation(sc.params, sc.positions, sc.velocities, sc.options, sc.boundary) as sim:
+    # batched handles search the neighbours in every step: so does the lone scene
+    o = type(sc.options).from_buffer_copy(bytes(sc.options))
+    o.neighbourSkin = 0.0
+    with sphlib.ParticleSimulation(sc.params, sc.positions, sc.velocities, o, sc.boundary) as sim:
         sim.step(count=steps)
         h, ids, start, end = sim.cells()
         return dict(pos=sim.positions(), vel=sim.velocities(), rho=sim.read(sphlib.FIELD_DENSITY),

@@ -133,12 +133,17 @@ def small():
     return scenes.dam_break(16, 16, 8, (0, 0, 0), (0.5, 0.5, 0.5), 5, "small", 1)
 
 
-def make(sphlib, sc, pos=None, vel=None, dt_scale=1):
+def make(sphlib, sc, pos=None, vel=None, dt_scale=1, skin=None):
+    """A handle of `sc` (optionally from another state, with a longer step, or
+    with another neighbourSkin: 0 runs the neighbour search in every step)."""
     p = P.SimulationParameters.from_buffer_copy(bytes(sc.params))
     p.timeStep = float(np.float32(p.timeStep * dt_scale))
     p.timeStepSubParticles = p.timeStep
+    o = P.Options.from_buffer_copy(bytes(sc.options))
+    if skin is not None:
+        o.neighbourSkin = skin
     return sphlib.ParticleSimulation(p, sc.positions if pos is None else pos,
-                                     sc.velocities if vel is None else vel, sc.options, sc.boundary)
+                                     sc.velocities if vel is None else vel, o, sc.boundary)
 
 
 def density_at(sphlib, sc, pos, vel):
@@ -334,7 +339,8 @@ def test_audit_rolls_back_to_the_plain_solver(sphlib):
         pos, vel = sim.positions(), sim.velocities()
         rep = sim.corrector_report()
     assert rep.audits == k and rep.rollbacks == k and rep.maxAuditError > 0
-    with make(sphlib, sc) as plain:
+    # the audit's plain solver searches the neighbours in every step
+    with make(sphlib, sc, skin=0.0) as plain:
         plain.step(count=k * stride)
         np.testing.assert_array_equal(pos, plain.positions())
         np.testing.assert_array_equal(vel, plain.velocities())
