@@ -193,9 +193,9 @@ def kernel_sources_sha16():
 
 def profiled_traffic(workload):
     """DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of
-    k_density and k_force from profiles/traffic_<workload>.md, for the kernel
-    sources that capture was made from; {} when there is no capture or the
-    sources have changed since."""
+    the density and force kernels (k_density*, k_force*) from
+    profiles/traffic_<workload>.md, for the kernel sources that capture was
+    made from; {} when there is no capture or the sources have changed since."""
     path = os.path.join(ROOT, "profiles", f"traffic_{workload}.md")
     out = {}
     try:
@@ -205,7 +205,7 @@ def profiled_traffic(workload):
     sha = kernel_sources_sha16()
     for line in lines:
         cells = [c.strip() for c in line.strip().strip("|").split("|")]
-        if len(cells) >= 4 and cells[0] in ("k_density", "k_force") and cells[3] == sha:
+        if len(cells) >= 4 and cells[0].startswith(("k_density", "k_force")) and cells[3] == sha:
             try:
                 out[cells[0]] = float(cells[1])
             except ValueError:
@@ -243,7 +243,7 @@ def kernel_roofline(kernel, n, C, g3, pairs, t_s, hbm_gbs, fp32, traffic=None):
     its compulsory bytes at the measured HBM peak and its flops at the FP32
     peak; `frac` is the HBM fraction (the contract's bound), `combined_frac`
     = max(T_bytes, T_flop) / T."""
-    if kernel == "k_density":
+    if kernel.startswith("k_density"):
         byts = DENSITY_BYTES_PER_PARTICLE * n
         flop = DENSITY_FLOP_PER_PAIR * (pairs + n)
     else:
@@ -774,8 +774,12 @@ def run_ours(args):
     sms = torch.cuda.get_device_properties(local).multi_processor_count
     fp32 = fp32_peak(sms, clk.get("sm_max_mhz") or 2070.0)
     traffic = profiled_traffic(sc.name)
+    # the kernels a plain step of this handle runs: the list forms when the
+    # scene reuses neighbour lists
+    lists_on = float(sc.options.neighbourSkin) > 0
+    kd, kf = ("k_density_lists", "k_force_lists") if lists_on else ("k_density", "k_force")
     roofs = {k: kernel_roofline(k, n, C, g3, pairs, t, peak, fp32, traffic.get(k))
-             for k, t in (("k_density", density_avg_s), ("k_force", force_avg_s))}
+             for k, t in ((kd, density_avg_s), (kf, force_avg_s))}
     for r in roofs.values():
         r["peak_source"] = peak_kind
         r["timing"] = (f"50 back-to-back launches of {r['kernel']} on one step's sorted state, CUDA events on "
@@ -843,8 +847,8 @@ def run_ours(args):
                    "d2h_bytes_per_step": n * 12, "steps": e2e_steps,
                    "path": "sph_write(VD, VEL) + sph_step + sph_read(VD), pinned host buffers"},
            "roofline": roofs[dominant],
-           "roofline_density": roofs["k_density"],
-           "roofline_force": roofs["k_force"],
+           "roofline_density": roofs[kd],
+           "roofline_force": roofs[kf],
            "stages_us": {k: round(v[0] / v[1] * 1e3, 2) for k, v in stages.items()}}
     if batched is not None:
         out["batched"] = batched

@@ -306,7 +306,7 @@ static void enqueue_lists(sph_sim* s, const GridDev& g, const PhysDev& ph, int c
     mark(ST_RANK);
     launch_rank_gather(n, s->sb, s->pos, s->vel, g, s->posS, s->velS, st, &s->vl);
     mark(ST_DENSITY);
-    launch_density_lists(n, s->posS, rows_of(s), g, ph, s->map, s->rho4S, s->vl, s->cfg, true, true, st);
+    launch_density_lists(n, s->posS, s->velS, rows_of(s), g, ph, s->map, s->rho4S, s->vl, s->cfg, true, true, st);
     // the sorted copies are now this step's own: a reuse the audit granted is used up
     cudaMemsetAsync(s->reuse, 0, sizeof(int), st);
     mark(ST_FORCE);
@@ -1411,7 +1411,7 @@ sph_status sph_time_kernel(sph_handle s, int stage, int reps, float* microsecond
     auto launch = [&]() {
         if (lists) {
             if (stage == ST_DENSITY)
-                launch_density_lists(n, s->posS, rows_of(s), g, ph, s->map, s->rho4S, s->vl, s->cfg, false, true,
+                launch_density_lists(n, s->posS, s->velS, rows_of(s), g, ph, s->map, s->rho4S, s->vl, s->cfg, false, true,
                                      st);
             else
                 launch_force_lists(n, s->posS, s->velS, s->rho4S, s->sb.workIds, ph, s->map, s->O.boxCollision,
@@ -1427,7 +1427,7 @@ sph_status sph_time_kernel(sph_handle s, int stage, int reps, float* microsecond
     if (stage == ST_FORCE) {  // the masks of the current tuning
         StepConfig c = s->cfg;
         if (lists)
-            launch_density_lists(n, s->posS, rows_of(s), g, ph, s->map, s->rho4S, s->vl, c, false, true, st);
+            launch_density_lists(n, s->posS, s->velS, rows_of(s), g, ph, s->map, s->rho4S, s->vl, c, false, true, st);
         else
             launch_density(n, s->posS, rows_of(s), g, ph, s->map, s->rho4S, s->rowStart, s->rowMask, c, st);
     }

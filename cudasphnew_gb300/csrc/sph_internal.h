@@ -219,7 +219,9 @@ void launch_rank_gather(int n, SortBuffers sb, const float4* pos, const float4* 
 // Density stage over reused neighbour lists: the build form (the reference's
 // rows and the skin rows, recording the lists) and the list form; each
 // returns at once unless the step is of its kind.
-void launch_density_lists(int n, const float4* posS, RowTables T, GridDev g, PhysDev ph, MapDev map,
+// Besides rho4S, each particle's p/rho^2 and 1/rho go to the fourth lanes of
+// its sorted position and velocity, where the list force stage reads them.
+void launch_density_lists(int n, float4* posS, float4* velS, RowTables T, GridDev g, PhysDev ph, MapDev map,
                           float4* rho4S, const NeighbourLists& L, const StepConfig& cfg, bool build, bool reuse,
                           cudaStream_t s);
 // After a write of the positions: the largest distance from the build

@@ -121,7 +121,7 @@ __device__ __forceinline__ bool within_r2(float r2, float R2) {  // r2 >= 0 or N
 
 template <bool KAHAN>
 __global__ void __launch_bounds__(256, 4)
-k_density_build(int n, const float4* __restrict__ posS, RowTables T, GridDev g, PhysDev ph, MapDev map,
+k_density_build(int n, float4* posS, float4* velS, RowTables T, GridDev g, PhysDev ph, MapDev map,
                 float4* __restrict__ rho4S, NeighbourLists L) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || !L.flags[VL_BUILD_NOW]) return;
@@ -204,6 +204,10 @@ k_density_build(int n, const float4* __restrict__ posS, RowTables T, GridDev g, 
     const float p = ph.stiffness * (rho - ph.restDensity);
     const float inv = 1.0f / rho;
     rho4S[i] = make_float4(rho, p, p * inv * inv, inv);
+    // what the force stage needs of a neighbour besides its position and
+    // velocity rides in their unused fourth lanes: two loads per pair, not three
+    posS[i].w = p * inv * inv;
+    velS[i].w = inv;
 }
 
 // List form: each recorded row's candidates within R, in the recorded order;
@@ -212,7 +216,7 @@ k_density_build(int n, const float4* __restrict__ posS, RowTables T, GridDev g, 
 // wrote).  The next row's entries are loaded before the current row is walked.
 template <bool KAHAN>
 __global__ void __launch_bounds__(256, 8)
-k_density_lists(int n, const float4* __restrict__ posS, PhysDev ph, MapDev map, float4* __restrict__ rho4S,
+k_density_lists(int n, float4* posS, float4* velS, PhysDev ph, MapDev map, float4* __restrict__ rho4S,
                 NeighbourLists L) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || L.flags[VL_BUILD_NOW]) return;
@@ -273,6 +277,10 @@ k_density_lists(int n, const float4* __restrict__ posS, PhysDev ph, MapDev map, 
     const float p = ph.stiffness * (rho - ph.restDensity);
     const float inv = 1.0f / rho;
     rho4S[i] = make_float4(rho, p, p * inv * inv, inv);
+    // what the force stage needs of a neighbour besides its position and
+    // velocity rides in their unused fourth lanes: two loads per pair, not three
+    posS[i].w = p * inv * inv;
+    velS[i].w = inv;
 }
 
 // ---------------------------------------------------------------------------
@@ -751,13 +759,15 @@ k_force_lists(int n, const float4* __restrict__ posS, const float4* __restrict__
         const int rows = L.rows[i];
         int svN = __ldg(L.start + i);
         uint2 mN = __ldg(L.exact + i);
+        // a neighbour's p/rho^2 and 1/rho ride in the fourth lanes of its
+        // sorted position and velocity (written by the density stage)
         auto pairs = [&](RowSums<TENSION>& R, int base, unsigned int m) {
             R.hits += __popc(m);
             while (m) {
                 const int t = base + __ffs(m) - 1;
                 m &= m - 1u;
-                R.template add<false>(ph, Pair(ph, xi, vi, __ldg(posS + t), __ldg(velS + t)), ri.z,
-                                      __ldg(rho4S + t));
+                const float4 xj = __ldg(posS + t), vj = __ldg(velS + t);
+                R.template add<false>(ph, Pair(ph, xi, vi, xj, vj), ri.z, make_float4(0.f, 0.f, xj.w, vj.w));
             }
         };
 #pragma unroll 1
@@ -773,8 +783,10 @@ k_force_lists(int n, const float4* __restrict__ posS, const float4* __restrict__
             if (sv < 0) {
                 for (int t = sv & 0x7fffffff; t < (int)m.x; t++) {
                     const float4 xj = __ldg(posS + t);
-                    if (neighbour_r2(dist2(xi, xj), h2))
-                        R.add(ph, Pair(ph, xi, vi, xj, __ldg(velS + t)), ri.z, __ldg(rho4S + t));
+                    if (neighbour_r2(dist2(xi, xj), h2)) {
+                        const float4 vj = __ldg(velS + t);
+                        R.add(ph, Pair(ph, xi, vi, xj, vj), ri.z, make_float4(0.f, 0.f, xj.w, vj.w));
+                    }
                 }
             } else {
                 pairs(R, sv, m.x);
@@ -787,7 +799,7 @@ k_force_lists(int n, const float4* __restrict__ posS, const float4* __restrict__
         float acc[3];
         force_finish<KAHAN, TENSION, false>(A, xi, vi, ri, ph, map, collideFlag, x, v, acc, mapDist, mapN, xi);
         const int id = workIds[i];
-        pos[id] = make_float4(x.x, x.y, x.z, xi.w);
+        pos[id] = make_float4(x.x, x.y, x.z, 0.f);  // (the sorted copy's fourth lane holds p/rho^2)
         vel[id] = make_float4(v.x, v.y, v.z, 0.f);
         accS[i] = make_float4(acc[0], acc[1], acc[2], 0.f);
         const float4 b = __ldg(L.posB + i);
@@ -1275,18 +1287,19 @@ void launch_list_displacement(int n, const float4* pos, const int* workIds, cons
     k_list_displacement<<<(n + 255) / 256, 256, 0, s>>>(n, pos, workIds, L);
 }
 
-void launch_density_lists(int n, const float4* posS, RowTables T, GridDev g, PhysDev ph, MapDev map, float4* rho4S,
-                          const NeighbourLists& L, const StepConfig& cfg, bool build, bool reuse, cudaStream_t s) {
+void launch_density_lists(int n, float4* posS, float4* velS, RowTables T, GridDev g, PhysDev ph, MapDev map,
+                          float4* rho4S, const NeighbourLists& L, const StepConfig& cfg, bool build, bool reuse,
+                          cudaStream_t s) {
     if (n <= 0) return;
     const int bs = cfg.densityBlock > 0 ? cfg.densityBlock : 128;
     const int grid = (n + bs - 1) / bs;
     if (build) {
-        if (cfg.kahan) k_density_build<true><<<grid, bs, 0, s>>>(n, posS, T, g, ph, map, rho4S, L);
-        else k_density_build<false><<<grid, bs, 0, s>>>(n, posS, T, g, ph, map, rho4S, L);
+        if (cfg.kahan) k_density_build<true><<<grid, bs, 0, s>>>(n, posS, velS, T, g, ph, map, rho4S, L);
+        else k_density_build<false><<<grid, bs, 0, s>>>(n, posS, velS, T, g, ph, map, rho4S, L);
     }
     if (reuse) {
-        if (cfg.kahan) k_density_lists<true><<<grid, bs, 0, s>>>(n, posS, ph, map, rho4S, L);
-        else k_density_lists<false><<<grid, bs, 0, s>>>(n, posS, ph, map, rho4S, L);
+        if (cfg.kahan) k_density_lists<true><<<grid, bs, 0, s>>>(n, posS, velS, ph, map, rho4S, L);
+        else k_density_lists<false><<<grid, bs, 0, s>>>(n, posS, velS, ph, map, rho4S, L);
     }
 }
 
