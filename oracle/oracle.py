@@ -378,3 +378,60 @@ def render_splats(view, proj, passes, width, height):
     rgba[empty] = 255
     winner = np.where(empty, -1, key & 0xFFFFFFFF)
     return rgba, winner
+
+
+# ---------------------------------------------------------------------------
+# The reference's own plain-step code on the host (oracle/_ref/libsph_ref.so,
+# built by oracle/build_ref.py where the reference checkout is present).
+# ---------------------------------------------------------------------------
+REF_LIB_PATH = os.path.join(HERE, "_ref", "libsph_ref.so")
+_ref = None
+
+
+def ref_build() -> str | None:
+    """Builds the reference harness if the checkout is present; its path or None."""
+    import build_ref
+    return build_ref.build()
+
+
+def ref_available() -> bool:
+    return os.path.exists(REF_LIB_PATH) or ref_build() is not None
+
+
+def ref_lib():
+    global _ref
+    if _ref is None:
+        if not os.path.exists(REF_LIB_PATH) and ref_build() is None:
+            raise RuntimeError("the reference checkout is absent: oracle/_ref cannot be built")
+        L = ctypes.CDLL(REF_LIB_PATH)
+        vp = ctypes.c_void_p
+        L.ref_step_plain.argtypes = [vp] * 8 + [ctypes.c_float, ctypes.c_float, ctypes.c_int] + [vp] * 4
+        L.ref_step_plain.restype = ctypes.c_int
+        _ref = L
+    return _ref
+
+
+def ref_step_plain(p: SimulationParameters, bm: BoundaryMaps | None, pos: np.ndarray, vel: np.ndarray,
+                   collide: bool) -> dict:
+    """One plain step of the reference's own code (Advance, plus
+    handleCollisions when `collide`): the cell tables and the new state."""
+    n = int(p.numParticles)
+    vd = np.ascontiguousarray(pos, np.float32).reshape(n, 3).copy()
+    sd = np.zeros((n, 10), np.float32)
+    sd[:, 6:9] = np.asarray(vel, np.float32).reshape(n, 3)
+    C = p.num_cells
+    h, ids = np.zeros(n, np.int32), np.zeros(n, np.int32)
+    start, end = np.zeros(C, np.int32), np.zeros(C, np.int32)
+    if bm is not None:
+        dims = np.asarray(bm.dims, np.uint32)
+        origin = np.asarray([bm.desc.gridStart[a] for a in range(3)], np.float32)
+        maps = [_ptr(bm.dist), _ptr(bm.dens), _ptr(bm.visc), _ptr(dims), _ptr(origin)]
+        spacing, rest = float(bm.desc.gridSpacing), float(bm.desc.restDistance)
+    else:
+        maps, spacing, rest = [None] * 5, 1.0, 0.0
+    rc = ref_lib().ref_step_plain(ctypes.byref(p), _ptr(vd), _ptr(sd), *maps, spacing, rest, 1 if collide else 0,
+                                  _ptr(h), _ptr(ids), _ptr(start), _ptr(end))
+    if rc:
+        raise ValueError("a particle hashed outside the reference's cell tables")
+    return dict(hash=h, ids=ids, start=start, end=end, rho=sd[:, 1].copy(), p=sd[:, 2].copy(),
+                acc=sd[:, 3:6].copy(), pos=vd, vel=sd[:, 6:9].copy())
