@@ -291,25 +291,46 @@ def load_oracle():
     return oracle, cores
 
 
-def cpu_baseline(sc, max_seconds=20.0, max_steps=50):
-    """The oracle's FP32 restatement of the reference step on all host cores,
-    on a bounded number of full steps of the same scene."""
-    oracle, cores = load_oracle()
+def reference_stepper(oracle, cores, sc):
+    """A plain step of the reference on the host cores: the reference's own
+    kernels compiled for the host (oracle/_ref: its compute_particle_hash,
+    density, acceleration, integrate_euler and collision_handling kernels, the
+    threads of each spread over the cores) when that build is available, else
+    the oracle's FP32 restatement of them (bit-identical on every pinned
+    scene).  Returns (step(x, v) -> (x', v'), kind, description)."""
     bm = oracle.boundary_maps(sc.boundary) if sc.boundary is not None else None
-    x, v = sc.positions, sc.velocities
-    r = oracle.step_plain(sc.params, sc.options, bm, x, v)  # warm-up step
-    x, v = r["pos"], r["vel"]
+    if oracle.ref_available():
+        oracle.ref_set_threads(cores)
+        collide = bool(sc.options.boxCollision)
+
+        def step(x, v):
+            r = oracle.ref_step_plain(sc.params, bm, x, v, collide)
+            return r["pos"], r["vel"]
+        return step, "reference", ("the reference's own kernels compiled for the host, each kernel's threads "
+                                   "spread over the cores with OpenMP (its gravity acts along y; the work per "
+                                   "step is the scene's)")
+
+    def step(x, v):
+        r = oracle.step_plain(sc.params, sc.options, bm, x, v)
+        return r["pos"], r["vel"]
+    return step, "port", "FP32 restatement of the reference, OpenMP over particles"
+
+
+def cpu_baseline(sc, max_seconds=20.0, max_steps=50):
+    """The reference step on all host cores (reference_stepper), on a bounded
+    number of full steps of the same scene."""
+    oracle, cores = load_oracle()
+    step, kind, what = reference_stepper(oracle, cores, sc)
+    x, v = step(sc.positions, sc.velocities)  # warm-up step
     steps, t0 = 0, time.perf_counter()
     while True:
-        r = oracle.step_plain(sc.params, sc.options, bm, x, v)
-        x, v = r["pos"], r["vel"]
+        x, v = step(x, v)
         steps += 1
         el = time.perf_counter() - t0
         if el > max_seconds or steps >= max_steps:
             break
-    return {"value": sc.n * steps / el, "unit": UNIT, "cores": cores, "cpu": cpu_model(), "kind": "port",
-            "sample": f"{steps} full steps of the {sc.n}-particle scene after 1 warm-up step "
-                      f"({el:.1f} s, FP32 restatement of the reference, OpenMP over particles)"}
+    return {"value": sc.n * steps / el, "unit": UNIT, "cores": cores, "cpu": cpu_model(), "kind": kind,
+            "sample": f"{steps} full steps of the {sc.n}-particle scene after 1 warm-up step ({el:.1f} s, {what})"}
 
 
 def cpu_baseline_two_scale(sc, max_seconds=15.0, max_steps=20):
@@ -363,15 +384,13 @@ def run_reference(args):
     # each step is one full CPU step of the workload; W warm-up steps, then K
     # timed steps, bounded to ~2 minutes of CPU time
     oracle, cores = load_oracle()
-    bm = oracle.boundary_maps(sc.boundary) if sc.boundary is not None else None
+    step, kind, what = reference_stepper(oracle, cores, sc)
     x, v = sc.positions, sc.velocities
     for _ in range(args.warmup):
-        r = oracle.step_plain(sc.params, sc.options, bm, x, v)
-        x, v = r["pos"], r["vel"]
+        x, v = step(x, v)
     steps, t0 = 0, time.perf_counter()
     while steps < args.steps:
-        r = oracle.step_plain(sc.params, sc.options, bm, x, v)
-        x, v = r["pos"], r["vel"]
+        x, v = step(x, v)
         steps += 1
         if time.perf_counter() - t0 > 120.0:
             break
@@ -384,11 +403,10 @@ def run_reference(args):
            "config": {"workload": sc.name, "particles": sc.n, "cells": sc.params.num_cells,
                       "boundary_map": list(sc.boundary.dims()) if sc.boundary is not None else None,
                       "parallelism": "replicas" if world > 1 else "single"},
-           "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores, "cpu": cpu_model(), "kind": "port",
+           "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores, "cpu": cpu_model(), "kind": kind,
                             "sample": f"{steps} of {args.steps} requested full steps after {args.warmup} "
-                                      f"warm-up steps (bounded to ~2 min), FP32 restatement of the reference "
-                                      f"(the reference itself does not build: Windows/GL headers, "
-                                      f"removed CUDA texture references)"},
+                                      f"warm-up steps (bounded to ~2 min), {what} (the reference's application "
+                                      f"does not build: Windows/GL headers, removed CUDA texture references)"},
            "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
 

@@ -8,7 +8,8 @@ enums and SimulationParameters, and from CUDASPHNEW/particle_simulation.cu
 the definitions of the functions listed below, copied as they are, in that
 order, into oracle/_ref/ref_types.inc and oracle/_ref/ref_funcs.inc.  Those
 files and the library are build outputs (oracle/_ref/ is not committed).
-Where the checkout is absent the recipe does nothing.
+Where the checkout is absent, files extracted earlier are compiled as they
+are; with neither, the recipe does nothing.
 
     python oracle/build_ref.py [<reference checkout>]
 """
@@ -70,24 +71,31 @@ def types(header: str) -> str:
 
 
 def build(ref: str | None = None, force: bool = False) -> str | None:
+    """Extracts the reference's functions (where the checkout is present) and
+    compiles the harness.  Without the checkout, files extracted earlier in
+    oracle/_ref/ (they travel with a copy of the working tree) are compiled
+    as they are; with neither, nothing is built (None)."""
     d = reference_dir(ref)
     cu, h = os.path.join(d, "particle_simulation.cu"), os.path.join(d, "particle_simulation.h")
-    if not (os.path.exists(cu) and os.path.exists(h)):
+    types_inc, funcs_inc = os.path.join(OUT, "ref_types.inc"), os.path.join(OUT, "ref_funcs.inc")
+    have_checkout = os.path.exists(cu) and os.path.exists(h)
+    if not have_checkout and not (os.path.exists(types_inc) and os.path.exists(funcs_inc)):
         return None
     harness = os.path.join(HERE, "ref_harness.cpp")
     if (not force and os.path.exists(LIB_PATH)
             and os.path.getmtime(LIB_PATH) >= max(os.path.getmtime(harness), os.path.getmtime(__file__))):
         return LIB_PATH
     os.makedirs(OUT, exist_ok=True)
-    src = open(cu, encoding="latin-1").read()
-    with open(os.path.join(OUT, "ref_types.inc"), "w") as f:
-        f.write(types(open(h, encoding="latin-1").read()))
-    with open(os.path.join(OUT, "ref_funcs.inc"), "w") as f:
-        for name in FUNCTIONS:
-            f.write(definition(src, name))
+    if have_checkout:
+        src = open(cu, encoding="latin-1").read()
+        with open(types_inc, "w") as f:
+            f.write(types(open(h, encoding="latin-1").read()))
+        with open(funcs_inc, "w") as f:
+            for name in FUNCTIONS:
+                f.write(definition(src, name))
     tmp = LIB_PATH + ".tmp"
-    cmd = ["g++", "-std=c++17", "-O2", "-shared", "-fPIC", "-ffp-contract=off", "-ftrivial-auto-var-init=zero",
-           "-w", "-I", HERE, harness, "-o", tmp]
+    cmd = ["g++", "-std=c++17", "-O2", "-fopenmp", "-shared", "-fPIC", "-ffp-contract=off",
+           "-ftrivial-auto-var-init=zero", "-w", "-I", HERE, harness, "-o", tmp]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"build of the reference harness failed:\n{r.stderr}")

@@ -407,6 +407,7 @@ def ref_lib():
         vp = ctypes.c_void_p
         L.ref_step_plain.argtypes = [vp] * 8 + [ctypes.c_float, ctypes.c_float, ctypes.c_int] + [vp] * 4
         L.ref_step_plain.restype = ctypes.c_int
+        L.ref_set_threads.argtypes = [ctypes.c_int]
         _ref = L
     return _ref
 
@@ -435,3 +436,8 @@ def ref_step_plain(p: SimulationParameters, bm: BoundaryMaps | None, pos: np.nda
         raise ValueError("a particle hashed outside the reference's cell tables")
     return dict(hash=h, ids=ids, start=start, end=end, rho=sd[:, 1].copy(), p=sd[:, 2].copy(),
                 acc=sd[:, 3:6].copy(), pos=vd, vel=sd[:, 6:9].copy())
+
+
+def ref_set_threads(n: int) -> None:
+    """Host threads the reference harness spreads a kernel's threads over."""
+    ref_lib().ref_set_threads(int(n))

@@ -8,9 +8,10 @@
 // oracle/_ref/ref_funcs.inc; nothing of the reference is kept in this
 // repository.  This file supplies what those functions expect of CUDA:
 //   * float3 / int3 and the __device__, __global__ qualifiers;
-//   * blockIdx / blockDim / threadIdx, set by the launch loop below, which
-//     runs a kernel's threads one after another (every kernel used here
-//     reads only what earlier kernels wrote, as on the GPU);
+//   * blockIdx / blockDim / threadIdx (one copy per host thread), set by the
+//     launch loop below, which runs a kernel's threads over the host's cores
+//     with OpenMP (every kernel used here writes only its own thread's
+//     outputs and reads only what earlier kernels wrote, as on the GPU);
 //   * tex1Dfetch over the arrays the reference binds to its 1-D textures
 //     (particle_simulation.cu:28-39, bound at :1979-1994);
 //   * tex3D with the documented normalised, linear, clamped addressing of
@@ -37,6 +38,9 @@
 #include <cstring>
 #include <numeric>
 #include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 using std::abs;
 using std::max;
@@ -57,7 +61,7 @@ struct int3 {
 struct dim3 {
     unsigned int x = 0, y = 0, z = 0;
 };
-static dim3 blockIdx, blockDim, threadIdx;
+static thread_local dim3 blockIdx, blockDim, threadIdx;
 
 // The reference's texture references become plain arrays.
 template <class T>
@@ -118,18 +122,27 @@ static Tex3D gBoundaryDistances, gBoundaryDensities, gBoundaryViscosities;
 // the reference's device functions and kernels of the plain step
 #include "_ref/ref_funcs.inc"
 
-// Runs kernel(args...) for `n` threads in blocks of 256, one thread after another.
+// Runs kernel() for `n` threads in blocks of 256, spread over the host's cores.
 template <class F>
 static void launch(unsigned int n, F&& kernel) {
-    blockDim.x = 256;
-    for (unsigned int idx = 0; idx < n; idx++) {
-        blockIdx.x = idx / 256;
-        threadIdx.x = idx % 256;
+#pragma omp parallel for schedule(static)
+    for (long long idx = 0; idx < (long long)n; idx++) {
+        blockDim.x = 256;
+        blockIdx.x = (unsigned int)(idx / 256);
+        threadIdx.x = (unsigned int)(idx % 256);
         kernel();
     }
 }
 
 extern "C" {
+
+void ref_set_threads(int n) {
+#ifdef _OPENMP
+    omp_set_num_threads(n > 0 ? n : 1);
+#else
+    (void)n;
+#endif
+}
 
 // One plain step of the reference's code.  params: a SimulationParameters
 // image (180 bytes, the layout of particle_simulation.h:54-111).  vd: float[n*3]
