@@ -233,6 +233,10 @@ sph_status ensure_two_scale(sph_sim* s) {
     SPH_CUDA(dalloc(&T.subVelS, 8 * n));
     SPH_CUDA(dalloc(&s->subScanBlock, tiles + 2));
     cudaStream_t q = s->stream;
+    // index buffers start valid (0): an entry a failed step leaves unwritten
+    // still names a child slot or a fine cell
+    for (int* p : {T.subTmp, T.subSortedHash, T.subSortedIds})
+        SPH_CUDA(cudaMemsetAsync(p, 0, sizeof(int) * 8 * (size_t)n, q));
     SPH_CUDA(cudaMemsetAsync(T.state, 0, n4, q));
     SPH_CUDA(cudaMemsetAsync(T.counts, 0, sizeof(int) * 5, q));
     SPH_CUDA(cudaMemsetAsync(T.subPos, 0, sizeof(float4) * 8 * n, q));
@@ -302,9 +306,9 @@ static void enqueue_lists(sph_sim* s, const GridDev& g, const PhysDev& ph, int c
     mark(ST_SCAN);
     launch_cell_scan(g.numCells, s->sb, s->status, st);
     mark(ST_SCATTER);
-    launch_scatter(n, s->sb, st);
+    launch_scatter(n, s->sb, st, s->status);
     mark(ST_RANK);
-    launch_rank_gather(n, s->sb, s->pos, s->vel, g, s->posS, s->velS, st, &s->vl);
+    launch_rank_gather(n, s->sb, s->pos, s->vel, g, s->posS, s->velS, st, &s->vl, s->status);
     mark(ST_DENSITY);
     launch_density_lists(n, s->posS, s->velS, rows_of(s), g, ph, s->map, s->rho4S, s->vl, s->cfg, true, true, st);
     // the sorted copies are now this step's own: a reuse the audit granted is used up
@@ -333,9 +337,9 @@ void enqueue_coarse(sph_sim* s, const GridDev& g, const PhysDev& ph, int collide
     mark(ST_SCAN);
     launch_cell_scan(g.numCells, s->sb, s->status, st);
     mark(ST_SCATTER);
-    launch_scatter(n, s->sb, st);
+    launch_scatter(n, s->sb, st, s->status);
     mark(ST_RANK);
-    launch_rank_gather(n, s->sb, s->pos, s->vel, g, s->posS, s->velS, st);
+    launch_rank_gather(n, s->sb, s->pos, s->vel, g, s->posS, s->velS, st, nullptr, s->status);
     mark(ST_DENSITY);
     // density and forces read the sorted copies only
     launch_density(n, s->posS, rows_of(s), g, ph, s->map, s->rho4S, s->rowStart, s->rowMask, cfg, st);
@@ -356,8 +360,8 @@ void enqueue_density_only(sph_sim* s, const float4* pos, const float4* vel, bool
     PhysDev ph = make_phys(s->P, s->O);
     launch_hash_count(n, pos, g, s->sb, s->status, st);
     launch_cell_scan(g.numCells, s->sb, s->status, st);
-    launch_scatter(n, s->sb, st);
-    launch_rank_gather(n, s->sb, pos, vel, g, s->posS, s->velS, st);
+    launch_scatter(n, s->sb, st, s->status);
+    launch_rank_gather(n, s->sb, pos, vel, g, s->posS, s->velS, st, nullptr, s->status);
     StepConfig cfg = s->cfg;
     cfg.forceVariant = masks ? FORCE_PRETESTED : FORCE_MASK;  // whether to record the neighbour masks
     launch_density(n, s->posS, rows_of(s), g, ph, s->map, s->rho4S, s->rowStart, s->rowMask, cfg, st);
@@ -445,6 +449,10 @@ sph_status alloc_handle(sph_sim* s, int n, long long C) {
     SPH_CUDA(dalloc(&s->sb.workIds, n));
     SPH_CUDA(dalloc(&s->sb.halfOffset, (size_t)C + 1));
     SPH_CUDA(cudaMemsetAsync(s->sb.halfOffset, 0, sizeof(int) * ((size_t)C + 1), s->stream));
+    // index buffers start valid (0): an entry a failed step leaves unwritten
+    // still names a particle or a cell of the handle
+    for (int* p : {s->sb.tmpIds, s->sb.sortedHash, s->sb.sortedIds, s->sb.workIds})
+        SPH_CUDA(cudaMemsetAsync(p, 0, sizeof(int) * (size_t)n, s->stream));
     SPH_CUDA(dalloc(&s->scanBlock, (size_t)tiles + 2));
     s->sb.tileCounter = reinterpret_cast<unsigned int*>(s->scanBlock);
     s->sb.scanFlags = s->scanBlock + 2;
@@ -459,6 +467,8 @@ sph_status alloc_handle(sph_sim* s, int n, long long C) {
     SPH_CUDA(cudaMemsetAsync(s->reuse, 0, sizeof(int), s->stream));
     SPH_CUDA(cudaMemsetAsync(s->vel, 0, sizeof(float4) * n, s->stream));
     SPH_CUDA(cudaMemsetAsync(s->rho4S, 0, sizeof(float4) * n, s->stream));
+    SPH_CUDA(cudaMemsetAsync(s->posS, 0, sizeof(float4) * n, s->stream));
+    SPH_CUDA(cudaMemsetAsync(s->velS, 0, sizeof(float4) * n, s->stream));
     SPH_CUDA(cudaMemsetAsync(s->accS, 0, sizeof(float4) * n, s->stream));
     s->sdMass.assign(n, 0.0f);
     s->sdEnergy.assign(n, 0.0f);
@@ -488,10 +498,14 @@ GridDev grid_of(const sph_sim* s) {
     return g;
 }
 
+// Each latched condition is reported once: the word is cleared when it is
+// read back non-zero (a condition that persists, such as a particle still
+// outside the grid, is latched again by the next step).
 sph_status latched_status(sph_sim* s) {
     SPH_CUDA(cudaMemcpyAsync(s->statusHost, s->status, sizeof(unsigned int), cudaMemcpyDeviceToHost,
                              s->stream));
     SPH_CUDA(cudaStreamSynchronize(s->stream));
+    if (*s->statusHost) SPH_CUDA(cudaMemsetAsync(s->status, 0, sizeof(unsigned int), s->stream));
     return status_of_host_copy(s);
 }
 
@@ -888,6 +902,7 @@ sph_status sph_read(sph_handle s, int field, void* dst, size_t bytes) {
     // one synchronisation: the status word comes back with the data
     SPH_CUDA(cudaMemcpyAsync(s->statusHost, s->status, sizeof(unsigned int), cudaMemcpyDeviceToHost, q));
     SPH_CUDA(cudaStreamSynchronize(q));
+    if (*s->statusHost) SPH_CUDA(cudaMemsetAsync(s->status, 0, sizeof(unsigned int), q));  // reported once
     sph_status st = status_of_host_copy(s);
     if (st) return st;
     if (field == SPH_FIELD_SIMULATION_DATA) {
@@ -1243,8 +1258,8 @@ sph_status sph_autotune(sph_handle s, int reps, sph_tuning* chosen) {
     auto sortStages = [&]() {
         launch_hash_count(n, s->pos, g, s->sb, s->status, st);
         launch_cell_scan(g.numCells, s->sb, s->status, st);
-        launch_scatter(n, s->sb, st);
-        launch_rank_gather(n, s->sb, s->pos, s->vel, g, s->posS, s->velS, st);
+        launch_scatter(n, s->sb, st, s->status);
+        launch_rank_gather(n, s->sb, s->pos, s->vel, g, s->posS, s->velS, st, nullptr, s->status);
     };
     // each candidate is timed in step context: the sort stages run before
     // every timed launch, so caches hold what they hold in a real step; the

@@ -211,11 +211,16 @@ void launch_rel_to_abs(int n, const float4* pos, GridDev g, float* aos, int stri
 void launch_hash_count(int n, const float4* pos, GridDev g, SortBuffers sb, unsigned int* status,
                        cudaStream_t s, const NeighbourLists* lists = nullptr);
 void launch_cell_scan(int numCells, SortBuffers sb, unsigned int* status, cudaStream_t s);
-void launch_scatter(int n, SortBuffers sb, cudaStream_t s);
+// With `status`, the scatter leaves its outputs as they were once a scan
+// wait has given up (STATUS_DEVICE_WAIT).
+void launch_scatter(int n, SortBuffers sb, cudaStream_t s, const unsigned int* status = nullptr);
 // With `lists` and no build in this step, only the reference permutation is
 // ranked and the state is gathered into the kept working order (workIds).
+// With `status`, the pass leaves its outputs as they were once a scan wait
+// has given up (STATUS_DEVICE_WAIT).
 void launch_rank_gather(int n, SortBuffers sb, const float4* pos, const float4* vel, GridDev g,
-                        float4* posS, float4* velS, cudaStream_t s, const NeighbourLists* lists = nullptr);
+                        float4* posS, float4* velS, cudaStream_t s, const NeighbourLists* lists = nullptr,
+                        const unsigned int* status = nullptr);
 // Density stage over reused neighbour lists: the build form (the reference's
 // rows and the skin rows, recording the lists) and the list form; each
 // returns at once unless the step is of its kind.

@@ -15,6 +15,8 @@
 // thrust::sort_by_key produces in the reference (particle_simulation.cu:2340).
 #include <cuda/atomic>
 
+#include <cstdlib>
+
 #include "sph_device.cuh"
 
 namespace sph {
@@ -168,9 +170,15 @@ constexpr unsigned long long FLAG_AGG = 1ull << 32;
 constexpr unsigned long long FLAG_INC = 2ull << 32;
 constexpr int SPIN_LIMIT = 1 << 22;
 
+// `waitLimit` bounds each spin (polls); a negative limit abandons every wait
+// at its first poll (a test of the give-up path: every tile then takes its
+// predecessors as zero).  A tile that gives up latches STATUS_DEVICE_WAIT and
+// completes with a prefix that is a partial sum of the true one, so every
+// offset stays within [0, n] and every index derived from the offsets stays
+// inside its buffer (the step's results are then unspecified and reported).
 __global__ void __launch_bounds__(SCAN_THREADS)
 k_cell_scan(int total, int* __restrict__ cnt, int* __restrict__ out, unsigned long long* flags,
-            unsigned int* tileCounter, unsigned int* status, const int* __restrict__ skip) {
+            unsigned int* tileCounter, unsigned int* status, const int* __restrict__ skip, int waitLimit) {
     if (skip && *skip) return;  // every block: no tile is taken, none waited on
     __shared__ int s_tile;
     __shared__ int s_warp[SCAN_THREADS / 32];
@@ -244,8 +252,12 @@ k_cell_scan(int total, int* __restrict__ cnt, int* __restrict__ out, unsigned lo
                     cuda::atomic_ref<unsigned long long, cuda::thread_scope_device> other(flags[t]);
                     int spins = 0;
                     f = other.load(cuda::memory_order_acquire);
+                    if (waitLimit < 0) {
+                        atomicOr(status, STATUS_DEVICE_WAIT);
+                        f = FLAG_INC;  // the wait abandoned at once
+                    }
                     while ((f >> 32) == 0ull) {
-                        if (++spins > SPIN_LIMIT) {
+                        if (++spins > waitLimit) {
                             atomicOr(status, STATUS_DEVICE_WAIT);
                             f = FLAG_INC;  // give up: treat as zero, result flagged
                             break;
@@ -295,31 +307,46 @@ k_cell_scan(int total, int* __restrict__ cnt, int* __restrict__ out, unsigned lo
     }
 }
 
+// The look-back's poll limit: SPIN_LIMIT, or the integer in the environment
+// variable SPH_SCAN_WAIT_LIMIT (read at each launch; a captured step graph
+// keeps the value it was captured with).  Tests set it to exercise the
+// give-up path; -1 abandons every wait at once.
+static int scan_wait_limit() {
+    const char* e = getenv("SPH_SCAN_WAIT_LIMIT");
+    if (!e || !*e) return SPIN_LIMIT;
+    return (int)strtol(e, nullptr, 10);
+}
+
 void launch_cell_scan(int numCells, SortBuffers sb, unsigned int* status, cudaStream_t s) {
     int total = numCells + 1;
     int tiles = (total + SCAN_TILE - 1) / SCAN_TILE;
     // tile counter (first 16 bytes) and the tile states that follow it
     cudaMemsetAsync(sb.tileCounter, 0, 16 + sizeof(unsigned long long) * (size_t)tiles, s);
     k_cell_scan<<<tiles, SCAN_THREADS, 0, s>>>(total, sb.cnt, sb.cellOffset, sb.scanFlags,
-                                               sb.tileCounter, status, sb.skip);
+                                               sb.tileCounter, status, sb.skip, scan_wait_limit());
 }
 
 // ---------------------------------------------------------------------------
 // Stage 3: scatter ids into their cell segments (arrival order)
 // ---------------------------------------------------------------------------
+// After a scan wait gave up (status) the scatter and the rank pass leave
+// their outputs as they were: the step's results are unspecified and the
+// condition is reported.
 __global__ void k_scatter(int n, const int2* __restrict__ keySlot, const int* __restrict__ cellOffset,
-                          int* __restrict__ tmpIds, int* __restrict__ sortedHash, const int* __restrict__ skip) {
+                          int* __restrict__ tmpIds, int* __restrict__ sortedHash, const int* __restrict__ skip,
+                          const unsigned int* __restrict__ status) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n || (skip && *skip)) return;
+    if (i >= n || (skip && *skip) || (status && (*status & STATUS_DEVICE_WAIT))) return;
     int2 ks = keySlot[i];
     int dst = __ldg(cellOffset + ks.x) + ks.y;
     tmpIds[dst] = i;
     sortedHash[dst] = ks.x;
 }
 
-void launch_scatter(int n, SortBuffers sb, cudaStream_t s) {
+void launch_scatter(int n, SortBuffers sb, cudaStream_t s, const unsigned int* status) {
     if (n <= 0) return;
-    k_scatter<<<(n + 255) / 256, 256, 0, s>>>(n, sb.keySlot, sb.cellOffset, sb.tmpIds, sb.sortedHash, sb.skip);
+    k_scatter<<<(n + 255) / 256, 256, 0, s>>>(n, sb.keySlot, sb.cellOffset, sb.tmpIds, sb.sortedHash, sb.skip,
+                                              status);
 }
 
 // ---------------------------------------------------------------------------
@@ -350,9 +377,9 @@ __global__ void k_rank_gather(int n, const int* __restrict__ sortedHash, const i
                               const float4* __restrict__ vel, GridDev g_, const SceneDev* __restrict__ scenes,
                               int* __restrict__ sortedIds, int* __restrict__ workIds, int* __restrict__ halfOffset,
                               float4* __restrict__ posS, float4* __restrict__ velS, const int* __restrict__ skip,
-                              const unsigned int* __restrict__ vl) {
+                              const unsigned int* __restrict__ vl, const unsigned int* __restrict__ status) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n || (skip && *skip)) return;
+    if (k >= n || (skip && *skip) || (status && (*status & STATUS_DEVICE_WAIT))) return;
     int c = sortedHash[k];
     int s = __ldg(cellOffset + c), e = __ldg(cellOffset + c + 1);
     int my = tmpIds[k];
@@ -388,21 +415,21 @@ __global__ void k_rank_gather(int n, const int* __restrict__ sortedHash, const i
 }
 
 void launch_rank_gather(int n, SortBuffers sb, const float4* pos, const float4* vel, GridDev g, float4* posS,
-                        float4* velS, cudaStream_t s, const NeighbourLists* L) {
+                        float4* velS, cudaStream_t s, const NeighbourLists* L, const unsigned int* status) {
     if (n <= 0) return;
     const int grid = (n + 255) / 256;
     if (sb.scenes)
         k_rank_gather<true, false><<<grid, 256, 0, s>>>(n, sb.sortedHash, sb.cellOffset, sb.tmpIds, pos, vel, g,
                                                         sb.scenes, sb.sortedIds, sb.workIds, sb.halfOffset, posS,
-                                                        velS, sb.skip, nullptr);
+                                                        velS, sb.skip, nullptr, status);
     else if (g.rel)
         k_rank_gather<false, true><<<grid, 256, 0, s>>>(n, sb.sortedHash, sb.cellOffset, sb.tmpIds, pos, vel, g,
                                                         nullptr, sb.sortedIds, sb.workIds, sb.halfOffset, posS, velS,
-                                                        sb.skip, nullptr);
+                                                        sb.skip, nullptr, status);
     else
         k_rank_gather<false, false><<<grid, 256, 0, s>>>(n, sb.sortedHash, sb.cellOffset, sb.tmpIds, pos, vel, g,
                                                          nullptr, sb.sortedIds, sb.workIds, sb.halfOffset, posS,
-                                                         velS, sb.skip, L ? L->flags : nullptr);
+                                                         velS, sb.skip, L ? L->flags : nullptr, status);
 }
 
 // ---------------------------------------------------------------------------

@@ -380,3 +380,32 @@ def test_time_kernel_leaves_the_plain_step_state(sphlib):
         sim.step(count=2)
         ref.step(count=2)
         np.testing.assert_array_equal(sim.positions(), ref.positions())
+
+
+@pytest.mark.parametrize("skin", [0.0, 0.1])
+def test_scan_wait_give_up_is_reported_and_recovers(sphlib, orc, skin):
+    """The cell scan's look-back waits are bounded; a wait that gives up
+    latches SPH_ERR_DEVICE_WAIT.  SPH_SCAN_WAIT_LIMIT=-1 makes every wait give
+    up at its first poll (read at each eagerly enqueued step): the step must
+    stay inside its buffers, report the condition once, and the next step from
+    a written state must be the plain step again."""
+    import os
+    sc = scenes.config1()
+    o = P.Options.from_buffer_copy(bytes(sc.options))
+    o.neighbourSkin = skin
+    with sphlib.ParticleSimulation(sc.params, sc.positions, sc.velocities, o) as sim:
+        os.environ["SPH_SCAN_WAIT_LIMIT"] = "-1"
+        try:
+            sim.Advance()  # eager: the launch reads the limit
+            with pytest.raises(sphlib.SphError) as e:
+                sim.synchronize()
+            assert e.value.status == 5  # SPH_ERR_DEVICE_WAIT
+        finally:
+            del os.environ["SPH_SCAN_WAIT_LIMIT"]
+        sim.synchronize()  # reported once
+        sim.write_state(sc.positions, sc.velocities)
+        sim.Advance()
+        g = dict(zip(("hash", "ids", "start", "end"), sim.cells()))
+        g.update(rho=sim.read(sphlib.FIELD_DENSITY), p=sim.read(sphlib.FIELD_PRESSURE),
+                 acc=sim.read(sphlib.FIELD_ACCELERATION), pos=sim.positions(), vel=sim.velocities())
+    check_step(orc, sc, g, None)
