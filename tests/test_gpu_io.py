@@ -2,9 +2,12 @@
 buffers (sph_write, sph_read).
 
 A page-locked source is read by the unpacking kernel itself; a pageable one
-goes through a device staging buffer; read-back always gathers into staging
-and copies back by DMA.  Every route must move the same bits, and a step
-driven from page-locked buffers must equal one driven from pageable ones.
+goes through a device staging buffer.  Positions and velocities read back
+into page-locked memory are written there by the packing kernel (16-byte
+stores where the destination is 16-byte aligned, single floats where it is
+not); other fields and pageable destinations are gathered into staging and
+copied back by DMA.  Every route must move the same bits, and a step driven
+from page-locked buffers must equal one driven from pageable ones.
 """
 import ctypes
 
@@ -78,3 +81,26 @@ def test_step_from_pinned_equals_step_from_pageable(sphlib):
     for (xa, va), (xb, vb) in zip(*outs):
         np.testing.assert_array_equal(xa, xb)
         np.testing.assert_array_equal(va, vb)
+
+
+@pytest.mark.parametrize("shift", [0, 1, 3])
+def test_read_into_page_locked_memory_at_any_alignment(sphlib, shift):
+    # 693 particles: the last block of 256 is partial and 693 * 3 floats leave a
+    # ragged tail of single floats after the 16-byte stores
+    sc = scenes.dam_break(7, 9, 11, (0, 0, 0), (0.5, 0.5, 0.5), 3, "io_ragged", 0)
+    n = sc.n
+    assert n == 693
+    L = sphlib.load()
+    rng = np.random.default_rng(11)
+    v = rng.standard_normal((n, 3)).astype(np.float32)
+    with sphlib.ParticleSimulation(sc.params, sc.positions, sc.velocities, sc.options, sc.boundary) as sim:
+        sim.write_state(sc.positions, v)
+        sim.step(count=2)
+        for field, want in ((sphlib.FIELD_VERTEX_DATA, sim.positions()), (sphlib.FIELD_VELOCITY, sim.velocities())):
+            # a page-locked buffer entered `shift` floats after its start, with
+            # guard values around the destination
+            buf = torch.full((n * 3 + 8,), -7.0, dtype=torch.float32, pin_memory=True)
+            dst = buf[shift:shift + n * 3]
+            sphlib.check(L.sph_read(sim._h, field, ctypes.c_void_p(dst.data_ptr()), n * 12))
+            np.testing.assert_array_equal(dst.numpy().reshape(n, 3), want)
+            assert np.all(buf.numpy()[:shift] == -7.0) and np.all(buf.numpy()[shift + n * 3:] == -7.0)
