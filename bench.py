@@ -356,24 +356,23 @@ def cpu_baseline_two_scale(sc, max_seconds=15.0, max_steps=20):
 
 def cpu_baseline_batch(scs, max_seconds=20.0):
     """The batched workload on the CPU: every scene stepped in turn by the
-    oracle's FP32 plain step (all host cores), whole rounds over the 64
-    scenes until the time bound."""
+    reference step on all host cores (reference_stepper), whole rounds over
+    the 64 scenes until the time bound."""
     oracle, cores = load_oracle()
-    bms = [oracle.boundary_maps(sc.boundary) for sc in scs]
+    steppers = [reference_stepper(oracle, cores, sc) for sc in scs]
     state = [(sc.positions, sc.velocities) for sc in scs]
     rounds, t0 = 0, time.perf_counter()
     while True:
-        for k, sc in enumerate(scs):
-            r = oracle.step_plain(sc.params, sc.options, bms[k], *state[k])
-            state[k] = (r["pos"], r["vel"])
+        for k in range(len(scs)):
+            state[k] = steppers[k][0](*state[k])
         rounds += 1
         el = time.perf_counter() - t0
         if el > max_seconds or rounds >= 5:
             break
     n = sum(sc.n for sc in scs)
-    return {"value": n * rounds / el, "unit": UNIT, "cores": cores, "cpu": cpu_model(), "kind": "port",
+    return {"value": n * rounds / el, "unit": UNIT, "cores": cores, "cpu": cpu_model(), "kind": steppers[0][1],
             "sample": f"{rounds} step(s) of each of the {len(scs)} scenes ({n} particles, {el:.1f} s, "
-                      f"FP32 restatement of the reference step, OpenMP over particles)"}
+                      f"{steppers[0][2]})"}
 
 
 def run_reference(args):
@@ -704,21 +703,44 @@ def lists_leg(lib, torch, stream, sc, steps, tuning, late_start=1000, late_steps
     return out
 
 
-def batched_leg(lib, torch, stream, steps=200):
+def batched_leg(lib, torch, stream, steps=200, peaks=None):
     """The 64-scene batched workload (about 4.4M particles, seeded sizes and
     sphere obstacles): one handle, one launch per stage, one CUDA graph per
     step, autotuned; beside it the same scenes as 64 separate handles stepped
-    one after another (each with its own graph)."""
+    one after another (each with its own graph).  With `peaks` (HBM GB/s, its
+    source, FP32 flop/s) the batched density and force launches get a
+    roofline each, accounted as for one scene summed over the scenes."""
+    import numpy as np
     from cudasphnew_gb300 import scenes
     scs = scenes.config4()
     n = sum(sc.n for sc in scs)
+    roofs = None
     with lib.ParticleSimulation.batch(scs, scs[0].options) as sim:
         sim.set_stream(stream.cuda_stream)
         sim.step(count=3)
         tuning = sim.autotune(reps=3).as_dict()
         sim.step(count=3)
         ms = time_steps(torch, stream, sim, lib.SPH_STEP_PLAIN, steps)
-        cells = int(sim.scene_ranges()[1][-1])
+        fp, fc = sim.scene_ranges()
+        cells = int(fc[-1])
+        if peaks is not None:
+            hbm, hbm_kind, fp32 = peaks
+            sim.step(count=1)
+            pos_now = sim.positions()
+            t_d = sim.time_kernel("density", 20) / 1e6
+            t_f = sim.time_kernel("force", 20) / 1e6
+            pairs = sum(pair_count(pos_now[fp[k]:fp[k + 1]], float(sc.params.compactSupport))
+                        for k, sc in enumerate(scs))
+            g3 = sum(int(np.prod(sc.boundary.dims())) for sc in scs if sc.boundary is not None)
+            roofs = {}
+            for key, kern, t in (("roofline_density", "k_density", t_d), ("roofline_force", "k_force", t_f)):
+                r = kernel_roofline(kern, n, cells, g3, pairs, t, hbm, fp32)
+                r["peak_source"] = hbm_kind
+                r["timing"] = (f"20 back-to-back launches of the batched {kern} (all 64 scenes in one launch) "
+                               f"on one step's sorted state, CUDA events on the library's stream")
+                r["accounting"] = ("per-scene bytes and flops of the single-scene roofline summed over the scenes "
+                                   "(every scene's map counted once per launch)")
+                roofs[key] = r
     # the same scenes without batching, a bounded number of steps each
     k = max(steps // 10, 5)
     sims = [lib.ParticleSimulation(sc.params, sc.positions, sc.velocities, sc.options, sc.boundary) for sc in scs]
@@ -746,19 +768,56 @@ def batched_leg(lib, torch, stream, steps=200):
             "launches_per_step": 6, "graph": "one CUDA graph launch per step", "tuning": tuning,
             "separate_handles": {"value": n * k / (ms_sep / 1e3), "ms_per_step": ms_sep / k, "steps": k,
                                  "launches_per_step": 6 * len(scs)},
-            "l2": "no flush: working set of the 4.4M-particle batch far exceeds L2"}
+            "l2": "no flush: working set of the 4.4M-particle batch far exceeds L2", **(roofs or {})}
 
 
-def two_scale_leg(lib, torch, stream, steps=500):
+def two_scale_leg(lib, torch, stream, steps=500, peaks=None):
     """The 262,144-particle two-scale run (AdvanceTwoScale with persistent
-    children and merge-back), against the plain step of the same scene."""
+    children and merge-back), against the plain step of the same scene.
+    With `peaks` (HBM GB/s, its source, FP32 flop/s): stage times of a few
+    more two-scale steps (CUDA events between the stages, eager launches)
+    and a roofline of the fine level's density and force stages."""
+    import numpy as np
+    from scipy.spatial import cKDTree
     from cudasphnew_gb300 import scenes
     sc = scenes.config3()
+    fine = None
     with lib.ParticleSimulation(sc.params, sc.positions, sc.velocities, sc.options, sc.boundary) as sim:
         sim.set_stream(stream.cuda_stream)
         sim.step(mode=lib.SPH_STEP_TWO_SCALE, count=5)
         ms = time_steps(torch, stream, sim, lib.SPH_STEP_TWO_SCALE, steps)
         c = sim.counts()
+        if peaks is not None:
+            hbm, hbm_kind, fp32 = peaks
+            k = 20
+            sim.set_stage_timing(k)
+            sim.step(mode=lib.SPH_STEP_TWO_SCALE, count=k)
+            t = sim.stage_times()
+            sim.set_stage_timing(0)
+            stage_us = {name: 1e3 * v[0] / v[1] for name, v in t.items() if v[1] > 0}
+            cf = sim.counts()
+            ids = sim.read(lib.FIELD_SUB_IDS)
+            xs = sim.read(lib.FIELD_SUB_VERTEX_DATA)
+            n_reg, n_sub = 8 * cf.numParticlesSplit, cf.numSubParticles
+            hs = float(sc.params.compactSupportSub)
+            every = cKDTree(xs[ids[:n_sub]].astype(np.float64))
+            regular = cKDTree(xs[ids[:n_reg]].astype(np.float64))
+            pairs = int(regular.count_neighbors(every, hs)) - n_reg  # regular child i, any child j != i
+            cells = int(np.prod(list(sc.params.gridDimSubParticles)))
+            fine = {"stage_us": stage_us, "steps": k, "regular_children": n_reg, "children": n_sub}
+            for key, kern, stage in (("roofline_sub_density", "k_density", "sub_density"),
+                                     ("roofline_sub_force", "k_force", "sub_force")):
+                nk = n_reg if stage == "sub_density" else n_sub
+                r = kernel_roofline(kern, nk, cells if stage == "sub_force" else 0, 0, pairs,
+                                    stage_us[stage] / 1e6, hbm, fp32)
+                r["kernel"] = "k_ts_subdensity" if stage == "sub_density" else "k_ts_subforce"
+                r["peak_source"] = hbm_kind
+                r["timing"] = (f"stage interval '{stage}' (CUDA events around the launch, gaps included), "
+                               f"mean of {k} eager two-scale steps")
+                r["accounting"] = ("the plain step's per-particle bytes and per-pair flops applied to the fine "
+                                   "level (density: regular children; force: every child, which it integrates, "
+                                   "plus the fine cell table; no boundary maps at the fine level)")
+                fine[key] = r
         ms_plain = time_steps(torch, stream, sim, lib.SPH_STEP_PLAIN, steps)
     return {"workload": f"{sc.name}: {sc.n} coarse particles, split region [0.4, 0.6]^3, children merged back "
                         f"on exit", "unit": UNIT, "steps": steps,
@@ -766,7 +825,7 @@ def two_scale_leg(lib, torch, stream, steps=500):
             "children_at_end": c.numSubParticles, "split_at_end": c.numParticlesSplit,
             "boundary_at_end": c.numParticlesBoundary,
             "plain_ms_per_step": ms_plain / steps,
-            "graph": "one CUDA graph launch per step; counts stay on the device"}
+            "graph": "one CUDA graph launch per step; counts stay on the device", "fine_level": fine}
 
 
 def run_ours(args):
@@ -892,8 +951,8 @@ def run_ours(args):
         lists = lists_leg(lib, torch, stream, sc, args.steps, tuning)
     batched = two_scale = None
     if rank == 0 and not args.no_batched:
-        batched = batched_leg(lib, torch, stream)
-        two_scale = two_scale_leg(lib, torch, stream)
+        batched = batched_leg(lib, torch, stream, peaks=(peak, peak_kind, fp32))
+        two_scale = two_scale_leg(lib, torch, stream, peaks=(peak, peak_kind, fp32))
     learned = learned_1m = None
     if rank == 0 and not args.no_learned:
         learned, lcfg, model = learned_leg(lib, torch, stream)
@@ -925,7 +984,7 @@ def run_ours(args):
            "roofline": roofs[dominant],
            "roofline_density": roofs[kd],
            "roofline_force": roofs[kf],
-           "stages_us": {k: round(v[0] / v[1] * 1e3, 2) for k, v in stages.items()}}
+           "stages_us": {k: round(v[0] / v[1] * 1e3, 2) for k, v in stages.items() if v[1] > 0}}
     if batched is not None:
         out["batched"] = batched
         out["two_scale"] = two_scale

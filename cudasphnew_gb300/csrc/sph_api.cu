@@ -29,8 +29,9 @@ sph_status fail(sph_status st, const char* file, int line, const std::string& ms
     return st;
 }
 
-const char* kStageNames[ST_COUNT] = {"hash_count", "cell_scan", "scatter", "rank_gather",
-                                     "density", "force_integrate"};
+const char* kStageNames[ST_COUNT] = {"hash_count", "cell_scan",   "scatter",     "rank_gather",
+                                     "density",    "force_integrate", "ts_children", "sub_sort",
+                                     "sub_density", "sub_force"};
 
 }  // namespace
 
@@ -316,7 +317,7 @@ static void enqueue_lists(sph_sim* s, const GridDev& g, const PhysDev& ph, int c
     mark(ST_FORCE);
     launch_force_lists(n, s->posS, s->velS, s->rho4S, s->sb.workIds, ph, s->map, collide, s->vl, s->pos, s->vel,
                        s->accS, s->cfg, st);
-    mark(ST_COUNT);
+    mark(ST_FORCE + 1);  // the force stage's end
     s->lastStepLists = true;
 }
 
@@ -349,7 +350,7 @@ void enqueue_coarse(sph_sim* s, const GridDev& g, const PhysDev& ph, int collide
     if (!force) return;
     launch_force(n, s->posS, s->velS, s->rho4S, s->sb.workIds, rows_of(s), g, ph, s->map, collide, s->rowStart,
                  s->rowMask, s->pos, s->vel, s->accS, cfg, st, feat, s->status);
-    mark(ST_COUNT);
+    mark(ST_FORCE + 1);  // the force stage's end
 }
 
 void enqueue_density_only(sph_sim* s, const float4* pos, const float4* vel, bool masks) {
@@ -396,16 +397,27 @@ void enqueue_step(sph_sim* s, int mode, bool timing, bool lists) {
     cudaEvent_t* ev = nullptr;
     if (timing) {
         ev = &s->events[(size_t)s->timingNext * (ST_COUNT + 1)];
+        // the stages this step runs (the events of the others are recorded at
+        // its end, empty intervals that are not counted)
+        s->timingRan[s->timingNext] = (1u << (twoScale ? ST_COUNT : ST_TS_CHILDREN)) - 1u;
         s->timingNext = (s->timingNext + 1) % s->timingCap;
         s->timingFilled = std::min(s->timingFilled + 1, s->timingCap);
     }
+    auto mark = [&](int k) {
+        if (ev) cudaEventRecord(ev[k], st);
+    };
+    auto mark_rest = [&](int k0) {
+        for (int k = k0; k <= ST_COUNT; k++) mark(k);
+    };
     // AdvanceTwoScale always runs handleCollisions (:2170)
     const int collide = twoScale ? 1 : s->O.boxCollision;
     if (!twoScale && lists && s->vlOn) {
         enqueue_lists(s, g, ph, collide, ev);
+        mark_rest(ST_TS_CHILDREN + 1);
         return;
     }
     enqueue_coarse(s, g, ph, collide, ev);
+    if (!twoScale) mark_rest(ST_TS_CHILDREN + 1);
     if (twoScale) {
         // computeParticleState, collect, initializeSubParticles, projectQuantities
         // (:2157-2160) from the pre-integration sorted state, which the force
@@ -419,9 +431,13 @@ void enqueue_step(sph_sim* s, int mode, bool timing, bool lists) {
         const int cap = 8 * n;
         const GridDev sg = make_grid(s->P, true);
         PhysDev sph = make_sub_phys(s->P, s->O);
+        mark(ST_SUB_SORT);
         launch_ts_sub_sort(sg, s->ts, s->subSb, cap, s->status, st);
+        mark(ST_SUB_DENSITY);
         launch_ts_sub_density(sg, sph, s->ts, cap, st);
+        mark(ST_SUB_FORCE);
         launch_ts_sub_force(sg, sph, s->ts, cap, st);
+        mark(ST_COUNT);
     }
 }
 
@@ -1086,11 +1102,13 @@ sph_status sph_set_stage_timing(sph_handle s, int enable) {
     SPH_CUDA(cudaStreamSynchronize(s->stream));
     for (cudaEvent_t e : s->events) cudaEventDestroy(e);
     s->events.clear();
+    s->timingRan.clear();
     s->timingCap = s->timingNext = s->timingFilled = 0;
     if (enable > 0) {
         int cap = enable;
         s->events.resize((size_t)cap * (ST_COUNT + 1));
         for (auto& e : s->events) SPH_CUDA(cudaEventCreate(&e));
+        s->timingRan.assign((size_t)cap, 0u);
         s->timingCap = cap;
     }
     return SPH_OK;
@@ -1493,6 +1511,7 @@ sph_status sph_stage_times(sph_handle s, float* ms, int* counts, int capacity, i
     for (int slot = 0; slot < s->timingFilled; slot++) {
         cudaEvent_t* ev = &s->events[(size_t)slot * (ST_COUNT + 1)];
         for (int k = 0; k < ST_COUNT; k++) {
+            if (!(s->timingRan[slot] >> k & 1u)) continue;
             float t = 0.0f;
             SPH_CUDA(cudaEventElapsedTime(&t, ev[k], ev[k + 1]));
             ms[k] += t;

@@ -27,7 +27,23 @@ sph_status record_error(sph_status st, const char* file, int line, const std::st
 
 namespace sph {
 
-enum Stage { ST_HASH, ST_SCAN, ST_SCATTER, ST_RANK, ST_DENSITY, ST_FORCE, ST_COUNT };
+// The stages a step records events between (sph_set_stage_timing).  A plain
+// step runs the first six; a two-scale step also the coarse-to-fine hand-over
+// (states, split lists, children, projection) and the fine level's sort,
+// density and force.
+enum Stage {
+    ST_HASH,
+    ST_SCAN,
+    ST_SCATTER,
+    ST_RANK,
+    ST_DENSITY,
+    ST_FORCE,
+    ST_TS_CHILDREN,
+    ST_SUB_SORT,
+    ST_SUB_DENSITY,
+    ST_SUB_FORCE,
+    ST_COUNT
+};
 
 template <class T>
 cudaError_t dalloc(T** p, size_t count) {
@@ -108,6 +124,7 @@ struct sph_sim {
     // stage timing ring
     int timingCap = 0, timingNext = 0, timingFilled = 0;
     std::vector<cudaEvent_t> events;  // timingCap * (sph::ST_COUNT + 1)
+    std::vector<unsigned int> timingRan;  // per timed step: bit k set when stage k ran
 };
 
 

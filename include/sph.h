@@ -525,7 +525,12 @@ sph_status sph_autotune(sph_handle h, int reps, sph_tuning* chosen);
 /* Stage timing with CUDA events on the handle's stream (CudaTimer,
  * util.cpp:6-41, generalised to every stage).  After enabling, each step
  * records events between its stages; sph_stage_times() returns the summed
- * milliseconds per stage since the last call and resets them. */
+ * milliseconds and the number of timed steps per stage since the last call
+ * and resets them.  Stages (sph_stage_name): 0 hash_count, 1 cell_scan,
+ * 2 scatter, 3 rank_gather, 4 density, 5 force_integrate -- every plain and
+ * two-scale step -- then, in two-scale steps only, 6 ts_children (states,
+ * split lists, children, projection), 7 sub_sort, 8 sub_density, 9 sub_force.
+ * An interval holds its stage's launches and the gaps between them. */
 sph_status sph_set_stage_timing(sph_handle h, int enable);
 sph_status sph_stage_times(sph_handle h, float* ms, int* counts, int capacity, int* numStages);
 const char* sph_stage_name(int stage);

@@ -214,6 +214,28 @@ def test_two_scale_graph_matches_eager_and_is_deterministic(sphlib, child_mode):
             np.testing.assert_array_equal(a, b)
 
 
+def test_two_scale_stage_timing(sphlib):
+    """Stage timing of two-scale steps times the fine level too, and changes
+    no result (timed steps run eagerly, untimed ones as a graph)."""
+    sc = small_scene()
+    outs = []
+    for timed in (True, False):
+        with sphlib.ParticleSimulation(sc.params, sc.positions, sc.velocities, sc.options) as sim:
+            if timed:
+                sim.set_stage_timing(8)
+            sim.step(mode=sphlib.SPH_STEP_TWO_SCALE, count=3)
+            sim.step(count=2)
+            if timed:
+                t = sim.stage_times()
+                for k in ("hash_count", "cell_scan", "scatter", "rank_gather", "density", "force_integrate"):
+                    assert t[k][1] == 5 and t[k][0] > 0, k
+                for k in ("ts_children", "sub_sort", "sub_density", "sub_force"):
+                    assert t[k][1] == 3 and t[k][0] > 0, k
+            outs.append([sim.read(sphlib.FIELD_SUB_VERTEX_DATA), sim.positions(), sim.velocities()])
+    for a, b in zip(*outs):
+        np.testing.assert_array_equal(a, b)
+
+
 def test_config3_runs(sphlib):
     """The 262,144-particle two-scale configuration: counts and finiteness."""
     sc = scenes.config3()
