@@ -748,6 +748,9 @@ sph_status sph_step(sph_handle s, int mode) {
     if (mode != SPH_STEP_SUB_ONLY) {
         s->numTimeSteps++;
         s->stepped = true;
+        // whether the sorted copies match the lists (a replayed graph runs no
+        // host code, so this is set here and not only where the work is enqueued)
+        s->lastStepLists = mode == SPH_STEP_PLAIN && s->vlOn;
     }
     return SPH_OK;
 }
@@ -797,6 +800,7 @@ sph_status sph_step_many(sph_handle s, int mode, int count) {
     if (mode != SPH_STEP_SUB_ONLY) {
         s->numTimeSteps += (unsigned int)count;
         s->stepped = true;
+        s->lastStepLists = mode == SPH_STEP_PLAIN && s->vlOn;
     }
     return SPH_OK;
 }

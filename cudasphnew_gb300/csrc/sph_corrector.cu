@@ -157,17 +157,38 @@ void upload_norm(sph_sim* s, Corrector* C) {
 }
 
 // The learned step: a plain step of stride*dt, then features and correction.
+// One learned step.  With reused neighbour lists on, its sort and density
+// are those of a list step (the lists built when the decision says so, the
+// distance a particle may move before a rebuild being the same for the long
+// step) and the fused force stage walks the lists; otherwise the per-step
+// search with its recorded masks.
 void enqueue_learned(sph_sim* s, Corrector* C) {
     const int K = C->cfg.stride;
+    const int n = s->n;
+    cudaStream_t st = s->stream;
     GridDev g = grid_of(s);
     PhysDev ph = learned_phys(s, K);
-    enqueue_coarse(s, g, ph, s->O.boxCollision, nullptr, nullptr, false);
     StepConfig cfg = s->cfg;
-    cfg.forceVariant = FORCE_PRETESTED;
     const FeatureOut fo{C->record ? C->feat : nullptr, 1, s->O.boxCollision, ph.dt};
-    launch_force_learned(s->n, s->posS, s->velS, s->rho4S, s->sb.workIds, rows_of(s), g, ph, s->map,
+    if (s->vlOn) {
+        launch_hash_count(n, s->pos, g, s->sb, s->status, st, &s->vl);
+        launch_cell_scan(g.numCells, s->sb, s->status, st);
+        launch_scatter(n, s->sb, st, s->status);
+        launch_rank_gather(n, s->sb, s->pos, s->vel, g, s->posS, s->velS, st, &s->vl, s->status);
+        launch_density_lists(n, s->posS, s->velS, rows_of(s), g, ph, s->map, s->rho4S, s->vl, cfg, true, true, st);
+        // the sorted copies are now this step's own: a reuse the audit granted is used up
+        cudaMemsetAsync(s->reuse, 0, sizeof(int), st);
+        launch_force_learned(n, s->posS, s->velS, s->rho4S, s->sb.workIds, rows_of(s), g, ph, s->map,
+                             s->O.boxCollision, nullptr, nullptr, s->pos, s->vel, s->accS, cfg, fo, mdev(C),
+                             s->status, st, &s->vl);
+        s->lastStepLists = true;
+        return;
+    }
+    enqueue_coarse(s, g, ph, s->O.boxCollision, nullptr, nullptr, false);
+    cfg.forceVariant = FORCE_PRETESTED;
+    launch_force_learned(n, s->posS, s->velS, s->rho4S, s->sb.workIds, rows_of(s), g, ph, s->map,
                          s->O.boxCollision, s->rowStart, s->rowMask, s->pos, s->vel, s->accS, cfg, fo, mdev(C),
-                         s->status, s->stream);
+                         s->status, st);
 }
 
 void enqueue_audit(sph_sim* s, Corrector* C) {
@@ -178,11 +199,15 @@ void enqueue_audit(sph_sim* s, Corrector* C) {
     cudaMemcpyAsync(C->lVel, s->vel, bytes, cudaMemcpyDeviceToDevice, q);
     // The plain solver from the same start: its first step's sort and density
     // are the learned step's (neither depends on dt, and the sorted copies
-    // still hold the start state), so only its force stage runs; it writes
-    // every particle's new state.
-    launch_force(s->n, s->posS, s->velS, s->rho4S, s->sb.workIds, rows_of(s), grid_of(s), make_phys(s->P, s->O),
-                 s->map, s->O.boxCollision, s->rowStart, s->rowMask, s->pos, s->vel, s->accS, s->cfg, q, nullptr,
-                 s->status);
+    // still hold the start state), so only its force stage runs, over the
+    // same neighbours; it writes every particle's new state.
+    if (s->vlOn)
+        launch_force_lists(s->n, s->posS, s->velS, s->rho4S, s->sb.workIds, make_phys(s->P, s->O), s->map,
+                           s->O.boxCollision, s->vl, s->pos, s->vel, s->accS, s->cfg, q);
+    else
+        launch_force(s->n, s->posS, s->velS, s->rho4S, s->sb.workIds, rows_of(s), grid_of(s),
+                     make_phys(s->P, s->O), s->map, s->O.boxCollision, s->rowStart, s->rowMask, s->pos, s->vel,
+                     s->accS, s->cfg, q, nullptr, s->status);
     // the per-step search: the plain solver the audit replays is the one the
     // learned step's first plain step above belongs to
     for (int k = 1; k < C->cfg.stride; k++) enqueue_step(s, SPH_STEP_PLAIN, false, false);
@@ -259,6 +284,9 @@ sph_status corrector_step(sph_sim* s, int count, bool useGraph) {
             SPH_CUDA(cudaGetLastError());
         }
         C->sinceAudit = audit ? 0 : C->sinceAudit + 1;
+        // the lists match the sorted copies after a learned step over them;
+        // an audit ends with the per-step search
+        s->lastStepLists = !audit && s->vlOn;
         C->rep.learnedSteps++;
         C->recorded = C->recorded || C->record;
     }

@@ -107,12 +107,15 @@ void launch_audit_select(int n, const unsigned int* errBits, float tol, const fl
                          cudaStream_t s);
 
 // The learned step's force stage with the MLP fused in (sph_step.cu): the
-// pretested pair loop (the density stage must have recorded the masks),
-// wall terms, integration and collision, the features, the correction and
-// one write-back; the raw features also go to feat.feat when it is set.
+// pretested pair loop (the density stage must have recorded the masks), or
+// with `lists` the reused lists' exact masks (the list density stage must
+// have run), wall terms, integration and collision, the features, the
+// correction and one write-back; the raw features also go to feat.feat when
+// it is set.
 void launch_force_learned(int n, const float4* posS, const float4* velS, const float4* rho4S, const int* workIds,
                           RowTables T, GridDev g, PhysDev ph, MapDev map, int collide, const int* rowStart,
                           const unsigned int* rowMask, float4* pos, float4* vel, float4* accS, const StepConfig& cfg,
-                          const FeatureOut& feat, MlpDev m, unsigned int* status, cudaStream_t s);
+                          const FeatureOut& feat, MlpDev m, unsigned int* status, cudaStream_t s,
+                          const NeighbourLists* lists = nullptr);
 
 }  // namespace sph

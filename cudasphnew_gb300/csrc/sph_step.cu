@@ -999,8 +999,15 @@ static_assert(L_X % 1024 == 0 && L_BIAS % 16 == 0 && L_NORM % 16 == 0 && L_BAR %
 static_assert(L_BLOCKS_MAX * (L_SMEM + 1024) <= 227 * 1024 && L_BLOCKS_MAX * L_TMEM <= 512,
               "resident blocks per SM");
 
-template <bool KAHAN, bool TENSION, int BLOCKS>
-__global__ void __launch_bounds__(L_THREADS, BLOCKS) k_force_learned(ForceArgs F, MlpDev m, unsigned int* status) {
+// LISTS: the neighbours come from the reused lists' exact masks (as in
+// k_force_lists: the same pairs in the same order as the masks of the
+// per-step search at a building step, the neighbours' p/rho^2 and 1/rho from
+// the fourth lanes of their sorted position and velocity), and the kernel
+// records the largest squared distance of a corrected position from where
+// the particle was when the lists were built.
+template <bool KAHAN, bool TENSION, int BLOCKS, bool LISTS>
+__global__ void __launch_bounds__(L_THREADS, BLOCKS)
+k_force_learned(ForceArgs F, MlpDev m, unsigned int* status, NeighbourLists L) {
     using namespace mlp;
     extern __shared__ __align__(1024) unsigned char sm[];
     __shared__ int sOk;
@@ -1037,8 +1044,46 @@ __global__ void __launch_bounds__(L_THREADS, BLOCKS) k_force_learned(ForceArgs F
             const PhysDev& ph = F.ph;
             ForceTotals<KAHAN, TENSION> A;
             FeatSums fs;
+            if (LISTS) {
+                const int rows = L.rows[i];
+#pragma unroll 1
+                for (int row = 0; row < rows; row++) {
+                    RowSums<TENSION> R;
+                    R.clear();
+                    const int sv = __ldg(L.start + (size_t)row * F.n + i);
+                    const uint2 mk = __ldg(L.exact + (size_t)row * F.n + i);
+                    if (sv < 0) {
+                        for (int tt = sv & 0x7fffffff; tt < (int)mk.x; tt++) {
+                            const float4 xj = __ldg(F.posS + tt);
+                            if (neighbour_r2(dist2(xi, xj), ph.h2)) {
+                                const float4 vj = __ldg(F.velS + tt), rj = make_float4(0.f, 0.f, xj.w, vj.w);
+                                const Pair p(ph, xi, vi, xj, vj);
+                                R.add(ph, p, ri.z, rj);
+                                fs.add(ph, p, rj);
+                            }
+                        }
+                    } else {
+                        R.hits += __popc(mk.x) + __popc(mk.y);
 #pragma unroll
-            for (int row = 0; row < 9; row++) {
+                        for (int w = 0; w < 2; w++) {
+                            unsigned int b = w ? mk.y : mk.x;
+                            while (b) {
+                                const int tt = sv + 32 * w + __ffs(b) - 1;
+                                b &= b - 1u;
+                                const float4 xj = __ldg(F.posS + tt), vj = __ldg(F.velS + tt);
+                                const float4 rj = make_float4(0.f, 0.f, xj.w, vj.w);
+                                const Pair p(ph, xi, vi, xj, vj);
+                                R.template add<false>(ph, p, ri.z, rj);
+                                fs.add(ph, p, rj);
+                            }
+                        }
+                    }
+                    A.add(R);
+                    fs.cnt += R.hits;
+                }
+            }
+#pragma unroll
+            for (int row = 0; row < (LISTS ? 0 : 9); row++) {
                 RowSums<TENSION> R;
                 R.clear();
                 const int sv = __ldg(F.M.start + (size_t)row * F.n + i);
@@ -1119,7 +1164,7 @@ __global__ void __launch_bounds__(L_THREADS, BLOCKS) k_force_learned(ForceArgs F
             x = make_float3(x.x + c[0], x.y + c[1], x.z + c[2]);
             v = make_float3(v.x + c[3], v.y + c[4], v.z + c[5]);
             if (F.collide) collide(F.ph, x, v);
-            F.pos[id] = make_float4(x.x, x.y, x.z, xi.w);
+            F.pos[id] = make_float4(x.x, x.y, x.z, LISTS ? 0.f : xi.w);
             F.vel[id] = make_float4(v.x, v.y, v.z, 0.f);
         }
     } while (false);
@@ -1128,6 +1173,17 @@ __global__ void __launch_bounds__(L_THREADS, BLOCKS) k_force_learned(ForceArgs F
     if (sOk == 2 && t == 0) tc::mbar_wait(wbar, 0, WAIT_LIMIT);  // once more for the copy in flight
     tc::cta_sync();
     if (warp == 0) tc::tmem_dealloc(tb, L_TMEM);
+    if (LISTS) {  // as in k_force_lists
+        float d2 = 0.f;
+        if (valid) {
+            const float4 b = __ldg(L.posB + i);
+            const float dx = x.x - b.x, dy = x.y - b.y, dz = x.z - b.z;
+            d2 = dx * dx + dy * dy + dz * dz;
+            if (!(d2 == d2)) d2 = __uint_as_float(0x7f800000u);
+        }
+        const unsigned int w = __reduce_max_sync(0xffffffffu, __float_as_uint(d2));
+        if ((t & 31) == 0 && w > 0u && w > *(volatile unsigned int*)(L.flags + VL_DISP)) atomicMax(L.flags + VL_DISP, w);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -1229,37 +1285,49 @@ void launch_force(int n, const float4* posS, const float4* velS, const float4* r
     }
 }
 
-template <bool KAHAN, bool TENSION, int BLOCKS>
-static void force_learned_launch(const ForceArgs& F, MlpDev m, unsigned int* status, cudaStream_t s) {
-    ensure_dynamic_smem<k_force_learned<KAHAN, TENSION, BLOCKS>>(L_SMEM);
-    k_force_learned<KAHAN, TENSION, BLOCKS><<<(F.n + L_THREADS - 1) / L_THREADS, L_THREADS, L_SMEM, s>>>(F, m,
-                                                                                                       status);
+template <bool KAHAN, bool TENSION, int BLOCKS, bool LISTS>
+static void force_learned_launch(const ForceArgs& F, MlpDev m, unsigned int* status, const NeighbourLists& L,
+                                 cudaStream_t s) {
+    ensure_dynamic_smem<k_force_learned<KAHAN, TENSION, BLOCKS, LISTS>>(L_SMEM);
+    k_force_learned<KAHAN, TENSION, BLOCKS, LISTS>
+        <<<(F.n + L_THREADS - 1) / L_THREADS, L_THREADS, L_SMEM, s>>>(F, m, status, L);
 }
 
-template <bool KAHAN, bool TENSION>
-static void force_learned_dispatch(const ForceArgs& F, MlpDev m, unsigned int* status, cudaStream_t s) {
+template <bool KAHAN, bool TENSION, bool LISTS>
+static void force_learned_dispatch(const ForceArgs& F, MlpDev m, unsigned int* status, const NeighbourLists& L,
+                                   cudaStream_t s) {
     const int sms = device_sms();
     const long long blocks = (F.n + L_THREADS - 1) / L_THREADS;
-    if (blocks >= 2LL * L_BLOCKS_MAX * sms) force_learned_launch<KAHAN, TENSION, L_BLOCKS_MAX>(F, m, status, s);
-    else force_learned_launch<KAHAN, TENSION, 3>(F, m, status, s);
+    if (blocks >= 2LL * L_BLOCKS_MAX * sms)
+        force_learned_launch<KAHAN, TENSION, L_BLOCKS_MAX, LISTS>(F, m, status, L, s);
+    else
+        force_learned_launch<KAHAN, TENSION, 3, LISTS>(F, m, status, L, s);
 }
 
 void launch_force_learned(int n, const float4* posS, const float4* velS, const float4* rho4S, const int* workIds,
                           RowTables T, GridDev g, PhysDev ph, MapDev map, int collide, const int* rowStart,
                           const unsigned int* rowMask, float4* pos, float4* vel, float4* accS, const StepConfig& cfg,
-                          const FeatureOut& feat, MlpDev m, unsigned int* status, cudaStream_t s) {
+                          const FeatureOut& feat, MlpDev m, unsigned int* status, cudaStream_t s,
+                          const NeighbourLists* lists) {
     if (n <= 0) return;
     const FeatOut fo{feat.feat, feat.byId, feat.boxWalls, feat.dtL};
     ForceArgs F{n,  posS, velS, rho4S, workIds, T, g, ph, map, collide, cfg.prune,
                 RowMasks{const_cast<int*>(rowStart), const_cast<unsigned int*>(rowMask)}, pos, vel, accS, fo};
+    const NeighbourLists L = lists ? *lists : NeighbourLists{};
     const bool tension = ph.tension != 0.0f;
+#define SPH_FORCE_LEARNED(K, T)                                        \
+    do {                                                               \
+        if (lists) force_learned_dispatch<K, T, true>(F, m, status, L, s); \
+        else force_learned_dispatch<K, T, false>(F, m, status, L, s);      \
+    } while (0)
     if (cfg.kahan) {
-        if (tension) force_learned_dispatch<true, true>(F, m, status, s);
-        else force_learned_dispatch<true, false>(F, m, status, s);
+        if (tension) SPH_FORCE_LEARNED(true, true);
+        else SPH_FORCE_LEARNED(true, false);
     } else {
-        if (tension) force_learned_dispatch<false, true>(F, m, status, s);
-        else force_learned_dispatch<false, false>(F, m, status, s);
+        if (tension) SPH_FORCE_LEARNED(false, true);
+        else SPH_FORCE_LEARNED(false, false);
     }
+#undef SPH_FORCE_LEARNED
 }
 
 // After the positions were written: the largest squared distance of a

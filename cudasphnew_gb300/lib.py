@@ -497,7 +497,7 @@ class ParticleSimulation:
         return us.value
 
     def neighbour_builds(self) -> int:
-        """How many times the plain steps have built the reused neighbour lists."""
+        """How many times the plain and learned steps have built the reused neighbour lists."""
         b = ctypes.c_uint()
         check(load().sph_neighbour_builds(self._h, ctypes.byref(b)))
         return int(b.value)

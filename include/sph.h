@@ -98,7 +98,8 @@ typedef struct sph_options {
                            1024.  No reference counterpart. */
     float splitMin[3];  /* two-scale split region; reference: 0.2 <= x <= 0.5 */
     float splitMax[3];  /* (find_split_particles, :948) */
-    float neighbourSkin; /* plain steps of single-scene handles: the neighbour
+    float neighbourSkin; /* plain and learned steps of single-scene handles
+                            with absolute positions: the neighbour
                             candidates within (1 + neighbourSkin) * compactSupport
                             are recorded when the lists are built and reused by
                             later steps until some particle has moved more than
@@ -544,9 +545,9 @@ const char* sph_stage_name(int stage);
  * reference counterpart. */
 sph_status sph_time_kernel(sph_handle h, int stage, int reps, float* microseconds);
 
-/* How many times the handle's plain steps have built their reused neighbour
- * lists (sph_options.neighbourSkin; 0 when the handle has none).  Waits for
- * the handle's stream.  No reference counterpart. */
+/* How many times the handle's plain and learned steps have built their
+ * reused neighbour lists (sph_options.neighbourSkin; 0 when the handle has
+ * none).  Waits for the handle's stream.  No reference counterpart. */
 sph_status sph_neighbour_builds(sph_handle h, unsigned int* builds);
 
 /* Largest inputs sph_cell_tables_noalloc() accepts. */

@@ -263,18 +263,22 @@ def test_features_match_numpy(sphlib):
     assert np.abs(ref[:, 11:18]).max() > 0 and ref[:, 20:23].any()
 
 
+@pytest.mark.parametrize("skin", [0.0, 0.1])
 @pytest.mark.parametrize("scaled", [False, True])
-def test_learned_step_is_the_long_step_plus_the_prediction(sphlib, scaled):
+def test_learned_step_is_the_long_step_plus_the_prediction(sphlib, scaled, skin):
     """The fused force + MLP kernel against its definition: a plain step of
     stride*dt from the same state, plus the corrector's prediction from the
     recorded features (evaluated by the separate MLP kernel).  Particles the
-    correction pushes through a wall are collided a second time and left out."""
+    correction pushes through a wall are collided a second time and left out.
+    With neighbourSkin 0.1 the learned step builds the lists (a new handle's
+    first step) and walks them."""
     sc = tiny()
     stride = 4
     blob = scaled_blob(8) if scaled else random_blob(8)
     with make(sphlib, sc) as sim:
         sim.step(count=20)
         x0, v0 = sim.positions(), sim.velocities()
+    with make(sphlib, sc, x0, v0, skin=skin) as sim:
         sim.load_corrector(blob, stride=stride, auditInterval=0)
         sim.record_features()
         sim.step(mode=sphlib.SPH_STEP_LEARNED)
@@ -347,17 +351,47 @@ def test_audit_rolls_back_to_the_plain_solver(sphlib):
 
 
 def test_audit_keeps_the_learned_result_within_tolerance(sphlib):
+    # the per-step search (with reused lists the run with audits, which
+    # rebuild the lists after each, would differ from the one without by the
+    # rounding of the reused rows)
     sc = tiny()
     blob = random_blob(6)
     outs = []
     for interval, tol in ((1, 1e9), (0, 0.01)):
-        with make(sphlib, sc) as sim:
+        with make(sphlib, sc, skin=0.0) as sim:
             sim.load_corrector(blob, stride=4, auditInterval=interval, densityTolerance=tol)
             sim.step(mode=sphlib.SPH_STEP_LEARNED, count=3)
             outs.append((sim.positions(), sim.velocities(), sim.corrector_report()))
     np.testing.assert_array_equal(outs[0][0], outs[1][0])
     np.testing.assert_array_equal(outs[0][1], outs[1][1])
     assert outs[0][2].audits == 3 and outs[0][2].rollbacks == 0 and outs[1][2].audits == 0
+
+
+def test_learned_steps_over_reused_lists(sphlib):
+    """Learned steps over the reused neighbour lists against the per-step
+    search: the first (a building step) bit for bit, the later ones over the
+    lists built then within rounding of the search; the lists are reused."""
+    sc = small()
+    blob = random_blob(9)
+    with make(sphlib, sc) as sim:
+        sim.step(count=40)
+        x0, v0 = sim.positions(), sim.velocities()
+    outs, builds = [], []
+    for skin in (0.1, 0.0):
+        with make(sphlib, sc, x0, v0, skin=skin) as sim:
+            sim.load_corrector(blob, stride=4, auditInterval=0)
+            sim.step(mode=sphlib.SPH_STEP_LEARNED)
+            first = (sim.positions(), sim.velocities())
+            sim.step(mode=sphlib.SPH_STEP_LEARNED, count=7)
+            outs.append((first, (sim.positions(), sim.velocities())))
+            builds.append(sim.neighbour_builds())
+    (fa, la), (fb, lb) = outs
+    np.testing.assert_array_equal(fa[0], fb[0])
+    np.testing.assert_array_equal(fa[1], fb[1])
+    assert 1 <= builds[0] < 8 and builds[1] == 0
+    # eight long steps: the reused rows sum the same pairs in another grouping
+    assert np.abs(la[0] - lb[0]).max() <= 1e-6
+    assert np.abs(la[1] - lb[1]).max() <= 1e-4 * max(1.0, np.abs(lb[1]).max())
 
 
 def test_learned_graph_matches_eager(sphlib):
