@@ -172,7 +172,7 @@ void free_all(sph_sim* s) {
                     s->sb.halfOffset, s->scanBlock,
                     s->status, s->staging, s->map4, s->mapDist, s->rowStart, s->rowMask, s->diagBuf,
                     s->scenesDev, s->reuse, s->vl.start, s->vl.skin, s->vl.exact, s->vl.rows, s->vl.posB,
-                    s->vl.flags};
+                    s->vl.flags, s->vl.slotScene};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     void* tsPtrs[] = {s->ts.state,     s->ts.blockCounts, s->ts.counts,
@@ -263,7 +263,10 @@ sph_status ensure_two_scale(sph_sim* s) {
 
 // Enqueues one step of `mode` (no host synchronisation).
 void request_list_build(sph_sim* s) {
-    if (s->vlOn) cudaMemsetAsync(s->vl.flags + VL_BUILD, 1, sizeof(unsigned int), s->stream);
+    // every scene's VL_BUILD (any non-zero word requests)
+    if (s->vlOn)
+        cudaMemsetAsync(s->vl.flags + VL_BUILD * s->vl.numScenes, 1, sizeof(unsigned int) * s->vl.numScenes,
+                        s->stream);
     s->lastStepLists = false;
 }
 
@@ -273,18 +276,28 @@ void set_list_radius(sph_sim* s) {
     s->vl.radius2 = s->vl.radius * s->vl.radius;
     const float lim = 0.45f * skin * h;
     s->vl.dispLimit2 = lim * lim;
+    s->vl.skinFrac = skin;
 }
 
 sph_status alloc_lists(sph_sim* s) {
-    if (!(s->O.neighbourSkin > 0.0f) || s->O.cellRelative || s->numScenes > 1) return SPH_OK;
+    if (!(s->O.neighbourSkin > 0.0f) || s->O.cellRelative) return SPH_OK;
     const size_t n = (size_t)s->n;
+    const int S = std::max(s->numScenes, 1);
     SPH_CUDA(dalloc(&s->vl.start, VL_SLOTS * n));
     SPH_CUDA(dalloc(&s->vl.skin, VL_SLOTS * n));
     SPH_CUDA(dalloc(&s->vl.exact, VL_SLOTS * n));
     SPH_CUDA(dalloc(&s->vl.rows, n));
     SPH_CUDA(dalloc(&s->vl.posB, n));
-    SPH_CUDA(dalloc(&s->vl.flags, VL_FLAGS));
-    SPH_CUDA(cudaMemsetAsync(s->vl.flags, 0, sizeof(unsigned int) * VL_FLAGS, s->stream));
+    SPH_CUDA(dalloc(&s->vl.flags, (size_t)VL_FLAGS * S));
+    SPH_CUDA(cudaMemsetAsync(s->vl.flags, 0, sizeof(unsigned int) * VL_FLAGS * S, s->stream));
+    s->vl.numScenes = S;
+    if (S > 1) {  // each sorted slot's scene: scene k fills slots [sceneStart[k], sceneStart[k + 1])
+        std::vector<int> scene(n);
+        for (int k = 0; k < S; k++)
+            std::fill(scene.begin() + s->sceneStart[(size_t)k], scene.begin() + s->sceneStart[(size_t)k + 1], k);
+        SPH_CUDA(dalloc(&s->vl.slotScene, n));
+        SPH_CUDA(cudaMemcpy(s->vl.slotScene, scene.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+    }
     SPH_CUDA(cudaMemsetAsync(s->vl.rows, 0, n, s->stream));
     set_list_radius(s);
     s->vlOn = true;
@@ -316,7 +329,7 @@ static void enqueue_lists(sph_sim* s, const GridDev& g, const PhysDev& ph, int c
     cudaMemsetAsync(s->reuse, 0, sizeof(int), st);
     mark(ST_FORCE);
     launch_force_lists(n, s->posS, s->velS, s->rho4S, s->sb.workIds, ph, s->map, collide, s->vl, s->pos, s->vel,
-                       s->accS, s->cfg, st);
+                       s->accS, s->cfg, st, s->sb.scenes);
     mark(ST_FORCE + 1);  // the force stage's end
     s->lastStepLists = true;
 }
@@ -955,14 +968,14 @@ sph_status sph_write(sph_handle s, int field, const void* src, size_t bytes) {
                 in = s->staging;
             }
             launch_unpack_aos(in, 3, 0, n, field == SPH_FIELD_VERTEX_DATA ? s->pos : s->vel, q);
-            // the lists stay valid while every particle is within the rebuild
-            // distance of where it was at their build (velocities do not matter)
-            if (field == SPH_FIELD_VERTEX_DATA && s->vlOn && s->lastStepLists)
-                launch_list_displacement(n, s->pos, s->sb.workIds, s->vl, q);
             if (field == SPH_FIELD_VERTEX_DATA && s->O.cellRelative) launch_abs_to_rel(n, s->pos, grid_of(s), q);
             if (field == SPH_FIELD_VERTEX_DATA && s->numScenes > 1)  // restore the scene index lanes
                 for (int k = 0; k < s->numScenes; k++)
                     launch_set_scene(s->pos + s->sceneStart[k], (int)(s->sceneStart[k + 1] - s->sceneStart[k]), k, q);
+            // the lists stay valid while every particle is within the rebuild
+            // distance of where it was at their build (velocities do not matter)
+            if (field == SPH_FIELD_VERTEX_DATA && s->vlOn && s->lastStepLists)
+                launch_list_displacement(n, s->pos, s->sb.workIds, s->vl, q);
             break;
         }
         case SPH_FIELD_SIMULATION_DATA:
@@ -1162,7 +1175,8 @@ static sph_status autotune_lists(sph_sim* s, int reps, sph_tuning* chosen) {
                 {s->rho4S, nullptr, sizeof(float4) * n},        {s->accS, nullptr, sizeof(float4) * n},
                 {s->sb.sortedHash, nullptr, sizeof(int) * n},   {s->sb.sortedIds, nullptr, sizeof(int) * n},
                 {s->sb.workIds, nullptr, sizeof(int) * n},      {s->sb.cellOffset, nullptr, sizeof(int) * C1},
-                {s->sb.halfOffset, nullptr, sizeof(int) * C1},  {s->vl.flags, nullptr, sizeof(unsigned int) * VL_FLAGS},
+                {s->sb.halfOffset, nullptr, sizeof(int) * C1},
+                {s->vl.flags, nullptr, sizeof(unsigned int) * VL_FLAGS * s->vl.numScenes},
                 {s->vl.start, nullptr, sizeof(int) * VL_SLOTS * n},
                 {s->vl.skin, nullptr, sizeof(uint2) * VL_SLOTS * n},
                 {s->vl.exact, nullptr, sizeof(uint2) * VL_SLOTS * n},
@@ -1448,7 +1462,9 @@ sph_status sph_time_kernel(sph_handle s, int stage, int reps, float* microsecond
     // after a step over the reused neighbour lists the list forms are timed
     // (the density stage's list form: the lists match the sorted copies)
     const bool lists = s->vlOn && s->lastStepLists;
-    if (lists) SPH_CUDA(cudaMemsetAsync(s->vl.flags + VL_BUILD_NOW, 0, sizeof(unsigned int), st));
+    if (lists)
+        SPH_CUDA(cudaMemsetAsync(s->vl.flags + VL_BUILD_NOW * s->vl.numScenes, 0,
+                                 sizeof(unsigned int) * s->vl.numScenes, st));
     auto launch = [&]() {
         if (lists) {
             if (stage == ST_DENSITY)
@@ -1456,7 +1472,7 @@ sph_status sph_time_kernel(sph_handle s, int stage, int reps, float* microsecond
                                      st);
             else
                 launch_force_lists(n, s->posS, s->velS, s->rho4S, s->sb.workIds, ph, s->map, s->O.boxCollision,
-                                   s->vl, s->pos, s->vel, s->accS, s->cfg, st);
+                                   s->vl, s->pos, s->vel, s->accS, s->cfg, st, s->sb.scenes);
         } else if (stage == ST_DENSITY) {
             launch_density(n, s->posS, rows_of(s), g, ph, s->map, s->rho4S, s->rowStart, s->rowMask, s->cfg, st);
         } else {
@@ -1496,10 +1512,12 @@ sph_status sph_neighbour_builds(sph_handle s, unsigned int* builds) {
     if (!s || !builds) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "NULL argument");
     *builds = 0;
     if (!s->vlOn) return SPH_OK;
-    SPH_CUDA(cudaMemcpyAsync(s->statusHost, s->vl.flags + VL_COUNT, sizeof(unsigned int), cudaMemcpyDeviceToHost,
-                             s->stream));
+    // a batch: the scenes' builds summed
+    std::vector<unsigned int> c((size_t)s->vl.numScenes);
+    SPH_CUDA(cudaMemcpyAsync(c.data(), s->vl.flags + VL_COUNT * s->vl.numScenes, sizeof(unsigned int) * c.size(),
+                             cudaMemcpyDeviceToHost, s->stream));
     SPH_CUDA(cudaStreamSynchronize(s->stream));
-    *builds = *s->statusHost;
+    for (unsigned int v : c) *builds += v;
     return latched_status(s);
 }
 

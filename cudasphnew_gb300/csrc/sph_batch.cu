@@ -8,8 +8,10 @@
 // scan serve all scenes and no cell holds particles of two scenes.  The
 // step's kernels are the single-scene kernels in their batched form: each
 // particle reads its scene's grid, constants and boundary maps from a device
-// table.  A scene's arithmetic is exactly that of a handle holding only it,
-// so its results are bit-identical to running it alone.
+// table.  With reused neighbour lists every scene keeps its own build
+// decision (its own displacement and h).  A scene's arithmetic is exactly
+// that of a handle holding only it, so its results are bit-identical to
+// running it alone.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -125,6 +127,8 @@ sph_status sph_create_batch(const sph_scene* scenes, int numScenes, const sph_op
     BATCH_CUDA(cudaMemcpyAsync(s->scenesDev, table.data(), sizeof(SceneDev) * table.size(), cudaMemcpyHostToDevice,
                                q));
     s->sb.scenes = s->scenesDev;
+    // reused neighbour lists, one build decision per scene
+    if (sph_status sl = alloc_lists(s)) return bail(sl);
     BATCH_CUDA(cudaGetLastError());
     BATCH_CUDA(cudaStreamSynchronize(q));  // `table` leaves scope
 #undef BATCH_CUDA

@@ -137,6 +137,13 @@ struct RowTables {
 // follow from slot 9.  A window whose candidates within R span more than 64
 // places is kept unmasked: bit 31 of `start` set and the window end in the
 // low word of its masks.
+// Batched handles keep one set of flags per scene (field-major: field f of
+// scene k at flags[f * numScenes + k]); each scene decides its builds from
+// its own particles' displacement and its own h, so a scene in a batch
+// builds exactly when it would alone.  The list kernels take a slot's scene
+// from slotScene (the .w lane of the sorted position, which carries the
+// scene in the batch's other kernels, holds p/rho^2 once a list density
+// kernel has run).
 constexpr int VL_SLOTS = 16;  // rows within R <= 1.4 gridSpacing: at most 4 x 4
 constexpr int VL_INNER = 9;
 enum : int {
@@ -154,9 +161,13 @@ struct NeighbourLists {
                            //               .x = the window end
     unsigned char* rows;   // [n] slots in use (9 + the further rows)
     float4* posB;          // [n] positions at the build, working order
-    unsigned int* flags;   // [VL_FLAGS]
-    float radius, radius2; // R and R^2
-    float dispLimit2;      // (0.45 skin h)^2
+    unsigned int* flags;   // [VL_FLAGS][numScenes]
+    float radius, radius2; // R and R^2 (single-scene handles; a batch's kernels take each scene's h)
+    float dispLimit2;      // (0.45 skin h)^2 (likewise)
+    float skinFrac;        // sph_options.neighbourSkin
+    int numScenes;         // 1, or the batch's scene count
+    int* slotScene;        // batched handles: [n] the scene of each sorted slot (a scene's particles
+                           // always fill the same slot range: its cells follow the previous scene's)
 };
 
 // Launch configuration of the step (chosen per handle; see the autotuner).
@@ -231,13 +242,15 @@ void launch_density_lists(int n, float4* posS, float4* velS, RowTables T, GridDe
                           cudaStream_t s);
 // After a write of the positions: the largest distance from the build
 // positions, measured afresh (the lists stay if it is within the limit).
+// (Batched handles: each particle's scene from the .w lane of its position.)
 void launch_list_displacement(int n, const float4* pos, const int* workIds, const NeighbourLists& L,
                               cudaStream_t s);
 // Force stage over the lists' neighbour masks; also records the largest
-// displacement since the build.
+// displacement since the build.  With `scenes` (batched handles) each
+// particle's constants and maps come from its scene's record.
 void launch_force_lists(int n, const float4* posS, const float4* velS, const float4* rho4S, const int* workIds,
                         PhysDev ph, MapDev map, int collide, const NeighbourLists& L, float4* pos, float4* vel,
-                        float4* accS, const StepConfig& cfg, cudaStream_t s);
+                        float4* accS, const StepConfig& cfg, cudaStream_t s, const SceneDev* scenes = nullptr);
 void launch_density(int n, const float4* posS, RowTables T, GridDev g, PhysDev ph, MapDev map,
                     float4* rho4S, int* rowStart, unsigned int* rowMask, const StepConfig& cfg,
                     cudaStream_t s);

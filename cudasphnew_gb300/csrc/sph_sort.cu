@@ -130,23 +130,31 @@ void launch_pack_aos(const float4* in, int n, float* aos, int stride, int offset
 // start at that scene's cellBase in the concatenated cell space.
 // With REL the position is cell-relative and the hash comes from its packed
 // cell coordinates.
-// With `vl` (reused neighbour lists) the first thread decides whether this
-// step builds them: on request, or when some particle has moved farther than
-// the skin allows since the last build (or the displacement is not finite).
-// The kernels after this one read the decision.
+// With reused neighbour lists (`lists`) thread k < L.numScenes decides
+// whether scene k builds them in this step: on request, or when one of its
+// particles has moved farther than the skin allows since the last build (or
+// the displacement is not finite).  The kernels after this one read the
+// decision.
 template <bool BATCH, bool REL>
 __global__ void k_hash_count(int n, const float4* __restrict__ pos, GridDev g_, const SceneDev* __restrict__ scenes,
                              int* __restrict__ cnt, int2* __restrict__ keySlot, unsigned int* status,
-                             const int* __restrict__ skip, unsigned int* vl, float dispLimit2) {
+                             const int* __restrict__ skip, NeighbourLists L, int lists) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (vl && i == 0) {
-        const float d2 = __uint_as_float(vl[VL_DISP]);
-        const bool build = vl[VL_BUILD] != 0u || !(d2 <= dispLimit2);
-        vl[VL_BUILD_NOW] = build ? 1u : 0u;
-        vl[VL_BUILD] = 0u;
+    if (lists && i < L.numScenes) {
+        const int S = L.numScenes;
+        float lim2 = L.dispLimit2;
+        if (BATCH) {
+            const float lim = 0.45f * L.skinFrac * scenes[i].ph.h;
+            lim2 = lim * lim;
+        }
+        unsigned int* f = L.flags;
+        const float d2 = __uint_as_float(f[VL_DISP * S + i]);
+        const bool build = f[VL_BUILD * S + i] != 0u || !(d2 <= lim2);
+        f[VL_BUILD_NOW * S + i] = build ? 1u : 0u;
+        f[VL_BUILD * S + i] = 0u;
         if (build) {
-            vl[VL_DISP] = 0u;
-            vl[VL_COUNT] += 1u;
+            f[VL_DISP * S + i] = 0u;
+            f[VL_COUNT * S + i] += 1u;
         }
     }
     if (i >= n || (skip && *skip)) return;
@@ -173,17 +181,17 @@ __global__ void k_hash_count(int n, const float4* __restrict__ pos, GridDev g_, 
 void launch_hash_count(int n, const float4* pos, GridDev g, SortBuffers sb, unsigned int* status,
                        cudaStream_t s, const NeighbourLists* L) {
     if (n <= 0) return;
-    unsigned int* vl = L ? L->flags : nullptr;
-    const float lim = L ? L->dispLimit2 : 0.f;
+    const NeighbourLists VL = L ? *L : NeighbourLists{};
+    const int lists = L ? 1 : 0;
     if (sb.scenes)
         k_hash_count<true, false><<<(n + 255) / 256, 256, 0, s>>>(n, pos, g, sb.scenes, sb.cnt, sb.keySlot, status,
-                                                                  sb.skip, nullptr, 0.f);
+                                                                  sb.skip, VL, lists);
     else if (g.rel)
         k_hash_count<false, true><<<(n + 255) / 256, 256, 0, s>>>(n, pos, g, nullptr, sb.cnt, sb.keySlot, status,
-                                                                  sb.skip, nullptr, 0.f);
+                                                                  sb.skip, VL, 0);
     else
         k_hash_count<false, false><<<(n + 255) / 256, 256, 0, s>>>(n, pos, g, nullptr, sb.cnt, sb.keySlot, status,
-                                                                   sb.skip, vl, lim);
+                                                                   sb.skip, VL, lists);
 }
 
 // ---------------------------------------------------------------------------
@@ -404,13 +412,15 @@ __global__ void k_rank_gather(int n, const int* __restrict__ sortedHash, const i
                               const float4* __restrict__ vel, GridDev g_, const SceneDev* __restrict__ scenes,
                               int* __restrict__ sortedIds, int* __restrict__ workIds, int* __restrict__ halfOffset,
                               float4* __restrict__ posS, float4* __restrict__ velS, const int* __restrict__ skip,
-                              const unsigned int* __restrict__ vl, const unsigned int* __restrict__ status) {
+                              const unsigned int* __restrict__ vl, int vlScenes, const int* __restrict__ slotScene,
+                              const unsigned int* __restrict__ status) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n || (skip && *skip) || (status && (*status & STATUS_DEVICE_WAIT))) return;
     int c = sortedHash[k];
     int s = __ldg(cellOffset + c), e = __ldg(cellOffset + c + 1);
     int my = tmpIds[k];
-    if (vl && !vl[VL_BUILD_NOW]) {
+    const int sc = BATCH && vl ? slotScene[k] : 0;  // the scene of sorted slot k
+    if (vl && !vl[VL_BUILD_NOW * vlScenes + sc]) {
         int rId = 0;
         for (int t = s; t < e; t++) rId += __ldg(tmpIds + t) < my;
         sortedIds[s + rId] = my;
@@ -445,18 +455,21 @@ void launch_rank_gather(int n, SortBuffers sb, const float4* pos, const float4* 
                         float4* velS, cudaStream_t s, const NeighbourLists* L, const unsigned int* status) {
     if (n <= 0) return;
     const int grid = (n + 255) / 256;
+    const unsigned int* vl = L ? L->flags : nullptr;
+    const int vs = L ? L->numScenes : 1;
+    const int* ss = L ? L->slotScene : nullptr;
     if (sb.scenes)
         k_rank_gather<true, false><<<grid, 256, 0, s>>>(n, sb.sortedHash, sb.cellOffset, sb.tmpIds, pos, vel, g,
                                                         sb.scenes, sb.sortedIds, sb.workIds, sb.halfOffset, posS,
-                                                        velS, sb.skip, nullptr, status);
+                                                        velS, sb.skip, vl, vs, ss, status);
     else if (g.rel)
         k_rank_gather<false, true><<<grid, 256, 0, s>>>(n, sb.sortedHash, sb.cellOffset, sb.tmpIds, pos, vel, g,
                                                         nullptr, sb.sortedIds, sb.workIds, sb.halfOffset, posS, velS,
-                                                        sb.skip, nullptr, status);
+                                                        sb.skip, nullptr, 1, nullptr, status);
     else
         k_rank_gather<false, false><<<grid, 256, 0, s>>>(n, sb.sortedHash, sb.cellOffset, sb.tmpIds, pos, vel, g,
                                                          nullptr, sb.sortedIds, sb.workIds, sb.halfOffset, posS,
-                                                         velS, sb.skip, L ? L->flags : nullptr, status);
+                                                         velS, sb.skip, vl, vs, nullptr, status);
 }
 
 // ---------------------------------------------------------------------------

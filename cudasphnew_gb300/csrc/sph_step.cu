@@ -119,15 +119,24 @@ __device__ __forceinline__ bool within_r2(float r2, float R2) {  // r2 >= 0 or N
     return __float_as_uint(r2) <= __float_as_uint(R2);
 }
 
-template <bool KAHAN>
+// BATCH: the slot's scene supplies grid, constants, maps, R and the scene's
+// own decision.
+template <bool KAHAN, bool BATCH>
 __global__ void __launch_bounds__(256, 4)
-k_density_build(int n, float4* posS, float4* velS, RowTables T, GridDev g, PhysDev ph, MapDev map,
+k_density_build(int n, float4* posS, float4* velS, RowTables T, GridDev g_, PhysDev ph_, MapDev map_,
                 float4* __restrict__ rho4S, NeighbourLists L) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n || !L.flags[VL_BUILD_NOW]) return;
+    if (i >= n) return;
+    const int scene = BATCH ? L.slotScene[i] : 0;
+    if (!L.flags[VL_BUILD_NOW * L.numScenes + scene]) return;
     const float4 xi = posS[i];
+    const SceneDev* S = BATCH ? T.scenes + scene : nullptr;
+    const GridDev& g = BATCH ? S->g : g_;
+    const PhysDev& ph = BATCH ? S->ph : ph_;
+    const MapDev& map = BATCH ? S->map : map_;
     const Stencil st = stencil(xi, ph.h, g);
-    const float h2 = ph.h2, R = L.radius, R2 = L.radius2, eps = 1e-3f * ph.h;
+    const float R = BATCH ? (1.0f + L.skinFrac) * ph.h : L.radius;
+    const float h2 = ph.h2, R2 = BATCH ? R * R : L.radius2, eps = 1e-3f * ph.h;
     float sum = 0.f, comp = 0.f;
     int extra = VL_INNER;  // next slot of a further row
     // `slot` >= 0: a fixed slot, written even when the row is empty
@@ -214,13 +223,17 @@ k_density_build(int n, float4* posS, float4* velS, RowTables T, GridDev g, PhysD
 // the row's neighbours within h of this step are recorded for the force
 // stage over the same window (empty and unmasked rows keep what the build
 // wrote).  The next row's entries are loaded before the current row is walked.
-template <bool KAHAN>
+template <bool KAHAN, bool BATCH>
 __global__ void __launch_bounds__(256, 8)
-k_density_lists(int n, float4* posS, float4* velS, PhysDev ph, MapDev map, float4* __restrict__ rho4S,
-                NeighbourLists L) {
+k_density_lists(int n, float4* posS, float4* velS, PhysDev ph_, MapDev map_, float4* __restrict__ rho4S,
+                NeighbourLists L, const SceneDev* __restrict__ scenes) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n || L.flags[VL_BUILD_NOW]) return;
+    if (i >= n) return;
+    const int scene = BATCH ? L.slotScene[i] : 0;
+    if (L.flags[VL_BUILD_NOW * L.numScenes + scene]) return;
     const float4 xi = posS[i];
+    const PhysDev& ph = BATCH ? scenes[scene].ph : ph_;
+    const MapDev& map = BATCH ? scenes[scene].map : map_;
     const float h2 = ph.h2;
     const int rows = L.rows[i];
     float sum = 0.f, comp = 0.f;
@@ -742,18 +755,37 @@ __global__ void __launch_bounds__(256, FEAT ? 3 : (BATCH || TENSION || REL || FO
 // Occupancy: 64 registers, four 256-thread blocks per SM, no spills (at 48
 // registers and five blocks the spills cost more than the warps gain).
 // ---------------------------------------------------------------------------
-template <bool KAHAN, bool TENSION>
+// Displacement since the build into the scene's flag: one atomic per warp (or
+// per scene a warp holds) that raises the recorded maximum.  Squared
+// distances are non-negative, so their bits order as the values do; the
+// maximum only grows, so a warp that does not exceed the value it reads
+// (possibly an older, smaller one) has nothing to add.
+template <bool BATCH>
+__device__ __forceinline__ void record_displacement(const NeighbourLists& L, int scene, float d2) {
+    const unsigned int v = __float_as_uint(d2);
+    const unsigned int peers = BATCH ? __match_any_sync(0xffffffffu, scene) : 0xffffffffu;
+    const unsigned int w = __reduce_max_sync(peers, v);
+    unsigned int* f = L.flags + VL_DISP * L.numScenes + scene;
+    if ((threadIdx.x & 31) == (unsigned int)(__ffs(peers) - 1) && w > 0u && w > *(volatile unsigned int*)f)
+        atomicMax(f, w);
+}
+
+template <bool KAHAN, bool TENSION, bool BATCH>
 __global__ void __launch_bounds__(256, 4)
 k_force_lists(int n, const float4* __restrict__ posS, const float4* __restrict__ velS,
-              const float4* __restrict__ rho4S, const int* __restrict__ workIds, PhysDev ph, MapDev map,
+              const float4* __restrict__ rho4S, const int* __restrict__ workIds, PhysDev ph_, MapDev map_,
               int collideFlag, NeighbourLists L, float4* __restrict__ pos, float4* __restrict__ vel,
-              float4* __restrict__ accS) {
+              float4* __restrict__ accS, const SceneDev* __restrict__ scenes) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     float d2 = 0.f;
+    int scene = 0;
     if (i < n) {
         const float4 xi = posS[i];
         const float4 vi = velS[i];
         const float4 ri = rho4S[i];
+        if (BATCH) scene = L.slotScene[i];
+        const PhysDev& ph = BATCH ? scenes[scene].ph : ph_;
+        const MapDev& map = BATCH ? scenes[scene].map : map_;
         const float h2 = ph.h2;
         ForceTotals<KAHAN, TENSION> A;
         const int rows = L.rows[i];
@@ -799,7 +831,8 @@ k_force_lists(int n, const float4* __restrict__ posS, const float4* __restrict__
         float acc[3];
         force_finish<KAHAN, TENSION, false>(A, xi, vi, ri, ph, map, collideFlag, x, v, acc, mapDist, mapN, xi);
         const int id = workIds[i];
-        pos[id] = make_float4(x.x, x.y, x.z, 0.f);  // (the sorted copy's fourth lane holds p/rho^2)
+        // (the sorted copy's fourth lane holds p/rho^2; a batch keeps the scene there)
+        pos[id] = make_float4(x.x, x.y, x.z, BATCH ? __int_as_float(scene) : 0.f);
         vel[id] = make_float4(v.x, v.y, v.z, 0.f);
         accS[i] = make_float4(acc[0], acc[1], acc[2], 0.f);
         const float4 b = __ldg(L.posB + i);
@@ -807,13 +840,7 @@ k_force_lists(int n, const float4* __restrict__ posS, const float4* __restrict__
         d2 = dx * dx + dy * dy + dz * dz;
         if (!(d2 == d2)) d2 = __uint_as_float(0x7f800000u);  // NaN: as far as it gets
     }
-    // squared distances are non-negative: their bits order as the values do.
-    // The recorded maximum only grows, so a warp that does not exceed the value
-    // it reads (possibly an older, smaller one) has nothing to add: this keeps
-    // the atomics on the one word to the few warps that raise it.
-    const unsigned int w = __reduce_max_sync(0xffffffffu, __float_as_uint(d2));
-    if ((threadIdx.x & 31) == 0 && w > 0u && w > *(volatile unsigned int*)(L.flags + VL_DISP))
-        atomicMax(L.flags + VL_DISP, w);
+    record_displacement<BATCH>(L, scene, d2);
 }
 
 // ---------------------------------------------------------------------------
@@ -1181,8 +1208,7 @@ k_force_learned(ForceArgs F, MlpDev m, unsigned int* status, NeighbourLists L) {
             d2 = dx * dx + dy * dy + dz * dz;
             if (!(d2 == d2)) d2 = __uint_as_float(0x7f800000u);
         }
-        const unsigned int w = __reduce_max_sync(0xffffffffu, __float_as_uint(d2));
-        if ((t & 31) == 0 && w > 0u && w > *(volatile unsigned int*)(L.flags + VL_DISP)) atomicMax(L.flags + VL_DISP, w);
+        record_displacement<false>(L, 0, d2);
     }
 }
 
@@ -1334,25 +1360,27 @@ void launch_force_learned(int n, const float4* posS, const float4* velS, const f
 // particle from where it was when the lists were built, in place of the one
 // the steps accumulated (the next step builds the lists again only if that
 // exceeds the rebuild distance).  flags[VL_DISP] must be zero on entry.
+template <bool BATCH>
 __global__ void k_list_displacement(int n, const float4* __restrict__ pos, const int* __restrict__ workIds,
                                     NeighbourLists L) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     float d2 = 0.f;
+    int scene = 0;
     if (k < n) {
         const float4 x = __ldg(pos + workIds[k]), b = __ldg(L.posB + k);
+        if (BATCH) scene = L.slotScene[k];
         const float dx = x.x - b.x, dy = x.y - b.y, dz = x.z - b.z;
         d2 = dx * dx + dy * dy + dz * dz;
         if (!(d2 == d2)) d2 = __uint_as_float(0x7f800000u);
     }
-    const unsigned int w = __reduce_max_sync(0xffffffffu, __float_as_uint(d2));
-    if ((threadIdx.x & 31) == 0 && w > 0u && w > *(volatile unsigned int*)(L.flags + VL_DISP))
-        atomicMax(L.flags + VL_DISP, w);
+    record_displacement<BATCH>(L, scene, d2);
 }
 
 void launch_list_displacement(int n, const float4* pos, const int* workIds, const NeighbourLists& L, cudaStream_t s) {
     if (n <= 0) return;
-    cudaMemsetAsync(L.flags + VL_DISP, 0, sizeof(unsigned int), s);
-    k_list_displacement<<<(n + 255) / 256, 256, 0, s>>>(n, pos, workIds, L);
+    cudaMemsetAsync(L.flags + VL_DISP * L.numScenes, 0, sizeof(unsigned int) * L.numScenes, s);
+    if (L.numScenes > 1) k_list_displacement<true><<<(n + 255) / 256, 256, 0, s>>>(n, pos, workIds, L);
+    else k_list_displacement<false><<<(n + 255) / 256, 256, 0, s>>>(n, pos, workIds, L);
 }
 
 void launch_density_lists(int n, float4* posS, float4* velS, RowTables T, GridDev g, PhysDev ph, MapDev map,
@@ -1361,32 +1389,57 @@ void launch_density_lists(int n, float4* posS, float4* velS, RowTables T, GridDe
     if (n <= 0) return;
     const int bs = cfg.densityBlock > 0 ? cfg.densityBlock : 128;
     const int grid = (n + bs - 1) / bs;
+    const bool batch = T.scenes != nullptr;
+#define SPH_DENSITY_BUILD(K, B) k_density_build<K, B><<<grid, bs, 0, s>>>(n, posS, velS, T, g, ph, map, rho4S, L)
+#define SPH_DENSITY_LISTS(K, B) \
+    k_density_lists<K, B><<<grid, bs, 0, s>>>(n, posS, velS, ph, map, rho4S, L, T.scenes)
     if (build) {
-        if (cfg.kahan) k_density_build<true><<<grid, bs, 0, s>>>(n, posS, velS, T, g, ph, map, rho4S, L);
-        else k_density_build<false><<<grid, bs, 0, s>>>(n, posS, velS, T, g, ph, map, rho4S, L);
+        if (cfg.kahan) {
+            if (batch) SPH_DENSITY_BUILD(true, true);
+            else SPH_DENSITY_BUILD(true, false);
+        } else {
+            if (batch) SPH_DENSITY_BUILD(false, true);
+            else SPH_DENSITY_BUILD(false, false);
+        }
     }
     if (reuse) {
-        if (cfg.kahan) k_density_lists<true><<<grid, bs, 0, s>>>(n, posS, velS, ph, map, rho4S, L);
-        else k_density_lists<false><<<grid, bs, 0, s>>>(n, posS, velS, ph, map, rho4S, L);
+        if (cfg.kahan) {
+            if (batch) SPH_DENSITY_LISTS(true, true);
+            else SPH_DENSITY_LISTS(true, false);
+        } else {
+            if (batch) SPH_DENSITY_LISTS(false, true);
+            else SPH_DENSITY_LISTS(false, false);
+        }
     }
+#undef SPH_DENSITY_BUILD
+#undef SPH_DENSITY_LISTS
 }
 
 void launch_force_lists(int n, const float4* posS, const float4* velS, const float4* rho4S, const int* workIds,
                         PhysDev ph, MapDev map, int collide, const NeighbourLists& L, float4* pos, float4* vel,
-                        float4* accS, const StepConfig& cfg, cudaStream_t s) {
+                        float4* accS, const StepConfig& cfg, cudaStream_t s, const SceneDev* scenes) {
     if (n <= 0) return;
     const int bs = cfg.forceBlock > 0 ? cfg.forceBlock : 128;
     const int grid = (n + bs - 1) / bs;
+    // (a batch's tension coefficient is the largest of its scenes': it selects
+    // whether the colour field is computed at all)
     const bool tension = ph.tension != 0.0f;
-#define SPH_FORCE_LISTS(K, T) \
-    k_force_lists<K, T><<<grid, bs, 0, s>>>(n, posS, velS, rho4S, workIds, ph, map, collide, L, pos, vel, accS)
+#define SPH_FORCE_LISTS(K, T, B)                                                                             \
+    k_force_lists<K, T, B><<<grid, bs, 0, s>>>(n, posS, velS, rho4S, workIds, ph, map, collide, L, pos, vel, \
+                                               accS, scenes)
+#define SPH_FORCE_LISTS_B(K, T)           \
+    do {                                  \
+        if (scenes) SPH_FORCE_LISTS(K, T, true);  \
+        else SPH_FORCE_LISTS(K, T, false);        \
+    } while (0)
     if (cfg.kahan) {
-        if (tension) SPH_FORCE_LISTS(true, true);
-        else SPH_FORCE_LISTS(true, false);
+        if (tension) SPH_FORCE_LISTS_B(true, true);
+        else SPH_FORCE_LISTS_B(true, false);
     } else {
-        if (tension) SPH_FORCE_LISTS(false, true);
-        else SPH_FORCE_LISTS(false, false);
+        if (tension) SPH_FORCE_LISTS_B(false, true);
+        else SPH_FORCE_LISTS_B(false, false);
     }
+#undef SPH_FORCE_LISTS_B
 #undef SPH_FORCE_LISTS
 }
 

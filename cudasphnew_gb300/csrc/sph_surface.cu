@@ -93,6 +93,7 @@ using namespace sph;
 extern "C" sph_status sph_surface_particles(sph_handle s, int* flags) {
     if (!s || !flags) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "NULL argument");
     if (!s->stepped) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "no step has run yet");
+    if (s->numScenes > 1) SPH_FAIL(SPH_ERR_NOT_SUPPORTED, "surface flags are per scene: not for batched handles");
     int* d = nullptr;
     SPH_CUDA(dalloc(&d, (size_t)s->n));
     GridDev g = grid_of(s);

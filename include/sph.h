@@ -98,8 +98,9 @@ typedef struct sph_options {
                            1024.  No reference counterpart. */
     float splitMin[3];  /* two-scale split region; reference: 0.2 <= x <= 0.5 */
     float splitMax[3];  /* (find_split_particles, :948) */
-    float neighbourSkin; /* plain and learned steps of single-scene handles
-                            with absolute positions: the neighbour
+    float neighbourSkin; /* plain and learned steps of handles with absolute
+                            positions (a batch decides its builds per scene,
+                            so a scene builds when it would alone): the neighbour
                             candidates within (1 + neighbourSkin) * compactSupport
                             are recorded when the lists are built and reused by
                             later steps until some particle has moved more than
@@ -443,7 +444,7 @@ sph_status sph_read_features(sph_handle h, float* dst, size_t bytes);
  * centre of mass lies farther than cmDistanceThresh * compactSupport from
  * it (the thresholds of SimulationParameters; the reference never fills its
  * list).  int[n], particle order. */
-sph_status sph_surface_particles(sph_handle h, int* flags);
+sph_status sph_surface_particles(sph_handle h, int* flags);  /* not for batched handles */
 
 /* Headless renderer: the sphere imposters of the reference's
  * TwoScaleStateSub renderer (twoscalestatesub.cpp:84-161,
@@ -547,7 +548,8 @@ sph_status sph_time_kernel(sph_handle h, int stage, int reps, float* microsecond
 
 /* How many times the handle's plain and learned steps have built their
  * reused neighbour lists (sph_options.neighbourSkin; 0 when the handle has
- * none).  Waits for the handle's stream.  No reference counterpart. */
+ * none; a batch: its scenes' builds summed).  Waits for the handle's stream.
+ * No reference counterpart. */
 sph_status sph_neighbour_builds(sph_handle h, unsigned int* builds);
 
 /* Largest inputs sph_cell_tables_noalloc() accepts. */

@@ -20,19 +20,25 @@ def small_batch():
             for k, (n, f) in enumerate(zip((1500, 4000, 700, 2500), (0.05, 0.2, 0.12, 0.08)))]
 
 
-def run_alone(sphlib, sc, steps):
-    # batched handles search the neighbours in every step: so does the lone scene
-    o = type(sc.options).from_buffer_copy(bytes(sc.options))
-    o.neighbourSkin = 0.0
-    with sphlib.ParticleSimulation(sc.params, sc.positions, sc.velocities, o, sc.boundary) as sim:
+def with_skin(o, skin):
+    o = type(o).from_buffer_copy(bytes(o))
+    if skin is not None:
+        o.neighbourSkin = skin
+    return o
+
+
+def run_alone(sphlib, sc, steps, skin=None):
+    with sphlib.ParticleSimulation(sc.params, sc.positions, sc.velocities, with_skin(sc.options, skin),
+                                   sc.boundary) as sim:
         sim.step(count=steps)
         h, ids, start, end = sim.cells()
         return dict(pos=sim.positions(), vel=sim.velocities(), rho=sim.read(sphlib.FIELD_DENSITY),
-                    acc=sim.read(sphlib.FIELD_ACCELERATION), hash=h, ids=ids, start=start, end=end)
+                    acc=sim.read(sphlib.FIELD_ACCELERATION), hash=h, ids=ids, start=start, end=end,
+                    builds=sim.neighbour_builds())
 
 
-def run_batch(sphlib, scs, steps, autotune=False):
-    with sphlib.ParticleSimulation.batch(scs, scs[0].options) as sim:
+def run_batch(sphlib, scs, steps, autotune=False, skin=None):
+    with sphlib.ParticleSimulation.batch(scs, with_skin(scs[0].options, skin)) as sim:
         if autotune:
             sim.autotune(reps=2)
         sim.step(count=steps)
@@ -40,7 +46,7 @@ def run_batch(sphlib, scs, steps, autotune=False):
         h, ids, start, end = sim.cells()
         return fp, fc, dict(pos=sim.positions(), vel=sim.velocities(), rho=sim.read(sphlib.FIELD_DENSITY),
                             p=sim.read(sphlib.FIELD_PRESSURE), acc=sim.read(sphlib.FIELD_ACCELERATION),
-                            hash=h, ids=ids, start=start, end=end)
+                            hash=h, ids=ids, start=start, end=end, builds=sim.neighbour_builds())
 
 
 def check_scene(k, fp, fc, b, a):
@@ -58,14 +64,32 @@ def check_scene(k, fp, fc, b, a):
     np.testing.assert_array_equal(en[occ], a["end"][occ] + p0)
 
 
-def test_batch_is_bit_identical_to_scenes_alone(sphlib):
+@pytest.mark.parametrize("skin", [0.0, 0.1])
+def test_batch_is_bit_identical_to_scenes_alone(sphlib, skin):
     scs = small_batch()
     steps = 6
-    fp, fc, b = run_batch(sphlib, scs, steps)
+    fp, fc, b = run_batch(sphlib, scs, steps, skin=skin)
     assert list(np.diff(fp)) == [sc.n for sc in scs]
     assert list(np.diff(fc)) == [sc.params.num_cells for sc in scs]
     for k, sc in enumerate(scs):
-        check_scene(k, fp, fc, b, run_alone(sphlib, sc, steps))
+        check_scene(k, fp, fc, b, run_alone(sphlib, sc, steps, skin=skin))
+
+
+def test_batch_rebuilds_each_scenes_lists_when_that_scene_would_alone(sphlib):
+    """Scenes moving at different speeds rebuild their reused neighbour lists
+    at different steps; each scene's results stay bit-identical to the scene
+    run alone, and the batch's builds are the scenes' builds summed."""
+    scs = small_batch()
+    for k, sc in enumerate(scs):
+        sc.velocities[:, 0] = 0.3 * k  # scene 0 at rest, scene 3 at 0.9 m/s
+    steps = 40
+    fp, fc, b = run_batch(sphlib, scs, steps)
+    alone = [run_alone(sphlib, sc, steps) for sc in scs]
+    for k in range(len(scs)):
+        check_scene(k, fp, fc, b, alone[k])
+    builds = [a["builds"] for a in alone]
+    assert builds[0] < builds[-1] and len(set(builds)) > 1
+    assert b["builds"] == sum(builds)
 
 
 def test_batch_autotune_keeps_results(sphlib):
