@@ -714,6 +714,8 @@ def batched_leg(lib, torch, stream, steps=200, peaks=None):
     from cudasphnew_gb300 import scenes
     scs = scenes.config4()
     n = sum(sc.n for sc in scs)
+    lists = float(scs[0].options.neighbourSkin) > 0
+    launches = 7 if lists else 6
     roofs = None
     with lib.ParticleSimulation.batch(scs, scs[0].options) as sim:
         sim.set_stream(stream.cuda_stream)
@@ -733,7 +735,8 @@ def batched_leg(lib, torch, stream, steps=200, peaks=None):
                         for k, sc in enumerate(scs))
             g3 = sum(int(np.prod(sc.boundary.dims())) for sc in scs if sc.boundary is not None)
             roofs = {}
-            for key, kern, t in (("roofline_density", "k_density", t_d), ("roofline_force", "k_force", t_f)):
+            kd, kf = ("k_density_lists", "k_force_lists") if lists else ("k_density", "k_force")
+            for key, kern, t in (("roofline_density", kd, t_d), ("roofline_force", kf, t_f)):
                 r = kernel_roofline(kern, n, cells, g3, pairs, t, hbm, fp32)
                 r["peak_source"] = hbm_kind
                 r["timing"] = (f"20 back-to-back launches of the batched {kern} (all 64 scenes in one launch) "
@@ -765,9 +768,10 @@ def batched_leg(lib, torch, stream, steps=200, peaks=None):
     return {"workload": f"{len(scs)} dam breaks, {n} particles (log-uniform 4,096..262,144 per scene), "
                         f"{cells} cells, one 64^3 sphere map each",
             "unit": UNIT, "steps": steps, "value": n * steps / (ms / 1e3), "ms_per_step": ms / steps,
-            "launches_per_step": 6, "graph": "one CUDA graph launch per step", "tuning": tuning,
+            "launches_per_step": launches, "graph": "one CUDA graph launch per step", "tuning": tuning,
+            "neighbour_lists": "reused, one build decision per scene" if lists else "per-step search",
             "separate_handles": {"value": n * k / (ms_sep / 1e3), "ms_per_step": ms_sep / k, "steps": k,
-                                 "launches_per_step": 6 * len(scs)},
+                                 "launches_per_step": launches * len(scs)},
             "l2": "no flush: working set of the 4.4M-particle batch far exceeds L2", **(roofs or {})}
 
 
