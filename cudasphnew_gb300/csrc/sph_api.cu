@@ -270,6 +270,12 @@ void request_list_build(sph_sim* s) {
     s->lastStepLists = false;
 }
 
+// Before a sort outside the list steps: the cell tables it builds are current.
+static void mark_tables_current(sph_sim* s) {
+    if (s->vlOn)
+        cudaMemsetAsync(s->vl.flags + VL_FLAGS * s->vl.numScenes + VL_STALE, 0, sizeof(unsigned int), s->stream);
+}
+
 void set_list_radius(sph_sim* s) {
     const float h = s->P.compactSupport, skin = s->O.neighbourSkin;
     s->vl.radius = (1.0f + skin) * h;
@@ -288,8 +294,8 @@ sph_status alloc_lists(sph_sim* s) {
     SPH_CUDA(dalloc(&s->vl.exact, VL_SLOTS * n));
     SPH_CUDA(dalloc(&s->vl.rows, n));
     SPH_CUDA(dalloc(&s->vl.posB, n));
-    SPH_CUDA(dalloc(&s->vl.flags, (size_t)VL_FLAGS * S));
-    SPH_CUDA(cudaMemsetAsync(s->vl.flags, 0, sizeof(unsigned int) * VL_FLAGS * S, s->stream));
+    SPH_CUDA(dalloc(&s->vl.flags, (size_t)VL_FLAGS * S + VL_GLOBAL));
+    SPH_CUDA(cudaMemsetAsync(s->vl.flags, 0, sizeof(unsigned int) * (VL_FLAGS * S + VL_GLOBAL), s->stream));
     s->vl.numScenes = S;
     if (S > 1) {  // each sorted slot's scene: scene k fills slots [sceneStart[k], sceneStart[k + 1])
         std::vector<int> scene(n);
@@ -318,9 +324,9 @@ static void enqueue_lists(sph_sim* s, const GridDev& g, const PhysDev& ph, int c
     mark(ST_HASH);
     launch_hash_count(n, s->pos, g, s->sb, s->status, st, &s->vl);
     mark(ST_SCAN);
-    launch_cell_scan(g.numCells, s->sb, s->status, st);
+    launch_cell_scan(g.numCells, s->sb, s->status, st, &s->vl);
     mark(ST_SCATTER);
-    launch_scatter(n, s->sb, st, s->status);
+    launch_scatter(n, s->sb, st, s->status, &s->vl);
     mark(ST_RANK);
     launch_rank_gather(n, s->sb, s->pos, s->vel, g, s->posS, s->velS, st, &s->vl, s->status);
     mark(ST_DENSITY);
@@ -340,6 +346,7 @@ void enqueue_coarse(sph_sim* s, const GridDev& g, const PhysDev& ph, int collide
     const int n = s->n;
     // the per-step search rewrites the sorted copies and the working order
     request_list_build(s);
+    mark_tables_current(s);
     StepConfig cfg = s->cfg;
     // the feature form and the fused learned form read the density stage's masks
     if (feat || !force) cfg.forceVariant = FORCE_PRETESTED;
@@ -372,6 +379,7 @@ void enqueue_density_only(sph_sim* s, const float4* pos, const float4* vel, bool
     request_list_build(s);
     GridDev g = grid_of(s);
     PhysDev ph = make_phys(s->P, s->O);
+    mark_tables_current(s);
     launch_hash_count(n, pos, g, s->sb, s->status, st);
     launch_cell_scan(g.numCells, s->sb, s->status, st);
     launch_scatter(n, s->sb, st, s->status);
@@ -1033,6 +1041,30 @@ sph_status sph_read_cells(sph_handle s, int level, int* sortedHash, int* sortedI
     const int n = s->n;
     const int C = (int)s->numCellsTotal;
     cudaStream_t q = s->stream;
+    if (s->vlOn) {
+        // a step over the reused lists that built none skipped the tables:
+        // built now from that step's sorted copies, as it would have built them
+        unsigned int* stale = s->vl.flags + VL_FLAGS * s->vl.numScenes + VL_STALE;
+        SPH_CUDA(cudaMemcpyAsync(s->statusHost, stale, sizeof(unsigned int), cudaMemcpyDeviceToHost, q));
+        SPH_CUDA(cudaStreamSynchronize(q));
+        if (*s->statusHost) {
+            float4* scratch = nullptr;
+            unsigned int* st2 = nullptr;
+            cudaError_t e = dalloc(&scratch, (size_t)n);
+            if (e == cudaSuccess) e = dalloc(&st2, 1);
+            // the step reported its conditions already: the rebuild's go to a word of their own
+            if (e == cudaSuccess) e = cudaMemsetAsync(st2, 0, sizeof(unsigned int), q);
+            if (e == cudaSuccess) {
+                launch_rebuild_tables(n, s->posS, s->sb.workIds, s->vl.slotScene, grid_of(s), s->sb, scratch, st2,
+                                      q);
+                e = cudaMemsetAsync(stale, 0, sizeof(unsigned int), q);
+            }
+            if (e == cudaSuccess) e = cudaStreamSynchronize(q);
+            cudaFree(scratch);
+            cudaFree(st2);
+            SPH_CUDA(e);
+        }
+    }
     if (sortedHash)
         SPH_CUDA(cudaMemcpyAsync(sortedHash, s->sb.sortedHash, sizeof(int) * n, cudaMemcpyDeviceToHost, q));
     if (sortedIds)
@@ -1176,7 +1208,7 @@ static sph_status autotune_lists(sph_sim* s, int reps, sph_tuning* chosen) {
                 {s->sb.sortedHash, nullptr, sizeof(int) * n},   {s->sb.sortedIds, nullptr, sizeof(int) * n},
                 {s->sb.workIds, nullptr, sizeof(int) * n},      {s->sb.cellOffset, nullptr, sizeof(int) * C1},
                 {s->sb.halfOffset, nullptr, sizeof(int) * C1},
-                {s->vl.flags, nullptr, sizeof(unsigned int) * VL_FLAGS * s->vl.numScenes},
+                {s->vl.flags, nullptr, sizeof(unsigned int) * (VL_FLAGS * s->vl.numScenes + VL_GLOBAL)},
                 {s->vl.start, nullptr, sizeof(int) * VL_SLOTS * n},
                 {s->vl.skin, nullptr, sizeof(uint2) * VL_SLOTS * n},
                 {s->vl.exact, nullptr, sizeof(uint2) * VL_SLOTS * n},

@@ -172,8 +172,8 @@ void enqueue_learned(sph_sim* s, Corrector* C) {
     const FeatureOut fo{C->record ? C->feat : nullptr, 1, s->O.boxCollision, ph.dt};
     if (s->vlOn) {
         launch_hash_count(n, s->pos, g, s->sb, s->status, st, &s->vl);
-        launch_cell_scan(g.numCells, s->sb, s->status, st);
-        launch_scatter(n, s->sb, st, s->status);
+        launch_cell_scan(g.numCells, s->sb, s->status, st, &s->vl);
+        launch_scatter(n, s->sb, st, s->status, &s->vl);
         launch_rank_gather(n, s->sb, s->pos, s->vel, g, s->posS, s->velS, st, &s->vl, s->status);
         launch_density_lists(n, s->posS, s->velS, rows_of(s), g, ph, s->map, s->rho4S, s->vl, cfg, true, true, st);
         // the sorted copies are now this step's own: a reuse the audit granted is used up

@@ -153,6 +153,12 @@ enum : int {
     VL_COUNT = 3,      // builds so far
     VL_FLAGS = 4,
 };
+// Two words after the per-scene flags: whether this step sorts (some scene
+// builds; a step that builds nothing keeps the working order and skips the
+// hash, scan and scatter), and whether the cell tables on the device are
+// older than the last step (it skipped them; sph_read_cells rebuilds them
+// from that step's sorted copies).
+enum : int { VL_SORT = 0, VL_STALE = 1, VL_GLOBAL = 2 };
 struct NeighbourLists {
     int* start;            // [VL_SLOTS][n] window start (bit 31: unmasked window)
     uint2* skin;           // [VL_SLOTS][n] candidates within R (bit k: start + k; .x bits 0-31), or
@@ -161,7 +167,7 @@ struct NeighbourLists {
                            //               .x = the window end
     unsigned char* rows;   // [n] slots in use (9 + the further rows)
     float4* posB;          // [n] positions at the build, working order
-    unsigned int* flags;   // [VL_FLAGS][numScenes]
+    unsigned int* flags;   // [VL_FLAGS][numScenes], then [VL_GLOBAL]
     float radius, radius2; // R and R^2 (single-scene handles; a batch's kernels take each scene's h)
     float dispLimit2;      // (0.45 skin h)^2 (likewise)
     float skinFrac;        // sph_options.neighbourSkin
@@ -221,17 +227,30 @@ void launch_rel_to_abs(int n, const float4* pos, GridDev g, float* aos, int stri
 // neighbour lists (VL_BUILD_NOW).
 void launch_hash_count(int n, const float4* pos, GridDev g, SortBuffers sb, unsigned int* status,
                        cudaStream_t s, const NeighbourLists* lists = nullptr);
-void launch_cell_scan(int numCells, SortBuffers sb, unsigned int* status, cudaStream_t s);
+// With `lists`, the scan and the scatter return at once in a step that
+// builds no lists (VL_SORT clear), and so does the hash pass (whose checks of
+// the state the rank pass then makes).
+void launch_cell_scan(int numCells, SortBuffers sb, unsigned int* status, cudaStream_t s,
+                      const NeighbourLists* lists = nullptr);
 // With `status`, the scatter leaves its outputs as they were once a scan
 // wait has given up (STATUS_DEVICE_WAIT).
-void launch_scatter(int n, SortBuffers sb, cudaStream_t s, const unsigned int* status = nullptr);
+void launch_scatter(int n, SortBuffers sb, cudaStream_t s, const unsigned int* status = nullptr,
+                    const NeighbourLists* lists = nullptr);
+// The cell tables of the sorted copies' positions (sortedHash, sortedIds,
+// cellOffset) after a step that skipped them; the working order, the sorted
+// copies and the lists stay as they are.  `scratch`: n float4.
+void launch_rebuild_tables(int n, const float4* posS, const int* workIds, const int* slotScene, GridDev g,
+                           SortBuffers sb, float4* scratch, unsigned int* status, cudaStream_t s);
 // With `lists` and no build in this step, only the reference permutation is
 // ranked and the state is gathered into the kept working order (workIds).
 // With `status`, the pass leaves its outputs as they were once a scan wait
 // has given up (STATUS_DEVICE_WAIT).
+// In a step that sorts nothing (lists, VL_SORT clear) the pass only gathers
+// the state into the kept order and makes the hash pass's checks (non-finite
+// positions, positions outside the grid), latching them in `status`.
 void launch_rank_gather(int n, SortBuffers sb, const float4* pos, const float4* vel, GridDev g,
                         float4* posS, float4* velS, cudaStream_t s, const NeighbourLists* lists = nullptr,
-                        const unsigned int* status = nullptr);
+                        unsigned int* status = nullptr);
 // Density stage over reused neighbour lists: the build form (the reference's
 // rows and the skin rows, recording the lists) and the list form; each
 // returns at once unless the step is of its kind.

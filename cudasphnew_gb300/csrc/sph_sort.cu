@@ -130,33 +130,14 @@ void launch_pack_aos(const float4* in, int n, float* aos, int stride, int offset
 // start at that scene's cellBase in the concatenated cell space.
 // With REL the position is cell-relative and the hash comes from its packed
 // cell coordinates.
-// With reused neighbour lists (`lists`) thread k < L.numScenes decides
-// whether scene k builds them in this step: on request, or when one of its
-// particles has moved farther than the skin allows since the last build (or
-// the displacement is not finite).  The kernels after this one read the
-// decision.
+// With reused neighbour lists the pass returns at once in a step that builds
+// none (k_list_decide has decided; the rank pass checks the state instead).
 template <bool BATCH, bool REL>
 __global__ void k_hash_count(int n, const float4* __restrict__ pos, GridDev g_, const SceneDev* __restrict__ scenes,
                              int* __restrict__ cnt, int2* __restrict__ keySlot, unsigned int* status,
-                             const int* __restrict__ skip, NeighbourLists L, int lists) {
+                             const int* __restrict__ skip, const unsigned int* __restrict__ sortFlag) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (lists && i < L.numScenes) {
-        const int S = L.numScenes;
-        float lim2 = L.dispLimit2;
-        if (BATCH) {
-            const float lim = 0.45f * L.skinFrac * scenes[i].ph.h;
-            lim2 = lim * lim;
-        }
-        unsigned int* f = L.flags;
-        const float d2 = __uint_as_float(f[VL_DISP * S + i]);
-        const bool build = f[VL_BUILD * S + i] != 0u || !(d2 <= lim2);
-        f[VL_BUILD_NOW * S + i] = build ? 1u : 0u;
-        f[VL_BUILD * S + i] = 0u;
-        if (build) {
-            f[VL_DISP * S + i] = 0u;
-            f[VL_COUNT * S + i] += 1u;
-        }
-    }
+    if (sortFlag && !*sortFlag) return;
     if (i >= n || (skip && *skip)) return;
     float4 p = pos[i];
     const GridDev& g = BATCH ? scenes[__float_as_int(p.w)].g : g_;
@@ -178,20 +159,58 @@ __global__ void k_hash_count(int n, const float4* __restrict__ pos, GridDev g_, 
     keySlot[i] = make_int2(h, slot);
 }
 
+// Reused neighbour lists: whether each scene builds them in this step (on
+// request, or when one of its particles has moved farther than the skin
+// allows since the last build, or the displacement is not finite; thread k
+// decides scene k), whether the step sorts (some scene builds) and whether
+// it leaves the cell tables stale (it does not sort).  One block.
+__global__ void k_list_decide(NeighbourLists L, const SceneDev* __restrict__ scenes) {
+    __shared__ int anyBuild;
+    if (threadIdx.x == 0) anyBuild = 0;
+    __syncthreads();
+    const int S = L.numScenes;
+    unsigned int* f = L.flags;
+    for (int k = threadIdx.x; k < S; k += blockDim.x) {
+        float lim2 = L.dispLimit2;
+        if (scenes) {
+            const float lim = 0.45f * L.skinFrac * scenes[k].ph.h;
+            lim2 = lim * lim;
+        }
+        const float d2 = __uint_as_float(f[VL_DISP * S + k]);
+        const bool build = f[VL_BUILD * S + k] != 0u || !(d2 <= lim2);
+        f[VL_BUILD_NOW * S + k] = build ? 1u : 0u;
+        f[VL_BUILD * S + k] = 0u;
+        if (build) {
+            f[VL_DISP * S + k] = 0u;
+            f[VL_COUNT * S + k] += 1u;
+            anyBuild = 1;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        f[VL_FLAGS * S + VL_SORT] = anyBuild ? 1u : 0u;
+        f[VL_FLAGS * S + VL_STALE] = anyBuild ? 0u : 1u;
+    }
+}
+
+static const unsigned int* sort_flag(const NeighbourLists* L) {
+    return L ? L->flags + VL_FLAGS * L->numScenes + VL_SORT : nullptr;
+}
+
 void launch_hash_count(int n, const float4* pos, GridDev g, SortBuffers sb, unsigned int* status,
                        cudaStream_t s, const NeighbourLists* L) {
     if (n <= 0) return;
-    const NeighbourLists VL = L ? *L : NeighbourLists{};
-    const int lists = L ? 1 : 0;
+    if (L) k_list_decide<<<1, 256, 0, s>>>(*L, sb.scenes);
+    const unsigned int* sf = sort_flag(L);
     if (sb.scenes)
         k_hash_count<true, false><<<(n + 255) / 256, 256, 0, s>>>(n, pos, g, sb.scenes, sb.cnt, sb.keySlot, status,
-                                                                  sb.skip, VL, lists);
+                                                                  sb.skip, sf);
     else if (g.rel)
         k_hash_count<false, true><<<(n + 255) / 256, 256, 0, s>>>(n, pos, g, nullptr, sb.cnt, sb.keySlot, status,
-                                                                  sb.skip, VL, 0);
+                                                                  sb.skip, nullptr);
     else
         k_hash_count<false, false><<<(n + 255) / 256, 256, 0, s>>>(n, pos, g, nullptr, sb.cnt, sb.keySlot, status,
-                                                                   sb.skip, VL, lists);
+                                                                   sb.skip, sf);
 }
 
 // ---------------------------------------------------------------------------
@@ -213,8 +232,10 @@ constexpr int SPIN_LIMIT = 1 << 22;
 // inside its buffer (the step's results are then unspecified and reported).
 __global__ void __launch_bounds__(SCAN_THREADS)
 k_cell_scan(int total, int* __restrict__ cnt, int* __restrict__ out, unsigned long long* flags,
-            unsigned int* tileCounter, unsigned int* status, const int* __restrict__ skip, int waitLimit) {
-    if (skip && *skip) return;  // every block: no tile is taken, none waited on
+            unsigned int* tileCounter, unsigned int* status, const int* __restrict__ skip, int waitLimit,
+            const unsigned int* __restrict__ sortFlag) {
+    // every block alike: no tile is taken, none waited on
+    if ((skip && *skip) || (sortFlag && !*sortFlag)) return;
     __shared__ int s_tile;
     __shared__ int s_warp[SCAN_THREADS / 32];
     __shared__ int s_prefix;
@@ -352,13 +373,13 @@ static int scan_wait_limit() {
     return (int)strtol(e, nullptr, 10);
 }
 
-void launch_cell_scan(int numCells, SortBuffers sb, unsigned int* status, cudaStream_t s) {
+void launch_cell_scan(int numCells, SortBuffers sb, unsigned int* status, cudaStream_t s, const NeighbourLists* L) {
     int total = numCells + 1;
     int tiles = (total + SCAN_TILE - 1) / SCAN_TILE;
     // tile counter (first 16 bytes) and the tile states that follow it
     cudaMemsetAsync(sb.tileCounter, 0, 16 + sizeof(unsigned long long) * (size_t)tiles, s);
     k_cell_scan<<<tiles, SCAN_THREADS, 0, s>>>(total, sb.cnt, sb.cellOffset, sb.scanFlags,
-                                               sb.tileCounter, status, sb.skip, scan_wait_limit());
+                                               sb.tileCounter, status, sb.skip, scan_wait_limit(), sort_flag(L));
 }
 
 // ---------------------------------------------------------------------------
@@ -369,19 +390,19 @@ void launch_cell_scan(int numCells, SortBuffers sb, unsigned int* status, cudaSt
 // condition is reported.
 __global__ void k_scatter(int n, const int2* __restrict__ keySlot, const int* __restrict__ cellOffset,
                           int* __restrict__ tmpIds, int* __restrict__ sortedHash, const int* __restrict__ skip,
-                          const unsigned int* __restrict__ status) {
+                          const unsigned int* __restrict__ status, const unsigned int* __restrict__ sortFlag) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n || (skip && *skip) || (status && (*status & STATUS_DEVICE_WAIT))) return;
+    if (i >= n || (skip && *skip) || (status && (*status & STATUS_DEVICE_WAIT)) || (sortFlag && !*sortFlag)) return;
     int2 ks = keySlot[i];
     int dst = __ldg(cellOffset + ks.x) + ks.y;
     tmpIds[dst] = i;
     sortedHash[dst] = ks.x;
 }
 
-void launch_scatter(int n, SortBuffers sb, cudaStream_t s, const unsigned int* status) {
+void launch_scatter(int n, SortBuffers sb, cudaStream_t s, const unsigned int* status, const NeighbourLists* L) {
     if (n <= 0) return;
     k_scatter<<<(n + 255) / 256, 256, 0, s>>>(n, sb.keySlot, sb.cellOffset, sb.tmpIds, sb.sortedHash, sb.skip,
-                                              status);
+                                              status, sort_flag(L));
 }
 
 // ---------------------------------------------------------------------------
@@ -413,13 +434,30 @@ __global__ void k_rank_gather(int n, const int* __restrict__ sortedHash, const i
                               int* __restrict__ sortedIds, int* __restrict__ workIds, int* __restrict__ halfOffset,
                               float4* __restrict__ posS, float4* __restrict__ velS, const int* __restrict__ skip,
                               const unsigned int* __restrict__ vl, int vlScenes, const int* __restrict__ slotScene,
-                              const unsigned int* __restrict__ status) {
+                              unsigned int* status) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n || (skip && *skip) || (status && (*status & STATUS_DEVICE_WAIT))) return;
+    const int sc = BATCH && vl ? slotScene[k] : 0;  // the scene of sorted slot k
+    if (vl && !vl[VL_FLAGS * vlScenes + VL_SORT]) {
+        // no sort in this step: the state gathered into the kept order, with
+        // the hash pass's checks of each position
+        const int w = workIds[k];
+        const float4 p = __ldg(pos + w);
+        posS[k] = p;
+        velS[k] = __ldg(vel + w);
+        const GridDev& g = BATCH ? scenes[sc].g : g_;
+        if (!(isfinite(p.x) && isfinite(p.y) && isfinite(p.z))) {
+            atomicOr(status, STATUS_NON_FINITE);
+        } else {
+            bool outside = false;
+            particle_hash(p, g, &outside);
+            if (outside) atomicOr(status, STATUS_OUT_OF_DOMAIN);
+        }
+        return;
+    }
     int c = sortedHash[k];
     int s = __ldg(cellOffset + c), e = __ldg(cellOffset + c + 1);
     int my = tmpIds[k];
-    const int sc = BATCH && vl ? slotScene[k] : 0;  // the scene of sorted slot k
     if (vl && !vl[VL_BUILD_NOW * vlScenes + sc]) {
         int rId = 0;
         for (int t = s; t < e; t++) rId += __ldg(tmpIds + t) < my;
@@ -452,7 +490,7 @@ __global__ void k_rank_gather(int n, const int* __restrict__ sortedHash, const i
 }
 
 void launch_rank_gather(int n, SortBuffers sb, const float4* pos, const float4* vel, GridDev g, float4* posS,
-                        float4* velS, cudaStream_t s, const NeighbourLists* L, const unsigned int* status) {
+                        float4* velS, cudaStream_t s, const NeighbourLists* L, unsigned int* status) {
     if (n <= 0) return;
     const int grid = (n + 255) / 256;
     const unsigned int* vl = L ? L->flags : nullptr;
@@ -470,6 +508,44 @@ void launch_rank_gather(int n, SortBuffers sb, const float4* pos, const float4* 
         k_rank_gather<false, false><<<grid, 256, 0, s>>>(n, sb.sortedHash, sb.cellOffset, sb.tmpIds, pos, vel, g,
                                                          nullptr, sb.sortedIds, sb.workIds, sb.halfOffset, posS,
                                                          velS, sb.skip, vl, vs, nullptr, status);
+}
+
+// ---------------------------------------------------------------------------
+// Cell tables after a step that skipped them (reused lists, no build): the
+// step's positions are those of its sorted copies (in the kept working
+// order), so the tables are rebuilt from them -- the hash, scan and scatter
+// over the positions put back in particle order, then the rank by id within
+// each cell -- exactly as the step would have built them.
+// ---------------------------------------------------------------------------
+__global__ void k_unsort_positions(int n, const float4* __restrict__ posS, const int* __restrict__ workIds,
+                                   const int* __restrict__ slotScene, float4* __restrict__ out) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const float4 p = posS[k];  // (its fourth lane holds p/rho^2: the scene, for a batch, from the slot)
+    out[workIds[k]] = make_float4(p.x, p.y, p.z, slotScene ? __int_as_float(slotScene[k]) : 0.f);
+}
+
+__global__ void k_rank_ids(int n, const int* __restrict__ sortedHash, const int* __restrict__ cellOffset,
+                           const int* __restrict__ tmpIds, int* __restrict__ sortedIds) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int c = sortedHash[k];
+    const int s = __ldg(cellOffset + c), e = __ldg(cellOffset + c + 1);
+    const int my = tmpIds[k];
+    int rId = 0;
+    for (int t = s; t < e; t++) rId += __ldg(tmpIds + t) < my;
+    sortedIds[s + rId] = my;
+}
+
+void launch_rebuild_tables(int n, const float4* posS, const int* workIds, const int* slotScene, GridDev g,
+                           SortBuffers sb, float4* scratch, unsigned int* status, cudaStream_t s) {
+    if (n <= 0) return;
+    sb.skip = nullptr;
+    k_unsort_positions<<<(n + 255) / 256, 256, 0, s>>>(n, posS, workIds, slotScene, scratch);
+    launch_hash_count(n, scratch, g, sb, status, s, nullptr);
+    launch_cell_scan(g.numCells, sb, status, s, nullptr);
+    launch_scatter(n, sb, s, status, nullptr);
+    k_rank_ids<<<(n + 255) / 256, 256, 0, s>>>(n, sb.sortedHash, sb.cellOffset, sb.tmpIds, sb.sortedIds);
 }
 
 // ---------------------------------------------------------------------------
