@@ -107,9 +107,10 @@ typedef struct sph_options {
                             0.45 * neighbourSkin * compactSupport since, when
                             they are built again (a Verlet list; a pair that
                             comes within compactSupport in the meantime was
-                            within the skin when they were built).  The cell
-                            tables, hash and permutation are still built, bit
-                            exact, in every step; only the order in which the
+                            within the skin when they were built).  A step
+                            that builds no lists skips the hash, sort and cell
+                            tables (sph_read_cells builds that step's tables
+                            when asked, bit exact); only the order in which the
                             neighbour sums are taken follows the lists.  0: the
                             neighbour search runs in every step, as the
                             reference does (compute_particle_density_pressure,
@@ -297,7 +298,10 @@ sph_status sph_write(sph_handle h, int field, const void* src, size_t bytes);
 /* The neighbour-search tables of the last step (SaveInfoTable, :2709-2783):
  * sorted hashes, sorted particle ids (the sort permutation), and the
  * cell start/end lists with 0xFFFFFFFF for empty cells.  level 0 is the
- * particle grid, level 1 the sub-particle grid.  Any pointer may be NULL. */
+ * particle grid, level 1 the sub-particle grid.  Any pointer may be NULL.
+ * After a step over reused neighbour lists that built none (it skips the
+ * tables) the level-0 tables are built here from the state that step
+ * started from, as the step would have built them. */
 sph_status sph_read_cells(sph_handle h, int level, int* sortedHash, int* sortedIds,
                           int* cellStart, int* cellEnd);
 
