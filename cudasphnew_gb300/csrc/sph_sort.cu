@@ -15,6 +15,7 @@
 // thrust::sort_by_key produces in the reference (particle_simulation.cu:2340).
 #include <cuda/atomic>
 
+#include <algorithm>
 #include <cstdlib>
 
 #include "sph_device.cuh"
@@ -136,27 +137,36 @@ template <bool BATCH, bool REL>
 __global__ void k_hash_count(int n, const float4* __restrict__ pos, GridDev g_, const SceneDev* __restrict__ scenes,
                              int* __restrict__ cnt, int2* __restrict__ keySlot, unsigned int* status,
                              const int* __restrict__ skip, const unsigned int* __restrict__ sortFlag) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (sortFlag && !*sortFlag) return;
-    if (i >= n || (skip && *skip)) return;
-    float4 p = pos[i];
-    const GridDev& g = BATCH ? scenes[__float_as_int(p.w)].g : g_;
-    bool outside = false;
-    const bool finite = isfinite(p.x) && isfinite(p.y) && isfinite(p.z);
-    if (!finite) {
-        atomicOr(status, STATUS_NON_FINITE);
-        p = make_float4(g.origin[0], g.origin[1], g.origin[2], 0.f);
+    if ((sortFlag && !*sortFlag) || (skip && *skip)) return;
+    // one wave of blocks striding over the particles (a step that returns
+    // at once then costs one wave; the arrival order in a cell is ranked
+    // away later, so the grid shape changes no result)
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float4 p = pos[i];
+        const GridDev& g = BATCH ? scenes[__float_as_int(p.w)].g : g_;
+        bool outside = false;
+        const bool finite = isfinite(p.x) && isfinite(p.y) && isfinite(p.z);
+        if (!finite) {
+            atomicOr(status, STATUS_NON_FINITE);
+            p = make_float4(g.origin[0], g.origin[1], g.origin[2], 0.f);
+        }
+        int h;
+        if (REL) {
+            const int3 c = finite ? rel_cell(p) : make_int3(0, 0, 0);
+            h = g.cellBase + g.dim[0] * (g.dim[1] * c.z + c.y) + c.x;
+        } else {
+            h = particle_hash(p, g, &outside);
+        }
+        if (outside) atomicOr(status, STATUS_OUT_OF_DOMAIN);
+        int slot = atomicAdd(cnt + h, 1);
+        keySlot[i] = make_int2(h, slot);
     }
-    int h;
-    if (REL) {
-        const int3 c = finite ? rel_cell(p) : make_int3(0, 0, 0);
-        h = g.cellBase + g.dim[0] * (g.dim[1] * c.z + c.y) + c.x;
-    } else {
-        h = particle_hash(p, g, &outside);
-    }
-    if (outside) atomicOr(status, STATUS_OUT_OF_DOMAIN);
-    int slot = atomicAdd(cnt + h, 1);
-    keySlot[i] = make_int2(h, slot);
+}
+
+// Blocks of 256 threads for the striding sort passes: one full wave.
+static int stride_blocks(int n) {
+    const int want = (n + 255) / 256;
+    return std::max(1, std::min(want, device_sms() * (2048 / 256)));
 }
 
 // Reused neighbour lists: whether each scene builds them in this step (on
@@ -202,15 +212,14 @@ void launch_hash_count(int n, const float4* pos, GridDev g, SortBuffers sb, unsi
     if (n <= 0) return;
     if (L) k_list_decide<<<1, 256, 0, s>>>(*L, sb.scenes);
     const unsigned int* sf = sort_flag(L);
+    const int grid = stride_blocks(n);
     if (sb.scenes)
-        k_hash_count<true, false><<<(n + 255) / 256, 256, 0, s>>>(n, pos, g, sb.scenes, sb.cnt, sb.keySlot, status,
-                                                                  sb.skip, sf);
+        k_hash_count<true, false><<<grid, 256, 0, s>>>(n, pos, g, sb.scenes, sb.cnt, sb.keySlot, status, sb.skip, sf);
     else if (g.rel)
-        k_hash_count<false, true><<<(n + 255) / 256, 256, 0, s>>>(n, pos, g, nullptr, sb.cnt, sb.keySlot, status,
-                                                                  sb.skip, nullptr);
+        k_hash_count<false, true><<<grid, 256, 0, s>>>(n, pos, g, nullptr, sb.cnt, sb.keySlot, status, sb.skip,
+                                                       nullptr);
     else
-        k_hash_count<false, false><<<(n + 255) / 256, 256, 0, s>>>(n, pos, g, nullptr, sb.cnt, sb.keySlot, status,
-                                                                   sb.skip, sf);
+        k_hash_count<false, false><<<grid, 256, 0, s>>>(n, pos, g, nullptr, sb.cnt, sb.keySlot, status, sb.skip, sf);
 }
 
 // ---------------------------------------------------------------------------
@@ -391,18 +400,19 @@ void launch_cell_scan(int numCells, SortBuffers sb, unsigned int* status, cudaSt
 __global__ void k_scatter(int n, const int2* __restrict__ keySlot, const int* __restrict__ cellOffset,
                           int* __restrict__ tmpIds, int* __restrict__ sortedHash, const int* __restrict__ skip,
                           const unsigned int* __restrict__ status, const unsigned int* __restrict__ sortFlag) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n || (skip && *skip) || (status && (*status & STATUS_DEVICE_WAIT)) || (sortFlag && !*sortFlag)) return;
-    int2 ks = keySlot[i];
-    int dst = __ldg(cellOffset + ks.x) + ks.y;
-    tmpIds[dst] = i;
-    sortedHash[dst] = ks.x;
+    if ((skip && *skip) || (status && (*status & STATUS_DEVICE_WAIT)) || (sortFlag && !*sortFlag)) return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        int2 ks = keySlot[i];
+        int dst = __ldg(cellOffset + ks.x) + ks.y;
+        tmpIds[dst] = i;
+        sortedHash[dst] = ks.x;
+    }
 }
 
 void launch_scatter(int n, SortBuffers sb, cudaStream_t s, const unsigned int* status, const NeighbourLists* L) {
     if (n <= 0) return;
-    k_scatter<<<(n + 255) / 256, 256, 0, s>>>(n, sb.keySlot, sb.cellOffset, sb.tmpIds, sb.sortedHash, sb.skip,
-                                              status, sort_flag(L));
+    k_scatter<<<stride_blocks(n), 256, 0, s>>>(n, sb.keySlot, sb.cellOffset, sb.tmpIds, sb.sortedHash, sb.skip,
+                                               status, sort_flag(L));
 }
 
 // ---------------------------------------------------------------------------
