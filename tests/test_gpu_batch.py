@@ -121,6 +121,9 @@ def test_batch_takes_plain_steps_only(sphlib):
                 sim.step(mode=mode)
         with pytest.raises(sphlib.SphError):
             sim.diagnostics()
+        sim.step()
+        with pytest.raises(sphlib.SphError):
+            sim.surface_particles()  # per scene: not for batched handles
 
 
 def test_batched_workload_runs(sphlib):
