@@ -184,6 +184,19 @@ void free_all(sph_sim* s) {
     for (void* p : tsPtrs)
         if (p) cudaFree(p);
     if (s->statusHost) cudaFreeHost(s->statusHost);
+    for (cudaStream_t q : {s->upStream, s->downStream})
+        if (q) {
+            cudaStreamSynchronize(q);
+            cudaStreamDestroy(q);
+        }
+    for (int k = 0; k < 2; k++) {
+        if (s->upLand[k]) cudaFree(s->upLand[k]);
+        if (s->upReady[k]) cudaEventDestroy(s->upReady[k]);
+        if (s->upFree[k]) cudaEventDestroy(s->upFree[k]);
+    }
+    if (s->downStage) cudaFree(s->downStage);
+    if (s->downReady) cudaEventDestroy(s->downReady);
+    if (s->downFree) cudaEventDestroy(s->downFree);
     if (s->ownStream) cudaStreamDestroy(s->ownStream);
 }
 
@@ -695,6 +708,7 @@ sph_status sph_create(const SimulationParameters* params, const sph_options* opt
 sph_status sph_destroy(sph_handle s) {
     if (!s) return SPH_OK;
     cudaStreamSynchronize(s->stream);
+    if (s->downStream) cudaStreamSynchronize(s->downStream);
     free_all(s);
     delete s;
     return SPH_OK;
@@ -828,7 +842,10 @@ sph_status sph_step_many(sph_handle s, int mode, int count) {
 
 sph_status sph_synchronize(sph_handle s) {
     if (!s) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "handle is NULL");
-    return latched_status(s);
+    sph_status st = latched_status(s);
+    // asynchronous reads finish on the side stream
+    if (s->downStream) SPH_CUDA(cudaStreamSynchronize(s->downStream));
+    return st;
 }
 
 namespace {
@@ -888,13 +905,57 @@ sph_status read_two_scale(sph_sim* s, int field, void* dst, size_t bytes) {
 
 }  // namespace
 
-sph_status sph_read(sph_handle s, int field, void* dst, size_t bytes) {
-    if (!s || !dst) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "NULL argument");
-    if (field == SPH_FIELD_STATE || (field >= SPH_FIELD_SUB_VERTEX_DATA && field <= SPH_FIELD_DEFAULT_IDS)) {
-        sph_status st = latched_status(s);
-        if (st) return st;
-        return read_two_scale(s, field, dst, bytes);
+// Whether the stream has queued work that has not finished (not while it is
+// being captured: a captured stream takes the plain path).
+static bool stream_busy(cudaStream_t q) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(q, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return false;
+    const cudaError_t e = cudaStreamQuery(q);
+    if (e == cudaErrorNotReady) {
+        cudaGetLastError();  // (not an error: clear it)
+        return true;
     }
+    return false;
+}
+
+// The side streams, their buffers and events, made on first use (all or
+// nothing).
+static cudaError_t ensure_side_streams(sph_sim* s) {
+    if (s->upStream) return cudaSuccess;
+    const size_t n3 = 3 * (size_t)s->n;
+    cudaStream_t up = nullptr, down = nullptr;
+    float *land[2] = {nullptr, nullptr}, *stage = nullptr;
+    cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    cudaError_t e = cudaStreamCreateWithFlags(&up, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&down, cudaStreamNonBlocking);
+    for (int k = 0; k < 2 && e == cudaSuccess; k++) e = dalloc(&land[k], n3);
+    if (e == cudaSuccess) e = dalloc(&stage, n3);
+    for (int k = 0; k < 6 && e == cudaSuccess; k++) e = cudaEventCreateWithFlags(&ev[k], cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+        for (float* p : {land[0], land[1], stage})
+            if (p) cudaFree(p);
+        for (cudaEvent_t x : ev)
+            if (x) cudaEventDestroy(x);
+        for (cudaStream_t q : {up, down})
+            if (q) cudaStreamDestroy(q);
+        return e;
+    }
+    s->upStream = up;
+    s->downStream = down;
+    for (int k = 0; k < 2; k++) {
+        s->upLand[k] = land[k];
+        s->upReady[k] = ev[k];
+        s->upFree[k] = ev[2 + k];
+    }
+    s->downStage = stage;
+    s->downReady = ev[4];
+    s->downFree = ev[5];
+    return cudaSuccess;
+}
+
+// The fields of the particle grid; `wait`: return when the data is there
+// and report the latched conditions, else only enqueue (no host-side step).
+static sph_status read_field(sph_sim* s, int field, void* dst, size_t bytes, bool wait) {
     const int n = s->n;
     size_t need = 0;
     switch (field) {
@@ -913,9 +974,16 @@ sph_status sph_read(sph_handle s, int field, void* dst, size_t bytes) {
     // for a pack into device memory and a DMA copy); the other fields and
     // pageable destinations go through the staging buffer and one DMA copy
     float* direct = nullptr;
-    if ((field == SPH_FIELD_VERTEX_DATA && !s->O.cellRelative) || field == SPH_FIELD_VELOCITY)
+    if (wait && ((field == SPH_FIELD_VERTEX_DATA && !s->O.cellRelative) || field == SPH_FIELD_VELOCITY))
         direct = static_cast<float*>(host_device_ptr(dst));
     float* out = direct ? direct : s->staging;
+    if (!wait) {
+        // packed on the handle's stream into a buffer of its own, copied to
+        // the host by DMA on the side stream: the next step need not wait
+        SPH_CUDA(ensure_side_streams(s));
+        SPH_CUDA(cudaStreamWaitEvent(q, s->downFree, 0));
+        out = s->downStage;
+    }
     switch (field) {
         case SPH_FIELD_VERTEX_DATA:
             if (s->O.cellRelative) launch_rel_to_abs(n, s->pos, grid_of(s), out, 3, nullptr, q);
@@ -943,6 +1011,13 @@ sph_status sph_read(sph_handle s, int field, void* dst, size_t bytes) {
             break;
     }
     SPH_CUDA(cudaGetLastError());
+    if (!wait) {
+        SPH_CUDA(cudaEventRecord(s->downReady, q));
+        SPH_CUDA(cudaStreamWaitEvent(s->downStream, s->downReady, 0));
+        SPH_CUDA(cudaMemcpyAsync(dst, s->downStage, need, cudaMemcpyDeviceToHost, s->downStream));
+        SPH_CUDA(cudaEventRecord(s->downFree, s->downStream));
+        return SPH_OK;
+    }
     if (!direct) SPH_CUDA(cudaMemcpyAsync(dst, s->staging, need, cudaMemcpyDeviceToHost, q));
     // one synchronisation: the status word comes back with the data
     SPH_CUDA(cudaMemcpyAsync(s->statusHost, s->status, sizeof(unsigned int), cudaMemcpyDeviceToHost, q));
@@ -960,6 +1035,23 @@ sph_status sph_read(sph_handle s, int field, void* dst, size_t bytes) {
     return SPH_OK;
 }
 
+sph_status sph_read(sph_handle s, int field, void* dst, size_t bytes) {
+    if (!s || !dst) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (field == SPH_FIELD_STATE || (field >= SPH_FIELD_SUB_VERTEX_DATA && field <= SPH_FIELD_DEFAULT_IDS)) {
+        sph_status st = latched_status(s);
+        if (st) return st;
+        return read_two_scale(s, field, dst, bytes);
+    }
+    return read_field(s, field, dst, bytes, true);
+}
+
+sph_status sph_read_async(sph_handle s, int field, void* dst, size_t bytes) {
+    if (!s || !dst) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (field < SPH_FIELD_VERTEX_DATA || field > SPH_FIELD_PRESSURE || field == SPH_FIELD_SIMULATION_DATA)
+        SPH_FAIL(SPH_ERR_NOT_SUPPORTED, "sph_read_async takes VD, velocity, acceleration, density or pressure");
+    return read_field(s, field, dst, bytes, false);
+}
+
 sph_status sph_write(sph_handle s, int field, const void* src, size_t bytes) {
     if (!s || !src) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "NULL argument");
     const int n = s->n;
@@ -971,11 +1063,27 @@ sph_status sph_write(sph_handle s, int field, const void* src, size_t bytes) {
             if (bytes < sizeof(float) * 3 * (size_t)n) SPH_FAIL(SPH_ERR_INVALID_ARGUMENT, "source too small");
             // page-locked sources are read by the unpacking kernel itself
             const float* in = static_cast<const float*>(host_device_ptr(src));
+            float4* target = field == SPH_FIELD_VERTEX_DATA ? s->pos : s->vel;
             if (!in) {
                 SPH_CUDA(cudaMemcpyAsync(s->staging, src, sizeof(float) * 3 * (size_t)n, cudaMemcpyHostToDevice, q));
-                in = s->staging;
+                launch_unpack_aos(s->staging, 3, 0, n, target, q);
+            } else if (stream_busy(q)) {
+                // the handle's stream still has work: a DMA copy on the side
+                // stream lands the data beside that work (the copy engines,
+                // not the SMs the queued kernels hold), and the handle's stream
+                // unpacks it into place once it has landed
+                SPH_CUDA(ensure_side_streams(s));
+                const int k = field == SPH_FIELD_VERTEX_DATA ? 0 : 1;
+                SPH_CUDA(cudaStreamWaitEvent(s->upStream, s->upFree[k], 0));
+                SPH_CUDA(cudaMemcpyAsync(s->upLand[k], src, sizeof(float) * 3 * (size_t)n, cudaMemcpyHostToDevice,
+                                         s->upStream));
+                SPH_CUDA(cudaEventRecord(s->upReady[k], s->upStream));
+                SPH_CUDA(cudaStreamWaitEvent(q, s->upReady[k], 0));
+                launch_unpack_aos(s->upLand[k], 3, 0, n, target, q);
+                SPH_CUDA(cudaEventRecord(s->upFree[k], q));
+            } else {
+                launch_unpack_aos(in, 3, 0, n, target, q);
             }
-            launch_unpack_aos(in, 3, 0, n, field == SPH_FIELD_VERTEX_DATA ? s->pos : s->vel, q);
             if (field == SPH_FIELD_VERTEX_DATA && s->O.cellRelative) launch_abs_to_rel(n, s->pos, grid_of(s), q);
             if (field == SPH_FIELD_VERTEX_DATA && s->numScenes > 1)  // restore the scene index lanes
                 for (int k = 0; k < s->numScenes; k++)

@@ -74,6 +74,19 @@ struct sph_sim {
                                         // (set by an accepting audit, used up by the next step)
     unsigned int* statusHost = nullptr; // pinned copy
     float* staging = nullptr;           // device AoS staging, n*10 floats
+    // Uploads from page-locked sources while the handle's stream is busy: DMA
+    // copies on a stream of their own into landing buffers (AoS), unpacked on
+    // the handle's stream once landed, so the host link and the work queued
+    // there overlap.  Asynchronous reads: packed on the handle's stream into
+    // a buffer of their own, copied to the host by DMA on another stream.
+    cudaStream_t upStream = nullptr;
+    float* upLand[2] = {nullptr, nullptr};           // positions, velocities: float[3n]
+    cudaEvent_t upReady[2] = {nullptr, nullptr};     // landed
+    cudaEvent_t upFree[2] = {nullptr, nullptr};      // unpacked: the landing buffer may be refilled
+    cudaStream_t downStream = nullptr;
+    float* downStage = nullptr;                      // float[3n]
+    cudaEvent_t downReady = nullptr;                 // packed
+    cudaEvent_t downFree = nullptr;                  // copied to the host: the buffer may be refilled
     std::vector<float> sdMass, sdEnergy;  // SD_MASS / SD_ENERGY columns (never touched by the step)
 
     // boundary maps

@@ -42,6 +42,7 @@ SIGNATURES = {
     "sph_step_many": (_i, [_vp, _i, _i]),
     "sph_synchronize": (_i, [_vp]),
     "sph_read": (_i, [_vp, _i, _vp, ctypes.c_size_t]),
+    "sph_read_async": (_i, [_vp, _i, _vp, ctypes.c_size_t]),
     "sph_write": (_i, [_vp, _i, _vp, ctypes.c_size_t]),
     "sph_read_cells": (_i, [_vp, _i, _vp, _vp, _vp, _vp]),
     "sph_get_counts": (_i, [_vp, _vp]),

@@ -291,9 +291,23 @@ sph_status sph_read(sph_handle h, int field, void* dst, size_t bytes);
 /* Overwrites a field from host memory (SPH_FIELD_VERTEX_DATA,
  * SPH_FIELD_VELOCITY or SPH_FIELD_SIMULATION_DATA).  A page-locked source of
  * positions or velocities is read by the unpacking kernel itself, later on
- * the handle's stream (as an asynchronous copy from pinned memory would be):
- * keep it unchanged until the next synchronising call. */
+ * the handle's stream (as an asynchronous copy from pinned memory would be);
+ * when that stream still has work queued, the upload runs beside it on a
+ * stream of its own, into a device buffer that is copied into place on the
+ * handle's stream once it has landed, so the host link and the queued work
+ * overlap.  Either way: keep the source unchanged until the next
+ * synchronising call. */
 sph_status sph_write(sph_handle h, int field, const void* src, size_t bytes);
+
+/* sph_read without waiting: enqueues the read of a field of the particle
+ * grid (VD, velocity, acceleration, density or pressure) on the handle's
+ * stream and returns.  The destination holds the field once the stream has
+ * reached that point (sph_synchronize); the conditions steps latch are
+ * reported by the next synchronising call.  A loop of sph_write (page-locked
+ * sources), sph_step and sph_read_async thus overlaps each step's uploads
+ * with the work and read-back queued before them.  No reference
+ * counterpart. */
+sph_status sph_read_async(sph_handle h, int field, void* dst, size_t bytes);
 
 /* The neighbour-search tables of the last step (SaveInfoTable, :2709-2783):
  * sorted hashes, sorted particle ids (the sort permutation), and the

@@ -104,3 +104,64 @@ def test_read_into_page_locked_memory_at_any_alignment(sphlib, shift):
             sphlib.check(L.sph_read(sim._h, field, ctypes.c_void_p(dst.data_ptr()), n * 12))
             np.testing.assert_array_equal(dst.numpy().reshape(n, 3), want)
             assert np.all(buf.numpy()[:shift] == -7.0) and np.all(buf.numpy()[shift + n * 3:] == -7.0)
+
+
+def test_pipelined_loop_equals_the_blocking_loop(sphlib):
+    """write (page-locked) + step + sph_read_async in a loop -- each step's
+    uploads issued while the previous step and its read-back are still queued,
+    so they take the overlapped path -- gives every step's result bit for bit
+    as write + step + sph_read does."""
+    sc = scenes.config1()
+    n = sc.n
+    L = sphlib.load()
+    rng = np.random.default_rng(3)
+    steps = 6
+    xs = [pinned((sc.positions + rng.uniform(-2e-4, 2e-4, sc.positions.shape)).astype(np.float32))
+          for _ in range(steps)]
+    vs = [pinned(rng.uniform(-0.5, 0.5, (n, 3)).astype(np.float32)) for _ in range(steps)]
+    results = {}
+    for mode in ("blocking", "pipelined"):
+        outs = [torch.zeros((n, 3), dtype=torch.float32, pin_memory=True) for _ in range(steps)]
+        with sphlib.ParticleSimulation(sc.params, sc.positions, sc.velocities, sc.options, sc.boundary) as sim:
+            sim.step(count=2)
+            sim.synchronize()
+            for k in range(steps):
+                sphlib.check(L.sph_write(sim._h, sphlib.FIELD_VERTEX_DATA, ctypes.c_void_p(xs[k].data_ptr()), n * 12))
+                sphlib.check(L.sph_write(sim._h, sphlib.FIELD_VELOCITY, ctypes.c_void_p(vs[k].data_ptr()), n * 12))
+                sphlib.check(L.sph_step(sim._h, sphlib.SPH_STEP_PLAIN))
+                read = L.sph_read if mode == "blocking" else L.sph_read_async
+                sphlib.check(read(sim._h, sphlib.FIELD_VERTEX_DATA, ctypes.c_void_p(outs[k].data_ptr()), n * 12))
+            sim.synchronize()
+        results[mode] = [o.numpy().copy() for o in outs]
+    for a, b in zip(results["blocking"], results["pipelined"]):
+        np.testing.assert_array_equal(a, b)
+    assert not np.array_equal(results["blocking"][0], results["blocking"][1])
+
+
+def test_write_while_busy_is_ordered_before_later_work(sphlib):
+    """A page-locked write issued while steps are still queued lands before
+    anything enqueued after it: the next read returns the written state."""
+    sc = scenes.config1()
+    n = sc.n
+    L = sphlib.load()
+    rng = np.random.default_rng(9)
+    x = pinned((sc.positions + rng.uniform(-1e-4, 1e-4, sc.positions.shape)).astype(np.float32))
+    v = pinned(rng.standard_normal((n, 3)).astype(np.float32))
+    with sphlib.ParticleSimulation(sc.params, sc.positions, sc.velocities, sc.options, sc.boundary) as sim:
+        sim.step(count=2)
+        sim.synchronize()
+        sphlib.check(L.sph_step_many(sim._h, sphlib.SPH_STEP_PLAIN, 20))  # queued, not waited for
+        sphlib.check(L.sph_write(sim._h, sphlib.FIELD_VERTEX_DATA, ctypes.c_void_p(x.data_ptr()), n * 12))
+        sphlib.check(L.sph_write(sim._h, sphlib.FIELD_VELOCITY, ctypes.c_void_p(v.data_ptr()), n * 12))
+        np.testing.assert_array_equal(sim.positions(), x.numpy())
+        np.testing.assert_array_equal(sim.velocities(), v.numpy())
+
+
+def test_read_async_refuses_host_side_fields(sphlib):
+    sc = scenes.dam_break(8, 8, 8, (0, 0, 0), (0.5, 0.5, 0.5), 3, "io_tiny", 0)
+    L = sphlib.load()
+    with sphlib.ParticleSimulation(sc.params, sc.positions, sc.velocities, sc.options, sc.boundary) as sim:
+        sim.step()
+        buf = np.zeros(sc.n * 10, np.float32)
+        for field in (sphlib.FIELD_SIMULATION_DATA, sphlib.FIELD_STATE):
+            assert L.sph_read_async(sim._h, field, buf.ctypes.data, buf.nbytes) != 0
