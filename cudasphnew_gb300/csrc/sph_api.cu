@@ -324,10 +324,11 @@ sph_status alloc_lists(sph_sim* s) {
     return SPH_OK;
 }
 
-// A plain step over the reused neighbour lists: the reference's hash, sort
-// and cell tables as in every step, the state gathered into the lists'
-// working order, then the density stage (building the lists when this step
-// must) and the force stage over them.
+// A plain step over the reused neighbour lists: the decision, the
+// reference's hash, sort and cell tables when some scene builds (a step that
+// builds nothing skips them; sph_read_cells builds its tables on demand),
+// the state gathered into the lists' working order, then the density stage
+// (building the lists when this step must) and the force stage over them.
 static void enqueue_lists(sph_sim* s, const GridDev& g, const PhysDev& ph, int collide, cudaEvent_t* ev) {
     cudaStream_t st = s->stream;
     const int n = s->n;

@@ -223,8 +223,9 @@ void launch_pack_aos(const float4* in, int n, float* aos, int stride, int offset
 // back to absolute (AoS with `stride` floats per particle and/or float4s).
 void launch_abs_to_rel(int n, float4* pos, GridDev g, cudaStream_t s);
 void launch_rel_to_abs(int n, const float4* pos, GridDev g, float* aos, int stride, float4* out4, cudaStream_t s);
-// With `lists`, the first thread also decides whether this step builds the
-// neighbour lists (VL_BUILD_NOW).
+// With `lists`, a one-block kernel first decides whether each scene builds
+// the neighbour lists in this step (VL_BUILD_NOW) and whether the step sorts
+// (VL_SORT); the hash pass returns at once when it does not.
 void launch_hash_count(int n, const float4* pos, GridDev g, SortBuffers sb, unsigned int* status,
                        cudaStream_t s, const NeighbourLists* lists = nullptr);
 // With `lists`, the scan and the scatter return at once in a step that
