@@ -208,9 +208,9 @@ void enqueue_audit(sph_sim* s, Corrector* C) {
         launch_force(s->n, s->posS, s->velS, s->rho4S, s->sb.workIds, rows_of(s), grid_of(s),
                      make_phys(s->P, s->O), s->map, s->O.boxCollision, s->rowStart, s->rowMask, s->pos, s->vel,
                      s->accS, s->cfg, q, nullptr, s->status);
-    // the per-step search: the plain solver the audit replays is the one the
-    // learned step's first plain step above belongs to
-    for (int k = 1; k < C->cfg.stride; k++) enqueue_step(s, SPH_STEP_PLAIN, false, false);
+    // the rest of the plain solver, as the first plain step above: over the
+    // learned step's lists (reused while they hold) or with the per-step search
+    for (int k = 1; k < C->cfg.stride; k++) enqueue_step(s, SPH_STEP_PLAIN, false, s->vlOn);
     enqueue_density_only(s, s->pos, s->vel);
     launch_unpermute(s->n, s->sb.workIds, s->rho4S, 0, C->rhoB, 1, 0, q);
     // last: the learned result, with the neighbour masks, so that when the

@@ -334,18 +334,38 @@ def test_training_lowers_loss_and_corrects_the_long_step(sphlib):
 
 
 def test_audit_rolls_back_to_the_plain_solver(sphlib):
+    # the per-step search (the lists' form: the next test)
     sc = tiny()
     blob = random_blob(5)
     k, stride = 3, 4
-    with make(sphlib, sc) as sim:
+    with make(sphlib, sc, skin=0.0) as sim:
         sim.load_corrector(blob, stride=stride, auditInterval=1, densityTolerance=0.0)
         sim.step(mode=sphlib.SPH_STEP_LEARNED, count=k)
         pos, vel = sim.positions(), sim.velocities()
         rep = sim.corrector_report()
     assert rep.audits == k and rep.rollbacks == k and rep.maxAuditError > 0
-    # the audit's plain solver searches the neighbours in every step
     with make(sphlib, sc, skin=0.0) as plain:
         plain.step(count=k * stride)
+        np.testing.assert_array_equal(pos, plain.positions())
+        np.testing.assert_array_equal(vel, plain.velocities())
+
+
+def test_audit_over_the_lists_rolls_back_to_the_plain_solver(sphlib):
+    """With reused neighbour lists the audit's plain solver is the plain
+    solver over the lists: one audited step with tolerance 0 gives the bits
+    of four plain steps of a new handle (the first builds the lists, the
+    others reuse them)."""
+    sc = tiny()
+    stride = 4
+    with make(sphlib, sc) as sim:
+        sim.load_corrector(random_blob(5), stride=stride, auditInterval=1, densityTolerance=0.0)
+        sim.step(mode=sphlib.SPH_STEP_LEARNED)
+        pos, vel = sim.positions(), sim.velocities()
+        rep = sim.corrector_report()
+    assert rep.audits == 1 and rep.rollbacks == 1
+    with make(sphlib, sc) as plain:
+        plain.step(count=stride)
+        assert plain.neighbour_builds() == 1
         np.testing.assert_array_equal(pos, plain.positions())
         np.testing.assert_array_equal(vel, plain.velocities())
 
