@@ -165,3 +165,50 @@ def test_read_async_refuses_host_side_fields(sphlib):
         buf = np.zeros(sc.n * 10, np.float32)
         for field in (sphlib.FIELD_SIMULATION_DATA, sphlib.FIELD_STATE):
             assert L.sph_read_async(sim._h, field, buf.ctypes.data, buf.nbytes) != 0
+
+
+@pytest.mark.parametrize("pinned_dst", [True, False])
+def test_read_async_fields_equal_blocking_reads(sphlib, pinned_dst):
+    """Every field sph_read_async takes, into page-locked or pageable memory,
+    holds after sph_synchronize what sph_read gives."""
+    sc = scenes.config1()
+    n = sc.n
+    L = sphlib.load()
+    fields = {sphlib.FIELD_VERTEX_DATA: 3, sphlib.FIELD_VELOCITY: 3, sphlib.FIELD_ACCELERATION: 3,
+              sphlib.FIELD_DENSITY: 1, sphlib.FIELD_PRESSURE: 1}
+    with sphlib.ParticleSimulation(sc.params, sc.positions, sc.velocities, sc.options, sc.boundary) as sim:
+        sim.step(count=3)
+        outs = {}
+        for f, c in fields.items():
+            if pinned_dst:
+                buf = torch.zeros((n * c,), dtype=torch.float32, pin_memory=True)
+                ptr, arr = buf.data_ptr(), buf.numpy()
+            else:
+                arr = np.zeros(n * c, np.float32)
+                ptr = arr.ctypes.data
+            sphlib.check(L.sph_read_async(sim._h, f, ctypes.c_void_p(ptr), n * c * 4))
+            outs[f] = (arr, buf if pinned_dst else None)
+        sim.synchronize()
+        for f, (arr, _) in outs.items():
+            np.testing.assert_array_equal(arr.reshape(sim.read(f).shape), sim.read(f))
+
+
+def test_batch_writes_while_busy_keep_scene_lanes(sphlib):
+    """A batched handle's page-locked writes issued behind queued steps land
+    in order and keep each particle's scene."""
+    scs = [scenes.batched_scene(k, f, 300 + i, f"io{i}") for i, (k, f) in enumerate(((1500, 0.05), (2500, 0.1)))]
+    L = sphlib.load()
+    with sphlib.ParticleSimulation.batch(scs, scs[0].options) as sim:
+        n = sim.n
+        sim.step(count=2)
+        x, v = sim.positions(), sim.velocities()
+        px, pv = pinned(x), pinned(v)
+        sphlib.check(L.sph_step_many(sim._h, sphlib.SPH_STEP_PLAIN, 10))  # queued
+        sphlib.check(L.sph_write(sim._h, sphlib.FIELD_VERTEX_DATA, ctypes.c_void_p(px.data_ptr()), n * 12))
+        sphlib.check(L.sph_write(sim._h, sphlib.FIELD_VELOCITY, ctypes.c_void_p(pv.data_ptr()), n * 12))
+        sim.step(count=3)
+        got = sim.positions()
+    with sphlib.ParticleSimulation.batch(scs, scs[0].options) as ref:
+        ref.step(count=2)
+        ref.step(count=3)
+        np.testing.assert_array_equal(got, ref.positions())
