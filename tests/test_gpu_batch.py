@@ -92,6 +92,31 @@ def test_batch_rebuilds_each_scenes_lists_when_that_scene_would_alone(sphlib):
     assert b["builds"] == sum(builds)
 
 
+def test_batch_graph_steps_equal_eager_steps(sphlib):
+    """Steps replayed from the captured step graph and steps launched one by
+    one (no graph) give the same bits, with scenes building their lists at
+    different steps: the per-scene decisions made on the device alone select
+    which kernels work for which scene."""
+    scs = small_batch()
+    for k, sc in enumerate(scs):
+        sc.velocities[:, 0] = 0.3 * k
+    outs = []
+    for graph in (True, False):
+        with sphlib.ParticleSimulation.batch(scs, with_skin(scs[0].options, None)) as sim:
+            if graph:
+                sim.step(count=40)
+            else:
+                for _ in range(40):
+                    sim.step()
+            h, ids, start, end = sim.cells()
+            outs.append(dict(pos=sim.positions(), vel=sim.velocities(), rho=sim.read(sphlib.FIELD_DENSITY),
+                             acc=sim.read(sphlib.FIELD_ACCELERATION), hash=h, ids=ids, start=start, end=end,
+                             builds=sim.neighbour_builds()))
+    assert len(scs) < outs[0]["builds"] < 40 * len(scs)
+    for key in outs[0]:
+        np.testing.assert_array_equal(outs[1][key], outs[0][key], err_msg=key)
+
+
 def test_batch_autotune_keeps_results(sphlib):
     scs = small_batch()
     _, _, b0 = run_batch(sphlib, scs, 4)

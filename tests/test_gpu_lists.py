@@ -66,6 +66,26 @@ def moving_scene(speed, seed=5):
     return sc
 
 
+def test_graph_steps_equal_eager_steps(sphlib):
+    """Steps replayed from the captured step graph and steps launched one by
+    one (no graph) give the same bits, across builds and reuses: the decision
+    made on the device alone selects which kernels work in each step."""
+    sc = moving_scene(1.0)
+    outs = []
+    for graph in (True, False):
+        with sphlib.ParticleSimulation(sc.params, sc.positions, sc.velocities, with_skin(sc, 0.1),
+                                       sc.boundary) as sim:
+            if graph:
+                sim.step(count=24)
+            else:
+                for _ in range(24):
+                    sim.step()
+            outs.append(state(sphlib, sim) | {"builds": sim.neighbour_builds()})
+    assert 1 < outs[0]["builds"] < 24
+    for k in outs[0]:
+        np.testing.assert_array_equal(outs[1][k], outs[0][k], err_msg=k)
+
+
 def test_reusing_steps_match_the_oracle_across_builds(sphlib, orc):
     """12 steps at up to 2 m/s per axis (up to 3.5e-4 m per step against a
     rebuild distance of 0.45 * 0.1 h = 1.1e-3 m): the lists are built every few
