@@ -761,8 +761,12 @@ __global__ void __launch_bounds__(256, FEAT ? 3 : (BATCH || TENSION || REL || FO
 // k_force.  The next row's entries are loaded before the current row is
 // walked.  It also records, for the decision at the next step, the largest
 // squared distance of a particle from where it was when the lists were built.
-// Occupancy: 64 registers, four 256-thread blocks per SM, no spills (at 48
-// registers and five blocks the spills cost more than the warps gain).
+// Occupancy: at most 56 registers, so nine 128-thread blocks fit on an SM
+// (36 warps; at 64 registers eight): the single-scene forms spill 4-16
+// bytes, the batched ones up to 88, and both run 1-2 % faster per step than
+// at 64 registers without spills.  At 48 registers (ten blocks) the spills
+// cost more than the warps gain.  A register cap, not a launch bound, so any
+// block size the autotuner tries stays launchable.
 // ---------------------------------------------------------------------------
 // Displacement since the build into the scene's flag: one atomic per warp (or
 // per scene a warp holds) that raises the recorded maximum.  Squared
@@ -780,7 +784,7 @@ __device__ __forceinline__ void record_displacement(const NeighbourLists& L, int
 }
 
 template <bool KAHAN, bool TENSION, bool BATCH>
-__global__ void __launch_bounds__(256, 4)
+__global__ void __maxnreg__(56)
 k_force_lists(int n, const float4* __restrict__ posS, const float4* __restrict__ velS,
               const float4* __restrict__ rho4S, const int* __restrict__ workIds, PhysDev ph_, MapDev map_,
               int collideFlag, NeighbourLists L, float4* __restrict__ pos, float4* __restrict__ vel,
