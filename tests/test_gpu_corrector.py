@@ -370,6 +370,36 @@ def test_audit_over_the_lists_rolls_back_to_the_plain_solver(sphlib):
         np.testing.assert_array_equal(vel, plain.velocities())
 
 
+def test_audit_at_the_default_tolerance_rolls_back_a_drifting_corrector(sphlib):
+    """At the default 1 % density tolerance the audit keeps a corrector that
+    adds nothing (the uncorrected long step's densities differ from four
+    short steps' by far less) and rolls back one whose corrections move
+    particles by up to a few tenths of their spacing: every audited step
+    then ends in the plain solver's state, bit for bit."""
+    sc = tiny()
+    k, stride = 3, 4
+    zero = random_blob(7)
+    zero[:NPARAM] = 0.0                      # the network gives 0 ...
+    zero[NPARAM + 48:NPARAM + 54] = 0.0      # ... and the target means are 0: no correction
+    drift = random_blob(7)
+    drift[NPARAM + 54:NPARAM + 60] *= 30.0   # target deviations 0.3-3 mm (spacing 12.5 mm)
+    assert abs(sphlib.CorrectorConfig.default().densityTolerance - 0.01) < 1e-9
+    reports, states = [], []
+    for blob in (zero, drift):
+        with make(sphlib, sc, skin=0.0) as sim:
+            sim.load_corrector(blob, stride=stride, auditInterval=1)
+            sim.step(mode=sphlib.SPH_STEP_LEARNED, count=k)
+            reports.append(sim.corrector_report())
+            states.append((sim.positions(), sim.velocities()))
+    kept, rolled = reports
+    assert kept.audits == k and kept.rollbacks == 0 and kept.maxAuditError < 0.01
+    assert rolled.audits == k and rolled.rollbacks == k and rolled.maxAuditError > 0.01
+    with make(sphlib, sc, skin=0.0) as plain:
+        plain.step(count=k * stride)
+        np.testing.assert_array_equal(states[1][0], plain.positions())
+        np.testing.assert_array_equal(states[1][1], plain.velocities())
+
+
 def test_audit_keeps_the_learned_result_within_tolerance(sphlib):
     # the per-step search (with reused lists the run with audits, which
     # rebuild the lists after each, would differ from the one without by the
