@@ -181,13 +181,39 @@ def pair_count(pos, h):
     return int(t.count_neighbors(t, h)) - len(pos)
 
 
+def code_of(src):
+    """C/C++ source without its comments and blank lines, each line stripped:
+    what the compiler sees, so an edit of comments alone keeps the hash."""
+    out, i, n = [], 0, len(src)
+    while i < n:
+        c = src[i]
+        if c in "\"'":  # a string or character literal, escapes included
+            j = i + 1
+            while j < n and src[j] != c and src[j] != "\n":
+                j += 2 if src[j] == "\\" else 1
+            out.append(src[i:j + 1])
+            i = j + 1
+        elif src.startswith("//", i):
+            j = src.find("\n", i)
+            i = n if j < 0 else j
+        elif src.startswith("/*", i):
+            j = src.find("*/", i + 2)
+            i = n if j < 0 else j + 2
+            out.append(" ")
+        else:
+            out.append(c)
+            i += 1
+    return "\n".join(line.strip() for line in "".join(out).splitlines() if line.strip())
+
+
 def kernel_sources_sha16():
-    """Hash of the neighbour kernels' source files (see KERNEL_SOURCES)."""
+    """Hash of the code of the neighbour kernels' source files (see
+    KERNEL_SOURCES), comments and blank lines left out."""
     import hashlib
     d = hashlib.sha256()
     for f in KERNEL_SOURCES:
-        with open(os.path.join(ROOT, f), "rb") as fh:
-            d.update(fh.read())
+        with open(os.path.join(ROOT, f), encoding="utf-8") as fh:
+            d.update(code_of(fh.read()).encode())
     return d.hexdigest()[:16]
 
 

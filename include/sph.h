@@ -283,9 +283,10 @@ sph_status sph_synchronize(sph_handle h);
 
 /* Copies a field to host memory (GetParticleState, SaveParticleInfo,
  * :2238-2243, :2785-2852).  `bytes` must be at least the field's size.
- * Returns when the data is in place.  The field is gathered into a device
- * staging buffer and copied back by one DMA copy (the fastest route to a
- * page-locked destination as well). */
+ * Returns when the data is in place.  Positions and velocities bound for a
+ * page-locked destination are packed into it by the kernel itself, over the
+ * host link; other fields and pageable destinations are gathered into a
+ * device staging buffer and copied back by one DMA copy. */
 sph_status sph_read(sph_handle h, int field, void* dst, size_t bytes);
 
 /* Overwrites a field from host memory (SPH_FIELD_VERTEX_DATA,

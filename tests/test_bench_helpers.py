@@ -88,3 +88,11 @@ def test_peak_source(tmp_path, monkeypatch):
     assert bench.load_peaks() == (6800.0, "fallback")
     (tmp_path / "MEASURED_PEAKS.json").write_text(json.dumps({"hbm_gbs": 6788.3}))
     assert bench.load_peaks() == (6788.3, "measured")
+
+
+def test_kernel_hash_ignores_comments_only():
+    src = 'int a = 1; // one\n/* block\n   comment */\nconst char* s = "//x /* y */";\n\nchar c = \'"\';\n'
+    code = bench.code_of(src)
+    assert code == 'int a = 1;\nconst char* s = "//x /* y */";\nchar c = \'"\';'
+    assert bench.code_of(src.replace("one", "two").replace("block", "other")) == code
+    assert bench.code_of(src.replace("a = 1", "a = 2")) != code
