@@ -112,7 +112,8 @@ def load_peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+    """nvidia-smi clocks / throttle reasons sampled every 20 ms (the timed
+    region of the default run lasts about 0.15 s)."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -128,7 +129,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "20"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except Exception:
             self.proc = None
@@ -141,6 +142,13 @@ class ClockSampler:
             parts = [p.strip() for p in line.split(",")]
             if len(parts) >= 9:
                 self.samples.append((time.time(), parts))
+
+    def wait_running(self, timeout=5.0):
+        """Returns once the first sample is in (or after `timeout` seconds),
+        so that the sampling covers the region that follows."""
+        t_end = time.time() + timeout
+        while self.proc and not self.samples and time.time() < t_end:
+            time.sleep(0.01)
 
     def stop(self):
         if self.proc:
@@ -902,6 +910,7 @@ def run_ours(args):
     builds0 = sim.neighbour_builds()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
+    clocks.wait_running()
     barrier(dist)
     torch.cuda.synchronize()
     t_wall0 = time.time()
