@@ -96,3 +96,18 @@ def test_kernel_hash_ignores_comments_only():
     assert code == 'int a = 1;\nconst char* s = "//x /* y */";\nchar c = \'"\';'
     assert bench.code_of(src.replace("one", "two").replace("block", "other")) == code
     assert bench.code_of(src.replace("a = 1", "a = 2")) != code
+
+
+def test_clock_summary_reads_the_timed_region():
+    def row(sm, reasons=("Not Active",) * 4):
+        return ["0", str(sm), "2070", "900", "0x0", *reasons]
+    c = bench.ClockSampler(0)
+    c.samples = [(0.5, row(1000)), (1.0, row(2070)), (1.1, row(2060)),
+                 (1.2, row(2070, ("Not Active", "Not Active", "Not Active", "Active"))), (3.0, row(900))]
+    s = c.summary(0.9, 1.3)
+    assert s["window"] == "timed_region" and s["samples"] == 3
+    assert s["sm_mhz"] == 2070.0 and s["sm_max_mhz"] == 2070.0 and s["reasons"] == ["sw_power_cap"]
+    # fewer than two samples inside: the whole run's samples, and said so
+    s = c.summary(2.9, 3.1)
+    assert s["window"] == "warmup_and_timed_region" and s["samples"] == 5
+    assert bench.ClockSampler(0).summary(0, 1)["samples"] == 0
