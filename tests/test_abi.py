@@ -131,6 +131,26 @@ def test_status_strings_and_errors_without_gpu(sphlib):
     assert st == 1 and b"27-cell stencil" in L.sph_last_error()
 
 
+def test_empty_and_oversized_inputs_are_refused_without_gpu(sphlib):
+    """No particles, or more than the 2^30 the index types hold, are refused
+    before any device call, and so is every call on no handle."""
+    L = sphlib.load()
+    buf = (ctypes.c_float * 12)()
+    h = ctypes.c_void_p()
+    for count in (0, (1 << 30) + 1):
+        p = P.dam_break_params((0, 0, 0), (1, 1, 1), 4)
+        p.numParticles = count
+        st = L.sph_create(ctypes.byref(p), None, buf, None, None, ctypes.byref(h))
+        assert st == 1 and h.value is None and b"numParticles" in L.sph_last_error()
+    assert L.sph_step(None, 0) == 1
+    assert L.sph_step_many(None, 0, 2) == 1
+    assert L.sph_read(None, 0, buf, 48) == 1
+    assert L.sph_read_async(None, 0, buf, 48) == 1
+    assert L.sph_write(None, 0, buf, 48) == 1
+    assert L.sph_synchronize(None) == 1
+    assert L.sph_destroy(None) == 0
+
+
 def test_boundary_dims_without_gpu(sphlib):
     import numpy as np
     p = P.example01_params()
