@@ -45,7 +45,7 @@ FORCE_FLOP_PER_PAIR = 40
 # The source files the neighbour kernels are compiled from: a DRAM traffic
 # figure recorded under profiles/ holds only while their hash is unchanged.
 KERNEL_SOURCES = ["cudasphnew_gb300/csrc/" + f for f in
-                  ("sph_step.cu", "sph_device.cuh", "sph_internal.h", "sph_sim.h", "sph_mlp_tile.cuh",
+                  ("sph_step.cu", "sph_device.cuh", "sph_internal.h", "sph_mlp_tile.cuh", "sph_corrector.h",
                    "sph_tc.cuh")] + ["include/sph.h"]
 
 

@@ -403,6 +403,18 @@ void enqueue_density_only(sph_sim* s, const float4* pos, const float4* vel, bool
     launch_density(n, s->posS, rows_of(s), g, ph, s->map, s->rho4S, s->rowStart, s->rowMask, cfg, st);
 }
 
+void enqueue_list_density(sph_sim* s, const float4* pos, const float4* vel) {
+    cudaStream_t st = s->stream;
+    const int n = s->n;
+    GridDev g = grid_of(s);
+    PhysDev ph = make_phys(s->P, s->O);
+    launch_hash_count(n, pos, g, s->sb, s->status, st, &s->vl);
+    launch_cell_scan(g.numCells, s->sb, s->status, st, &s->vl);
+    launch_scatter(n, s->sb, st, s->status, &s->vl);
+    launch_rank_gather(n, s->sb, pos, vel, g, s->posS, s->velS, st, &s->vl, s->status);
+    launch_density_lists(n, s->posS, s->velS, rows_of(s), g, ph, s->map, s->rho4S, s->vl, s->cfg, true, true, st);
+}
+
 void invalidate_graphs(sph_sim* s) {
     s->graphValid = false;
     s->graphGen++;

@@ -13,8 +13,9 @@
 //
 // Audit.  Every auditInterval-th learned step runs from a saved copy of the
 // state both as a learned step and as `stride` plain steps of dt; densities
-// of both results are computed and when the largest per-particle relative
-// difference exceeds densityTolerance the plain result is kept.  The choice
+// of both results are computed (over the reused lists when the handle has
+// them) and when the largest per-particle relative difference exceeds
+// densityTolerance the plain result is kept.  The choice
 // is made on the device, so learned and audit steps are each one CUDA graph.
 #include <cuda_runtime.h>
 
@@ -211,6 +212,24 @@ void enqueue_audit(sph_sim* s, Corrector* C) {
     // the rest of the plain solver, as the first plain step above: over the
     // learned step's lists (reused while they hold) or with the per-step search
     for (int k = 1; k < C->cfg.stride; k++) enqueue_step(s, SPH_STEP_PLAIN, false, s->vlOn);
+    if (s->vlOn) {
+        // Both densities over the lists, as a list step takes its density:
+        // the plain result's (its distance from the build positions is the
+        // one its last force stage recorded), then the learned result's
+        // after measuring its own distance (a build it needs centres the
+        // lists on it).  Then the kept state's distance, for the next step.
+        enqueue_list_density(s, s->pos, s->vel);
+        launch_unpermute(s->n, s->sb.workIds, s->rho4S, 0, C->rhoB, 1, 0, q);
+        launch_list_displacement(s->n, C->lPos, s->sb.workIds, s->vl, q);
+        enqueue_list_density(s, C->lPos, C->lVel);
+        launch_unpermute(s->n, s->sb.workIds, s->rho4S, 0, C->rhoA, 1, 0, q);
+        cudaMemsetAsync(C->errBits, 0, sizeof(unsigned int), q);
+        launch_audit(s->n, C->rhoA, C->rhoB, C->errBits, q);
+        launch_audit_select(s->n, C->errBits, C->cfg.densityTolerance, C->lPos, C->lVel, s->pos, s->vel,
+                            C->counters, nullptr, q);
+        launch_list_displacement(s->n, s->pos, s->sb.workIds, s->vl, q);
+        return;
+    }
     enqueue_density_only(s, s->pos, s->vel);
     launch_unpermute(s->n, s->sb.workIds, s->rho4S, 0, C->rhoB, 1, 0, q);
     // last: the learned result, with the neighbour masks, so that when the
@@ -284,9 +303,10 @@ sph_status corrector_step(sph_sim* s, int count, bool useGraph) {
             SPH_CUDA(cudaGetLastError());
         }
         C->sinceAudit = audit ? 0 : C->sinceAudit + 1;
-        // the lists match the sorted copies after a learned step over them;
-        // an audit ends with the per-step search
-        s->lastStepLists = !audit && s->vlOn;
+        // learned steps and audits over the lists leave sorted copies that
+        // match the lists (an audit: the learned result's, and the kept
+        // state's distance from the build positions recorded)
+        s->lastStepLists = s->vlOn;
         C->rep.learnedSteps++;
         C->recorded = C->recorded || C->record;
     }

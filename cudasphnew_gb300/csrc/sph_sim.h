@@ -172,6 +172,11 @@ void enqueue_coarse(sph_sim* s, const GridDev& g, const PhysDev& ph, int collide
 // copies (posS, velS, rho4S) and cell tables, with the neighbour masks when
 // `masks`; nothing is integrated.
 void enqueue_density_only(sph_sim* s, const float4* pos, const float4* vel, bool masks = false);
+// The front of a step over the reused lists for the state (pos, vel): the
+// decision (from the distance recorded for the lists), the sort stages when
+// it builds, the gather into the working order and the density stage in the
+// form the decision selects; nothing is integrated.
+void enqueue_list_density(sph_sim* s, const float4* pos, const float4* vel);
 // Marks every captured step graph of the handle stale.
 void invalidate_graphs(sph_sim* s);
 

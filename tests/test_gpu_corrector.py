@@ -444,6 +444,32 @@ def test_learned_steps_over_reused_lists(sphlib):
     assert np.abs(la[1] - lb[1]).max() <= 1e-4 * max(1.0, np.abs(lb[1]).max())
 
 
+def test_learned_steps_after_an_audit_over_the_lists(sphlib):
+    """An audit over the reused lists takes both densities over them and
+    leaves lists that hold for the state it keeps: the learned steps after
+    an accepting audit match, within rounding, those of a new handle started
+    from the kept state (which builds its lists there)."""
+    sc = small()
+    blob = random_blob(9)
+    with make(sphlib, sc) as sim:
+        sim.step(count=40)
+        x0, v0 = sim.positions(), sim.velocities()
+    with make(sphlib, sc, x0, v0) as sim:
+        sim.load_corrector(blob, stride=4, auditInterval=2, densityTolerance=1e9)
+        sim.step(mode=sphlib.SPH_STEP_LEARNED, count=2)  # a learned step, then an audited one
+        rep = sim.corrector_report()
+        assert rep.audits == 1 and rep.rollbacks == 0 and rep.maxAuditError > 0
+        x1, v1 = sim.positions(), sim.velocities()
+        sim.step(mode=sphlib.SPH_STEP_LEARNED)           # over the lists the audit left
+        a = (sim.positions(), sim.velocities())
+    with make(sphlib, sc, x1, v1) as sim:
+        sim.load_corrector(blob, stride=4, auditInterval=0)
+        sim.step(mode=sphlib.SPH_STEP_LEARNED)
+        b = (sim.positions(), sim.velocities())
+    assert np.abs(a[0] - b[0]).max() <= 1e-6
+    assert np.abs(a[1] - b[1]).max() <= 1e-4 * max(1.0, np.abs(b[1]).max())
+
+
 def test_learned_graph_matches_eager(sphlib):
     sc = tiny()
     blob = random_blob(7)
